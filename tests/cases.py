@@ -1,0 +1,81 @@
+"""Seeded test and benchmark cases (shared by tests, fixture generation and bench).
+
+Synthetic inputs only: particle centres are drawn from numpy's PCG64 generator
+with a minimum periodic separation; the fluid starts at rest.
+"""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+from icep_kapsel_gb300 import abi  # noqa: E402
+
+
+def positions(n, L, minsep, seed, max_tries=200000):
+    """n centres uniform in [0,L)^3 with periodic separation >= minsep."""
+    rng = np.random.default_rng(seed)
+    L = np.asarray(L, dtype=np.float64) * np.ones(3)
+    out = []
+    tries = 0
+    while len(out) < n:
+        tries += 1
+        if tries > max_tries:
+            raise RuntimeError("cannot place %d particles with separation %g" % (n, minsep))
+        x = rng.uniform(0.0, 1.0, 3) * L
+        ok = True
+        for y in out:
+            d = x - y
+            d -= L * np.round(d / L)
+            if np.dot(d, d) < minsep * minsep:
+                ok = False
+                break
+        if ok:
+            out.append(x)
+    return np.array(out).reshape(n, 3)
+
+
+def ns_case(n=32, npart=8, minsep=10.0, seed=1, rotation=1, dt=0.05, motor=True):
+    """Plain SPM DNS: n^3, dx=1, rho=eta=1, spheres a=4 xi=2, WCA 12:6,
+    particle 0 pushed by a body-frame force 0.01 along x (a motor species;
+    the reference requires ROTATION ON for motor particles)."""
+    x = positions(npart, n, minsep, seed)
+    spec = [0] + [1] * (npart - 1) if motor else [0] * npart
+    p = abi.make_params(nx=n, ny=n, nz=n, n_particles=npart, n_species=2 if motor else 1,
+                        rotation=rotation, dt=dt, a=4.0, a_xi=2.0, lj_epsilon=1.0, lj_powers=0,
+                        lj_truncate=1,
+                        janus_propulsion=[abi.MOTOR, abi.NO_PROPULSION] if motor else [abi.NO_PROPULSION],
+                        janus_force=[[0.01, 0.0, 0.0], [0.0, 0.0, 0.0]])
+    return p, abi.make_particles(x, spec=spec)
+
+
+def icep_case(n=32, npart=4, minsep=12.0, seed=2, a=4.0, eps_f=1.0, eps_p=10.0, e_ext=(0.01, 0.0, 0.0),
+              tol=1e-6, maxit=2000, dt=0.01, per_particle_eps=None, solver=abi.SOLVER_REF,
+              precision=abi.FP64):
+    """Electrolyte + Dielectric_property ON, salt (z=+-1, Onsager 7.24,
+    Debye length 10 a), kBT=1, Dielectric_cst=1 (the reference's sample
+    input values), uniform external field."""
+    x = positions(npart, n, minsep, seed)
+    eps = None
+    if per_particle_eps is not None:
+        lo, hi = per_particle_eps
+        eps = np.random.default_rng(seed + 1000).uniform(lo, hi, npart)
+    p = abi.make_params(nx=n, ny=n, nz=n, n_particles=npart, n_species=1, sw_eq=abi.ELECTROLYTE,
+                        dielectric=1, dielectric_cst=1.0, eps_fluid=eps_f, eps_particle_top=eps_p,
+                        eps_particle_bottom=eps_p, external_field=1, e_ext=list(e_ext),
+                        potential_tol=tol, potential_iter=maxit, kbt=1.0, debye_length=10.0,
+                        onsager_pos=7.24, onsager_neg=7.24, valency_pos=1.0, valency_neg=-1.0,
+                        dt=dt, a=a, a_xi=2.0, rotation=0, per_particle_eps=1 if eps is not None else 0,
+                        solver=solver, precision=precision)
+    return p, abi.make_particles(x, eps_p=eps)
+
+
+def lj_dense_case(n=32, npart=24, seed=7, minsep=7.2):
+    """Particles closer than the WCA cutoff (2^(1/6) * 8 = 8.98) so that the
+    cell-list scan and its multiplicity at 32^3 (2 cells per side) matter."""
+    x = positions(npart, n, minsep, seed)
+    p = abi.make_params(nx=n, ny=n, nz=n, n_particles=npart, n_species=1, rotation=0, dt=0.05)
+    return p, abi.make_particles(x)

@@ -1,0 +1,78 @@
+// common.cuh -- shared definitions of the GB300 ICEP library (sm_103a).
+//
+// Grid fields use the reference's layout [NX][NY][NZ_], NZ_ = 2*(NZ/2+1),
+// z fastest; k-space values are interleaved (re,im) pairs in the same buffer
+// with kz = 0..NZ/2 (fft_wrapper.h:681-723 in the reference). R is the
+// storage/arithmetic type of the fields: double (FP64 mode) or float (the
+// FFT/field type of MIXED mode). Particles are always FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/icep_gb300.h"
+
+#define ICEP_CUDA_CHECK(call)                                                        \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      fprintf(stderr, "icep_gb300: CUDA error %s at %s:%d\n", cudaGetErrorString(e_), \
+              __FILE__, __LINE__);                                                   \
+      return ICEP_ERR_CUDA;                                                          \
+    }                                                                                \
+  } while (0)
+
+
+namespace icep {
+
+template <typename R>
+struct cplx {
+  R x, y;
+};
+
+// Geometry of one grid (shared by every kernel).
+struct Grid {
+  int nx, ny, nz;  // mesh
+  int hnz;         // NZ/2 + 1 complex values per z row
+  int nzp;         // NZ_ = 2*hnz doubles per z row
+  int trn[3];      // 2/3-rule limits (N+2)/3
+  double wave[3];  // 2 pi / L
+  double dx;
+  __host__ __device__ long nf() const { return (long)nx * ny * nzp; }
+  __host__ __device__ long nreal() const { return (long)nx * ny * nz; }
+  __host__ __device__ long nmodes() const { return (long)nx * ny * hnz; }
+};
+
+__host__ __device__ inline long gidx(const Grid &g, int i, int j, int k) {
+  return ((long)i * g.ny + j) * g.nzp + k;
+}
+__host__ __device__ inline int kx_of(const Grid &g, int i) { return (i > g.nx / 2) ? i - g.nx : i; }
+__host__ __device__ inline int ky_of(const Grid &g, int j) { return (j > g.ny / 2) ? j - g.ny : j; }
+__host__ __device__ inline bool in_two_third(const Grid &g, int i, int j, int kz) {
+  int ax = (i <= g.nx / 2) ? i : g.nx - i;
+  int ay = (j <= g.ny / 2) ? j : g.ny - j;
+  return ax < g.trn[0] && ay < g.trn[1] && kz < g.trn[2];
+}
+
+inline unsigned div_up(long a, long b) { return (unsigned)((a + b - 1) / b); }
+
+// Field slots of a context (ids shared with the oracle and the C-ABI).
+enum FieldId {
+  F_ZETA0 = 0, F_ZETA1, F_U0, F_U1, F_U2, F_UP0, F_UP1, F_UP2, F_PHI, F_PHI_SUM,
+  F_F0, F_F1, F_F2, F_POT, F_EPS, F_GE0, F_GE1, F_GE2, F_C0, F_C1, F_RHO, F_WORK,
+  F_SN0, F_SN1, F_SN2, F_NS0_0, F_NS0_1, F_NS1_0, F_NS1_1, F_CRHS0, F_CRHS1,
+  F_WV1, F_WV3_0, F_WV3_1, F_WV3_2,
+  // Krylov work vectors (padded fields)
+  F_KR, F_KR0, F_KP, F_KV, F_KS, F_KT, F_KX, F_KB, F_KY, F_KZ,
+  F_COUNT
+};
+
+// Up to 5 fields transformed by one batched launch.
+template <typename R>
+struct FieldBatch {
+  R *p[5];
+  int n;
+};
+
+}  // namespace icep

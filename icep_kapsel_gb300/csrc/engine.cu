@@ -1,0 +1,768 @@
+// engine.cu -- device state and step orchestration of one ICEP simulation.
+//
+// The call order of each phase follows the reference function named in its
+// comment; kernels live in fft.cu, fields.cu, particles.cu and krylov.cu.
+#include <float.h>
+#include <math.h>
+#include <string.h>
+
+#include <cstdio>
+#include <vector>
+
+#include "engine.cuh"
+#include "fields.cuh"
+#include "krylov.cuh"
+
+namespace icep {
+
+namespace {
+
+bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+template <typename R>
+class Engine : public EngineBase {
+ public:
+  icep_params P;
+  Grid g;
+  cudaStream_t s = nullptr;
+  FFTPlan<R> fft;
+  R *f[F_COUNT];
+  double *stage = nullptr;  // FP64 staging for get/set of FP32 fields
+  icep_particle *dp = nullptr;
+  icep_particle *hp = nullptr;  // pinned
+  int np = 0;
+  int *dsek = nullptr;
+  int npd = 0;
+  PartParams pp;
+  double *ukdc = nullptr;    // device double[3]
+  double *e_ext_n = nullptr; // device double[3]: E_ext * NX*NY*NZ
+  double *partials = nullptr;
+  double *scal = nullptr;
+  double *hscal = nullptr;  // pinned
+  int *ljwork = nullptr;
+  int ljwork_ints = 0;
+  int *dpairs_n = nullptr;
+  double radius, xi, hxi, nu;
+  double valency_e[2], onsager[2];
+  bool electrolyte;
+
+  ~Engine() override {
+    if (s) cudaStreamSynchronize(s);
+    for (int i = 0; i < F_COUNT; i++) cudaFree(f[i]);
+    fft_plan_free(fft);
+    cudaFree(stage);
+    cudaFree(dp);
+    cudaFreeHost(hp);
+    cudaFree(dsek);
+    cudaFree(ukdc);
+    cudaFree(e_ext_n);
+    cudaFree(partials);
+    cudaFree(scal);
+    cudaFreeHost(hscal);
+    cudaFree(ljwork);
+    cudaFree(dpairs_n);
+    if (s) cudaStreamDestroy(s);
+  }
+
+  cudaStream_t stream() const override { return s; }
+
+  int fail(int code, const char *msg) {
+    err = msg;
+    return code;
+  }
+  int cuda_status(const char *where) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      err = std::string(where) + ": " + cudaGetErrorString(e);
+      return ICEP_ERR_CUDA;
+    }
+    return ICEP_OK;
+  }
+
+  int setup(const icep_params &p, const icep_particle *parts, int n) {
+    for (int i = 0; i < F_COUNT; i++) f[i] = nullptr;
+    P = p;
+    if (!pow2(p.nx) || !pow2(p.ny) || !pow2(p.nz) || p.nx < 16 || p.ny < 16 || p.nz < 16 || p.nx > 256 ||
+        p.ny > 256 || p.nz > 256)
+      return fail(ICEP_ERR_UNSUPPORTED, "mesh sizes must be powers of two in [16, 256]");
+    if (n != p.n_particles || n < 0) return fail(ICEP_ERR_ARG, "particle count mismatch");
+    if (p.n_species < 1 || p.n_species > ICEP_MAX_SPECIES) return fail(ICEP_ERR_ARG, "n_species out of range");
+    if (p.dt <= 0 || p.dx <= 0 || p.rho <= 0 || p.eta <= 0) return fail(ICEP_ERR_ARG, "non-positive dt/dx/rho/eta");
+    for (int q = 0; q < n; q++)
+      if (parts[q].spec < 0 || parts[q].spec >= p.n_species) return fail(ICEP_ERR_ARG, "particle species out of range");
+    electrolyte = (p.sw_eq == ICEP_ELECTROLYTE);
+    if (electrolyte && !p.dielectric)
+      return fail(ICEP_ERR_UNSUPPORTED, "Electrolyte requires Dielectric_property ON on this path");
+    if (p.sw_eq != ICEP_NAVIER_STOKES && p.sw_eq != ICEP_ELECTROLYTE) return fail(ICEP_ERR_UNSUPPORTED, "SW_EQ");
+    g.nx = p.nx; g.ny = p.ny; g.nz = p.nz;
+    g.hnz = p.nz / 2 + 1;
+    g.nzp = 2 * g.hnz;
+    const int N[3] = {p.nx, p.ny, p.nz};
+    for (int d = 0; d < 3; d++) {
+      g.trn[d] = (N[d] + 2) / 3;
+      g.wave[d] = 2.0 * M_PI / (N[d] * p.dx);
+    }
+    g.dx = p.dx;
+    radius = p.a * p.dx;
+    xi = p.a_xi * p.dx;
+    hxi = 0.5 * xi;
+    nu = p.eta / p.rho;
+    valency_e[0] = p.valency_pos * p.elementary_charge;
+    valency_e[1] = p.valency_neg * p.elementary_charge;
+    onsager[0] = p.onsager_pos;
+    onsager[1] = p.onsager_neg;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(ICEP_ERR_CUDA, "cudaStreamCreate failed (no GPU?)");
+    const size_t fb = sizeof(R) * g.nf();
+    for (int i = 0; i < F_COUNT; i++) {
+      if (cudaMalloc(&f[i], fb) != cudaSuccess) return fail(ICEP_ERR_CUDA, "cudaMalloc of fields failed");
+      cudaMemsetAsync(f[i], 0, fb, s);
+    }
+    if (sizeof(R) != sizeof(double) && cudaMalloc(&stage, sizeof(double) * g.nf()) != cudaSuccess)
+      return fail(ICEP_ERR_CUDA, "cudaMalloc of staging failed");
+    if (fft_plan_init(fft, g) != ICEP_OK) return fail(ICEP_ERR_CUDA, "FFT plan setup failed");
+    // Particle_domain (profile.cxx:25-74)
+    std::vector<int> sek;
+    const int nh = (int)p.a + (int)p.a_xi + 2;
+    const double max_r = radius + hxi + 1.7321 * p.dx;
+    for (int i = -nh; i <= nh; i++)
+      for (int j = -nh; j <= nh; j++)
+        for (int k = -nh; k <= nh; k++) {
+          const double d = sqrt((i * p.dx) * (i * p.dx) + (j * p.dx) * (j * p.dx) + (k * p.dx) * (k * p.dx));
+          if (d < max_r) {
+            sek.push_back(i);
+            sek.push_back(j);
+            sek.push_back(k);
+          }
+        }
+    npd = (int)(sek.size() / 3);
+    if (2 * nh + 1 > p.nx || 2 * nh + 1 > p.ny || 2 * nh + 1 > p.nz)
+      return fail(ICEP_ERR_UNSUPPORTED, "particle stencil wider than the box");
+    cudaMalloc(&dsek, sizeof(int) * sek.size());
+    cudaMemcpyAsync(dsek, sek.data(), sizeof(int) * sek.size(), cudaMemcpyHostToDevice, s);
+    np = n;
+    cudaMalloc(&dp, sizeof(icep_particle) * (n > 0 ? n : 1));
+    cudaMallocHost(&hp, sizeof(icep_particle) * (n > 0 ? n : 1));
+    for (int q = 0; q < n; q++) {
+      hp[q] = parts[q];
+      if (!p.per_particle_eps) hp[q].eps_p = p.eps_particle_top;
+    }
+    cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * n, cudaMemcpyHostToDevice, s);
+    // particle parameters (Set_global_parameters, input.cxx:286-300, 404-440)
+    memset(&pp, 0, sizeof(pp));
+    pp.dx = p.dx; pp.radius = radius; pp.xi = xi; pp.hxi = hxi;
+    for (int d = 0; d < 3; d++) {
+      pp.L[d] = N[d] * p.dx;
+      pp.N[d] = N[d];
+    }
+    pp.nzp = g.nzp;
+    pp.rotation = p.rotation;
+    pp.np = n;
+    pp.np_domain = npd;
+    pp.eps_f = p.eps_fluid;
+    pp.dt = p.dt;
+    pp.rho = p.rho;
+    pp.lj_eps = p.lj_epsilon;
+    pp.lj_dia = 2.0 * radius;
+    pp.lj_powers = p.lj_powers;
+    double arc;
+    if (p.lj_truncate > 0)
+      arc = (p.lj_powers == 0) ? pow(2., 1. / 6.) : (p.lj_powers == 1) ? pow(2., 1. / 12.) : pow(2., 1. / 18.);
+    else if (p.lj_truncate == 0) {
+      int nmin = N[0] < N[1] ? N[0] : N[1];
+      nmin = nmin < N[2] ? nmin : N[2];
+      arc = nmin * p.dx * .5 / pp.lj_dia;
+      if (arc > 2.5) arc = 2.5;
+    } else
+      arc = 0.;
+    pp.r_cutoff = arc * pp.lj_dia;
+    pp.lj_on = p.lj_truncate >= 0;
+    pp.n_species = p.n_species;
+    for (int q = 0; q < ICEP_MAX_SPECIES; q++) {
+      const double mass = p.mass_ratio[q] * p.rho * 4. / 3. * M_PI * radius * radius * radius;
+      pp.imass[q] = (mass > 0) ? 1. / mass : 0.0;
+      pp.imoi[q] = (mass > 0) ? 1. / (2. / 5. * mass * radius * radius) : 0.0;
+      pp.mass_ratio[q] = p.mass_ratio[q];
+      pp.motor[q] = (q < p.n_species && p.janus_propulsion[q] == ICEP_MOTOR) ? 1 : 0;
+      for (int d = 0; d < 3; d++) {
+        pp.jforce[q][d] = p.janus_force[q][d];
+        pp.jtorque[q][d] = p.janus_torque[q][d];
+      }
+    }
+    pp.g = p.g;
+    pp.g_direction = p.g_direction;
+    cudaMalloc(&ukdc, sizeof(double) * 3);
+    cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
+    cudaMalloc(&e_ext_n, sizeof(double) * 3);
+    {
+      double en[3];
+      const double amp = (double)p.nx * p.ny * p.nz;
+      for (int d = 0; d < 3; d++) en[d] = p.e_ext[d] * amp;
+      cudaMemcpy(e_ext_n, en, sizeof(en), cudaMemcpyHostToDevice);
+    }
+    cudaMalloc(&partials, sizeof(double) * 2 * DOT_BLOCKS);
+    cudaMalloc(&scal, sizeof(double) * S_COUNT);
+    cudaMemsetAsync(scal, 0, sizeof(double) * S_COUNT, s);
+    cudaMallocHost(&hscal, sizeof(double) * S_COUNT);
+    const int ncell = (p.nx / 16) * (p.ny / 16) * (p.nz / 16);
+    ljwork_ints = 2 * (ncell + 1) + (n > 0 ? n : 1);
+    cudaMalloc(&ljwork, sizeof(int) * ljwork_ints);
+    cudaMalloc(&dpairs_n, sizeof(int));
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("setup");
+    return cuda_status("setup");
+  }
+
+  // ---------------------------------------------------------------- helpers
+  void zero(int id) { cudaMemsetAsync(f[id], 0, sizeof(R) * g.nf(), s); }
+  void copy(int dst, int src) { cudaMemcpyAsync(f[dst], f[src], sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s); }
+  void r2c(R *a, R *b = nullptr, R *c = nullptr, R *d = nullptr, R *e = nullptr) {
+    fft_r2c(fft, batch(a, b, c, d, e), s);
+  }
+  void c2r(R *a, R *b = nullptr, R *c = nullptr, R *d = nullptr, R *e = nullptr) {
+    fft_c2r(fft, batch(a, b, c, d, e), s);
+  }
+  R *const *vec(int id0) { return &f[id0]; }
+
+  // Zeta_k2u (operate_omega.h:138-141)
+  void zeta_k2u() {
+    zeta_k2u_k<R>(g, f[F_ZETA0], f[F_ZETA1], ukdc, f[F_U0], f[F_U1], f[F_U2], s);
+    c2r(f[F_U0], f[F_U1], f[F_U2]);
+  }
+  // U2advection_k (operate_omega.cxx:12-98) on real u into adv0/adv1
+  void u2advection_k(int a0, int a1) {
+    advection_products<R>(g, f[F_U0], f[F_U1], f[F_U2], f[a0], f[a1], s);
+    r2c(f[F_U0], f[F_U1], f[F_U2], f[a0], f[a1]);
+    advection_combine<R>(g, f[F_U0], f[F_U1], f[F_U2], f[a0], f[a1], s);
+  }
+  // Solenoidal_u (operate_omega.h:109-116)
+  void solenoidal_u(int id0) {
+    r2c(f[id0], f[id0 + 1], f[id0 + 2]);
+    truncate_23<R>(g, batch(f[id0], f[id0 + 1], f[id0 + 2]), s);
+    solenoidal_uk<R>(g, f[id0], f[id0 + 1], f[id0 + 2], s);
+    c2r(f[id0], f[id0 + 1], f[id0 + 2]);
+  }
+  // NS_solver_slavedEuler (fluid_solver.cxx:340-366)
+  void ns_solver_slaved_euler() {
+    truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
+    zeta_k2u();
+    u2advection_k(F_NS0_0, F_NS0_1);
+    ns_slaved_update<R>(g, f[F_ZETA0], f[F_ZETA1], f[F_NS0_0], f[F_NS0_1], nu, P.dt, s);
+  }
+  // Make_phi_particle_sum (make_phi.cxx:229-275)
+  void make_phi_particle_sum() {
+    zero(F_PHI_SUM);
+    scatter_profile<R>(pp, dp, dsek, f[F_PHI_SUM], nullptr, PROF_PHI, s);
+    zero(F_PHI);
+    phi_clip<R>(g, f[F_PHI_SUM], f[F_PHI], s);
+  }
+  // Make_u_particle_sum (make_phi.cxx:329-370)
+  void make_u_particle_sum() {
+    for (int d = 0; d < 3; d++) zero(F_UP0 + d);
+    scatter_up<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_UP0], f[F_UP1], f[F_UP2], s);
+  }
+  // Make_f_particle_dt_sole + Add_f_particle (f_particle.h:37-95)
+  void f_particle_sole_and_add() {
+    f_nonsole<R>(g, vec(F_F0), vec(F_UP0), f[F_PHI], vec(F_U0), s);
+    solenoidal_u(F_F0);
+    add_vec<R>(g, vec(F_U0), vec(F_F0), R(1), s);
+  }
+  // Make_dielectric_field (operate_dielectric.cxx:270-309): phi_sin into
+  // phi_id; per-particle permittivity (extension) accumulates into aux_id.
+  void make_dielectric_field(int phi_id, int aux_id) {
+    zero(phi_id);
+    R *aux = nullptr;
+    if (P.per_particle_eps) {
+      zero(aux_id);
+      aux = f[aux_id];
+    }
+    scatter_profile<R>(pp, dp, dsek, f[phi_id], aux, PROF_PHI_SIN, s);
+    eps_from_profile<R>(g, f[F_EPS], f[phi_id], aux, P.eps_fluid, P.eps_particle_top, P.dielectric_cst, s);
+  }
+  // Conc_k2charge_field_no_surfase_charge (operate_dielectric.cxx:135-160)
+  void conc_k2charge(int rho_id, int phi_id, int tmp_id) {
+    for (int n = 0; n < 2; n++) {
+      copy(tmp_id, F_C0 + n);
+      c2r(f[tmp_id]);
+      charge_add<R>(g, f[rho_id], f[tmp_id], f[phi_id], valency_e[n], n == 0, s);
+    }
+  }
+  // Ax (operate_dielectric.cxx:485-522) on padded real fields
+  void apply_A(const R *x, R *y) {
+    copy_real<R>(g, x, y, s);
+    r2c(y);
+    grad_k<R>(g, y, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], R(1), true, nullptr, s);
+    c2r(f[F_WV3_0], f[F_WV3_1], f[F_WV3_2]);
+    eps_face_mul<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EPS], s);
+    r2c(f[F_WV3_0], f[F_WV3_1], f[F_WV3_2]);
+    div_k<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], y, true, s);
+    c2r(y);
+    matvecs++;
+  }
+  // Build_rhs (operate_dielectric.cxx:524-540)
+  void build_rhs(int rhs_id, int rho_id) {
+    eps_face_E<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EPS], P.e_ext[0], P.e_ext[1], P.e_ext[2], s);
+    r2c(f[F_WV3_0], f[F_WV3_1], f[F_WV3_2]);
+    div_k<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[rhs_id], true, s);
+    c2r(f[rhs_id]);
+    axpby_real<R>(g, f[rho_id], f[rhs_id], R(-1), R(1), s);
+  }
+  int read_scal() {
+    cudaMemcpyAsync(hscal, scal, sizeof(double) * S_COUNT, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("solver sync");
+    return ICEP_OK;
+  }
+
+  // Spectral preconditioner: y = M^-1 x
+  void precond(const R *x, R *y, double eps_ref) {
+    copy_real<R>(g, x, y, s);
+    r2c(y);
+    inv_laplace_k<R>(g, y, eps_ref, s);
+    c2r(y);
+  }
+
+  /*
+   * BiCGSTAB on padded fields F_KB (b) and F_KX (x, guess in / solution out).
+   * spectral == false: identity preconditioner, Eigen's stopping rule on the
+   * recursively updated residual and its restart rule (the REF solver).
+   * spectral == true: right preconditioner M^-1 (constant-eps_ref spectral
+   * inverse), b projected onto mean zero (the range of the operator, whose
+   * null space is the constants), convergence confirmed on the true residual.
+   */
+  int bicgstab(double tol, int maxit, bool spectral, double eps_ref, int *iters, double *rel_err) {
+    R *b = f[F_KB], *x = f[F_KX], *r = f[F_KR], *r0 = f[F_KR0], *p = f[F_KP], *v = f[F_KV];
+    R *sv = f[F_KS], *t = f[F_KT], *y = f[F_KY], *z = f[F_KZ];
+    if (spectral) {
+      sum_real<R>(g, b, partials, scal, S_AUX0, s);
+      sub_mean<R>(g, b, scal, S_AUX0, s);
+    }
+    apply_A(x, t);
+    sub_real<R>(g, b, t, r, s);
+    copy_real<R>(g, r, r0, s);
+    dots<R>(g, r0, r0, b, b, 2, partials, scal, S_R0R, s);
+    int st = read_scal();
+    if (st) return st;
+    double r0sq = hscal[S_R0R], bsq = hscal[S_R0R + 1];
+    if (bsq == 0.0) {
+      zero(F_KX);
+      *iters = 0;
+      *rel_err = 0.0;
+      return ICEP_OK;
+    }
+    zero(F_KV);
+    zero(F_KP);
+    double rho = 1, alpha = 1, w = 1;
+    const double tol2 = tol * tol * bsq, eps2 = DBL_EPSILON * DBL_EPSILON;
+    double rr = r0sq, rho_new = r0sq;
+    int i = 0, restarts = 0;
+    while (i < maxit) {
+      if (!(rr > tol2)) {
+        if (!spectral) break;
+        // confirm on the true residual
+        apply_A(x, t);
+        sub_real<R>(g, b, t, r, s);
+        dots<R>(g, r, r, r, r, 1, partials, scal, S_RR, s);
+        if ((st = read_scal())) return st;
+        rr = hscal[S_RR];
+        if (!(rr > tol2)) break;
+        copy_real<R>(g, r, r0, s);
+        r0sq = rr;
+        rho_new = rr;
+        zero(F_KV);
+        zero(F_KP);
+        rho = 1; alpha = 1; w = 1;
+      }
+      const double rho_old = rho;
+      rho = rho_new;
+      if (fabs(rho) < eps2 * r0sq) {
+        apply_A(x, t);
+        sub_real<R>(g, b, t, r, s);
+        copy_real<R>(g, r, r0, s);
+        dots<R>(g, r, r, r, r, 1, partials, scal, S_RR, s);
+        if ((st = read_scal())) return st;
+        rho = r0sq = hscal[S_RR];
+        if (restarts++ == 0) i = 0;
+      }
+      const double beta = (rho / rho_old) * (alpha / w);
+      bicg_p<R>(g, p, r, v, beta, w, s);
+      const R *yy = p;
+      if (spectral) {
+        precond(p, y, eps_ref);
+        yy = y;
+      }
+      apply_A(yy, v);
+      dots<R>(g, r0, v, r0, v, 1, partials, scal, S_R0V, s);
+      bicg_s<R>(g, sv, r, v, rho, scal, s);
+      const R *zz = sv;
+      if (spectral) {
+        precond(sv, z, eps_ref);
+        zz = z;
+      }
+      apply_A(zz, t);
+      dots<R>(g, t, t, t, sv, 2, partials, scal, S_TT, s);
+      bicg_xr<R>(g, x, r, yy, zz, sv, t, rho, scal, s);
+      dots<R>(g, r0, r, r, r, 2, partials, scal, S_R0R, s);
+      if ((st = read_scal())) return st;
+      alpha = rho / hscal[S_R0V];
+      w = (hscal[S_TT] > 0.0) ? hscal[S_TS] / hscal[S_TT] : 0.0;
+      rho_new = hscal[S_R0R];
+      rr = hscal[S_RR];
+      ++i;
+      if (!std::isfinite(rr)) break;
+    }
+    *iters = i;
+    *rel_err = sqrt(rr / bsq);
+    return ICEP_OK;
+  }
+
+  double mean_eps() {
+    sum_real<R>(g, f[F_EPS], partials, scal, S_AUX1, s);
+    if (read_scal()) return 1.0;
+    return hscal[S_AUX1] / (double)g.nreal();
+  }
+
+  // Charge_field2potential_dielectric_LO (operate_dielectric.cxx:542-572)
+  int solve_potential(int rho_id, int pot_id, int rhs_id) {
+    build_rhs(rhs_id, rho_id);
+    copy_real<R>(g, f[rhs_id], f[F_KB], s);
+    copy_real<R>(g, f[pot_id], f[F_KX], s);
+    int it = 0;
+    double er = 0.0;
+    int st;
+    const bool spectral = (P.solver == ICEP_SOLVER_SPECTRAL);
+    const double eref = spectral ? mean_eps() : 1.0;
+    if ((st = bicgstab(P.potential_tol, P.potential_iter, spectral, eref, &it, &er))) return st;
+    if (it == P.potential_iter) {  // retry from a zero guess (operate_dielectric.cxx:563-570)
+      zero(F_KX);
+      copy_real<R>(g, f[rhs_id], f[F_KB], s);
+      if ((st = bicgstab(P.potential_tol, P.potential_iter, spectral, eref, &it, &er))) return st;
+    }
+    last_iters = it;
+    last_error = er;
+    copy_real<R>(g, f[F_KX], f[pot_id], s);
+    return ICEP_OK;
+  }
+
+  // staggered gradient of a real field (R2C, i k, shift, C2R), the field kept
+  void staggered_grad(int a_id, int g0, int tmp) {
+    copy(tmp, a_id);
+    r2c(f[tmp]);
+    grad_k<R>(g, f[tmp], f[g0], f[g0 + 1], f[g0 + 2], R(1), true, nullptr, s);
+    c2r(f[g0], f[g0 + 1], f[g0 + 2]);
+  }
+
+  // Make_Maxwell_force_x_on_fluid (operate_dielectric.cxx:611-764)
+  int maxwell_force(int rho_id) {
+    make_dielectric_field(F_F0, F_WORK);
+    conc_k2charge(rho_id, F_F0, F_F1);
+    int st = solve_potential(rho_id, F_POT, F_F2);
+    if (st) return st;
+    staggered_grad(F_EPS, F_GE0, F_WV1);
+    staggered_grad(F_POT, F_F0, F_WV1);
+    maxwell_e2<R>(g, f[F_F0], f[F_F1], f[F_F2], f[F_WV1], P.e_ext[0], P.e_ext[1], P.e_ext[2], P.external_field, s);
+    maxwell_face<R>(g, vec(F_F0), f[rho_id], f[F_WV1], vec(F_GE0), P.e_ext[0], P.e_ext[1], P.e_ext[2],
+                    P.external_field, s);
+    for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
+    interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);
+    for (int d = 0; d < 3; d++) copy(F_GE0 + d, F_F0 + d);
+    return ICEP_OK;
+  }
+
+  // NSsolute_solver_Euler (fluid_solver.cxx:318-338), Dielectric branch of
+  // Rhs_NS_Nernst_Planck (:246-292) and Rhs_NS_solute (:184-230)
+  void nssolute_solver_euler() {
+    // staggered grad of the potential minus E_ext, interpolated to nodes
+    copy(F_WV1, F_POT);
+    r2c(f[F_WV1]);
+    grad_k<R>(g, f[F_WV1], f[F_F0], f[F_F1], f[F_F2], R(1), true, P.external_field ? e_ext_n : nullptr, s);
+    c2r(f[F_F0], f[F_F1], f[F_F2]);
+    for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
+    interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);
+    truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
+    zeta_k2u();
+    for (int d = 0; d < 3; d++) zero(F_SN0 + d);
+    scatter_normal<R>(pp, dp, dsek, f[F_SN0], f[F_SN1], f[F_SN2], s);
+    for (int n = 0; n < 2; n++) {
+      truncate_23<R>(g, batch(f[F_C0 + n]), s);
+      // Diffusion_flux_single: grad(kBT L c)
+      grad_k<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], (R)(P.kbt * onsager[n]), false, nullptr, s);
+      c2r(f[F_UP0], f[F_UP1], f[F_UP2]);
+      copy(F_CRHS0 + n, F_C0 + n);
+      c2r(f[F_CRHS0 + n]);
+      np_flux_electric<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_F0), onsager[n] * valency_e[n], s);
+      np_impermeability<R>(g, vec(F_UP0), vec(F_SN0), s);
+      np_flux_advection<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_U0), s);
+      r2c(f[F_UP0], f[F_UP1], f[F_UP2]);
+      div_k<R>(g, f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n], false, s);
+    }
+    u2advection_k(F_NS1_0, F_NS1_1);
+    euler_update<R>(g, f[F_ZETA0], f[F_ZETA1], f[F_NS1_0], f[F_NS1_1], f[F_C0], f[F_C1], f[F_CRHS0], f[F_CRHS1],
+                    nu, P.dt, s);
+  }
+
+  int lj_into_fr() {
+    if (!pp.lj_on) return ICEP_OK;
+    return lj_force(pp, dp, ljwork, ljwork_ints, nullptr, 0, nullptr, s);
+  }
+
+  // Time_evolution_hydro (sp_3d_ns.cxx:24-186)
+  int time_evolution_hydro() {
+    int st;
+    if (!electrolyte) ns_solver_slaved_euler();
+    else nssolute_solver_euler();
+    truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
+    zeta_k2u();
+    if (!P.fixed_particle) md_position(pp, dp, ts != 0, s);
+    make_phi_particle_sum();
+    if (electrolyte) {
+      for (int d = 0; d < 3; d++) {
+        zero(F_UP0 + d);
+        zero(F_F0 + d);
+      }
+      f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], true, s);
+      if ((st = maxwell_force(F_UP0))) return st;
+      add_vec<R>(g, vec(F_U0), vec(F_F0), (R)(P.dt / P.rho), s);
+      solenoidal_u(F_U0);
+    }
+    f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], false, s);
+    if (!P.fixed_particle) {
+      if ((st = lj_into_fr())) return fail(st, "LJ cell list");
+      md_velocity(pp, dp, ts != 0, s);
+    }
+    make_u_particle_sum();
+    f_particle_sole_and_add();
+    r2c(f[F_U0], f[F_U1], f[F_U2]);
+    u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
+    return cuda_status("step");
+  }
+
+  // Init_rho_ion_dielectric without surface charge (operate_electrolyte.cxx:864-979)
+  void init_ions() {
+    zero(F_PHI);
+    scatter_profile<R>(pp, dp, dsek, f[F_PHI], nullptr, PROF_PHI, s);
+    const double z0 = P.valency_pos, z1 = P.valency_neg;
+    const double rho_inf = P.kbt * P.dielectric_cst * P.eps_fluid /
+                           ((P.elementary_charge * P.debye_length * radius) * (P.elementary_charge * P.debye_length * radius));
+    const double cp = rho_inf / (z0 * (z0 - z1)), cm = -rho_inf / (z1 * (z0 - z1));
+    for (int n = 0; n < 2; n++) {
+      zero(F_C0 + n);
+      fill_real<R>(g, f[F_C0 + n], (R)(n ? cm : cp), s);
+      r2c(f[F_C0 + n]);
+    }
+  }
+
+  // ------------------------------------------------------------ interface
+  int init_state() override {
+    // x_nopbc = x (Init_Particle, init_particle.cxx:389)
+    cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (int q = 0; q < np; q++)
+      for (int d = 0; d < 3; d++) hp[q].x_nopbc[d] = hp[q].x[d];
+    cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
+    // Init_zeta_k (init_fluid.cxx:10-26): fluid at rest
+    zero(F_ZETA0);
+    zero(F_ZETA1);
+    cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
+    // sp_3d_ns.cxx:431-446
+    make_phi_particle_sum();
+    make_u_particle_sum();
+    zeta_k2u();
+    f_particle_sole_and_add();
+    r2c(f[F_U0], f[F_U1], f[F_U2]);
+    u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
+    cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
+    if (electrolyte) {
+      for (int d = 0; d < 3; d++) zero(F_GE0 + d);
+      init_ions();
+      // Init_potential_dielectric (operate_dielectric.cxx:574-609)
+      make_dielectric_field(F_GE2, F_WORK);
+      conc_k2charge(F_GE1, F_GE2, F_GE0);
+      int st = solve_potential(F_GE1, F_POT, F_GE2);
+      if (st) return st;
+    }
+    ts = 0;
+    time = 0.0;
+    return cuda_status("init_state");
+  }
+
+  int step(int n) override {
+    for (int k = 0; k < n; k++) {
+      int st = time_evolution_hydro();
+      if (st) return st;
+      time += P.dt;
+      ts++;
+    }
+    return ICEP_OK;
+  }
+
+  int get_field(int id, double *host) override {
+    if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
+    if (sizeof(R) == sizeof(double)) {
+      cudaMemcpyAsync(host, f[id], sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
+    } else {
+      convert_f2d(g.nf(), (const float *)f[id], stage, s);
+      cudaMemcpyAsync(host, stage, sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_field");
+    return ICEP_OK;
+  }
+  int set_field(int id, const double *host) override {
+    if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
+    if (sizeof(R) == sizeof(double)) {
+      cudaMemcpyAsync(f[id], host, sizeof(double) * g.nf(), cudaMemcpyHostToDevice, s);
+    } else {
+      cudaMemcpyAsync(stage, host, sizeof(double) * g.nf(), cudaMemcpyHostToDevice, s);
+      convert_d2f(g.nf(), stage, (float *)f[id], s);
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_field");
+    return ICEP_OK;
+  }
+  int get_particles(icep_particle *h) override {
+    cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_particles");
+    memcpy(h, hp, sizeof(icep_particle) * np);
+    return ICEP_OK;
+  }
+  int set_particles(const icep_particle *h) override {
+    cudaStreamSynchronize(s);
+    memcpy(hp, h, sizeof(icep_particle) * np);
+    if (!P.per_particle_eps)
+      for (int q = 0; q < np; q++) hp[q].eps_p = P.eps_particle_top;
+    cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_particles");
+    return ICEP_OK;
+  }
+  int get_uk_dc(double *v) override {
+    double tmp[3];
+    cudaStreamSynchronize(s);
+    cudaMemcpy(tmp, ukdc, sizeof(tmp), cudaMemcpyDeviceToHost);
+    for (int d = 0; d < 3; d++) v[d] = tmp[d];
+    return cuda_status("get_uk_dc");
+  }
+  int set_uk_dc(const double *v) override {
+    cudaStreamSynchronize(s);
+    cudaMemcpy(ukdc, v, sizeof(double) * 3, cudaMemcpyHostToDevice);
+    return cuda_status("set_uk_dc");
+  }
+  int fft_host(double *a, bool forward) override {
+    int st = set_field(F_WORK, a);
+    if (st) return st;
+    if (forward) r2c(f[F_WORK]);
+    else c2r(f[F_WORK]);
+    return get_field(F_WORK, a);
+  }
+  int apply_A_host(const double *x, double *y) override {
+    std::vector<double> pad(g.nf(), 0.0);
+    for (long ij = 0; ij < (long)g.nx * g.ny; ij++)
+      memcpy(&pad[ij * g.nzp], x + ij * g.nz, sizeof(double) * g.nz);
+    int st = set_field(F_KP, pad.data());
+    if (st) return st;
+    apply_A(f[F_KP], f[F_KV]);
+    if ((st = get_field(F_KV, pad.data()))) return st;
+    for (long ij = 0; ij < (long)g.nx * g.ny; ij++)
+      memcpy(y + ij * g.nz, &pad[ij * g.nzp], sizeof(double) * g.nz);
+    return ICEP_OK;
+  }
+  int lj_pairs(int *pairs, int max_pairs, int *n) override {
+    int *dpairs = nullptr;
+    if (max_pairs > 0 && cudaMalloc(&dpairs, sizeof(int) * 2 * max_pairs) != cudaSuccess)
+      return fail(ICEP_ERR_CUDA, "cudaMalloc pairs");
+    cudaMemsetAsync(dpairs_n, 0, sizeof(int), s);
+    // the pair scan accumulates into fr: clear it first, as the harness does
+    cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    for (int q = 0; q < np; q++)
+      for (int d = 0; d < 3; d++) hp[q].fr[d] = 0.0;
+    cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
+    int st = lj_force(pp, dp, ljwork, ljwork_ints, dpairs, max_pairs, dpairs_n, s);
+    if (st) {
+      cudaFree(dpairs);
+      return fail(st, "LJ cell list");
+    }
+    cudaMemcpyAsync(n, dpairs_n, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
+    const int m = (*n < max_pairs) ? *n : max_pairs;
+    if (m > 0) cudaMemcpy(pairs, dpairs, sizeof(int) * 2 * m, cudaMemcpyDeviceToHost);
+    cudaFree(dpairs);
+    return cuda_status("lj_pairs");
+  }
+  int sync() override {
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("sync");
+    return ICEP_OK;
+  }
+
+  int call(int fn) override {
+    int st = ICEP_OK;
+    switch (fn) {
+      case C_ZETA_K2U_K:
+        zeta_k2u_k<R>(g, f[F_ZETA0], f[F_ZETA1], ukdc, f[F_U0], f[F_U1], f[F_U2], s);
+        break;
+      case C_ZETA_K2U: zeta_k2u(); break;
+      case C_U_K2ZETA_K:
+        u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
+        break;
+      case C_U2ADVECTION_K: u2advection_k(F_NS0_0, F_NS0_1); break;
+      case C_SOLENOIDAL_U: solenoidal_u(F_U0); break;
+      case C_NS_SLAVED_EULER: ns_solver_slaved_euler(); break;
+      case C_MAKE_PHI_SUM: make_phi_particle_sum(); break;
+      case C_MAKE_U_SUM: make_u_particle_sum(); break;
+      case C_F_HYDRO: f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], false, s); break;
+      case C_LJ: {
+        int n = 0;
+        st = lj_pairs(nullptr, 0, &n);
+        break;
+      }
+      case C_POS_EULER: md_position(pp, dp, false, s); break;
+      case C_POS_AB2: md_position(pp, dp, true, s); break;
+      case C_VEL_EULER:
+      case C_VEL_AB2:
+        if ((st = lj_into_fr())) break;
+        md_velocity(pp, dp, fn == C_VEL_AB2, s);
+        break;
+      case C_DIELECTRIC_FIELD: make_dielectric_field(F_WORK, F_WV1); break;
+      case C_BUILD_RHS: build_rhs(F_WORK, F_RHO); break;
+      case C_SOLVE_POTENTIAL: st = solve_potential(F_RHO, F_POT, F_WORK); break;
+      case C_MAXWELL: st = maxwell_force(F_RHO); break;
+      case C_NSSOLUTE_EULER: nssolute_solver_euler(); break;
+      case C_SURFACE_NORMAL:
+        for (int d = 0; d < 3; d++) zero(F_SN0 + d);
+        scatter_normal<R>(pp, dp, dsek, f[F_SN0], f[F_SN1], f[F_SN2], s);
+        break;
+      case C_F_PARTICLE_SOLE:
+        f_nonsole<R>(g, vec(F_F0), vec(F_UP0), f[F_PHI], vec(F_U0), s);
+        solenoidal_u(F_F0);
+        break;
+      case C_TRUNCATE: truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s); break;
+      case C_CHARGE_FIELD: conc_k2charge(F_RHO, F_WORK, F_UP0); break;
+      case C_INIT_ION: init_ions(); break;
+      default: return fail(ICEP_ERR_ARG, "unknown call id");
+    }
+    if (st) return st;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("call");
+    return cuda_status("call");
+  }
+};
+
+}  // namespace
+
+EngineBase *make_engine(const icep_params &p, const icep_particle *parts, int np, int *status, std::string &err) {
+  EngineBase *e = nullptr;
+  int st;
+  if (p.precision == ICEP_MIXED) {
+    auto *m = new Engine<float>();
+    st = m->setup(p, parts, np);
+    e = m;
+  } else {
+    auto *m = new Engine<double>();
+    st = m->setup(p, parts, np);
+    e = m;
+  }
+  if (st != ICEP_OK) {
+    err = e->err;
+    delete e;
+    e = nullptr;
+  }
+  if (status) *status = st;
+  return e;
+}
+
+}  // namespace icep

@@ -1,0 +1,46 @@
+// engine.cuh -- one simulation context on the GPU: device state, the step
+// sequence of Time_evolution_hydro (sp_3d_ns.cxx:24-186) and its phases.
+#pragma once
+#include <string>
+
+#include "common.cuh"
+#include "fft.cuh"
+#include "particles.cuh"
+
+namespace icep {
+
+struct EngineBase {
+  virtual ~EngineBase() {}
+  std::string err;
+  virtual int init_state() = 0;
+  virtual int step(int n) = 0;
+  virtual int get_field(int id, double *host) = 0;
+  virtual int set_field(int id, const double *host) = 0;
+  virtual int get_particles(icep_particle *h) = 0;
+  virtual int set_particles(const icep_particle *h) = 0;
+  virtual int get_uk_dc(double *v) = 0;
+  virtual int set_uk_dc(const double *v) = 0;
+  virtual int fft_host(double *a, bool forward) = 0;
+  virtual int call(int fn) = 0;
+  virtual int apply_A_host(const double *x, double *y) = 0;
+  virtual int lj_pairs(int *pairs, int max_pairs, int *n) = 0;
+  virtual int sync() = 0;
+  virtual cudaStream_t stream() const = 0;
+  int ts = 0;
+  double time = 0.0;
+  int last_iters = 0;
+  double last_error = 0.0;
+  long matvecs = 0;
+};
+
+EngineBase *make_engine(const icep_params &p, const icep_particle *parts, int np, int *status, std::string &err);
+
+// ids of Engine::call (same numbering as the oracle's ko_call)
+enum CallId {
+  C_ZETA_K2U_K = 1, C_U_K2ZETA_K, C_U2ADVECTION_K, C_SOLENOIDAL_U, C_NS_SLAVED_EULER,
+  C_MAKE_PHI_SUM, C_MAKE_U_SUM, C_F_HYDRO, C_LJ, C_POS_EULER, C_POS_AB2, C_VEL_EULER,
+  C_VEL_AB2, C_DIELECTRIC_FIELD, C_BUILD_RHS, C_SOLVE_POTENTIAL, C_MAXWELL, C_NSSOLUTE_EULER,
+  C_SURFACE_NORMAL, C_F_PARTICLE_SOLE, C_TRUNCATE, C_CHARGE_FIELD, C_INIT_ION, C_ZETA_K2U
+};
+
+}  // namespace icep

@@ -1,0 +1,45 @@
+// fft.cuh -- 3D real FFTs on the reference's padded layout.
+//
+// Forward (A2a_k, fft_wrapper.h:681-693): kernel exp(-i k.r), unnormalised.
+// Inverse (A_k2a, fft_wrapper.h:704-718): 1/N-normalised, with the
+// reference's treatment of the kz = 0 and kz = NZ/2 planes (Ooura's
+// rdft3dsort reads half of each plane and implies the rest by Hermitian
+// symmetry), reproduced by a Hermitian completion of those planes.
+//
+// Decomposition: z rows (real <-> half complex through an NZ/2-point complex
+// FFT), then complex pencils along y and x, each pencil staged in shared
+// memory and transformed by a Stockham radix-2 sweep.
+#pragma once
+#include "common.cuh"
+
+namespace icep {
+
+template <typename R>
+struct FFTPlan {
+  Grid g;
+  cplx<R> *tw_x = nullptr;    // exp(-2 pi i m / NX), m < NX
+  cplx<R> *tw_y = nullptr;    // exp(-2 pi i m / NY)
+  cplx<R> *tw_z = nullptr;    // exp(-2 pi i m / (NZ/2))
+  cplx<R> *tw_post = nullptr; // exp(-2 pi i k / NZ), k <= NZ/2
+};
+
+template <typename R>
+int fft_plan_init(FFTPlan<R> &p, const Grid &g);
+template <typename R>
+void fft_plan_free(FFTPlan<R> &p);
+
+// In-place batched transforms of fb.n fields (device pointers).
+template <typename R>
+void fft_r2c(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s);
+template <typename R>
+void fft_c2r(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s);
+
+template <typename R>
+inline FieldBatch<R> batch(R *a, R *b = nullptr, R *c = nullptr, R *d = nullptr, R *e = nullptr) {
+  FieldBatch<R> fb;
+  fb.p[0] = a; fb.p[1] = b; fb.p[2] = c; fb.p[3] = d; fb.p[4] = e;
+  fb.n = e ? 5 : d ? 4 : c ? 3 : b ? 2 : 1;
+  return fb;
+}
+
+}  // namespace icep

@@ -1,0 +1,607 @@
+// fields.cu -- grid-field kernels (see fields.cuh for the reference mapping).
+#include "fields.cuh"
+
+namespace icep {
+
+namespace {
+
+constexpr int TPB = 256;
+
+struct Mode {
+  int i, j, kz;
+  long im;  // index of the real part
+};
+
+// Grids hold at most 2^24 points, so 32-bit index arithmetic suffices.
+__device__ __forceinline__ bool mode_of(const Grid &g, long tl, Mode &m) {
+  if (tl >= g.nmodes()) return false;
+  const unsigned t = (unsigned)tl;
+  const unsigned plane = (unsigned)g.ny * (unsigned)g.hnz;
+  m.i = (int)(t / plane);
+  const unsigned r = t - (unsigned)m.i * plane;
+  m.j = (int)(r / (unsigned)g.hnz);
+  m.kz = (int)(r - (unsigned)m.j * (unsigned)g.hnz);
+  m.im = gidx(g, m.i, m.j, 2 * m.kz);
+  return true;
+}
+
+struct Pt {
+  int i, j, k;
+  long im;
+};
+
+__device__ __forceinline__ bool pt_of(const Grid &g, long tl, Pt &p) {
+  if (tl >= g.nreal()) return false;
+  const unsigned t = (unsigned)tl;
+  const unsigned plane = (unsigned)g.ny * (unsigned)g.nz;
+  p.i = (int)(t / plane);
+  const unsigned r = t - (unsigned)p.i * plane;
+  p.j = (int)(r / (unsigned)g.nz);
+  p.k = (int)(r - (unsigned)p.j * (unsigned)g.nz);
+  p.im = gidx(g, p.i, p.j, p.k);
+  return true;
+}
+
+__device__ __forceinline__ long wrapi(const Grid &g, int i, int j, int k) {
+  i = (i + g.nx) % g.nx;
+  j = (j + g.ny) % g.ny;
+  k = (k + g.nz) % g.nz;
+  return gidx(g, i, j, k);
+}
+
+template <typename R>
+__device__ __forceinline__ void kvec(const Grid &g, const Mode &m, R *k) {
+  k[0] = (R)g.wave[0] * (R)kx_of(g, m.i);
+  k[1] = (R)g.wave[1] * (R)ky_of(g, m.j);
+  k[2] = (R)g.wave[2] * (R)m.kz;
+}
+
+template <typename R>
+__device__ __forceinline__ R k2_of(const R *k) { return k[0] * k[0] + k[1] * k[1] + k[2] * k[2]; }
+
+__device__ __forceinline__ void sincos_t(double a, double *s, double *c) { sincos(a, s, c); }
+__device__ __forceinline__ void sincos_t(float a, float *s, float *c) { sincosf(a, s, c); }
+__device__ __forceinline__ double exp_t(double a) { return exp(a); }
+__device__ __forceinline__ float exp_t(float a) { return expf(a); }
+
+#define TID ((long)blockIdx.x * blockDim.x + threadIdx.x)
+
+// ---------------------------------------------------------------- k-space
+template <typename R>
+__global__ void k_truncate(FieldBatch<R> fb, Grid g) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  if (in_two_third(g, m.i, m.j, m.kz)) return;
+  R *a = fb.p[blockIdx.y];
+  a[m.im] = R(0);
+  a[m.im + 1] = R(0);
+}
+
+template <typename R>
+__global__ void k_zeta_k2u_k(Grid g, const R *z0, const R *z1, const double *ukdc, R *u0, R *u1, R *u2) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  const int KX = kx_of(g, m.i), KY = ky_of(g, m.j);
+  R kx = (R)g.wave[0] * (R)KX, ky = (R)g.wave[1] * (R)KY, kz = (R)g.wave[2] * (R)m.kz;
+  const R k2 = kx * kx + ky * ky + kz * kz;
+  const R ik2 = (k2 > R(0)) ? R(1) / k2 : R(0);
+  const R a_r = z0[m.im], a_i = z0[m.im + 1];
+  const R b_r = z1[m.im], b_i = z1[m.im + 1];
+  R wr0, wi0, wr1, wi1, wr2, wi2;
+  if (KX != 0) {
+    const R ikx = R(1) / kx;
+    wr0 = -ikx * (ky * a_r + kz * b_r);
+    wi0 = -ikx * (ky * a_i + kz * b_i);
+    wr1 = a_r; wi1 = a_i;
+    wr2 = b_r; wi2 = b_i;
+  } else if (KY != 0) {
+    const R r = -(kz / ky);
+    wr0 = b_r; wi0 = b_i;
+    wr1 = r * a_r; wi1 = r * a_i;
+    wr2 = a_r; wi2 = a_i;
+  } else {
+    wr0 = a_r; wi0 = a_i;
+    wr1 = b_r; wi1 = b_i;
+    wr2 = R(0); wi2 = R(0);
+  }
+  kx *= ik2; ky *= ik2; kz *= ik2;
+  R v0r = -(ky * wi2 - kz * wi1), v0i = (ky * wr2 - kz * wr1);
+  R v1r = -(kz * wi0 - kx * wi2), v1i = (kz * wr0 - kx * wr2);
+  R v2r = -(kx * wi1 - ky * wi0), v2i = (kx * wr1 - ky * wr0);
+  if (m.im == 0) {
+    v0r = (R)ukdc[0]; v1r = (R)ukdc[1]; v2r = (R)ukdc[2];
+  }
+  u0[m.im] = v0r; u0[m.im + 1] = v0i;
+  u1[m.im] = v1r; u1[m.im + 1] = v1i;
+  u2[m.im] = v2r; u2[m.im + 1] = v2i;
+}
+
+template <typename R>
+__global__ void k_u_k2zeta_k(Grid g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *ukdc) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R a0r = u0[m.im], a0i = u0[m.im + 1];
+  const R a1r = u1[m.im], a1i = u1[m.im + 1];
+  const R a2r = u2[m.im], a2i = u2[m.im + 1];
+  R wr[3], wi[3];
+  wr[0] = -(k[1] * a2i - k[2] * a1i); wi[0] = (k[1] * a2r - k[2] * a1r);
+  wr[1] = -(k[2] * a0i - k[0] * a2i); wi[1] = (k[2] * a0r - k[0] * a2r);
+  wr[2] = -(k[0] * a1i - k[1] * a0i); wi[2] = (k[0] * a1r - k[1] * a0r);
+  int a, b;
+  if (kx_of(g, m.i) != 0) { a = 1; b = 2; }
+  else if (ky_of(g, m.j) != 0) { a = 2; b = 0; }
+  else { a = 0; b = 1; }
+  z0[m.im] = wr[a]; z0[m.im + 1] = wi[a];
+  z1[m.im] = wr[b]; z1[m.im + 1] = wi[b];
+  if (m.im == 0) {
+    ukdc[0] = a0r; ukdc[1] = a1r; ukdc[2] = a2r;
+  }
+}
+
+template <typename R>
+__global__ void k_advection_combine(Grid g, R *u0, R *u1, R *u2, R *a0, R *a1) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R k1 = k[0], k2 = k[1], k3 = k[2];
+  const R k1k2 = k1 * k2, k2k3 = k2 * k3, k3k1 = k3 * k1;
+  int sa, sb;
+  if (kx_of(g, m.i) != 0) { sa = 1; sb = 2; }
+  else if (ky_of(g, m.j) != 0) { sa = 2; sb = 0; }
+  else { sa = 0; sb = 1; }
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const long im = m.im + c;
+    const R u2u3 = u0[im], u3u1 = u1[im], u1u2 = u2[im];
+    const R u22_u32 = a0[im], u32_u12 = a1[im];
+    const R u12_u22 = -u32_u12 - u22_u32;
+    R o[3];
+    o[0] = -(k2k3 * u22_u32 + (k3 - k2) * (k3 + k2) * u2u3 + k3k1 * u1u2 - k1k2 * u3u1);
+    o[1] = -(k3k1 * u32_u12 + (k1 - k3) * (k1 + k3) * u3u1 + k1k2 * u2u3 - k2k3 * u1u2);
+    o[2] = -(k1k2 * u12_u22 + (k2 - k1) * (k2 + k1) * u1u2 + k2k3 * u3u1 - k3k1 * u2u3);
+    u0[im] = o[0]; u1[im] = o[1]; u2[im] = o[2];
+    a0[im] = o[sa];
+    a1[im] = o[sb];
+  }
+}
+
+template <typename R>
+__global__ void k_ns_slaved(Grid g, R *z0, R *z1, const R *a0, const R *a1, double nu, double dt) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  if (!in_two_third(g, m.i, m.j, m.kz)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R k2 = k2_of(k);
+  const R ik2 = (k2 > R(0)) ? R(1) / k2 : R(0);
+  const R f = exp_t((R)(-nu * dt) * k2) - R(1);
+  const R inu = (R)(1. / nu);
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const long im = m.im + c;
+    const R x0 = z0[im], x1 = z1[im];
+    z0[im] = x0 + f * (x0 - inu * ik2 * a0[im]);
+    z1[im] = x1 + f * (x1 - inu * ik2 * a1[im]);
+  }
+}
+
+template <typename R>
+__global__ void k_solenoidal(Grid g, R *u0, R *u1, R *u2) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R k2 = k2_of(k);
+  const R ik2 = (k2 > R(0)) ? R(1) / k2 : R(0);
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const long im = m.im + c;
+    const R a = u0[im], b = u1[im], d = u2[im];
+    const R r = ik2 * (a * k[0] + b * k[1] + d * k[2]);
+    u0[im] = a - r * k[0];
+    u1[im] = b - r * k[1];
+    u2[im] = d - r * k[2];
+  }
+}
+
+template <typename R>
+__global__ void k_grad(Grid g, const R *a, R *d0, R *d1, R *d2, R scale, int shift, const double *e_ext_n) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R re = scale * a[m.im], im = scale * a[m.im + 1];
+  const R hdx = (R)(0.5 * g.dx);
+  R *d[3] = {d0, d1, d2};
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    R gr = -k[c] * im, gi = k[c] * re;
+    if (shift) {
+      R sn, cs;
+      sincos_t(hdx * k[c], &sn, &cs);
+      const R tr = gr * cs - gi * sn, ti = gr * sn + gi * cs;
+      gr = tr;
+      gi = ti;
+    }
+    if (e_ext_n && m.im == 0) gr -= (R)e_ext_n[c];
+    d[c][m.im] = gr;
+    d[c][m.im + 1] = gi;
+  }
+}
+
+template <typename R>
+__global__ void k_div(Grid g, const R *u0, const R *u1, const R *u2, R *div, int shift) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R *u[3] = {u0, u1, u2};
+  R sr = R(0), si = R(0);
+  if (!shift) {
+    R a = R(0), b = R(0);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      a += k[c] * u[c][m.im + 1];
+      b += k[c] * u[c][m.im];
+    }
+    div[m.im] = -a;
+    div[m.im + 1] = b;
+    return;
+  }
+  const R hdx = (R)(0.5 * g.dx);
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    R sn, cs;
+    sincos_t(hdx * k[c], &sn, &cs);
+    const R ksr = k[c] * cs, ksi = -k[c] * sn;
+    const R ur = u[c][m.im], ui = u[c][m.im + 1];
+    sr += ur * ksr - ui * ksi;
+    si += ur * ksi + ui * ksr;
+  }
+  div[m.im] = -si;
+  div[m.im + 1] = sr;
+}
+
+template <typename R>
+__global__ void k_euler(Grid g, R *z0, R *z1, R *r0, R *r1, R *c0, R *c1, const R *cr0, const R *cr1, double nu,
+                        double dt) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  if (!in_two_third(g, m.i, m.j, m.kz)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R k2 = k2_of(k);
+  const R nuk2 = (R)nu * k2, rdt = (R)dt;
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const long im = m.im + c;
+    const R q0 = r0[im] + -(nuk2 * z0[im]);
+    const R q1 = r1[im] + -(nuk2 * z1[im]);
+    r0[im] = q0;
+    r1[im] = q1;
+    z0[im] = z0[im] + rdt * q0;
+    z1[im] = z1[im] + rdt * q1;
+    c0[im] = c0[im] + rdt * cr0[im];
+    c1[im] = c1[im] + rdt * cr1[im];
+  }
+}
+
+template <typename R>
+__global__ void k_inv_laplace(Grid g, R *a, R ieps) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R k2 = k2_of(k);
+  const R f = (k2 > R(0)) ? -ieps / k2 : R(0);
+  a[m.im] *= f;
+  a[m.im + 1] *= f;
+}
+
+template <typename R>
+__global__ void k_scale_copy(long n, const R *x, R *y, R a) {
+  const long t = TID;
+  if (t < n) y[t] = a * x[t];
+}
+
+// ------------------------------------------------------------ real space
+template <typename R>
+__global__ void k_adv_products(Grid g, R *u0, R *u1, R *u2, R *a0, R *a1) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R x = u0[p.im], y = u1[p.im], z = u2[p.im];
+  u0[p.im] = y * z;
+  u1[p.im] = z * x;
+  u2[p.im] = x * y;
+  a0[p.im] = (y - z) * (y + z);
+  a1[p.im] = (z - x) * (z + x);
+}
+
+template <typename R>
+__global__ void k_phi_clip(Grid g, const R *phs, R *phi) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R v = phs[p.im];
+  phi[p.im] = (v < R(1)) ? v : R(1);
+}
+
+template <typename R>
+struct V3 {
+  R *p[3];
+};
+
+template <typename R>
+__global__ void k_f_nonsole(Grid g, V3<R> f, V3<R> up, const R *phi, V3<R> u) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R ph = phi[p.im];
+#pragma unroll
+  for (int d = 0; d < 3; d++) f.p[d][p.im] = up.p[d][p.im] - ph * u.p[d][p.im];
+}
+
+template <typename R>
+__global__ void k_add_vec(Grid g, V3<R> u, V3<R> f, R a) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+#pragma unroll
+  for (int d = 0; d < 3; d++) u.p[d][p.im] += f.p[d][p.im] * a;
+}
+
+template <typename R>
+__global__ void k_eps_from_profile(Grid g, R *eps, const R *phis, const R *epsw, double ef, double ep, double dc) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  if (epsw) eps[p.im] = (R)(ef * dc) + (R)dc * epsw[p.im];
+  else eps[p.im] = (R)(ef * dc) + (R)((ep - ef) * dc) * phis[p.im];
+}
+
+template <typename R>
+__global__ void k_charge_add(Grid g, R *rho, const R *c, const R *phi, double ze, int first) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R v = (R)ze * c[p.im] * (R(1) - phi[p.im]);
+  rho[p.im] = first ? v : rho[p.im] + v;
+}
+
+template <typename R>
+__global__ void k_eps_face_mul(Grid g, R *w0, R *w1, R *w2, const R *eps) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R e0 = eps[p.im];
+  w0[p.im] *= R(0.5) * (eps[wrapi(g, p.i + 1, p.j, p.k)] + e0);
+  w1[p.im] *= R(0.5) * (eps[wrapi(g, p.i, p.j + 1, p.k)] + e0);
+  w2[p.im] *= R(0.5) * (eps[wrapi(g, p.i, p.j, p.k + 1)] + e0);
+}
+
+template <typename R>
+__global__ void k_eps_face_E(Grid g, R *w0, R *w1, R *w2, const R *eps, double e0, double e1, double e2) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R s0 = R(0.5) * eps[p.im];
+  w0[p.im] = (R(0.5) * eps[wrapi(g, p.i + 1, p.j, p.k)] + s0) * (R)e0;
+  w1[p.im] = (R(0.5) * eps[wrapi(g, p.i, p.j + 1, p.k)] + s0) * (R)e1;
+  w2[p.im] = (R(0.5) * eps[wrapi(g, p.i, p.j, p.k + 1)] + s0) * (R)e2;
+}
+
+template <typename R>
+__global__ void k_axpby_real(Grid g, const R *x, R *y, R a, R b) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  y[p.im] = a * x[p.im] + b * y[p.im];
+}
+
+template <typename R>
+__global__ void k_interp_normal(Grid g, V3<R> out, V3<R> in) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  out.p[0][p.im] = R(0.5) * in.p[0][p.im] + R(0.5) * in.p[0][wrapi(g, p.i - 1, p.j, p.k)];
+  out.p[1][p.im] = R(0.5) * in.p[1][p.im] + R(0.5) * in.p[1][wrapi(g, p.i, p.j - 1, p.k)];
+  out.p[2][p.im] = R(0.5) * in.p[2][p.im] + R(0.5) * in.p[2][wrapi(g, p.i, p.j, p.k - 1)];
+}
+
+template <typename R>
+__global__ void k_maxwell_e2(Grid g, const R *f0, const R *f1, const R *f2, R *w1, double e0, double e1, double e2,
+                             int ext) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  R fw0 = -f0[p.im], fw1 = -f1[p.im], fw2 = -f2[p.im];
+  R bw0 = -f0[wrapi(g, p.i - 1, p.j, p.k)];
+  R bw1 = -f1[wrapi(g, p.i, p.j - 1, p.k)];
+  R bw2 = -f2[wrapi(g, p.i, p.j, p.k - 1)];
+  if (ext) {
+    fw0 += (R)e0; fw1 += (R)e1; fw2 += (R)e2;
+    bw0 += (R)e0; bw1 += (R)e1; bw2 += (R)e2;
+  }
+  const R a = (fw0 + bw0) / R(2), b = (fw1 + bw1) / R(2), c = (fw2 + bw2) / R(2);
+  w1[p.im] = a * a + b * b + c * c;
+}
+
+template <typename R>
+__global__ void k_maxwell_face(Grid g, V3<R> force, const R *rho, const R *w1, V3<R> ge, double e0, double e1,
+                               double e2, int ext) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R E[3] = {(R)e0, (R)e1, (R)e2};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const long ip = wrapi(g, p.i + (d == 0), p.j + (d == 1), p.k + (d == 2));
+    R efw = -force.p[d][p.im];
+    if (ext) efw += E[d];
+    const R rf = R(0.5) * rho[ip] + R(0.5) * rho[p.im];
+    const R e2v = R(0.5) * w1[p.im] + R(0.5) * w1[ip];
+    force.p[d][p.im] = rf * efw - e2v * ge.p[d][p.im] / R(2);
+  }
+}
+
+template <typename R>
+__global__ void k_np_flux_electric(Grid g, V3<R> flux, const R *c, V3<R> gp, double L_ze) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R cc = c[p.im], lz = (R)L_ze;
+#pragma unroll
+  for (int d = 0; d < 3; d++) flux.p[d][p.im] = flux.p[d][p.im] + cc * (gp.p[d][p.im] * lz);
+}
+
+template <typename R>
+__global__ void k_np_imperm(Grid g, V3<R> flux, V3<R> sn) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R n0 = sn.p[0][p.im], n1 = sn.p[1][p.im], n2 = sn.p[2][p.im];
+  const R nn = n0 * n0 + n1 * n1 + n2 * n2;
+  if (!(nn > R(0))) return;
+  const R f0 = flux.p[0][p.im], f1 = flux.p[1][p.im], f2 = flux.p[2][p.im];
+  const R dd = (f0 * n0 + f1 * n1 + f2 * n2) / nn;
+  flux.p[0][p.im] = f0 - n0 * dd;
+  flux.p[1][p.im] = f1 - n1 * dd;
+  flux.p[2][p.im] = f2 - n2 * dd;
+}
+
+template <typename R>
+__global__ void k_np_flux_adv(Grid g, V3<R> flux, const R *c, V3<R> u) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R cc = c[p.im];
+#pragma unroll
+  for (int d = 0; d < 3; d++) flux.p[d][p.im] += cc * -u.p[d][p.im];
+}
+
+template <typename R>
+__global__ void k_fill_real(Grid g, R *a, R v) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  a[p.im] = v;
+}
+
+template <typename R>
+V3<R> v3(R *const *p) {
+  V3<R> v;
+  v.p[0] = p[0]; v.p[1] = p[1]; v.p[2] = p[2];
+  return v;
+}
+
+inline unsigned nblk_modes(const Grid &g) { return div_up(g.nmodes(), TPB); }
+inline unsigned nblk_real(const Grid &g) { return div_up(g.nreal(), TPB); }
+
+}  // namespace
+
+template <typename R> void truncate_23(const Grid &g, const FieldBatch<R> &fb, cudaStream_t s) {
+  k_truncate<R><<<dim3(nblk_modes(g), fb.n), TPB, 0, s>>>(fb, g);
+}
+template <typename R> void zeta_k2u_k(const Grid &g, const R *z0, const R *z1, const double *uk_dc, R *u0, R *u1, R *u2, cudaStream_t s) {
+  k_zeta_k2u_k<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, uk_dc, u0, u1, u2);
+}
+template <typename R> void u_k2zeta_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *uk_dc, cudaStream_t s) {
+  k_u_k2zeta_k<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, z0, z1, uk_dc);
+}
+template <typename R> void advection_combine(const Grid &g, R *u0, R *u1, R *u2, R *a0, R *a1, cudaStream_t s) {
+  k_advection_combine<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, a0, a1);
+}
+template <typename R> void ns_slaved_update(const Grid &g, R *z0, R *z1, const R *a0, const R *a1, double nu, double dt, cudaStream_t s) {
+  k_ns_slaved<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, a0, a1, nu, dt);
+}
+template <typename R> void solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s) {
+  k_solenoidal<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2);
+}
+template <typename R> void grad_k(const Grid &g, const R *a, R *d0, R *d1, R *d2, R scale, bool shift, const double *e_ext_n, cudaStream_t s) {
+  k_grad<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, d0, d1, d2, scale, shift ? 1 : 0, e_ext_n);
+}
+template <typename R> void div_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *div, bool shift, cudaStream_t s) {
+  k_div<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, div, shift ? 1 : 0);
+}
+template <typename R> void euler_update(const Grid &g, R *z0, R *z1, R *r0, R *r1, R *c0, R *c1, const R *cr0, const R *cr1, double nu, double dt, cudaStream_t s) {
+  k_euler<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, r0, r1, c0, c1, cr0, cr1, nu, dt);
+}
+template <typename R> void inv_laplace_k(const Grid &g, R *a, double eps_ref, cudaStream_t s) {
+  k_inv_laplace<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, (R)(1.0 / eps_ref));
+}
+template <typename R> void scale_copy(const Grid &g, const R *x, R *y, R a, cudaStream_t s) {
+  k_scale_copy<R><<<div_up(g.nf(), TPB), TPB, 0, s>>>(g.nf(), x, y, a);
+}
+template <typename R> void advection_products(const Grid &g, R *u0, R *u1, R *u2, R *a0, R *a1, cudaStream_t s) {
+  k_adv_products<R><<<nblk_real(g), TPB, 0, s>>>(g, u0, u1, u2, a0, a1);
+}
+template <typename R> void phi_clip(const Grid &g, const R *phs, R *phi, cudaStream_t s) {
+  k_phi_clip<R><<<nblk_real(g), TPB, 0, s>>>(g, phs, phi);
+}
+template <typename R> void f_nonsole(const Grid &g, R *const *f, R *const *up, const R *phi, R *const *u, cudaStream_t s) {
+  k_f_nonsole<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(f), v3(up), phi, v3(u));
+}
+template <typename R> void add_vec(const Grid &g, R *const *u, R *const *f, R a, cudaStream_t s) {
+  k_add_vec<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(u), v3(f), a);
+}
+template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_sin, const R *eps_w, double ef, double ep, double dc, cudaStream_t s) {
+  k_eps_from_profile<R><<<nblk_real(g), TPB, 0, s>>>(g, eps, phi_sin, eps_w, ef, ep, dc);
+}
+template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s) {
+  k_charge_add<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c, phi, ze, first ? 1 : 0);
+}
+template <typename R> void eps_face_mul(const Grid &g, R *w0, R *w1, R *w2, const R *eps, cudaStream_t s) {
+  k_eps_face_mul<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps);
+}
+template <typename R> void eps_face_E(const Grid &g, R *w0, R *w1, R *w2, const R *eps, double e0, double e1, double e2, cudaStream_t s) {
+  k_eps_face_E<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps, e0, e1, e2);
+}
+template <typename R> void axpby_real(const Grid &g, const R *x, R *y, R a, R b, cudaStream_t s) {
+  k_axpby_real<R><<<nblk_real(g), TPB, 0, s>>>(g, x, y, a, b);
+}
+template <typename R> void interp_normal(const Grid &g, R *const *out, R *const *in, cudaStream_t s) {
+  k_interp_normal<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(out), v3(in));
+}
+template <typename R> void maxwell_e2(const Grid &g, const R *f0, const R *f1, const R *f2, R *w1, double e0, double e1, double e2, int ext, cudaStream_t s) {
+  k_maxwell_e2<R><<<nblk_real(g), TPB, 0, s>>>(g, f0, f1, f2, w1, e0, e1, e2, ext);
+}
+template <typename R> void maxwell_face(const Grid &g, R *const *force, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s) {
+  k_maxwell_face<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(force), rho, w1, v3(ge), e0, e1, e2, ext);
+}
+template <typename R> void np_flux_electric(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, cudaStream_t s) {
+  k_np_flux_electric<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(gp), L_ze);
+}
+template <typename R> void np_impermeability(const Grid &g, R *const *flux, R *const *sn, cudaStream_t s) {
+  k_np_imperm<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), v3(sn));
+}
+template <typename R> void np_flux_advection(const Grid &g, R *const *flux, const R *c, R *const *u, cudaStream_t s) {
+  k_np_flux_adv<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(u));
+}
+template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s) {
+  k_fill_real<R><<<nblk_real(g), TPB, 0, s>>>(g, a, v);
+}
+
+#define ICEP_INST(R)                                                                                                   \
+  template void truncate_23<R>(const Grid &, const FieldBatch<R> &, cudaStream_t);                                    \
+  template void zeta_k2u_k<R>(const Grid &, const R *, const R *, const double *, R *, R *, R *, cudaStream_t);        \
+  template void u_k2zeta_k<R>(const Grid &, const R *, const R *, const R *, R *, R *, double *, cudaStream_t);        \
+  template void advection_combine<R>(const Grid &, R *, R *, R *, R *, R *, cudaStream_t);                             \
+  template void ns_slaved_update<R>(const Grid &, R *, R *, const R *, const R *, double, double, cudaStream_t);       \
+  template void solenoidal_uk<R>(const Grid &, R *, R *, R *, cudaStream_t);                                           \
+  template void grad_k<R>(const Grid &, const R *, R *, R *, R *, R, bool, const double *, cudaStream_t);              \
+  template void div_k<R>(const Grid &, const R *, const R *, const R *, R *, bool, cudaStream_t);                      \
+  template void euler_update<R>(const Grid &, R *, R *, R *, R *, R *, R *, const R *, const R *, double, double,      \
+                                cudaStream_t);                                                                         \
+  template void scale_copy<R>(const Grid &, const R *, R *, R, cudaStream_t);                                          \
+  template void inv_laplace_k<R>(const Grid &, R *, double, cudaStream_t);                                             \
+  template void advection_products<R>(const Grid &, R *, R *, R *, R *, R *, cudaStream_t);                            \
+  template void phi_clip<R>(const Grid &, const R *, R *, cudaStream_t);                                               \
+  template void f_nonsole<R>(const Grid &, R *const *, R *const *, const R *, R *const *, cudaStream_t);               \
+  template void add_vec<R>(const Grid &, R *const *, R *const *, R, cudaStream_t);                                     \
+  template void eps_from_profile<R>(const Grid &, R *, const R *, const R *, double, double, double, cudaStream_t);    \
+  template void charge_add<R>(const Grid &, R *, const R *, const R *, double, bool, cudaStream_t);                    \
+  template void eps_face_mul<R>(const Grid &, R *, R *, R *, const R *, cudaStream_t);                                 \
+  template void eps_face_E<R>(const Grid &, R *, R *, R *, const R *, double, double, double, cudaStream_t);           \
+  template void axpby_real<R>(const Grid &, const R *, R *, R, R, cudaStream_t);                                       \
+  template void interp_normal<R>(const Grid &, R *const *, R *const *, cudaStream_t);                                  \
+  template void maxwell_e2<R>(const Grid &, const R *, const R *, const R *, R *, double, double, double, int,         \
+                              cudaStream_t);                                                                           \
+  template void maxwell_face<R>(const Grid &, R *const *, const R *, const R *, R *const *, double, double, double,    \
+                                int, cudaStream_t);                                                                    \
+  template void np_flux_electric<R>(const Grid &, R *const *, const R *, R *const *, double, cudaStream_t);            \
+  template void np_impermeability<R>(const Grid &, R *const *, R *const *, cudaStream_t);                              \
+  template void np_flux_advection<R>(const Grid &, R *const *, const R *, R *const *, cudaStream_t);                   \
+  template void fill_real<R>(const Grid &, R *, R, cudaStream_t);
+
+ICEP_INST(double)
+ICEP_INST(float)
+
+}  // namespace icep

@@ -1,0 +1,157 @@
+// icep_abi.cu -- the extern "C" entry points declared in include/icep_gb300.h.
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/icep_gb300.h"
+#include "engine.cuh"
+
+struct icep_ctx {
+  icep::EngineBase *e = nullptr;
+  std::string err;
+};
+
+namespace {
+int wrap(icep_ctx *c, int st) {
+  if (st != ICEP_OK && c && c->e) c->err = c->e->err;
+  return st;
+}
+bool ok(icep_ctx *c) { return c && c->e; }
+}  // namespace
+
+extern "C" {
+
+icep_ctx *icep_create(const icep_params *params, const icep_particle *particles, int n_particles, int *status) {
+  if (!params || (n_particles > 0 && !particles)) {
+    if (status) *status = ICEP_ERR_ARG;
+    return nullptr;
+  }
+  std::string err;
+  int st = ICEP_OK;
+  icep::EngineBase *e = icep::make_engine(*params, particles, n_particles, &st, err);
+  if (status) *status = st;
+  if (!e) {
+    fprintf(stderr, "icep_create: %s\n", err.c_str());
+    return nullptr;
+  }
+  icep_ctx *c = new icep_ctx();
+  c->e = e;
+  return c;
+}
+
+void icep_destroy(icep_ctx *ctx) {
+  if (!ctx) return;
+  delete ctx->e;
+  delete ctx;
+}
+
+const char *icep_last_error(const icep_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int icep_init_state(icep_ctx *c) { return ok(c) ? wrap(c, c->e->init_state()) : ICEP_ERR_ARG; }
+int icep_step(icep_ctx *c, int n) {
+  if (!ok(c) || n < 0) return ICEP_ERR_ARG;
+  return wrap(c, c->e->step(n));
+}
+
+int icep_get_field(icep_ctx *c, int field, double *host) {
+  if (!ok(c) || !host) return ICEP_ERR_ARG;
+  return wrap(c, c->e->get_field(field, host));
+}
+int icep_set_field(icep_ctx *c, int field, const double *host) {
+  if (!ok(c) || !host) return ICEP_ERR_ARG;
+  return wrap(c, c->e->set_field(field, host));
+}
+int icep_get_particles(icep_ctx *c, icep_particle *h) {
+  if (!ok(c) || !h) return ICEP_ERR_ARG;
+  return wrap(c, c->e->get_particles(h));
+}
+int icep_set_particles(icep_ctx *c, const icep_particle *h) {
+  if (!ok(c) || !h) return ICEP_ERR_ARG;
+  return wrap(c, c->e->set_particles(h));
+}
+int icep_get_uk_dc(icep_ctx *c, double *v) { return ok(c) && v ? wrap(c, c->e->get_uk_dc(v)) : ICEP_ERR_ARG; }
+int icep_set_uk_dc(icep_ctx *c, const double *v) { return ok(c) && v ? wrap(c, c->e->set_uk_dc(v)) : ICEP_ERR_ARG; }
+int icep_get_time(icep_ctx *c, int *ts, double *time) {
+  if (!ok(c)) return ICEP_ERR_ARG;
+  if (ts) *ts = c->e->ts;
+  if (time) *time = c->e->time;
+  return ICEP_OK;
+}
+int icep_set_time(icep_ctx *c, int ts, double time) {
+  if (!ok(c)) return ICEP_ERR_ARG;
+  c->e->ts = ts;
+  c->e->time = time;
+  return ICEP_OK;
+}
+
+int icep_time_evolution(icep_ctx *c, double *zeta0, double *zeta1, double *uk_dc, double *conc0, double *conc1,
+                        double *potential, icep_particle *particles, int nsteps) {
+  if (!ok(c) || !zeta0 || !zeta1 || !uk_dc || !particles || nsteps < 0) return ICEP_ERR_ARG;
+  int st;
+  icep::EngineBase *e = c->e;
+  if ((st = e->set_field(icep::F_ZETA0, zeta0)) || (st = e->set_field(icep::F_ZETA1, zeta1)) ||
+      (st = e->set_uk_dc(uk_dc)) || (st = e->set_particles(particles)))
+    return wrap(c, st);
+  if (conc0 && (st = e->set_field(icep::F_C0, conc0))) return wrap(c, st);
+  if (conc1 && (st = e->set_field(icep::F_C1, conc1))) return wrap(c, st);
+  if (potential && (st = e->set_field(icep::F_POT, potential))) return wrap(c, st);
+  if ((st = e->step(nsteps))) return wrap(c, st);
+  if ((st = e->get_field(icep::F_ZETA0, zeta0)) || (st = e->get_field(icep::F_ZETA1, zeta1)) ||
+      (st = e->get_uk_dc(uk_dc)) || (st = e->get_particles(particles)))
+    return wrap(c, st);
+  if (conc0 && (st = e->get_field(icep::F_C0, conc0))) return wrap(c, st);
+  if (conc1 && (st = e->get_field(icep::F_C1, conc1))) return wrap(c, st);
+  if (potential && (st = e->get_field(icep::F_POT, potential))) return wrap(c, st);
+  return ICEP_OK;
+}
+
+int icep_A2a_k(icep_ctx *c, double *a) { return ok(c) && a ? wrap(c, c->e->fft_host(a, true)) : ICEP_ERR_ARG; }
+int icep_A_k2a(icep_ctx *c, double *a) { return ok(c) && a ? wrap(c, c->e->fft_host(a, false)) : ICEP_ERR_ARG; }
+
+int icep_NS_solver_slavedEuler(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_NS_SLAVED_EULER)) : ICEP_ERR_ARG; }
+int icep_NSsolute_solver_Euler(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_NSSOLUTE_EULER)) : ICEP_ERR_ARG; }
+int icep_Make_phi_particle_sum(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_MAKE_PHI_SUM)) : ICEP_ERR_ARG; }
+int icep_Make_u_particle_sum(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_MAKE_U_SUM)) : ICEP_ERR_ARG; }
+int icep_Make_surface_normal(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_SURFACE_NORMAL)) : ICEP_ERR_ARG; }
+int icep_Calc_f_hydro_correct_precision(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_F_HYDRO)) : ICEP_ERR_ARG; }
+int icep_Calc_f_Lennard_Jones(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_LJ)) : ICEP_ERR_ARG; }
+int icep_lj_pairs(icep_ctx *c, int *pairs, int max_pairs, int *n_pairs) {
+  if (!ok(c) || !n_pairs || (max_pairs > 0 && !pairs)) return ICEP_ERR_ARG;
+  return wrap(c, c->e->lj_pairs(pairs, max_pairs, n_pairs));
+}
+int icep_MD_solver_position(icep_ctx *c, int ab2) {
+  return ok(c) ? wrap(c, c->e->call(ab2 ? icep::C_POS_AB2 : icep::C_POS_EULER)) : ICEP_ERR_ARG;
+}
+int icep_MD_solver_velocity(icep_ctx *c, int ab2) {
+  return ok(c) ? wrap(c, c->e->call(ab2 ? icep::C_VEL_AB2 : icep::C_VEL_EULER)) : ICEP_ERR_ARG;
+}
+int icep_Make_dielectric_field(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_DIELECTRIC_FIELD)) : ICEP_ERR_ARG; }
+int icep_Conc_k2charge_field(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_CHARGE_FIELD)) : ICEP_ERR_ARG; }
+int icep_Build_rhs(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_BUILD_RHS)) : ICEP_ERR_ARG; }
+int icep_Ax(icep_ctx *c, const double *x, double *ax) {
+  if (!ok(c) || !x || !ax) return ICEP_ERR_ARG;
+  return wrap(c, c->e->apply_A_host(x, ax));
+}
+int icep_Charge_field2potential_dielectric(icep_ctx *c, int *iterations, double *error) {
+  if (!ok(c)) return ICEP_ERR_ARG;
+  int st = wrap(c, c->e->call(icep::C_SOLVE_POTENTIAL));
+  if (iterations) *iterations = c->e->last_iters;
+  if (error) *error = c->e->last_error;
+  return st;
+}
+int icep_Make_Maxwell_force_x_on_fluid(icep_ctx *c) { return ok(c) ? wrap(c, c->e->call(icep::C_MAXWELL)) : ICEP_ERR_ARG; }
+int icep_solver_stats(icep_ctx *c, int *iterations, double *error, long *matvecs) {
+  if (!ok(c)) return ICEP_ERR_ARG;
+  if (iterations) *iterations = c->e->last_iters;
+  if (error) *error = c->e->last_error;
+  if (matvecs) *matvecs = c->e->matvecs;
+  return ICEP_OK;
+}
+void *icep_stream(icep_ctx *c) { return ok(c) ? (void *)c->e->stream() : nullptr; }
+int icep_synchronize(icep_ctx *c) { return ok(c) ? wrap(c, c->e->sync()) : ICEP_ERR_ARG; }
+
+/* generic dispatch used by the Python layer (same numbering as the oracle) */
+int icep_call(icep_ctx *c, int fn) { return ok(c) ? wrap(c, c->e->call(fn)) : ICEP_ERR_ARG; }
+
+}  // extern "C"

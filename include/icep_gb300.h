@@ -1,0 +1,152 @@
+/*
+ * icep_gb300.h -- C-ABI of the GB300 (sm_103a) implementation of the
+ * KAPSEL-ICEP per-timestep hot path.
+ *
+ * One context = one simulation on one GPU, one CUDA stream. All grid fields
+ * and the particle array live in device memory for the lifetime of the
+ * context; the host exchanges them in the reference's own layout
+ * ([NX][NY][NZ_] doubles, icep_types.h). Every call returns 0 on success and
+ * a positive status on failure (ICEP_ERR_*); no call exits the process and no
+ * device code traps (reference: fatal errors call exit(EXIT_FAILURE),
+ * macro.h:206-208).
+ *
+ * The reference seam each entry point replaces is cited as file:line of the
+ * reference project (Takuma6/icep_kapsel).
+ */
+#ifndef ICEP_GB300_H
+#define ICEP_GB300_H
+
+#include "icep_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ICEP_OK 0
+#define ICEP_ERR_ARG 1
+#define ICEP_ERR_CUDA 2
+#define ICEP_ERR_UNSUPPORTED 3
+#define ICEP_ERR_NOT_CONVERGED 4
+#define ICEP_ERR_STATE 5
+
+typedef struct icep_ctx icep_ctx;
+
+/* Field identifiers for icep_get_field / icep_set_field. */
+enum icep_field {
+  ICEP_F_ZETA0 = 0, ICEP_F_ZETA1, ICEP_F_U0, ICEP_F_U1, ICEP_F_U2,
+  ICEP_F_UP0, ICEP_F_UP1, ICEP_F_UP2, ICEP_F_PHI, ICEP_F_PHI_SUM,
+  ICEP_F_F0, ICEP_F_F1, ICEP_F_F2, ICEP_F_POTENTIAL, ICEP_F_EPSILON,
+  ICEP_F_GRAD_EPS0, ICEP_F_GRAD_EPS1, ICEP_F_GRAD_EPS2, ICEP_F_CONC0, ICEP_F_CONC1,
+  ICEP_F_RHO_FREE, ICEP_F_WORK, ICEP_F_SURFACE_NORMAL0, ICEP_F_SURFACE_NORMAL1,
+  ICEP_F_SURFACE_NORMAL2
+};
+
+/*
+ * Context setup. Replaces the parameter derivation and allocation of
+ * Set_global_parameters (input.cxx:286-440), Init_fft (fft_wrapper.cxx:166-199),
+ * Mem_alloc_var (sp_3d_ns.cxx:295-340) and the stencil of Particle_domain
+ * (profile.cxx:25-74). particles: n_particles entries, copied to the device.
+ */
+icep_ctx *icep_create(const icep_params *params, const icep_particle *particles, int n_particles, int *status);
+void icep_destroy(icep_ctx *ctx);
+/* Human-readable text of the last error of this context. */
+const char *icep_last_error(const icep_ctx *ctx);
+
+/*
+ * main()'s initialisation after Init_Particle (sp_3d_ns.cxx:425-457): fluid
+ * at rest with the rigidity force applied, and for Electrolyte +
+ * Dielectric_property ON the uniform salt (Init_rho_ion_dielectric,
+ * operate_electrolyte.cxx:912-979) and the first Poisson solve
+ * (Init_potential_dielectric, operate_dielectric.cxx:574-609).
+ */
+int icep_init_state(icep_ctx *ctx);
+
+/*
+ * nsteps of the time loop body (sp_3d_ns.cxx:524-525): Time_evolution_hydro
+ * (sp_3d_ns.cxx:24-186), the function the reference calls through the
+ * pointer Time_evolution (sp_3d_ns.cxx:10), then jikan.time += dt.
+ */
+int icep_step(icep_ctx *ctx, int nsteps);
+
+/*
+ * Drop-in form of one call of Time_evolution (sp_3d_ns.cxx:10) on host
+ * arrays: zeta (2 fields), uk_dc[3], conc (2 k-space fields, Electrolyte
+ * only, may be NULL), potential (1 real field, Dielectric only, may be NULL)
+ * and the particle array are uploaded, nsteps steps run on the GPU, and the
+ * same arrays are written back.
+ */
+int icep_time_evolution(icep_ctx *ctx, double *zeta0, double *zeta1, double *uk_dc, double *conc0, double *conc1,
+                        double *potential, icep_particle *particles, int nsteps);
+
+/* Field and particle exchange in the reference layout (host pointers). */
+int icep_get_field(icep_ctx *ctx, int field, double *host);
+int icep_set_field(icep_ctx *ctx, int field, const double *host);
+int icep_get_particles(icep_ctx *ctx, icep_particle *host);
+int icep_set_particles(icep_ctx *ctx, const icep_particle *host);
+int icep_get_uk_dc(icep_ctx *ctx, double *uk_dc);
+int icep_set_uk_dc(icep_ctx *ctx, const double *uk_dc);
+int icep_get_time(icep_ctx *ctx, int *ts, double *time);
+int icep_set_time(icep_ctx *ctx, int ts, double time);
+
+/* ---- phase entry points (operate on the context's device state) -------- */
+
+/* A2a_k / A_k2a (fft_wrapper.h:681-723) in place on a host array of
+ * NX*NY*NZ_ doubles. */
+int icep_A2a_k(icep_ctx *ctx, double *a);
+int icep_A_k2a(icep_ctx *ctx, double *a);
+
+/* NS_solver_slavedEuler (fluid_solver.cxx:340-366) on ZETA0/1, uk_dc. */
+int icep_NS_solver_slavedEuler(icep_ctx *ctx);
+/* NSsolute_solver_Euler (fluid_solver.cxx:318-338), Dielectric branch. */
+int icep_NSsolute_solver_Euler(icep_ctx *ctx);
+/* Make_phi_particle_sum (make_phi.cxx:229-275, 519-523): PHI, PHI_SUM. */
+int icep_Make_phi_particle_sum(icep_ctx *ctx);
+/* Make_u_particle_sum (make_phi.cxx:329-370, 532-536): UP0..2 (zeroed first). */
+int icep_Make_u_particle_sum(icep_ctx *ctx);
+/* Make_surface_normal (make_phi.cxx:17-61): SURFACE_NORMAL0..2. */
+int icep_Make_surface_normal(icep_ctx *ctx);
+/* Calc_f_hydro_correct_precision (md_force.cxx:340-449) from U0..2, PHI_SUM. */
+int icep_Calc_f_hydro_correct_precision(icep_ctx *ctx);
+/* Calc_f_Lennard_Jones (md_force.h:81-84 -> md_force.cxx:16-171) into fr
+ * (fr is cleared first). */
+int icep_Calc_f_Lennard_Jones(icep_ctx *ctx);
+/* The neighbour visits of the linked-cell scan: pairs (i, j), i > j, one
+ * entry per visit. *n_pairs receives the total (may exceed max_pairs). */
+int icep_lj_pairs(icep_ctx *ctx, int *pairs, int max_pairs, int *n_pairs);
+/* MD_solver_position_Euler/_AB2 (particle_solver.cxx:39-91) */
+int icep_MD_solver_position(icep_ctx *ctx, int ab2);
+/* MD_solver_velocity_Euler/_AB2_hydro (particle_solver.cxx:109-150, 252-295) */
+int icep_MD_solver_velocity(icep_ctx *ctx, int ab2);
+/* Make_dielectric_field (operate_dielectric.cxx:270-309): EPSILON, phi_sin in WORK. */
+int icep_Make_dielectric_field(icep_ctx *ctx);
+/* Conc_k2charge_field_no_surfase_charge (operate_dielectric.cxx:135-160):
+ * RHO_FREE from CONC0/1 and the profile in WORK. */
+int icep_Conc_k2charge_field(icep_ctx *ctx);
+/* Build_rhs (operate_dielectric.cxx:524-540): WORK from EPSILON, RHO_FREE. */
+int icep_Build_rhs(icep_ctx *ctx);
+/* Ax (operate_dielectric.cxx:485-522) with the context's EPSILON, on
+ * unpadded host vectors of NX*NY*NZ doubles (the MatrixReplacement matvec,
+ * LinearOperator.h:70-82). */
+int icep_Ax(icep_ctx *ctx, const double *x, double *ax);
+/*
+ * Charge_field2potential_dielectric (operate_dielectric.cxx:18-22, bound to
+ * _LO at :592): POTENTIAL from RHO_FREE and EPSILON with the context's solver
+ * (params.solver). iterations / error receive the statistics of the last
+ * solve (error: recursive residual for REF, true relative residual for
+ * SPECTRAL).
+ */
+int icep_Charge_field2potential_dielectric(icep_ctx *ctx, int *iterations, double *error);
+/* Make_Maxwell_force_x_on_fluid (operate_dielectric.cxx:611-764): F0..2. */
+int icep_Make_Maxwell_force_x_on_fluid(icep_ctx *ctx);
+/* Statistics of the last Poisson solve of the context. */
+int icep_solver_stats(icep_ctx *ctx, int *iterations, double *error, long *matvecs);
+/* Stream of the context (cudaStream_t as void*), for callers that order
+ * their own device work after the library's. */
+void *icep_stream(icep_ctx *ctx);
+/* Block until the context's queued work has finished. */
+int icep_synchronize(icep_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

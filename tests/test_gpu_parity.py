@@ -1,0 +1,260 @@
+"""GPU parity: the CUDA path (through the C-ABI) against the reference's golden
+fixtures and the C oracle, FP64 mode.
+
+Tolerances (relative L2 unless stated):
+  deterministic operators (FFT, k-space and real-space kernels, scatters,
+  gathers): 1e-12 -- both sides are FP64, only summation order and FFT
+  rounding differ;
+  anything downstream of a Krylov solve: a small multiple of the solver
+  tolerance, since two BiCGSTAB runs on differently rounded operators
+  diverge at rounding level and are only equal to the tolerance;
+  LJ neighbour visits: bit-exact multisets.
+"""
+import importlib.util
+import os
+
+import numpy as np
+import pytest
+
+import cases
+import pyoracle
+from icep_kapsel_gb300 import abi
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / (nb if nb > 0 else 1.0))
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name + ".npz"))
+
+
+def golden_module():
+    spec = importlib.util.spec_from_file_location("make_golden", os.path.join(GOLD, "make_golden.py"))
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    return mg
+
+
+@pytest.fixture(scope="module")
+def Sim():
+    from icep_kapsel_gb300.build import build
+    build()
+    from icep_kapsel_gb300.runtime import Simulation
+    return Simulation
+
+
+def test_fft16_golden(Sim):
+    g = load("fft16")
+    mg = golden_module()
+    p, parts = mg.small_case()
+    s = Sim(p, parts)
+    a = np.random.default_rng(11).standard_normal((16, 16, 18))
+    assert rel(s.fft_r2c(a), g["r2c"]) < 1e-13
+    assert rel(s.fft_c2r(a)[:, :, :16], g["c2r"]) < 1e-13
+
+
+@pytest.mark.parametrize("n", [32, 64, 128])
+def test_fft_sizes_against_oracle(Sim, n):
+    p, parts = cases.ns_case(n=n, npart=0, motor=False)
+    s = Sim(p, parts)
+    o = pyoracle.Oracle(p, parts)
+    rng = np.random.default_rng(n)
+    a = rng.standard_normal((n, n, n + 2))
+    assert rel(s.fft_r2c(a), o.fft_r2c(a)) < 1e-13
+    # non-Hermitian spectrum (half-plane semantics of the reference's inverse)
+    assert rel(s.fft_c2r(a)[:, :, :n], o.fft_c2r(a)[:, :, :n]) < 1e-13
+    x = a.copy()
+    x[:, :, n:] = 0
+    back = s.fft_c2r(s.fft_r2c(x))
+    assert rel(back[:, :, :n], x[:, :, :n]) < 1e-14
+
+
+def test_ops16_golden(Sim):
+    g = load("ops16")
+    mg = golden_module()
+    p, parts = mg.small_case()
+    o = Sim(p, parts)
+    f = mg.ops16_inputs(p)
+    tol = 1e-12
+    o.set("zeta0", f["zeta0"]); o.set("zeta1", f["zeta1"]); o.set_uk_dc(f["uk_dc"])
+    o.call("zeta_k2u_k")
+    for d in range(3):
+        assert rel(o.get("u%d" % d), g["zeta_k2u_k_u%d" % d]) < tol
+    o.call("u_k2zeta_k")
+    assert rel(o.get("zeta0"), g["u_k2zeta_k_zeta0"]) < tol
+    assert rel(o.get("zeta1"), g["u_k2zeta_k_zeta1"]) < tol
+    assert rel(o.uk_dc(), g["u_k2zeta_k_ukdc"]) < tol
+    for d in range(3):
+        o.set("u%d" % d, f["u%d" % d])
+    o.call("u2advection_k")
+    assert rel(o.get("ns0_0"), g["adv0"]) < tol
+    assert rel(o.get("ns0_1"), g["adv1"]) < tol
+    for d in range(3):
+        o.set("u%d" % d, f["u%d" % d])
+    o.call("solenoidal_u")
+    for d in range(3):
+        assert rel(o.get("u%d" % d)[:, :, :16], g["sol_u%d" % d]) < tol
+    o.call("make_phi_sum")
+    assert rel(o.get("phi")[:, :, :16], g["phi"]) < tol
+    assert rel(o.get("phi_sum")[:, :, :16], g["phi_sum"]) < tol
+    o.call("make_u_sum")
+    for d in range(3):
+        assert rel(o.get("up%d" % d)[:, :, :16], g["up%d" % d]) < tol
+    for d in range(3):
+        o.set("u%d" % d, f["u%d" % d])
+    o.call("f_hydro")
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    assert rel(pa["f_hydro"], g["f_hydro"]) < tol
+    assert rel(pa["torque_hydro"], g["torque_hydro"]) < tol
+    o.call("surface_normal")
+    for d in range(3):
+        assert rel(o.get("sn%d" % d)[:, :, :16], g["sn%d" % d]) < tol
+    o.call("dielectric_field")
+    assert rel(o.get("eps")[:, :, :16], g["eps"]) < tol
+    assert rel(o.get("work")[:, :, :16], g["phi_sin"]) < tol
+    o.call("init_ion")
+    assert rel(o.get("c0"), g["c0_init"]) < tol
+    assert rel(o.get("c1"), g["c1_init"]) < tol
+    o.set("c0", f["c0"]); o.set("c1", f["c1"])
+    o.call("charge_field")
+    assert rel(o.get("rho")[:, :, :16], g["rho"]) < tol
+    o.set("rho", f["rho"])
+    o.call("build_rhs")
+    assert rel(o.get("work")[:, :, :16], g["rhs"]) < tol
+    o.set("rho", f["rho"]); o.set("pot", f["pot"])
+    it, err = o.solve_potential()
+    a = o.get("pot")[:, :, :16]
+    b = g["pot_solved"]
+    assert rel(a - a.mean(), b - b.mean()) < 1e-8
+    assert err < 1e-10
+    o.set("rho", f["rho"]); o.set("pot", f["pot"])
+    o.set("c0", f["c0"]); o.set("c1", f["c0"])
+    o.call("maxwell")
+    for d in range(3):
+        assert rel(o.get("f%d" % d)[:, :, :16], g["maxwell_f%d" % d]) < 1e-7
+    o.set("zeta0", f["zeta0"]); o.set("zeta1", f["zeta1"]); o.set_uk_dc(f["uk_dc"])
+    o.set("c0", f["c0"]); o.set("c1", f["c1"]); o.set("pot", f["pot"])
+    o.call("nssolute_euler")
+    assert rel(o.get("zeta0"), g["np_zeta0"]) < tol
+    assert rel(o.get("zeta1"), g["np_zeta1"]) < tol
+    assert rel(o.get("c0"), g["np_c0"]) < tol
+    assert rel(o.get("c1"), g["np_c1"]) < tol
+    o.set("zeta0", f["zeta0"]); o.set("zeta1", f["zeta1"]); o.set_uk_dc(f["uk_dc"])
+    o.call("ns_slaved_euler")
+    assert rel(o.get("zeta0"), g["ns_zeta0"]) < tol
+    assert rel(o.get("zeta1"), g["ns_zeta1"]) < tol
+
+
+def test_ns32_three_steps_golden(Sim):
+    g = load("ns32")
+    p, parts = cases.ns_case()
+    o = Sim(p, parts)
+    o.init_state()
+    o.step(3)
+    assert rel(o.get("zeta0"), g["zeta0"]) < 1e-11
+    assert rel(o.get("zeta1"), g["zeta1"]) < 1e-11
+    assert rel(o.get("phi")[:, :, :32], g["phi"]) < 1e-13
+    assert rel(o.uk_dc(), g["uk_dc"]) < 1e-11
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    for k in ("x", "v", "omega", "q", "f_hydro_previous"):
+        assert rel(pa[k], g["p_" + k]) < 1e-10, k
+
+
+def test_ns32_hundred_steps_against_oracle(Sim):
+    """The full plain SPM DNS case (32^3, 8 spheres, motor force, 100 steps)."""
+    p, parts = cases.ns_case()
+    o = Sim(p, parts)
+    r = pyoracle.Oracle(p, parts)
+    o.init_state(); r.init_state()
+    o.step(100); r.step(100)
+    for k in ("zeta0", "zeta1"):
+        assert rel(o.get(k), r.get(k)) < 1e-10, k
+    assert rel(o.get("phi")[:, :, :32], r.get("phi")[:, :, :32]) < 1e-10
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    pb = abi.particles_to_numpy(r.particles(), p.n_particles)
+    for k in ("x", "v", "omega", "q"):
+        assert rel(pa[k], pb[k]) < 1e-10, k
+
+
+def test_icep32_two_steps_golden(Sim):
+    g = load("icep32")
+    p, parts = cases.icep_case(tol=1e-7)
+    o = Sim(p, parts)
+    o.init_state()
+    o.step(2)
+    for k in ("zeta0", "zeta1"):
+        assert rel(o.get(k), g[k]) < 2e-5, k
+    for k in ("c0", "c1"):
+        assert rel(o.get(k), g[k]) < 1e-9, k
+    a = o.get("pot")[:, :, :32]
+    assert rel(a - a.mean(), g["pot"] - g["pot"].mean()) < 2e-5
+    assert rel(o.get("eps")[:, :, :32], g["eps"]) < 1e-12
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    assert rel(pa["x"], g["p_x"]) < 1e-12
+    assert rel(pa["v"], g["p_v"]) < 2e-5
+
+
+def test_lj32_golden_and_neighbour_set(Sim):
+    g = load("lj32")
+    p, parts = cases.lj_dense_case()
+    o = Sim(p, parts)
+    o.call("lj")
+    fr = abi.particles_to_numpy(o.particles(), p.n_particles)["fr"]
+    assert rel(fr, g["fr"]) < 1e-13
+    r = pyoracle.Oracle(p, parts)
+    a = sorted(map(tuple, o.lj_pairs()))
+    b = sorted(map(tuple, r.lj_pairs()))
+    assert len(a) > 0 and a == b
+    # 32^3 has 2 cells per side: pairs in different cells are visited 2^m times
+    assert len(a) > len(set(a))
+
+
+def test_ax32_golden(Sim):
+    g = load("ax32")
+    p, parts = cases.icep_case(eps_f=1.0, eps_p=10.0)
+    o = Sim(p, parts)
+    o.call("dielectric_field")
+    x = np.random.default_rng(31).standard_normal(32 * 32 * 32)
+    assert rel(o.apply_A(x), g["ax"]) < 1e-12
+
+
+def test_icep64_against_oracle(Sim):
+    """The ICEP step at 64^3 (16 spheres a=5) for a few steps, FP64, REF solver."""
+    p, parts = cases.icep_case(n=64, npart=16, minsep=12.0, a=5.0, tol=1e-8, seed=3)
+    o = Sim(p, parts)
+    r = pyoracle.Oracle(p, parts)
+    o.init_state(); r.init_state()
+    o.step(3); r.step(3)
+    for k in ("zeta0", "zeta1"):
+        assert rel(o.get(k), r.get(k)) < 1e-5, k
+    for k in ("c0", "c1"):
+        assert rel(o.get(k), r.get(k)) < 1e-9, k
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    pb = abi.particles_to_numpy(r.particles(), p.n_particles)
+    assert rel(pa["x"], pb["x"]) < 1e-12
+    assert rel(pa["v"], pb["v"]) < 1e-5
+
+
+def test_spectral_solver_true_residual(Sim):
+    """SPECTRAL solver: converges on the true residual, agrees with REF."""
+    p, parts = cases.icep_case(n=32, eps_f=80.0, eps_p=2.0, e_ext=(0.0, 0.0, 0.1), tol=1e-10,
+                               solver=abi.SOLVER_SPECTRAL)
+    o = Sim(p, parts)
+    o.call("dielectric_field")
+    rho = np.zeros((32, 32, 34))
+    o.set("rho", rho)
+    o.set("pot", rho)
+    it, err = o.solve_potential()
+    assert err <= 1e-10
+    pot = o.get("pot")[:, :, :32].ravel()
+    # true residual from the operator itself
+    o.call("build_rhs")
+    b = o.get("work")[:, :, :32].ravel()
+    res = np.linalg.norm(b - b.mean() - o.apply_A(pot)) / np.linalg.norm(b - b.mean())
+    assert res < 1e-9

@@ -120,7 +120,7 @@ class Engine : public EngineBase {
     }
     if (sizeof(R) != sizeof(double) && cudaMalloc(&stage, sizeof(double) * g.nf()) != cudaSuccess)
       return fail(ICEP_ERR_CUDA, "cudaMalloc of staging failed");
-    if (fft_plan_init(fft, g) != ICEP_OK) return fail(ICEP_ERR_CUDA, "FFT plan setup failed");
+    if (fft_plan_init(fft, g, s) != ICEP_OK) return fail(ICEP_ERR_CUDA, "FFT plan setup failed");
     // Particle_domain (profile.cxx:25-74)
     std::vector<int> sek;
     const int nh = (int)p.a + (int)p.a_xi + 2;
@@ -140,6 +140,7 @@ class Engine : public EngineBase {
       return fail(ICEP_ERR_UNSUPPORTED, "particle stencil wider than the box");
     cudaMalloc(&dsek, sizeof(int) * sek.size());
     cudaMemcpyAsync(dsek, sek.data(), sizeof(int) * sek.size(), cudaMemcpyHostToDevice, s);
+    cudaStreamSynchronize(s);  // sek is a local vector
     np = n;
     cudaMalloc(&dp, sizeof(icep_particle) * (n > 0 ? n : 1));
     cudaMallocHost(&hp, sizeof(icep_particle) * (n > 0 ? n : 1));
@@ -198,7 +199,8 @@ class Engine : public EngineBase {
       double en[3];
       const double amp = (double)p.nx * p.ny * p.nz;
       for (int d = 0; d < 3; d++) en[d] = p.e_ext[d] * amp;
-      cudaMemcpy(e_ext_n, en, sizeof(en), cudaMemcpyHostToDevice);
+      cudaMemcpyAsync(e_ext_n, en, sizeof(en), cudaMemcpyHostToDevice, s);
+      cudaStreamSynchronize(s);
     }
     cudaMalloc(&partials, sizeof(double) * 2 * DOT_BLOCKS);
     cudaMalloc(&scal, sizeof(double) * S_COUNT);
@@ -633,14 +635,14 @@ class Engine : public EngineBase {
   }
   int get_uk_dc(double *v) override {
     double tmp[3];
+    cudaMemcpyAsync(tmp, ukdc, sizeof(tmp), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
-    cudaMemcpy(tmp, ukdc, sizeof(tmp), cudaMemcpyDeviceToHost);
     for (int d = 0; d < 3; d++) v[d] = tmp[d];
     return cuda_status("get_uk_dc");
   }
   int set_uk_dc(const double *v) override {
+    cudaMemcpyAsync(ukdc, v, sizeof(double) * 3, cudaMemcpyHostToDevice, s);
     cudaStreamSynchronize(s);
-    cudaMemcpy(ukdc, v, sizeof(double) * 3, cudaMemcpyHostToDevice);
     return cuda_status("set_uk_dc");
   }
   int fft_host(double *a, bool forward) override {
@@ -681,7 +683,8 @@ class Engine : public EngineBase {
     cudaMemcpyAsync(n, dpairs_n, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaStreamSynchronize(s);
     const int m = (*n < max_pairs) ? *n : max_pairs;
-    if (m > 0) cudaMemcpy(pairs, dpairs, sizeof(int) * 2 * m, cudaMemcpyDeviceToHost);
+    if (m > 0) cudaMemcpyAsync(pairs, dpairs, sizeof(int) * 2 * m, cudaMemcpyDeviceToHost, s);
+    cudaStreamSynchronize(s);
     cudaFree(dpairs);
     return cuda_status("lj_pairs");
   }

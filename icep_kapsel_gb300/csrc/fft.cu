@@ -223,8 +223,12 @@ int pencil_width() {
   return (sizeof(R) == 8) ? 8 : 16;
 }
 
+// Twiddle table exp(-2 pi i m / denom), m < n. Uploaded on the caller's
+// stream and waited for: a pageable-memory copy may still be in flight when
+// cudaMemcpy returns, and the library's non-blocking streams do not order
+// against the legacy stream.
 template <typename R>
-cplx<R> *upload_table(int n, int denom) {
+cplx<R> *upload_table(int n, int denom, cudaStream_t s) {
   std::vector<cplx<R>> h(n);
   for (int m = 0; m < n; m++) {
     long double a = -2.0L * 3.14159265358979323846264338327950288L * (long double)m / (long double)denom;
@@ -233,27 +237,32 @@ cplx<R> *upload_table(int n, int denom) {
   }
   cplx<R> *d = nullptr;
   if (cudaMalloc(&d, sizeof(cplx<R>) * (n > 0 ? n : 1)) != cudaSuccess) return nullptr;
-  cudaMemcpy(d, h.data(), sizeof(cplx<R>) * n, cudaMemcpyHostToDevice);
+  if (cudaMemcpyAsync(d, h.data(), sizeof(cplx<R>) * n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaFree(d);
+    return nullptr;
+  }
   return d;
 }
 
 }  // namespace
 
 template <typename R>
-int fft_plan_init(FFTPlan<R> &p, const Grid &g) {
+int fft_plan_init(FFTPlan<R> &p, const Grid &g, cudaStream_t s) {
   p.g = g;
-  p.tw_x = upload_table<R>(g.nx, g.nx);
-  p.tw_y = upload_table<R>(g.ny, g.ny);
-  p.tw_z = upload_table<R>(g.nz / 2, g.nz / 2);
-  p.tw_post = upload_table<R>(g.nz / 2 + 1, g.nz);
+  p.tw_x = upload_table<R>(g.nx, g.nx, s);
+  p.tw_y = upload_table<R>(g.ny, g.ny, s);
+  p.tw_z = upload_table<R>(g.nz / 2, g.nz / 2, s);
+  p.tw_post = upload_table<R>(g.nz / 2 + 1, g.nz, s);
   if (!p.tw_x || !p.tw_y || !p.tw_z || !p.tw_post) return ICEP_ERR_CUDA;
   const int W = pencil_width<R>();
+  const int WR = 2 * W;  // rows per block of the z-row kernels
   const size_t sm_pen = 2 * (size_t)((g.nx > g.ny) ? g.nx : g.ny) * W * sizeof(cplx<R>);
-  const size_t sm_row = (2 * (size_t)(g.nz / 2) * W + (size_t)W * (g.nz / 2 + 1)) * sizeof(cplx<R>);
+  const size_t sm_row = (2 * (size_t)(g.nz / 2) * WR + (size_t)WR * (g.nz / 2 + 1)) * sizeof(cplx<R>);
   cudaFuncSetAttribute(k_pencils<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_pen);
   cudaFuncSetAttribute(k_rows_r2c<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_row);
   cudaFuncSetAttribute(k_rows_c2r<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_row);
-  return ICEP_OK;
+  return (cudaGetLastError() == cudaSuccess) ? ICEP_OK : ICEP_ERR_CUDA;
 }
 
 template <typename R>
@@ -322,8 +331,8 @@ void fft_c2r(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s) {
   k_rows_c2r<R><<<grid, block, sm, s>>>(fb, g, W, p.tw_z, p.tw_post, scale);
 }
 
-template int fft_plan_init<double>(FFTPlan<double> &, const Grid &);
-template int fft_plan_init<float>(FFTPlan<float> &, const Grid &);
+template int fft_plan_init<double>(FFTPlan<double> &, const Grid &, cudaStream_t);
+template int fft_plan_init<float>(FFTPlan<float> &, const Grid &, cudaStream_t);
 template void fft_plan_free<double>(FFTPlan<double> &);
 template void fft_plan_free<float>(FFTPlan<float> &);
 template void fft_r2c<double>(const FFTPlan<double> &, const FieldBatch<double> &, cudaStream_t);

@@ -24,7 +24,7 @@ struct FFTPlan {
 };
 
 template <typename R>
-int fft_plan_init(FFTPlan<R> &p, const Grid &g);
+int fft_plan_init(FFTPlan<R> &p, const Grid &g, cudaStream_t s);
 template <typename R>
 void fft_plan_free(FFTPlan<R> &p);
 

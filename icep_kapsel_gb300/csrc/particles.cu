@@ -25,7 +25,9 @@ __device__ __forceinline__ long stencil_point(const PartParams &pp, const double
     const int xi = (int)v;
     const double res = (v - (double)xi) * pp.dx;
     const int cell = sek[3 * m + d];
-    rm[d] = (xi + cell + pp.N[d]) % pp.N[d];
+    // wrap in 64-bit: a non-finite or huge coordinate (a diverged run) still
+    // yields an index inside the grid
+    rm[d] = (int)((((long long)xi % pp.N[d]) + cell + 2LL * pp.N[d]) % pp.N[d]);
     r[d] = (double)cell * pp.dx - res;
     double x12 = xp[d] - rm[d] * pp.dx;
     x12 -= (double)nint_d(x12 / pp.L[d]) * pp.L[d];
@@ -212,9 +214,16 @@ struct CellGeom {
   double lcr;
 };
 
+__device__ __forceinline__ int cell_coord(const CellGeom &cg, double x, int d) {
+  int c = (int)(x / cg.lcr);
+  // positions are in [0, L) after PBC; clamp so that a non-finite position
+  // cannot index outside the cell arrays
+  return c < 0 ? 0 : (c >= cg.lc[d] ? cg.lc[d] - 1 : c);
+}
+
 __device__ __forceinline__ int cell_of(const CellGeom &cg, const double *x) {
   int mc[3];
-  for (int d = 0; d < 3; d++) mc[d] = (int)(x[d] / cg.lcr);
+  for (int d = 0; d < 3; d++) mc[d] = cell_coord(cg, x[d], d);
   return (mc[0] * cg.lc[1] + mc[1]) * cg.lc[2] + mc[2];
 }
 
@@ -248,7 +257,7 @@ __global__ void k_lj_gather(PartParams pp, CellGeom cg, icep_particle *p, const 
   double xa[3];
   for (int d = 0; d < 3; d++) xa[d] = p[a].x[d];
   int ic[3];
-  for (int d = 0; d < 3; d++) ic[d] = (int)(xa[d] / cg.lcr);
+  for (int d = 0; d < 3; d++) ic[d] = cell_coord(cg, xa[d], d);
   double f[3] = {0, 0, 0};
   for (int o0 = -1; o0 <= 1; o0++)
     for (int o1 = -1; o1 <= 1; o1++)

@@ -57,6 +57,11 @@ __host__ __device__ inline bool in_two_third(const Grid &g, int i, int j, int kz
 
 inline unsigned div_up(long a, long b) { return (unsigned)((a + b - 1) / b); }
 
+// Number of kernels this library has launched (all contexts); read by
+// icep_kernel_launches() so that a benchmark can report its launch count.
+extern unsigned long long g_kernel_launches;
+inline void count_launch() { __atomic_fetch_add(&g_kernel_launches, 1ULL, __ATOMIC_RELAXED); }
+
 // Field slots of a context (ids shared with the oracle and the C-ABI).
 enum FieldId {
   F_ZETA0 = 0, F_ZETA1, F_U0, F_U1, F_U2, F_UP0, F_UP1, F_UP2, F_PHI, F_PHI_SUM,

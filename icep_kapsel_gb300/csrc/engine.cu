@@ -45,11 +45,20 @@ class Engine : public EngineBase {
   double radius, xi, hxi, nu;
   double valency_e[2], onsager[2];
   bool electrolyte;
+  // FP64 shadow of the Poisson problem (MIXED precision only): permittivity,
+  // potential, right-hand side, residual and operator work fields.
+  enum { D_EPS = 0, D_X, D_B, D_R, D_W3_0, D_W3_1, D_W3_2, D_COUNT };
+  bool mixed = false;
+  FFTPlan<double> fft64;
+  double *d64[D_COUNT] = {nullptr};
+  bool x64_valid = false;
 
   ~Engine() override {
     if (s) cudaStreamSynchronize(s);
     for (int i = 0; i < F_COUNT; i++) cudaFree(f[i]);
     fft_plan_free(fft);
+    for (int i = 0; i < D_COUNT; i++) cudaFree(d64[i]);
+    if (mixed) fft_plan_free(fft64);
     cudaFree(stage);
     cudaFree(dp);
     cudaFreeHost(hp);
@@ -121,6 +130,15 @@ class Engine : public EngineBase {
     if (sizeof(R) != sizeof(double) && cudaMalloc(&stage, sizeof(double) * g.nf()) != cudaSuccess)
       return fail(ICEP_ERR_CUDA, "cudaMalloc of staging failed");
     if (fft_plan_init(fft, g, s) != ICEP_OK) return fail(ICEP_ERR_CUDA, "FFT plan setup failed");
+    mixed = (sizeof(R) != sizeof(double));
+    if (mixed && electrolyte) {
+      for (int i = 0; i < D_COUNT; i++) {
+        if (cudaMalloc(&d64[i], sizeof(double) * g.nf()) != cudaSuccess)
+          return fail(ICEP_ERR_CUDA, "cudaMalloc of FP64 Poisson fields failed");
+        cudaMemsetAsync(d64[i], 0, sizeof(double) * g.nf(), s);
+      }
+      if (fft_plan_init(fft64, g, s) != ICEP_OK) return fail(ICEP_ERR_CUDA, "FP64 FFT plan setup failed");
+    }
     // Particle_domain (profile.cxx:25-74)
     std::vector<int> sek;
     const int nh = (int)p.a + (int)p.a_xi + 2;
@@ -422,8 +440,85 @@ class Engine : public EngineBase {
     return hscal[S_AUX1] / (double)g.nreal();
   }
 
+  // ---- FP64 Poisson operator of the MIXED path (same dataflow as apply_A)
+  void apply_A64(const double *x, double *y) {
+    copy_real<double>(g, x, y, s);
+    fft_r2c(fft64, batch(y), s);
+    grad_k<double>(g, y, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], 1.0, true, nullptr, s);
+    fft_c2r(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
+    eps_face_mul<double>(g, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_EPS], s);
+    fft_r2c(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
+    div_k<double>(g, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], y, true, s);
+    fft_c2r(fft64, batch(y), s);
+    matvecs++;
+  }
+
+  /*
+   * MIXED precision Charge_field2potential_dielectric: iterative refinement.
+   * The FP64 system is A64 x = b64 with A64 the reference operator on the
+   * permittivity (double)eps and b64 = D^-.(eps_face E) - (double)rho
+   * projected to mean zero. The potential x64 is FP64 state kept between
+   * steps. Each outer step computes the true residual r = b64 - A64 x64 in
+   * FP64 and, while |r| > tol |b64|, solves A d = r in FP32 with the
+   * spectral-preconditioned BiCGSTAB to a relative tolerance that leaves a
+   * margin below the target, then x64 += d.
+   */
+  int solve_potential_mixed(int rho_id, int pot_id) {
+    const Grid &G = g;
+    if (!x64_valid) {
+      convert_f2d(G.nf(), (const float *)f[pot_id], d64[D_X], s);
+      x64_valid = true;
+    }
+    convert_f2d(G.nf(), (const float *)f[F_EPS], d64[D_EPS], s);
+    // b64
+    eps_face_E<double>(G, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_EPS], P.e_ext[0], P.e_ext[1], P.e_ext[2], s);
+    fft_r2c(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
+    div_k<double>(G, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_B], true, s);
+    fft_c2r(fft64, batch(d64[D_B]), s);
+    convert_f2d(G.nf(), (const float *)f[rho_id], d64[D_R], s);
+    axpby_real<double>(G, d64[D_R], d64[D_B], -1.0, 1.0, s);
+    sum_real<double>(G, d64[D_B], partials, scal, S_AUX0, s);
+    sub_mean<double>(G, d64[D_B], scal, S_AUX0, s);
+    dots<double>(G, d64[D_B], d64[D_B], d64[D_B], d64[D_B], 1, partials, scal, S_BB, s);
+    int st = read_scal();
+    if (st) return st;
+    const double bb = hscal[S_BB];
+    const double eref = mean_eps();
+    int total_inner = 0;
+    double rel = 0.0;
+    if (bb > 0.0) {
+      const double tol2 = P.potential_tol * P.potential_tol * bb;
+      for (int outer = 0; outer < 30; outer++) {
+        apply_A64(d64[D_X], d64[D_R]);
+        sub_real<double>(G, d64[D_B], d64[D_R], d64[D_R], s);
+        dots<double>(G, d64[D_R], d64[D_R], d64[D_R], d64[D_R], 1, partials, scal, S_RR, s);
+        if ((st = read_scal())) return st;
+        const double rr = hscal[S_RR];
+        rel = sqrt(rr / bb);
+        if (!(rr > tol2) || !std::isfinite(rr)) break;
+        // FP32 correction solve on the normalised residual
+        const double rn = sqrt(rr / (double)G.nreal());
+        scale_d2f(G, d64[D_R], (float *)f[F_KB], 1.0 / rn, s);
+        zero(F_KX);
+        double inner_tol = 0.25 * P.potential_tol * sqrt(bb / rr);
+        if (inner_tol < 2e-5) inner_tol = 2e-5;
+        if (inner_tol > 0.5) inner_tol = 0.5;
+        int it = 0;
+        double er = 0.0;
+        if ((st = bicgstab(inner_tol, P.potential_iter, true, eref, &it, &er))) return st;
+        total_inner += it;
+        add_f2d(G, (const float *)f[F_KX], d64[D_X], rn, s);
+      }
+    }
+    scale_d2f(G, d64[D_X], (float *)f[pot_id], 1.0, s);
+    last_iters = total_inner;
+    last_error = rel;
+    return ICEP_OK;
+  }
+
   // Charge_field2potential_dielectric_LO (operate_dielectric.cxx:542-572)
   int solve_potential(int rho_id, int pot_id, int rhs_id) {
+    if (mixed) return solve_potential_mixed(rho_id, pot_id);
     build_rhs(rhs_id, rho_id);
     copy_real<R>(g, f[rhs_id], f[F_KB], s);
     copy_real<R>(g, f[pot_id], f[F_KX], s);
@@ -598,6 +693,11 @@ class Engine : public EngineBase {
 
   int get_field(int id, double *host) override {
     if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
+    if (id == F_POT && mixed && x64_valid) {  // the potential is FP64 state
+      cudaMemcpyAsync(host, d64[D_X], sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_field");
+      return ICEP_OK;
+    }
     if (sizeof(R) == sizeof(double)) {
       cudaMemcpyAsync(host, f[id], sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
     } else {
@@ -609,6 +709,7 @@ class Engine : public EngineBase {
   }
   int set_field(int id, const double *host) override {
     if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
+    if (id == F_POT) x64_valid = false;
     if (sizeof(R) == sizeof(double)) {
       cudaMemcpyAsync(f[id], host, sizeof(double) * g.nf(), cudaMemcpyHostToDevice, s);
     } else {
@@ -688,6 +789,37 @@ class Engine : public EngineBase {
     cudaFree(dpairs);
     return cuda_status("lj_pairs");
   }
+  int time_kernel(int which, int nb, int reps, double *ms, double *bytes) override {
+    if (nb < 1 || nb > 5 || reps < 1) return fail(ICEP_ERR_ARG, "time_kernel arguments");
+    const int ids[5] = {F_WV3_0, F_WV3_1, F_WV3_2, F_KY, F_KZ};
+    FieldBatch<R> fb = batch(f[ids[0]], nb > 1 ? f[ids[1]] : nullptr, nb > 2 ? f[ids[2]] : nullptr,
+                             nb > 3 ? f[ids[3]] : nullptr, nb > 4 ? f[ids[4]] : nullptr);
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    auto one = [&]() {
+      if (which <= 6) fft_pass(fft, fb, which, s);
+      else if (which == 7) fft_r2c(fft, fb, s);
+      else if (which == 8) fft_c2r(fft, fb, s);
+      else apply_A(f[F_KP], f[F_KV]);
+    };
+    one();  // warm-up
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < reps; r++) one();
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = (double)t / reps;
+    const double field = (double)g.nreal() * sizeof(R);
+    if (which == 3) *bytes = 2.0 * 2.0 * g.nx * g.ny * 2 * sizeof(R) * nb;  // two planes read + written
+    else if (which <= 8) *bytes = 2.0 * field * nb;  // one field in, one out, per transform or pass
+    else *bytes = 17.0 * field;                      // Ax: 8 FFTs + the permittivity read
+    return cuda_status("time_kernel");
+  }
+
   int sync() override {
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("sync");
     return ICEP_OK;

@@ -34,6 +34,12 @@ void fft_r2c(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s);
 template <typename R>
 void fft_c2r(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s);
 
+// Single passes of the 3D transforms, for timing: 0 = z rows forward,
+// 1 = y pencils forward, 2 = x pencils forward, 3 = Hermitian completion,
+// 4 = x pencils inverse, 5 = y pencils inverse, 6 = z rows inverse.
+template <typename R>
+void fft_pass(const FFTPlan<R> &p, const FieldBatch<R> &fb, int pass, cudaStream_t s);
+
 template <typename R>
 inline FieldBatch<R> batch(R *a, R *b = nullptr, R *c = nullptr, R *d = nullptr, R *e = nullptr) {
   FieldBatch<R> fb;

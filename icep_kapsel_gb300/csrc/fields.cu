@@ -488,84 +488,111 @@ inline unsigned nblk_real(const Grid &g) { return div_up(g.nreal(), TPB); }
 }  // namespace
 
 template <typename R> void truncate_23(const Grid &g, const FieldBatch<R> &fb, cudaStream_t s) {
+  count_launch();
   k_truncate<R><<<dim3(nblk_modes(g), fb.n), TPB, 0, s>>>(fb, g);
 }
 template <typename R> void zeta_k2u_k(const Grid &g, const R *z0, const R *z1, const double *uk_dc, R *u0, R *u1, R *u2, cudaStream_t s) {
+  count_launch();
   k_zeta_k2u_k<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, uk_dc, u0, u1, u2);
 }
 template <typename R> void u_k2zeta_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *uk_dc, cudaStream_t s) {
+  count_launch();
   k_u_k2zeta_k<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, z0, z1, uk_dc);
 }
 template <typename R> void advection_combine(const Grid &g, R *u0, R *u1, R *u2, R *a0, R *a1, cudaStream_t s) {
+  count_launch();
   k_advection_combine<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, a0, a1);
 }
 template <typename R> void ns_slaved_update(const Grid &g, R *z0, R *z1, const R *a0, const R *a1, double nu, double dt, cudaStream_t s) {
+  count_launch();
   k_ns_slaved<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, a0, a1, nu, dt);
 }
 template <typename R> void solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s) {
+  count_launch();
   k_solenoidal<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2);
 }
 template <typename R> void grad_k(const Grid &g, const R *a, R *d0, R *d1, R *d2, R scale, bool shift, const double *e_ext_n, cudaStream_t s) {
+  count_launch();
   k_grad<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, d0, d1, d2, scale, shift ? 1 : 0, e_ext_n);
 }
 template <typename R> void div_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *div, bool shift, cudaStream_t s) {
+  count_launch();
   k_div<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, div, shift ? 1 : 0);
 }
 template <typename R> void euler_update(const Grid &g, R *z0, R *z1, R *r0, R *r1, R *c0, R *c1, const R *cr0, const R *cr1, double nu, double dt, cudaStream_t s) {
+  count_launch();
   k_euler<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, r0, r1, c0, c1, cr0, cr1, nu, dt);
 }
 template <typename R> void inv_laplace_k(const Grid &g, R *a, double eps_ref, cudaStream_t s) {
+  count_launch();
   k_inv_laplace<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, (R)(1.0 / eps_ref));
 }
 template <typename R> void scale_copy(const Grid &g, const R *x, R *y, R a, cudaStream_t s) {
+  count_launch();
   k_scale_copy<R><<<div_up(g.nf(), TPB), TPB, 0, s>>>(g.nf(), x, y, a);
 }
 template <typename R> void advection_products(const Grid &g, R *u0, R *u1, R *u2, R *a0, R *a1, cudaStream_t s) {
+  count_launch();
   k_adv_products<R><<<nblk_real(g), TPB, 0, s>>>(g, u0, u1, u2, a0, a1);
 }
 template <typename R> void phi_clip(const Grid &g, const R *phs, R *phi, cudaStream_t s) {
+  count_launch();
   k_phi_clip<R><<<nblk_real(g), TPB, 0, s>>>(g, phs, phi);
 }
 template <typename R> void f_nonsole(const Grid &g, R *const *f, R *const *up, const R *phi, R *const *u, cudaStream_t s) {
+  count_launch();
   k_f_nonsole<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(f), v3(up), phi, v3(u));
 }
 template <typename R> void add_vec(const Grid &g, R *const *u, R *const *f, R a, cudaStream_t s) {
+  count_launch();
   k_add_vec<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(u), v3(f), a);
 }
 template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_sin, const R *eps_w, double ef, double ep, double dc, cudaStream_t s) {
+  count_launch();
   k_eps_from_profile<R><<<nblk_real(g), TPB, 0, s>>>(g, eps, phi_sin, eps_w, ef, ep, dc);
 }
 template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s) {
+  count_launch();
   k_charge_add<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c, phi, ze, first ? 1 : 0);
 }
 template <typename R> void eps_face_mul(const Grid &g, R *w0, R *w1, R *w2, const R *eps, cudaStream_t s) {
+  count_launch();
   k_eps_face_mul<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps);
 }
 template <typename R> void eps_face_E(const Grid &g, R *w0, R *w1, R *w2, const R *eps, double e0, double e1, double e2, cudaStream_t s) {
+  count_launch();
   k_eps_face_E<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps, e0, e1, e2);
 }
 template <typename R> void axpby_real(const Grid &g, const R *x, R *y, R a, R b, cudaStream_t s) {
+  count_launch();
   k_axpby_real<R><<<nblk_real(g), TPB, 0, s>>>(g, x, y, a, b);
 }
 template <typename R> void interp_normal(const Grid &g, R *const *out, R *const *in, cudaStream_t s) {
+  count_launch();
   k_interp_normal<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(out), v3(in));
 }
 template <typename R> void maxwell_e2(const Grid &g, const R *f0, const R *f1, const R *f2, R *w1, double e0, double e1, double e2, int ext, cudaStream_t s) {
+  count_launch();
   k_maxwell_e2<R><<<nblk_real(g), TPB, 0, s>>>(g, f0, f1, f2, w1, e0, e1, e2, ext);
 }
 template <typename R> void maxwell_face(const Grid &g, R *const *force, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s) {
+  count_launch();
   k_maxwell_face<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(force), rho, w1, v3(ge), e0, e1, e2, ext);
 }
 template <typename R> void np_flux_electric(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, cudaStream_t s) {
+  count_launch();
   k_np_flux_electric<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(gp), L_ze);
 }
 template <typename R> void np_impermeability(const Grid &g, R *const *flux, R *const *sn, cudaStream_t s) {
+  count_launch();
   k_np_imperm<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), v3(sn));
 }
 template <typename R> void np_flux_advection(const Grid &g, R *const *flux, const R *c, R *const *u, cudaStream_t s) {
+  count_launch();
   k_np_flux_adv<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(u));
 }
 template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s) {
+  count_launch();
   k_fill_real<R><<<nblk_real(g), TPB, 0, s>>>(g, a, v);
 }
 

@@ -7,6 +7,10 @@
 #include "../../include/icep_gb300.h"
 #include "engine.cuh"
 
+namespace icep {
+unsigned long long g_kernel_launches = 0;
+}
+
 struct icep_ctx {
   icep::EngineBase *e = nullptr;
   std::string err;
@@ -150,6 +154,32 @@ int icep_solver_stats(icep_ctx *c, int *iterations, double *error, long *matvecs
 }
 void *icep_stream(icep_ctx *c) { return ok(c) ? (void *)c->e->stream() : nullptr; }
 int icep_synchronize(icep_ctx *c) { return ok(c) ? wrap(c, c->e->sync()) : ICEP_ERR_ARG; }
+
+int icep_time_kernel(icep_ctx *c, int which, int batch, int reps, double *ms, double *bytes) {
+  if (!ok(c) || !ms || !bytes) return ICEP_ERR_ARG;
+  return wrap(c, c->e->time_kernel(which, batch, reps, ms, bytes));
+}
+int icep_step_timed(icep_ctx *c, int nsteps, double *ms) {
+  if (!ok(c) || nsteps < 0 || !ms) return ICEP_ERR_ARG;
+  cudaStream_t s = c->e->stream();
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return ICEP_ERR_CUDA;
+  cudaEventRecord(e0, s);
+  int st = c->e->step(nsteps);
+  cudaEventRecord(e1, s);
+  cudaEventSynchronize(e1);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = (double)t;
+  return wrap(c, st);
+}
+unsigned long long icep_kernel_launches(void) { return __atomic_load_n(&icep::g_kernel_launches, __ATOMIC_RELAXED); }
+int icep_pin_host(void *p, size_t bytes) {
+  return (p && cudaHostRegister(p, bytes, cudaHostRegisterDefault) == cudaSuccess) ? ICEP_OK : ICEP_ERR_CUDA;
+}
+int icep_unpin_host(void *p) { return (p && cudaHostUnregister(p) == cudaSuccess) ? ICEP_OK : ICEP_ERR_CUDA; }
 
 /* generic dispatch used by the Python layer (same numbering as the oracle) */
 int icep_call(icep_ctx *c, int fn) { return ok(c) ? wrap(c, c->e->call(fn)) : ICEP_ERR_ARG; }

@@ -153,11 +153,17 @@ __global__ void k_d2f(long n, const double *x, float *y) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) y[t] = (float)x[t];
 }
-__global__ void k_add_f2d(Grid g, const float *x, double *y) {
+__global__ void k_add_f2d(Grid g, const float *x, double *y, double a) {
   const unsigned t = RTID;
   if (t >= (unsigned)g.nreal()) return;
   const long im = real_index(g, t);
-  y[im] += (double)x[im];
+  y[im] += a * (double)x[im];
+}
+__global__ void k_scale_d2f(Grid g, const double *x, float *y, double a) {
+  const unsigned t = RTID;
+  if (t >= (unsigned)g.nf()) return;
+  const unsigned k = t % (unsigned)g.nzp;
+  y[t] = (k < (unsigned)g.nz) ? (float)(a * x[t]) : 0.0f;
 }
 
 }  // namespace
@@ -165,47 +171,64 @@ __global__ void k_add_f2d(Grid g, const float *x, double *y) {
 template <typename R>
 void dots(const Grid &g, const R *a0, const R *b0, const R *a1, const R *b1, int n, double *partials, double *scal,
           int slot, cudaStream_t s) {
+  count_launch();
   k_dots<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a0, b0, a1, b1, n, partials);
+  count_launch();
   k_dots_final<<<1, 256, 0, s>>>(partials, DOT_BLOCKS, n, scal, slot);
 }
 template <typename R>
 void sum_real(const Grid &g, const R *a, double *partials, double *scal, int slot, cudaStream_t s) {
+  count_launch();
   k_sum<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a, partials);
+  count_launch();
   k_dots_final<<<1, 256, 0, s>>>(partials, DOT_BLOCKS, 1, scal, slot);
 }
 template <typename R>
 void bicg_p(const Grid &g, R *p, const R *r, const R *v, double beta, double w, cudaStream_t s) {
+  count_launch();
   k_bicg_p<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, p, r, v, (R)beta, (R)w);
 }
 template <typename R>
 void bicg_s(const Grid &g, R *sv, const R *r, const R *v, double rho, const double *scal, cudaStream_t s) {
+  count_launch();
   k_bicg_s<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, sv, r, v, rho, scal);
 }
 template <typename R>
 void bicg_xr(const Grid &g, R *x, R *r, const R *y, const R *z, const R *sv, const R *t, double rho,
              const double *scal, cudaStream_t s) {
+  count_launch();
   k_bicg_xr<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, x, r, y, z, sv, t, rho, scal);
 }
 template <typename R>
 void copy_real(const Grid &g, const R *x, R *y, cudaStream_t s) {
+  count_launch();
   k_copy_real<R><<<div_up(g.nf(), TPB), TPB, 0, s>>>(g, x, y);
 }
 template <typename R>
 void sub_real(const Grid &g, const R *b, const R *t, R *r, cudaStream_t s) {
+  count_launch();
   k_sub_real<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, b, t, r);
 }
 template <typename R>
 void sub_mean(const Grid &g, R *a, const double *scal, int slot, cudaStream_t s) {
+  count_launch();
   k_sub_mean<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, a, scal, slot);
 }
 void convert_f2d(long n, const float *x, double *y, cudaStream_t s) {
+  count_launch();
   k_f2d<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y);
 }
 void convert_d2f(long n, const double *x, float *y, cudaStream_t s) {
+  count_launch();
   k_d2f<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y);
 }
-void add_f2d(const Grid &g, const float *x, double *y, cudaStream_t s) {
-  k_add_f2d<<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, x, y);
+void add_f2d(const Grid &g, const float *x, double *y, double a, cudaStream_t s) {
+  count_launch();
+  k_add_f2d<<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, x, y, a);
+}
+void scale_d2f(const Grid &g, const double *x, float *y, double a, cudaStream_t s) {
+  count_launch();
+  k_scale_d2f<<<div_up(g.nf(), TPB), TPB, 0, s>>>(g, x, y, a);
 }
 
 #define KRY_INST(R)                                                                                              \

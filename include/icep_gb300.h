@@ -16,6 +16,8 @@
 #ifndef ICEP_GB300_H
 #define ICEP_GB300_H
 
+#include <stddef.h>
+
 #include "icep_types.h"
 
 #ifdef __cplusplus
@@ -140,6 +142,26 @@ int icep_Charge_field2potential_dielectric(icep_ctx *ctx, int *iterations, doubl
 int icep_Make_Maxwell_force_x_on_fluid(icep_ctx *ctx);
 /* Statistics of the last Poisson solve of the context. */
 int icep_solver_stats(icep_ctx *ctx, int *iterations, double *error, long *matvecs);
+/* Generic phase dispatch (ids of the step's phases, numbered as in the
+ * checker used by the tests). */
+int icep_call(icep_ctx *ctx, int fn);
+
+/* ---- measurement helpers (no reference counterpart) --------------------- */
+/* Average device time of `reps` launches of one kernel group on the
+ * context's stream (CUDA events): which 0..6 = one pass of the 3D FFT (z rows
+ * forward, y forward, x forward, Hermitian completion, x inverse, y inverse,
+ * z rows inverse), 7 = forward 3D FFT, 8 = inverse 3D FFT, 9 = Ax. batch:
+ * fields per launch (1..5). bytes: algorithmic bytes per launch. */
+int icep_time_kernel(icep_ctx *ctx, int which, int batch, int reps, double *ms, double *bytes);
+/* icep_step with CUDA events recorded on the context's stream around it;
+ * ms receives the device time of the nsteps steps. */
+int icep_step_timed(icep_ctx *ctx, int nsteps, double *ms);
+/* Kernels launched by this library so far (all contexts). */
+unsigned long long icep_kernel_launches(void);
+/* Page-lock / release a caller's host buffer for the drop-in transfers. */
+int icep_pin_host(void *ptr, size_t bytes);
+int icep_unpin_host(void *ptr);
+
 /* Stream of the context (cudaStream_t as void*), for callers that order
  * their own device work after the library's. */
 void *icep_stream(icep_ctx *ctx);

@@ -1204,7 +1204,7 @@ static double vdot(long n, const double *a, const double *b) {
 static long bicgstab(ko_ctx *c, const double *b, double *x, double tol, long maxit, double *err) {
   const long n = c->nu;
   double *r = (double *)malloc(sizeof(double) * n), *r0 = (double *)malloc(sizeof(double) * n);
-  double *v = (double *)calloc(n, sizeof(double)), *p = (double *)calloc(n, sizeof(double));
+  double *v = (double *)calloc((size_t)n, sizeof(double)), *p = (double *)calloc((size_t)n, sizeof(double));
   double *s = (double *)malloc(sizeof(double) * n), *t = (double *)malloc(sizeof(double) * n);
   apply_A(c, x, t);
   for (long k = 0; k < n; k++) r[k] = b[k] - t[k];
@@ -1249,6 +1249,108 @@ done:
   return i;
 }
 
+/* Spectral inverse of the constant-permittivity operator, y = M^-1 x:
+ * y(k) = -x(k) / (eps_ref |k|^2), y(0) = 0 (preconditioner of the plain
+ * GPU method; no counterpart in the reference). */
+static void precond_spectral(ko_ctx *c, const double *x, double *y, double eps_ref) {
+  double *w = c->f[F_WV1];
+  zero_real(c, w);
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      memcpy(w + IDX(c, i, j, 0), x + ((long)i * c->ny + j) * c->nz, sizeof(double) * c->nz);
+  fft_r2c(c, w);
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      for (int kz = 0; kz < c->hnz; kz++) {
+        double k2 = k2_of(c, i, j, kz);
+        double f = (k2 > 0.0) ? -1.0 / (eps_ref * k2) : 0.0;
+        long im = IDX(c, i, j, 2 * kz);
+        w[im] *= f;
+        w[im + 1] *= f;
+      }
+  fft_c2r(c, w);
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      memcpy(y + ((long)i * c->ny + j) * c->nz, w + IDX(c, i, j, 0), sizeof(double) * c->nz);
+}
+
+/*
+ * The plain method of the GPU path (ICEP_SOLVER_SPECTRAL): BiCGSTAB right-
+ * preconditioned by precond_spectral, b projected to mean zero (the range of
+ * the singular operator), convergence confirmed on the true residual
+ * |b - A x| <= tol |b|. Same loop as bicgstab() otherwise.
+ */
+static long bicgstab_spectral(ko_ctx *c, double *b, double *x, double tol, long maxit, double *err) {
+  const long n = c->nu;
+  double mean = 0.0;
+  for (long k = 0; k < n; k++) mean += b[k];
+  mean /= (double)n;
+  for (long k = 0; k < n; k++) b[k] -= mean;
+  double eref = 0.0;
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      for (int k = 0; k < c->nz; k++) eref += c->f[F_EPS][IDX(c, i, j, k)];
+  eref /= (double)n;
+  double *r = (double *)malloc(sizeof(double) * n), *r0 = (double *)malloc(sizeof(double) * n);
+  double *v = (double *)calloc((size_t)n, sizeof(double)), *p = (double *)calloc((size_t)n, sizeof(double));
+  double *s = (double *)malloc(sizeof(double) * n), *t = (double *)malloc(sizeof(double) * n);
+  double *y = (double *)malloc(sizeof(double) * n), *z = (double *)malloc(sizeof(double) * n);
+  apply_A(c, x, t);
+  for (long k = 0; k < n; k++) r[k] = b[k] - t[k];
+  memcpy(r0, r, sizeof(double) * n);
+  double r0_sq = vdot(n, r0, r0), b_sq = vdot(n, b, b);
+  long i = 0;
+  if (b_sq == 0) {
+    memset(x, 0, sizeof(double) * n);
+    *err = 0.0;
+  } else {
+    double rho = 1, alpha = 1, w = 1, rr = r0_sq, rho_new = r0_sq;
+    const double tol2 = tol * tol * b_sq, eps2 = DBL_EPSILON * DBL_EPSILON;
+    long restarts = 0;
+    while (i < maxit) {
+      if (!(rr > tol2)) {
+        apply_A(c, x, t);
+        for (long k = 0; k < n; k++) r[k] = b[k] - t[k];
+        rr = vdot(n, r, r);
+        if (!(rr > tol2)) break;
+        memcpy(r0, r, sizeof(double) * n);
+        r0_sq = rho_new = rr;
+        memset(v, 0, sizeof(double) * n);
+        memset(p, 0, sizeof(double) * n);
+        rho = alpha = w = 1;
+      }
+      double rho_old = rho;
+      rho = rho_new;
+      if (fabs(rho) < eps2 * r0_sq) {
+        apply_A(c, x, t);
+        for (long k = 0; k < n; k++) r[k] = b[k] - t[k];
+        memcpy(r0, r, sizeof(double) * n);
+        rho = r0_sq = vdot(n, r, r);
+        if (restarts++ == 0) i = 0;
+      }
+      double beta = (rho / rho_old) * (alpha / w);
+      for (long k = 0; k < n; k++) p[k] = r[k] + beta * (p[k] - w * v[k]);
+      precond_spectral(c, p, y, eref);
+      apply_A(c, y, v);
+      alpha = rho / vdot(n, r0, v);
+      for (long k = 0; k < n; k++) s[k] = r[k] - alpha * v[k];
+      precond_spectral(c, s, z, eref);
+      apply_A(c, z, t);
+      double tt = vdot(n, t, t);
+      w = (tt > 0.0) ? vdot(n, t, s) / tt : 0.0;
+      for (long k = 0; k < n; k++) x[k] += alpha * y[k] + w * z[k];
+      for (long k = 0; k < n; k++) r[k] = s[k] - w * t[k];
+      rho_new = vdot(n, r0, r);
+      rr = vdot(n, r, r);
+      ++i;
+    }
+    *err = sqrt(rr / b_sq);
+  }
+  free(r); free(r0); free(v); free(p); free(s); free(t); free(y); free(z);
+  return i;
+}
+
 /* Charge_field2potential_dielectric_LO (operate_dielectric.cxx:542-572) */
 static void solve_potential(ko_ctx *c, const double *rho, double *pot, double *rhs_work) {
   const long n = c->nu;
@@ -1260,10 +1362,23 @@ static void solve_potential(ko_ctx *c, const double *rho, double *pot, double *r
       memcpy(x + ((long)i * c->ny + j) * c->nz, pot + IDX(c, i, j, 0), sizeof(double) * c->nz);
     }
   double err;
-  long it = bicgstab(c, b, x, c->P.potential_tol, c->P.potential_iter, &err);
-  if (it == c->P.potential_iter) {
-    memset(x, 0, sizeof(double) * n);
+  long it;
+  if (c->P.solver == ICEP_SOLVER_SPECTRAL) {
+    double *b2 = (double *)malloc(sizeof(double) * n);
+    memcpy(b2, b, sizeof(double) * n);
+    it = bicgstab_spectral(c, b2, x, c->P.potential_tol, c->P.potential_iter, &err);
+    if (it == c->P.potential_iter) {
+      memset(x, 0, sizeof(double) * n);
+      memcpy(b2, b, sizeof(double) * n);
+      it = bicgstab_spectral(c, b2, x, c->P.potential_tol, c->P.potential_iter, &err);
+    }
+    free(b2);
+  } else {
     it = bicgstab(c, b, x, c->P.potential_tol, c->P.potential_iter, &err);
+    if (it == c->P.potential_iter) {
+      memset(x, 0, sizeof(double) * n);
+      it = bicgstab(c, b, x, c->P.potential_tol, c->P.potential_iter, &err);
+    }
   }
   c->last_iters = it;
   c->last_error = err;

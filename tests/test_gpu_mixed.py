@@ -1,0 +1,78 @@
+"""MIXED precision (FP32 fields, FFTs and inner Krylov; FP64 particles, k=0
+mode and Poisson true residual with iterative refinement) against the FP64
+path. Tolerances are per field, relative L2 after a few steps:
+
+  potential (mean removed)   2e-5   (FP32 permittivity/charge; FP64 solve)
+  zeta, u                    1e-3   (FP32 FFTs; small fields, relative error)
+  concentrations             1e-6   (dominated by the uniform salt)
+  particle positions         1e-9   (FP64 integration of FP32-sized forces)
+  particle velocities        1e-3
+The Poisson solve itself must reach the 1e-8 true FP64 residual.
+"""
+import numpy as np
+import pytest
+
+import cases
+import pyoracle
+from icep_kapsel_gb300 import abi
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / (nb if nb > 0 else 1.0))
+
+
+@pytest.fixture(scope="module")
+def Sim():
+    from icep_kapsel_gb300.build import build
+    build()
+    from icep_kapsel_gb300.runtime import Simulation
+    return Simulation
+
+
+def icep(n, npart, precision, tol=1e-8, seed=3):
+    return cases.icep_case(n=n, npart=npart, minsep=10.0, seed=seed, a=4.0, eps_f=80.0, eps_p=3.0,
+                           e_ext=(0.0, 0.0, 0.1), tol=tol, maxit=1000, dt=0.01, per_particle_eps=(1.0, 5.0),
+                           solver=abi.SOLVER_SPECTRAL, precision=precision)
+
+
+@pytest.mark.parametrize("n,npart", [(64, 32), (128, 512)])
+def test_mixed_against_fp64(Sim, n, npart):
+    pm, parts = icep(n, npart, abi.MIXED)
+    pd, parts_d = icep(n, npart, abi.FP64)
+    m = Sim(pm, parts)
+    d = Sim(pd, parts_d)
+    m.init_state(); d.init_state()
+    _, err_m, _ = m.solver_stats()
+    assert err_m <= 1e-8
+    m.step(3); d.step(3)
+    _, err_m, _ = m.solver_stats()
+    assert err_m <= 1e-8
+    nz = pm.nz
+    a, b = m.get("pot")[:, :, :nz], d.get("pot")[:, :, :nz]
+    assert rel(a - a.mean(), b - b.mean()) < 2e-5
+    for k in ("zeta0", "zeta1"):
+        assert rel(m.get(k), d.get(k)) < 1e-3, k
+    for k in ("c0", "c1"):
+        assert rel(m.get(k), d.get(k)) < 1e-6, k
+    pa = abi.particles_to_numpy(m.particles(), npart)
+    pb = abi.particles_to_numpy(d.particles(), npart)
+    assert rel(pa["x"], pb["x"]) < 1e-9
+    assert rel(pa["v"], pb["v"]) < 1e-3
+
+
+def test_fp64_spectral_against_oracle_per_particle_eps(Sim):
+    """The plain (spectral) solver and the per-particle permittivity, FP64 GPU
+    against the FP64 oracle restating the same algorithm."""
+    p, parts = icep(32, 6, abi.FP64, tol=1e-10, seed=5)
+    g = Sim(p, parts)
+    o = pyoracle.Oracle(p, parts)
+    g.init_state(); o.init_state()
+    g.step(2); o.step(2)
+    assert rel(g.get("eps")[:, :, :32], o.get("eps")[:, :, :32]) < 1e-13
+    a, b = g.get("pot")[:, :, :32], o.get("pot")[:, :, :32]
+    assert rel(a - a.mean(), b - b.mean()) < 1e-8
+    for k in ("zeta0", "zeta1", "c0", "c1"):
+        assert rel(g.get(k), o.get(k)) < 1e-8, k

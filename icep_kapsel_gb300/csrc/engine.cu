@@ -4,6 +4,7 @@
 // comment; kernels live in fft.cu, fields.cu, particles.cu and krylov.cu.
 #include <float.h>
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <cstdio>
@@ -49,6 +50,15 @@ class Engine : public EngineBase {
   // potential, right-hand side, residual and operator work fields.
   enum { D_EPS = 0, D_X, D_B, D_R, D_W3_0, D_W3_1, D_W3_2, D_COUNT };
   bool mixed = false;
+  // optional per-phase device timing of the step (CUDA events at phase
+  // boundaries, accumulated in ms)
+  static constexpr int NPH = 10;
+  bool phase_on = false;
+  cudaEvent_t ph_ev[NPH + 1];
+  double ph_ms[NPH] = {0};
+  void mark(int k) {
+    if (phase_on) cudaEventRecord(ph_ev[k], s);
+  }
   FFTPlan<double> fft64;
   double *d64[D_COUNT] = {nullptr};
   bool x64_valid = false;
@@ -70,6 +80,8 @@ class Engine : public EngineBase {
     cudaFreeHost(hscal);
     cudaFree(ljwork);
     cudaFree(dpairs_n);
+    if (phase_on)
+      for (int k = 0; k <= NPH; k++) cudaEventDestroy(ph_ev[k]);
     if (s) cudaStreamDestroy(s);
   }
 
@@ -228,6 +240,11 @@ class Engine : public EngineBase {
     ljwork_ints = 2 * (ncell + 1) + (n > 0 ? n : 1);
     cudaMalloc(&ljwork, sizeof(int) * ljwork_ints);
     cudaMalloc(&dpairs_n, sizeof(int));
+    const char *pe = getenv("ICEP_PHASE_PROFILE");
+    if (pe && pe[0] == '1') {
+      phase_on = true;
+      for (int k = 0; k <= NPH; k++) cudaEventCreate(&ph_ev[k]);
+    }
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("setup");
     return cuda_status("setup");
   }
@@ -553,6 +570,12 @@ class Engine : public EngineBase {
     conc_k2charge(rho_id, F_F0, F_F1);
     int st = solve_potential(rho_id, F_POT, F_F2);
     if (st) return st;
+    maxwell_stress(rho_id);
+    return ICEP_OK;
+  }
+  // the part of Make_Maxwell_force_x_on_fluid after the Poisson solve
+  // (operate_dielectric.cxx:651-763)
+  void maxwell_stress(int rho_id) {
     staggered_grad(F_EPS, F_GE0, F_WV1);
     staggered_grad(F_POT, F_F0, F_WV1);
     maxwell_e2<R>(g, f[F_F0], f[F_F1], f[F_F2], f[F_WV1], P.e_ext[0], P.e_ext[1], P.e_ext[2], P.external_field, s);
@@ -561,7 +584,6 @@ class Engine : public EngineBase {
     for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
     interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);
     for (int d = 0; d < 3; d++) copy(F_GE0 + d, F_F0 + d);
-    return ICEP_OK;
   }
 
   // NSsolute_solver_Euler (fluid_solver.cxx:318-338), Dielectric branch of
@@ -604,31 +626,57 @@ class Engine : public EngineBase {
   // Time_evolution_hydro (sp_3d_ns.cxx:24-186)
   int time_evolution_hydro() {
     int st;
+    mark(0);
     if (!electrolyte) ns_solver_slaved_euler();
     else nssolute_solver_euler();
+    mark(1);
     truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
     zeta_k2u();
     if (!P.fixed_particle) md_position(pp, dp, ts != 0, s);
     make_phi_particle_sum();
+    mark(2);
     if (electrolyte) {
       for (int d = 0; d < 3; d++) {
         zero(F_UP0 + d);
         zero(F_F0 + d);
       }
       f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], true, s);
-      if ((st = maxwell_force(F_UP0))) return st;
+      make_dielectric_field(F_F0, F_WORK);
+      conc_k2charge(F_UP0, F_F0, F_F1);
+      mark(3);
+      if ((st = solve_potential(F_UP0, F_POT, F_F2))) return st;
+      mark(4);
+      maxwell_stress(F_UP0);
+      mark(5);
       add_vec<R>(g, vec(F_U0), vec(F_F0), (R)(P.dt / P.rho), s);
       solenoidal_u(F_U0);
+    } else {
+      mark(3);
+      mark(4);
+      mark(5);
     }
+    mark(6);
     f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], false, s);
     if (!P.fixed_particle) {
       if ((st = lj_into_fr())) return fail(st, "LJ cell list");
       md_velocity(pp, dp, ts != 0, s);
     }
+    mark(7);
     make_u_particle_sum();
     f_particle_sole_and_add();
+    mark(8);
     r2c(f[F_U0], f[F_U1], f[F_U2]);
     u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
+    mark(9);
+    mark(10);
+    if (phase_on) {
+      cudaEventSynchronize(ph_ev[10]);
+      for (int k = 0; k < NPH; k++) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ph_ev[k], ph_ev[k + 1]);
+        ph_ms[k] += t;
+      }
+    }
     return cuda_status("step");
   }
 
@@ -798,9 +846,10 @@ class Engine : public EngineBase {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     auto one = [&]() {
-      if (which <= 6) fft_pass(fft, fb, which, s);
+      if (which <= 3) fft_pass(fft, fb, which, s);
       else if (which == 7) fft_r2c(fft, fb, s);
       else if (which == 8) fft_c2r(fft, fb, s);
+      else if (which == 10 && mixed && d64[D_X]) apply_A64(d64[D_X], d64[D_R]);
       else apply_A(f[F_KP], f[F_KV]);
     };
     one();  // warm-up
@@ -814,10 +863,15 @@ class Engine : public EngineBase {
     cudaEventDestroy(e1);
     *ms = (double)t / reps;
     const double field = (double)g.nreal() * sizeof(R);
-    if (which == 3) *bytes = 2.0 * 2.0 * g.nx * g.ny * 2 * sizeof(R) * nb;  // two planes read + written
-    else if (which <= 8) *bytes = 2.0 * field * nb;  // one field in, one out, per transform or pass
+    if (which <= 8) *bytes = 2.0 * field * nb;  // one field in, one out, per transform or pass
+    else if (which == 10) *bytes = 17.0 * (double)g.nreal() * sizeof(double);
     else *bytes = 17.0 * field;                      // Ax: 8 FFTs + the permittivity read
     return cuda_status("time_kernel");
+  }
+
+  int phase_times(double *ms, int n) override {
+    for (int k = 0; k < n && k < NPH; k++) ms[k] = ph_ms[k];
+    return phase_on ? ICEP_OK : ICEP_ERR_STATE;
   }
 
   int sync() override {

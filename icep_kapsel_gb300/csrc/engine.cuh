@@ -27,10 +27,12 @@ struct EngineBase {
   virtual int sync() = 0;
   virtual cudaStream_t stream() const = 0;
   // Time `reps` back-to-back launches of one kernel group on the context's
-  // stream with CUDA events: which = 0..6 one FFT pass (fft_pass), 7 = R2C,
+  // stream with CUDA events: which = 0..3 one FFT pass (fft_pass), 7 = R2C,
   // 8 = C2R, 9 = Ax. ms: average per launch; bytes: algorithmic bytes moved
   // per launch (read + write of the fields touched, one field = N*sizeof).
   virtual int time_kernel(int which, int batch, int reps, double *ms, double *bytes) = 0;
+  // accumulated device time per step phase (ICEP_PHASE_PROFILE=1 at create)
+  virtual int phase_times(double *ms, int n) = 0;
   int ts = 0;
   double time = 0.0;
   int last_iters = 0;

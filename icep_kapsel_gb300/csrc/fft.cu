@@ -1,13 +1,22 @@
 // fft.cu -- batched 3D real FFT kernels (see fft.cuh).
 //
 // Every 1D transform is a Stockham autosort FFT with radix-8/4/2 stages held
-// in registers: a pencil of N complex values is processed by T = N/8 threads,
-// each owning one radix-8 (or two radix-4, four radix-2) butterflies per
-// stage; stages exchange data through a padded shared-memory tile [N][W+1]
-// (W pencils per block, conflict-free). Complex pencils along y and x read
-// their first stage straight from global memory and write their last stage
-// straight back (coalesced across the W adjacent pencils). The inverse is
-// conj(FFT(conj(x))), so only forward kernels and twiddles exist.
+// in registers (block_fft): a pencil of N complex values is split into N/8
+// work items per stage, each one radix-8 (or two radix-4, four radix-2)
+// butterflies; the items of all pencils a block owns are spread over its
+// threads, and stages exchange data through padded shared-memory tiles
+// (element e of pencil w at tile[e*sw + w], conflict-free). The inverse is
+// conj(FFT(conj(x))), so only forward butterflies and twiddles exist.
+//
+// A 3D transform is two passes when an x-plane fits in shared memory:
+//   forward: plane pass (z rows real->complex, then y pencils) + x pass;
+//   inverse: x pass + plane pass (y pencils, then z rows complex->real).
+// Larger planes use separate z-row and y-pencil passes. The reference's
+// treatment of the kz = 0 and kz = NZ/2 planes in its inverse (Ooura's
+// rdft3dsort reads half of each plane, the rest is implied by Hermitian
+// symmetry) is reproduced inside the inverse passes: the i-direction part on
+// the four special x pencils as they are loaded, the j-direction part on the
+// two special columns of each x-plane.
 #include <math.h>
 #include <vector>
 
@@ -25,6 +34,8 @@ template <typename R>
 __device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
   return cplx<R>{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
 }
+template <typename R>
+__device__ __forceinline__ cplx<R> cconj(cplx<R> a) { return cplx<R>{a.x, -a.y}; }
 template <typename R>
 __device__ __forceinline__ cplx<R> mul_mi(cplx<R> a) { return cplx<R>{a.y, -a.x}; }  // * (-i)
 template <typename R>
@@ -87,260 +98,389 @@ struct Plan {
   }
 };
 
-// A global pencil: element e at data[base + e*stride].
+// ---- stage sources and sinks --------------------------------------------
 template <typename R>
-struct GPencil {
-  cplx<R> *data;
-  long base;
-  long stride;
-  bool valid;
+struct SmemT {  // shared tile, element e of pencil w at t[e*sw + w]
+  cplx<R> *t;
+  int sw;
+  __device__ __forceinline__ cplx<R> load(int w, int e) const { return t[e * sw + w]; }
+  __device__ __forceinline__ void store(int w, int e, cplx<R> v) const { t[e * sw + w] = v; }
 };
 
-// One Stockham stage of radix RAD on pencil w. Ls: product of the previous
-// radices. Input index jb + q*N/RAD, twiddle exp(-2 pi i p q/(Ls RAD)),
-// output index k*Ls*RAD + p + Ls*q (jb = k*Ls + p).
-// mode bit 0: read from global (first stage), bit 1: write to global (last).
-template <typename R, int N, int RAD>
-__device__ __forceinline__ void stage(const cplx<R> *__restrict__ src, cplx<R> *__restrict__ dst, int sw, int w, int tid,
-                                      int Ls, const cplx<R> *__restrict__ tws, const GPencil<R> &gp, int mode,
+template <typename R>
+struct GPencils {  // global pencils: element e of pencil w at data[base + w*pstride + e*estride]
+  cplx<R> *data;
+  long base, pstride, estride;
+  int nvalid;
+  __device__ __forceinline__ cplx<R> load(int w, int e) const {
+    return (w < nvalid) ? data[base + w * pstride + e * estride] : cplx<R>{0, 0};
+  }
+  __device__ __forceinline__ void store(int w, int e, cplx<R> v) const {
+    if (w < nvalid) data[base + w * pstride + e * estride] = v;
+  }
+};
+
+// x pencils of the inverse transform. The pencils (j, kz) with j in {0, NY/2}
+// and kz in {0, NZ/2} get the i-direction half of the reference's Hermitian
+// completion as they are read: kz = 0 keeps i <= NX/2, kz = NZ/2 keeps
+// i > NX/2, the other entries read conj(X(NX - i)); i in {0, NX/2} keep their
+// real part. Reads come straight from global memory, and the pass writes
+// its output only after the first stage has finished everywhere.
+template <typename R>
+struct GPencilsXInv {
+  GPencils<R> g;
+  int ny, hnz, nx;
+  __device__ __forceinline__ cplx<R> load(int w, int e) const {
+    if (w >= g.nvalid) return cplx<R>{0, 0};
+    const long q = g.base + w;  // pencil index j*hnz + kz
+    const int j = (int)(q / hnz), kz = (int)(q - (long)j * hnz);
+    const cplx<R> v = g.data[q + e * g.estride];
+    if ((j == 0 || j == ny / 2) && (kz == 0 || kz == hnz - 1)) {
+      if (e == 0 || e == nx / 2) return cplx<R>{v.x, R(0)};
+      const bool kept = (kz == 0) ? (e <= nx / 2) : (e > nx / 2);
+      if (!kept) return cconj(g.data[q + (nx - e) * g.estride]);
+    }
+    return v;
+  }
+  __device__ __forceinline__ void store(int w, int e, cplx<R> v) const { g.store(w, e, v); }
+};
+
+// One Stockham stage of radix RAD over Wp pencils. Ls: product of the
+// previous radices. Item jb of pencil w reads elements jb + q*N/RAD, applies
+// twiddles exp(-2 pi i p q/(Ls RAD)), and writes k*Ls*RAD + p + Ls*q
+// (jb = k*Ls + p). Items are distributed over all threads of the block, the
+// pencil index fastest (coalesced global access for adjacent pencils).
+template <typename R, int N, int RAD, int WP, class Src, class Dst>
+__device__ __forceinline__ void stage(const Src &src, const Dst &dst, int Ls, const cplx<R> *__restrict__ tws,
                                       bool conj_in, bool conj_out) {
   constexpr int T = N / 8;
-  constexpr int NB = 8 / RAD;  // butterflies per thread
+  constexpr int NB = 8 / RAD;
+  const int nthr = blockDim.x * blockDim.y;
+  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
+  constexpr int items = WP * T;
+  for (int it = lin; it < items; it += nthr) {
+    const int w = it % WP, tid = it / WP;
 #pragma unroll
-  for (int m = 0; m < NB; m++) {
-    const int jb = tid + T * m;
-    const int p = jb & (Ls - 1);
-    const int k = jb / Ls;
-    cplx<R> v[RAD];
+    for (int m = 0; m < NB; m++) {
+      const int jb = tid + T * m;
+      const int p = jb & (Ls - 1);
+      const int k = jb / Ls;
+      cplx<R> v[RAD];
 #pragma unroll
-    for (int q = 0; q < RAD; q++) {
-      const int e = jb + q * (N / RAD);
-      cplx<R> x;
-      if (mode & 1) x = gp.valid ? gp.data[gp.base + e * gp.stride] : cplx<R>{0, 0};
-      else x = src[e * sw + w];
-      v[q] = conj_if(x, conj_in);
-    }
-    if (Ls > 1) {
-      const int step = N / (Ls * RAD);
+      for (int q = 0; q < RAD; q++) v[q] = conj_if(src.load(w, jb + q * (N / RAD)), conj_in);
+      if (Ls > 1) {
+        const int step = N / (Ls * RAD);
 #pragma unroll
-      for (int q = 1; q < RAD; q++) v[q] = cmul(v[q], tws[(p * q * step) & (N - 1)]);
-    }
-    dftr<R, RAD>(v);
-#pragma unroll
-    for (int q = 0; q < RAD; q++) {
-      const int o = k * Ls * RAD + p + Ls * q;
-      const cplx<R> y = conj_if(v[q], conj_out);
-      if (mode & 2) {
-        if (gp.valid) gp.data[gp.base + o * gp.stride] = y;
-      } else {
-        dst[o * sw + w] = y;
+        for (int q = 1; q < RAD; q++) v[q] = cmul(v[q], tws[(p * q * step) & (N - 1)]);
       }
+      dftr<R, RAD>(v);
+#pragma unroll
+      for (int q = 0; q < RAD; q++) dst.store(w, k * Ls * RAD + p + Ls * q, conj_if(v[q], conj_out));
     }
   }
 }
 
-// Full length-N transform of pencil w (every thread of the block calls it).
-// in_global/out_global select the first stage's source and the last stage's
-// sink; tiles a/b alternate. Returns the tile holding the result when the
-// last stage does not write to global memory.
-template <typename R, int N>
-__device__ cplx<R> *pencil_fft(cplx<R> *a, cplx<R> *b, int sw, int w, int tid, const cplx<R> *tws,
-                               const GPencil<R> &gp, bool in_global, bool out_global, bool inverse) {
-  cplx<R> *src = a, *dst = b;
+// Length-N transforms of Wp pencils. The first stage reads `in`, the last
+// writes `out`; intermediate stages alternate between tiles a and b (both of
+// stride sw). A __syncthreads follows every stage.
+template <typename R, int N, int WP, class In, class Out>
+__device__ __forceinline__ void block_fft(const In &in, const Out &out, cplx<R> *a, cplx<R> *b, int sw,
+                                          const cplx<R> *tws, bool inverse) {
+  SmemT<R> ta{a, sw}, tb{b, sw};
   int Ls = 1;
 #pragma unroll
   for (int s = 0; s < Plan<N>::nstages; s++) {
-    constexpr int dummy = 0;
-    (void)dummy;
     const int rad = Plan<N>::radix(s);
     const bool first = (s == 0), last = (s == Plan<N>::nstages - 1);
-    const int mode = (first && in_global ? 1 : 0) | (last && out_global ? 2 : 0);
     const bool ci = first && inverse, co = last && inverse;
-    if (rad == 8) stage<R, N, 8>(src, dst, sw, w, tid, Ls, tws, gp, mode, ci, co);
-    else if (rad == 4) stage<R, N, 4>(src, dst, sw, w, tid, Ls, tws, gp, mode, ci, co);
-    else stage<R, N, 2>(src, dst, sw, w, tid, Ls, tws, gp, mode, ci, co);
-    Ls *= rad;
-    if (!(last && out_global)) {
-      __syncthreads();
-      cplx<R> *t = src;
-      src = dst;
-      dst = t;
+    const SmemT<R> &tsrc = (s & 1) ? tb : ta;
+    const SmemT<R> &tdst = (s & 1) ? ta : tb;
+    if (first && last) {
+      if (rad == 8) stage<R, N, 8, WP>(in, out, Ls, tws, ci, co);
+    } else if (first) {
+      if (rad == 8) stage<R, N, 8, WP>(in, tb, Ls, tws, ci, co);
+      else if (rad == 4) stage<R, N, 4, WP>(in, tb, Ls, tws, ci, co);
+      else stage<R, N, 2, WP>(in, tb, Ls, tws, ci, co);
+    } else if (last) {
+      if (rad == 8) stage<R, N, 8, WP>(tsrc, out, Ls, tws, ci, co);
+      else if (rad == 4) stage<R, N, 4, WP>(tsrc, out, Ls, tws, ci, co);
+      else stage<R, N, 2, WP>(tsrc, out, Ls, tws, ci, co);
+    } else {
+      if (rad == 8) stage<R, N, 8, WP>(tsrc, tdst, Ls, tws, ci, co);
+      else if (rad == 4) stage<R, N, 4, WP>(tsrc, tdst, Ls, tws, ci, co);
+      else stage<R, N, 2, WP>(tsrc, tdst, Ls, tws, ci, co);
     }
+    Ls *= rad;
+    __syncthreads();
   }
-  return src;
 }
 
 template <typename R>
-__device__ __forceinline__ void load_twiddles(cplx<R> *tws, const cplx<R> *__restrict__ tw, int n) {
+__device__ __forceinline__ void load_table(cplx<R> *dst, const cplx<R> *__restrict__ src, int n) {
   const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  for (int q = lin; q < n; q += nthr) tws[q] = tw[q];
+  for (int q = lin; q < n; q += nthr) dst[q] = src[q];
 }
 
-// Complex FFT along y (axis 1) or x (axis 0); W pencils per block, blockDim (W, N/8).
-template <typename R, int N>
-__global__ void __launch_bounds__(1024) k_pencils(FieldBatch<R> fb, Grid g, int axis, int W, int tiles_per_row,
-                                                  const cplx<R> *__restrict__ tw, int inverse) {
+// z row split/merge of the real transform (H = NZ/2):
+//   forward  X[k] = E[k] + exp(-2 pi i k/NZ) O[k],  E, O from Z[k], conj Z[H-k]
+//   inverse  Z[k] = (X[k] + conj X[H-k]) + i exp(+2 pi i k/NZ)(X[k] - conj X[H-k])
+template <typename R>
+__device__ __forceinline__ cplx<R> split_fwd(cplx<R> z, cplx<R> c /* conj Z[H-k] */, cplx<R> pw) {
+  const R er = R(0.5) * (z.x + c.x), ei = R(0.5) * (z.y + c.y);
+  const R orr = R(0.5) * (z.y - c.y), oi = R(-0.5) * (z.x - c.x);
+  return cplx<R>{er + (pw.x * orr - pw.y * oi), ei + (pw.x * oi + pw.y * orr)};
+}
+template <typename R>
+__device__ __forceinline__ cplx<R> merge_inv(cplx<R> x, cplx<R> c /* conj X[H-k] */, cplx<R> pw) {
+  const R sr = x.x + c.x, si = x.y + c.y;
+  const R dr = x.x - c.x, di = x.y - c.y;
+  const R wr = pw.x, wi = -pw.y;  // exp(+2 pi i k/NZ)
+  const R tr = wr * dr - wi * di, ti = wr * di + wi * dr;
+  return cplx<R>{sr - ti, si + tr};
+}
+
+// ---- plane kernels (one block per x-plane and field) ---------------------
+// smem: tw_y[NY] | tw_z[H] | post[H+1] | A | B, A/B of plane_tile() complex.
+__host__ __device__ constexpr int plane_tile(int ny, int h) {
+  return (h * (ny + 1) > ny * (h + 2)) ? h * (ny + 1) : ny * (h + 2);
+}
+
+template <typename R, int NY, int H>
+__global__ void __launch_bounds__(1024) k_plane_fwd(FieldBatch<R> fb, Grid g, const cplx<R> *__restrict__ twy,
+                                                    const cplx<R> *__restrict__ twz, const cplx<R> *__restrict__ post) {
+  extern __shared__ unsigned char smem_raw[];
+  cplx<R> *sty = reinterpret_cast<cplx<R> *>(smem_raw);
+  cplx<R> *stz = sty + NY;
+  cplx<R> *spost = stz + H;
+  cplx<R> *A = spost + (H + 1);
+  cplx<R> *B = A + plane_tile(NY, H);
+  const int i = blockIdx.x;
+  R *data = fb.p[blockIdx.y];
+  const int nthr = blockDim.x * blockDim.y, lin = threadIdx.y * blockDim.x + threadIdx.x;
+  load_table(sty, twy, NY);
+  load_table(stz, twz, H);
+  load_table(spost, post, H + 1);
+  // rows j of the plane as H-point complex pencils, element-major in A
+  const R *plane = data + (long)i * NY * g.nzp;
+  constexpr int rsw = NY + 1;
+  for (int q = lin; q < NY * H; q += nthr) {
+    const int j = q / H, e = q - j * H;
+    const R *rp = plane + (long)j * g.nzp;
+    A[e * rsw + j] = cplx<R>{rp[2 * e], rp[2 * e + 1]};
+  }
+  __syncthreads();
+  // z transforms: A -> (B, ...); with an even number of stages the result is in A
+  constexpr int zst = Plan<H>::nstages;
+  cplx<R> *zres = (zst & 1) ? B : A;
+  cplx<R> *ybuf = (zst & 1) ? A : B;
+  block_fft<R, H, NY>(SmemT<R>{A, rsw}, SmemT<R>{zres, rsw}, A, B, rsw, stz, false);
+  // split into the half spectrum, y-pencil layout: element j of pencil k at ybuf[j*ysw + k]
+  constexpr int ysw = H + 2;
+  for (int q = lin; q < NY * (H + 1); q += nthr) {
+    const int j = q / (H + 1), k = q - j * (H + 1);
+    const int k1 = (k == H) ? 0 : k, k2 = (k == 0) ? 0 : H - k;
+    ybuf[j * ysw + k] = split_fwd(zres[k1 * rsw + j], cconj(zres[k2 * rsw + j]), spost[k]);
+  }
+  __syncthreads();
+  // y transforms of the H+1 columns, last stage to global (coalesced over kz)
+  GPencils<R> outp{reinterpret_cast<cplx<R> *>(data), (long)i * NY * g.hnz, 1, g.hnz, H + 1};
+  cplx<R> *other = (ybuf == A) ? B : A;
+  block_fft<R, NY, H + 1>(SmemT<R>{ybuf, ysw}, outp, ybuf, other, ysw, sty, false);
+}
+
+template <typename R, int NY, int H>
+__global__ void __launch_bounds__(1024) k_plane_inv(FieldBatch<R> fb, Grid g, const cplx<R> *__restrict__ twy,
+                                                    const cplx<R> *__restrict__ twz, const cplx<R> *__restrict__ post,
+                                                    R scale) {
+  extern __shared__ unsigned char smem_raw[];
+  cplx<R> *sty = reinterpret_cast<cplx<R> *>(smem_raw);
+  cplx<R> *stz = sty + NY;
+  cplx<R> *spost = stz + H;
+  cplx<R> *A = spost + (H + 1);
+  cplx<R> *B = A + plane_tile(NY, H);
+  const int i = blockIdx.x;
+  R *data = fb.p[blockIdx.y];
+  const cplx<R> *cplane = reinterpret_cast<const cplx<R> *>(data) + (long)i * NY * g.hnz;
+  const int nthr = blockDim.x * blockDim.y, lin = threadIdx.y * blockDim.x + threadIdx.x;
+  load_table(sty, twy, NY);
+  load_table(stz, twz, H);
+  load_table(spost, post, H + 1);
+  constexpr int ysw = H + 2;
+  for (int q = lin; q < NY * (H + 1); q += nthr) {
+    const int j = q / (H + 1), k = q - j * (H + 1);
+    A[j * ysw + k] = cplane[q];
+  }
+  __syncthreads();
+  // j-direction half of the Hermitian completion on the kz = 0 and kz = NZ/2
+  // columns: kz = 0 keeps rows 1..NY/2-1, kz = NZ/2 keeps rows NY/2+1..NY-1.
+  for (int j = 1 + lin; j < NY / 2; j += nthr) {
+    A[(NY - j) * ysw + 0] = cconj(A[j * ysw + 0]);
+    A[j * ysw + H] = cconj(A[(NY - j) * ysw + H]);
+  }
+  __syncthreads();
+  // y inverse transforms of the H+1 columns
+  constexpr int yst = Plan<NY>::nstages;
+  cplx<R> *yres = (yst & 1) ? B : A;
+  cplx<R> *zbuf = (yst & 1) ? A : B;
+  block_fft<R, NY, H + 1>(SmemT<R>{A, ysw}, SmemT<R>{yres, ysw}, A, B, ysw, sty, true);
+  // merge into H-point complex rows (element-major, pencil = row j); the
+  // imaginary parts of kz = 0 and kz = NZ/2 are ignored
+  constexpr int rsw = NY + 1;
+  for (int q = lin; q < NY * H; q += nthr) {
+    const int j = q / H, k = q - j * H;
+    cplx<R> x = yres[j * ysw + k];
+    cplx<R> c = yres[j * ysw + (H - k)];
+    if (k == 0) {
+      x.y = R(0);
+      c.y = R(0);
+    }
+    zbuf[k * rsw + j] = merge_inv(x, cconj(c), spost[k]);
+  }
+  __syncthreads();
+  constexpr int zst = Plan<H>::nstages;
+  cplx<R> *other = (zbuf == A) ? B : A;
+  cplx<R> *zres = (zst & 1) ? other : zbuf;
+  block_fft<R, H, NY>(SmemT<R>{zbuf, rsw}, SmemT<R>{zres, rsw}, zbuf, other, rsw, stz, true);
+  R *plane = data + (long)i * NY * g.nzp;
+  for (int q = lin; q < NY * (H + 1); q += nthr) {
+    const int j = q / (H + 1), m = q - j * (H + 1);
+    R *rp = plane + (long)j * g.nzp;
+    if (m < H) {
+      const cplx<R> v = zres[m * rsw + j];
+      rp[2 * m] = v.x * scale;
+      rp[2 * m + 1] = v.y * scale;
+    } else {
+      rp[2 * H] = R(0);  // padding of a real-space row
+      rp[2 * H + 1] = R(0);
+    }
+  }
+}
+
+// ---- separate passes (planes too large for shared memory) ---------------
+// x (axis 0) or y (axis 1) complex pencils, W adjacent pencils per block.
+template <typename R, int N, bool INV, int W>
+__global__ void __launch_bounds__(512) k_pencils(FieldBatch<R> fb, Grid g, int axis, int tiles_per_row,
+                                                 const cplx<R> *__restrict__ tw) {
   extern __shared__ unsigned char smem_raw[];
   const int sw = W + 1;
   cplx<R> *tws = reinterpret_cast<cplx<R> *>(smem_raw);
   cplx<R> *ta = tws + N;
   cplx<R> *tb = ta + N * sw;
-  GPencil<R> gp;
-  gp.data = reinterpret_cast<cplx<R> *>(fb.p[blockIdx.y]);
-  const int w = threadIdx.x, tid = threadIdx.y;
+  cplx<R> *data = reinterpret_cast<cplx<R> *>(fb.p[blockIdx.y]);
+  GPencils<R> gp;
+  gp.data = data;
   if (axis == 1) {
     const int i = blockIdx.x / tiles_per_row;
-    const int kz = (blockIdx.x % tiles_per_row) * W + w;
-    gp.valid = kz < g.hnz;
-    gp.base = (long)i * g.ny * g.hnz + kz;
-    gp.stride = g.hnz;
+    const int kz0 = (blockIdx.x % tiles_per_row) * W;
+    gp.base = (long)i * g.ny * g.hnz + kz0;
+    gp.pstride = 1;
+    gp.estride = g.hnz;
+    gp.nvalid = g.hnz - kz0 < W ? g.hnz - kz0 : W;
   } else {
-    const long q = (long)blockIdx.x * W + w;
-    gp.valid = q < (long)g.ny * g.hnz;
-    gp.base = q;
-    gp.stride = (long)g.ny * g.hnz;
+    const long q0 = (long)blockIdx.x * W;
+    const long nq = (long)g.ny * g.hnz;
+    gp.base = q0;
+    gp.pstride = 1;
+    gp.estride = nq;
+    gp.nvalid = (int)(nq - q0 < W ? nq - q0 : W);
   }
-  load_twiddles(tws, tw, N);
+  load_table(tws, tw, N);
   __syncthreads();
-  pencil_fft<R, N>(ta, tb, sw, w, tid, tws, gp, true, true, inverse != 0);
-}
-
-// z rows, forward: NZ reals -> NZ/2+1 complex through an H = NZ/2-point
-// complex FFT of z[m] = x[2m] + i x[2m+1] and X[k] = E[k] + exp(-2 pi i k/NZ) O[k].
-template <typename R, int H>
-__global__ void __launch_bounds__(1024) k_rows_r2c(FieldBatch<R> fb, Grid g, int W, const cplx<R> *__restrict__ tw,
-                                                   const cplx<R> *__restrict__ post) {
-  extern __shared__ unsigned char smem_raw[];
-  const int sw = W + 1;
-  cplx<R> *tws = reinterpret_cast<cplx<R> *>(smem_raw);
-  cplx<R> *ta = tws + H;
-  cplx<R> *tb = ta + H * sw;
-  R *data = fb.p[blockIdx.y];
-  const long nrows = (long)g.nx * g.ny;
-  const long row0 = (long)blockIdx.x * W;
-  const int nthr = blockDim.x * blockDim.y;
-  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
-  load_twiddles(tws, tw, H);
-  for (int q = lin; q < W * H; q += nthr) {  // row-major, coalesced
-    const int w = q / H, e = q - w * H;
-    const long row = row0 + w;
-    cplx<R> v{0, 0};
-    if (row < nrows) {
-      const R *rp = data + row * g.nzp;
-      v.x = rp[2 * e];
-      v.y = rp[2 * e + 1];
-    }
-    ta[e * sw + w] = v;
-  }
-  __syncthreads();
-  GPencil<R> gp{nullptr, 0, 0, false};
-  cplx<R> *Z = pencil_fft<R, H>(ta, tb, sw, threadIdx.x, threadIdx.y, tws, gp, false, false, false);
-  for (int q = lin; q < W * (H + 1); q += nthr) {
-    const int wr = q / (H + 1), k = q - wr * (H + 1);
-    const long row = row0 + wr;
-    if (row >= nrows) continue;
-    const int k1 = (k == H) ? 0 : k, k2 = (k == 0) ? 0 : H - k;
-    const cplx<R> z = Z[k1 * sw + wr];
-    cplx<R> c = Z[k2 * sw + wr];
-    c.y = -c.y;
-    const R er = R(0.5) * (z.x + c.x), ei = R(0.5) * (z.y + c.y);
-    const R orr = R(0.5) * (z.y - c.y), oi = R(-0.5) * (z.x - c.x);
-    const cplx<R> pw = post[k];
-    R *rp = data + row * g.nzp;
-    rp[2 * k] = er + (pw.x * orr - pw.y * oi);
-    rp[2 * k + 1] = ei + (pw.x * oi + pw.y * orr);
+  if (INV && axis == 0) {
+    GPencilsXInv<R> in{gp, g.ny, g.hnz, g.nx};
+    block_fft<R, N, W>(in, gp, ta, tb, sw, tws, true);
+  } else {
+    block_fft<R, N, W>(gp, gp, ta, tb, sw, tws, INV);
   }
 }
 
-// z rows, inverse: half spectrum -> NZ reals, scaled; the imaginary parts of
-// kz = 0 and kz = NZ/2 are ignored (as in a standard real inverse).
-template <typename R, int H>
-__global__ void __launch_bounds__(1024) k_rows_c2r(FieldBatch<R> fb, Grid g, int W, const cplx<R> *__restrict__ tw,
-                                                   const cplx<R> *__restrict__ post, R scale) {
-  extern __shared__ unsigned char smem_raw[];
-  const int sw = W + 1;
-  cplx<R> *tws = reinterpret_cast<cplx<R> *>(smem_raw);
-  cplx<R> *ta = tws + H;
-  cplx<R> *tb = ta + H * sw;
-  cplx<R> *sx = tb + H * sw;  // staged half spectrum, rows of H+1 (+1 pad)
-  const int sxw = H + 2;
-  R *data = fb.p[blockIdx.y];
-  const long nrows = (long)g.nx * g.ny;
-  const long row0 = (long)blockIdx.x * W;
-  const int nthr = blockDim.x * blockDim.y;
-  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
-  load_twiddles(tws, tw, H);
-  for (int q = lin; q < W * (H + 1); q += nthr) {
-    const int w = q / (H + 1), k = q - w * (H + 1);
-    const long row = row0 + w;
-    cplx<R> v{0, 0};
-    if (row < nrows) {
-      const R *rp = data + row * g.nzp;
-      v.x = rp[2 * k];
-      v.y = (k == 0 || k == H) ? R(0) : rp[2 * k + 1];
-    }
-    sx[w * sxw + k] = v;
-  }
-  __syncthreads();
-  for (int q = lin; q < W * H; q += nthr) {
-    const int w = q / H, k = q - w * H;
-    const cplx<R> x = sx[w * sxw + k];
-    cplx<R> c = sx[w * sxw + (H - k)];
-    c.y = -c.y;
-    const R sr = x.x + c.x, si = x.y + c.y;
-    const R dr = x.x - c.x, di = x.y - c.y;
-    const cplx<R> pw = post[k];  // exp(-2 pi i k/NZ); use its conjugate
-    const R wr = pw.x, wi = -pw.y;
-    const R tr = wr * dr - wi * di, ti = wr * di + wi * dr;
-    ta[k * sw + w] = cplx<R>{sr - ti, si + tr};
-  }
-  __syncthreads();
-  GPencil<R> gp{nullptr, 0, 0, false};
-  cplx<R> *z = pencil_fft<R, H>(ta, tb, sw, threadIdx.x, threadIdx.y, tws, gp, false, false, true);
-  for (int q = lin; q < W * H; q += nthr) {
-    const int wr = q / H, m = q - wr * H;
-    const long row = row0 + wr;
-    if (row >= nrows) continue;
-    R *rp = data + row * g.nzp;
-    const cplx<R> v = z[m * sw + wr];
-    rp[2 * m] = v.x * scale;
-    rp[2 * m + 1] = v.y * scale;
-    if (m == 0) {  // padding of a real-space row
-      rp[g.nz] = R(0);
-      rp[g.nz + 1] = R(0);
-    }
-  }
-}
-
-// Hermitian completion of the kz = 0 and kz = NZ/2 planes with the kept
-// halves of the reference's inverse (rdft3dsort, fftsg3d.c:645-667):
-// kz = 0 keeps 1 <= j <= NY/2-1 and (j in {0,NY/2}, i <= NX/2); kz = NZ/2
-// keeps the complement; self-conjugate points keep their real part.
-// Dropped entries read their (kept) mirror, kept entries are only written at
-// self-conjugate points, so the update is race-free in place.
+// j-direction half of the Hermitian completion (used with the separate
+// y pass, before it): per x-plane, columns kz = 0 and kz = NZ/2.
 template <typename R>
-__global__ void k_herm_project(FieldBatch<R> fb, Grid g) {
+__global__ void k_herm_columns(FieldBatch<R> fb, Grid g) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long plane = (long)g.nx * g.ny;
-  if (t >= 2 * plane) return;
-  const int pz = (int)(t / plane);
-  const long ij = t - pz * plane;
-  const int i = (int)(ij / g.ny), j = (int)(ij - (long)i * g.ny);
-  const int kz = pz ? g.nz / 2 : 0;
-  const int mi = (g.nx - i) % g.nx, mj = (g.ny - j) % g.ny;
-  bool kept;
-  if (j >= 1 && j <= g.ny / 2 - 1) kept = true;
-  else if (j == 0 || j == g.ny / 2) kept = (i <= g.nx / 2);
-  else kept = false;
-  if (pz) kept = !kept;
+  const int half = g.ny / 2;
+  if (t >= (long)g.nx * (half - 1)) return;
+  const int i = (int)(t / (half - 1)), j = 1 + (int)(t - (long)i * (half - 1));
+  cplx<R> *c = reinterpret_cast<cplx<R> *>(fb.p[blockIdx.y]) + (long)i * g.ny * g.hnz;
+  c[(long)(g.ny - j) * g.hnz] = cconj(c[(long)j * g.hnz]);
+  c[(long)j * g.hnz + g.hnz - 1] = cconj(c[(long)(g.ny - j) * g.hnz + g.hnz - 1]);
+}
+
+// z rows (H = NZ/2), W rows per block.
+template <typename R, int H, bool INV, int W>
+__global__ void __launch_bounds__(512) k_rows(FieldBatch<R> fb, Grid g, const cplx<R> *__restrict__ tw,
+                                              const cplx<R> *__restrict__ post, R scale) {
+  extern __shared__ unsigned char smem_raw[];
+  const int sw = W + 1;
+  cplx<R> *tws = reinterpret_cast<cplx<R> *>(smem_raw);
+  cplx<R> *spost = tws + H;
+  cplx<R> *A = spost + (H + 1);
+  cplx<R> *B = A + (H + 2) * sw;
   R *data = fb.p[blockIdx.y];
-  const long at = gidx(g, i, j, 2 * kz);
-  if (mi == i && mj == j) {
-    data[at + 1] = R(0);
-  } else if (!kept) {
-    const long m = gidx(g, mi, mj, 2 * kz);
-    data[at] = data[m];
-    data[at + 1] = -data[m + 1];
+  const long nrows = (long)g.nx * g.ny;
+  const long row0 = (long)blockIdx.x * W;
+  const int nthr = blockDim.x * blockDim.y, lin = threadIdx.y * blockDim.x + threadIdx.x;
+  load_table(tws, tw, H);
+  load_table(spost, post, H + 1);
+  constexpr int st = Plan<H>::nstages;
+  if (!INV) {
+    for (int q = lin; q < W * H; q += nthr) {
+      const int w = q / H, e = q - w * H;
+      const long row = row0 + w;
+      cplx<R> v{0, 0};
+      if (row < nrows) {
+        const R *rp = data + row * g.nzp;
+        v = cplx<R>{rp[2 * e], rp[2 * e + 1]};
+      }
+      A[e * sw + w] = v;
+    }
+    __syncthreads();
+    cplx<R> *Z = (st & 1) ? B : A;
+    block_fft<R, H, W>(SmemT<R>{A, sw}, SmemT<R>{Z, sw}, A, B, sw, tws, false);
+    for (int q = lin; q < W * (H + 1); q += nthr) {
+      const int w = q / (H + 1), k = q - w * (H + 1);
+      const long row = row0 + w;
+      if (row >= nrows) continue;
+      const int k1 = (k == H) ? 0 : k, k2 = (k == 0) ? 0 : H - k;
+      const cplx<R> x = split_fwd(Z[k1 * sw + w], cconj(Z[k2 * sw + w]), spost[k]);
+      R *rp = data + row * g.nzp;
+      rp[2 * k] = x.x;
+      rp[2 * k + 1] = x.y;
+    }
+  } else {
+    for (int q = lin; q < W * (H + 1); q += nthr) {
+      const int w = q / (H + 1), k = q - w * (H + 1);
+      const long row = row0 + w;
+      cplx<R> v{0, 0};
+      if (row < nrows) {
+        const R *rp = data + row * g.nzp;
+        v = cplx<R>{rp[2 * k], (k == 0 || k == H) ? R(0) : rp[2 * k + 1]};
+      }
+      B[k * sw + w] = v;
+    }
+    __syncthreads();
+    for (int q = lin; q < W * H; q += nthr) {
+      const int w = q / H, k = q - w * H;
+      A[k * sw + w] = merge_inv(B[k * sw + w], cconj(B[(H - k) * sw + w]), spost[k]);
+    }
+    __syncthreads();
+    cplx<R> *Z = (st & 1) ? B : A;
+    block_fft<R, H, W>(SmemT<R>{A, sw}, SmemT<R>{Z, sw}, A, B, sw, tws, true);
+    for (int q = lin; q < W * (H + 1); q += nthr) {
+      const int w = q / (H + 1), m = q - w * (H + 1);
+      const long row = row0 + w;
+      if (row >= nrows) continue;
+      R *rp = data + row * g.nzp;
+      if (m < H) {
+        const cplx<R> v = Z[m * sw + w];
+        rp[2 * m] = v.x * scale;
+        rp[2 * m + 1] = v.y * scale;
+      } else {
+        rp[2 * H] = R(0);
+        rp[2 * H + 1] = R(0);
+      }
+    }
   }
 }
 
@@ -371,22 +511,61 @@ cplx<R> *upload_table(int n, int denom, cudaStream_t s) {
   return d;
 }
 
-// ---- launch helpers (template dispatch on the transform length) ---------
+// ---- launch helpers -------------------------------------------------------
+constexpr size_t PLANE_SMEM_MAX = 200 * 1024;
+
+template <typename R>
+size_t plane_smem(int ny, int h) {
+  return ((size_t)ny + h + (h + 1) + 2 * (size_t)plane_tile(ny, h)) * sizeof(cplx<R>);
+}
 template <typename R>
 size_t pencil_smem(int n) {
-  const int W = pencil_width<R>();
-  return ((size_t)n + 2 * (size_t)n * (W + 1)) * sizeof(cplx<R>);
+  return ((size_t)n + 2 * (size_t)n * (pencil_width<R>() + 1)) * sizeof(cplx<R>);
 }
 template <typename R>
 constexpr int row_width() {
   return 2 * pencil_width<R>();
 }
 template <typename R>
-size_t row_smem(int h, bool inverse) {
-  const int W = row_width<R>();
-  size_t s = ((size_t)h + 2 * (size_t)h * (W + 1)) * sizeof(cplx<R>);
-  if (inverse) s += (size_t)W * (h + 2) * sizeof(cplx<R>);
-  return s;
+size_t row_smem(int h) {
+  return ((size_t)h + (h + 1) + 2 * (size_t)(h + 2) * (row_width<R>() + 1)) * sizeof(cplx<R>);
+}
+
+template <typename R>
+bool use_plane(const Grid &g) {
+  return g.ny <= 128 && g.nz <= 128 && plane_smem<R>(g.ny, g.nz / 2) <= PLANE_SMEM_MAX;
+}
+
+template <typename R, int NY, int H>
+void launch_plane_nh(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, cudaStream_t s) {
+  const size_t sm = plane_smem<R>(NY, H);
+  count_launch();
+  if (!inverse) {
+    k_plane_fwd<R, NY, H><<<dim3(p.g.nx, fb.n), 1024, sm, s>>>(fb, p.g, p.tw_y, p.tw_z, p.tw_post);
+  } else {
+    const R scale = (R)(1.0 / ((double)p.g.nx * p.g.ny * p.g.nz));
+    k_plane_inv<R, NY, H><<<dim3(p.g.nx, fb.n), 1024, sm, s>>>(fb, p.g, p.tw_y, p.tw_z, p.tw_post, scale);
+  }
+}
+
+template <typename R, int NY>
+void launch_plane_n(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, cudaStream_t s) {
+  switch (p.g.nz / 2) {
+    case 8: launch_plane_nh<R, NY, 8>(p, fb, inverse, s); break;
+    case 16: launch_plane_nh<R, NY, 16>(p, fb, inverse, s); break;
+    case 32: launch_plane_nh<R, NY, 32>(p, fb, inverse, s); break;
+    default: launch_plane_nh<R, NY, 64>(p, fb, inverse, s); break;
+  }
+}
+
+template <typename R>
+void launch_plane(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, cudaStream_t s) {
+  switch (p.g.ny) {
+    case 16: launch_plane_n<R, 16>(p, fb, inverse, s); break;
+    case 32: launch_plane_n<R, 32>(p, fb, inverse, s); break;
+    case 64: launch_plane_n<R, 64>(p, fb, inverse, s); break;
+    default: launch_plane_n<R, 128>(p, fb, inverse, s); break;
+  }
 }
 
 template <typename R, int N>
@@ -395,9 +574,13 @@ void launch_pencils_n(const FFTPlan<R> &p, const FieldBatch<R> &fb, int axis, bo
   constexpr int W = pencil_width<R>();
   const int tiles_per_row = (g.hnz + W - 1) / W;
   const unsigned nblk = axis == 1 ? (unsigned)(g.nx * tiles_per_row) : div_up((long)g.ny * g.hnz, W);
+  const dim3 block(W, N / 8 < 512 / W ? N / 8 : 512 / W);
   count_launch();
-  k_pencils<R, N><<<dim3(nblk, fb.n), dim3(W, N / 8), pencil_smem<R>(N), s>>>(
-      fb, g, axis, W, tiles_per_row, axis == 0 ? p.tw_x : p.tw_y, inverse ? 1 : 0);
+  const cplx<R> *tw = axis == 0 ? p.tw_x : p.tw_y;
+  if (inverse)
+    k_pencils<R, N, true, W><<<dim3(nblk, fb.n), block, pencil_smem<R>(N), s>>>(fb, g, axis, tiles_per_row, tw);
+  else
+    k_pencils<R, N, false, W><<<dim3(nblk, fb.n), block, pencil_smem<R>(N), s>>>(fb, g, axis, tiles_per_row, tw);
 }
 
 template <typename R>
@@ -416,14 +599,11 @@ void launch_rows_n(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, c
   const Grid &g = p.g;
   constexpr int W = row_width<R>();
   const dim3 grid(div_up((long)g.nx * g.ny, W), fb.n);
-  const dim3 block(W, H / 8);
+  const dim3 block(W, H / 8 < 512 / W ? H / 8 : 512 / W);
+  const R scale = (R)(1.0 / ((double)g.nx * g.ny * g.nz));
   count_launch();
-  if (!inverse) {
-    k_rows_r2c<R, H><<<grid, block, row_smem<R>(H, false), s>>>(fb, g, W, p.tw_z, p.tw_post);
-  } else {
-    const R scale = (R)(1.0 / ((double)g.nx * g.ny * g.nz));
-    k_rows_c2r<R, H><<<grid, block, row_smem<R>(H, true), s>>>(fb, g, W, p.tw_z, p.tw_post, scale);
-  }
+  if (inverse) k_rows<R, H, true, W><<<grid, block, row_smem<R>(H), s>>>(fb, g, p.tw_z, p.tw_post, scale);
+  else k_rows<R, H, false, W><<<grid, block, row_smem<R>(H), s>>>(fb, g, p.tw_z, p.tw_post, scale);
 }
 
 template <typename R>
@@ -438,20 +618,38 @@ void launch_rows(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, cud
 }
 
 template <typename R>
-void launch_herm(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s) {
-  const long n = 2L * p.g.nx * p.g.ny;
+void launch_herm_columns(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s) {
+  const long n = (long)p.g.nx * (p.g.ny / 2 - 1);
   count_launch();
-  k_herm_project<R><<<dim3(div_up(n, 256), fb.n), 256, 0, s>>>(fb, p.g);
+  k_herm_columns<R><<<dim3(div_up(n, 256), fb.n), 256, 0, s>>>(fb, p.g);
 }
 
+template <typename R, int NY, int H>
+void set_plane_attr() {
+  cudaFuncSetAttribute(k_plane_fwd<R, NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plane_smem<R>(NY, H));
+  cudaFuncSetAttribute(k_plane_inv<R, NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)plane_smem<R>(NY, H));
+}
 template <typename R, int N>
 void set_pencil_attr() {
-  cudaFuncSetAttribute(k_pencils<R, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pencil_smem<R>(N));
+  constexpr int W = pencil_width<R>();
+  cudaFuncSetAttribute(k_pencils<R, N, false, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pencil_smem<R>(N));
+  cudaFuncSetAttribute(k_pencils<R, N, true, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pencil_smem<R>(N));
 }
 template <typename R, int H>
 void set_row_attr() {
-  cudaFuncSetAttribute(k_rows_r2c<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem<R>(H, false));
-  cudaFuncSetAttribute(k_rows_c2r<R, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem<R>(H, true));
+  constexpr int W = row_width<R>();
+  cudaFuncSetAttribute(k_rows<R, H, false, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem<R>(H));
+  cudaFuncSetAttribute(k_rows<R, H, true, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem<R>(H));
+}
+
+template <typename R, int NY>
+void set_plane_attr_ny(int h) {
+  switch (h) {
+    case 8: set_plane_attr<R, NY, 8>(); break;
+    case 16: set_plane_attr<R, NY, 16>(); break;
+    case 32: set_plane_attr<R, NY, 32>(); break;
+    default: set_plane_attr<R, NY, 64>(); break;
+  }
 }
 
 }  // namespace
@@ -464,6 +662,14 @@ int fft_plan_init(FFTPlan<R> &p, const Grid &g, cudaStream_t s) {
   p.tw_z = upload_table<R>(g.nz / 2, g.nz / 2, s);
   p.tw_post = upload_table<R>(g.nz / 2 + 1, g.nz, s);
   if (!p.tw_x || !p.tw_y || !p.tw_z || !p.tw_post) return ICEP_ERR_CUDA;
+  if (use_plane<R>(g)) {
+    switch (g.ny) {
+      case 16: set_plane_attr_ny<R, 16>(g.nz / 2); break;
+      case 32: set_plane_attr_ny<R, 32>(g.nz / 2); break;
+      case 64: set_plane_attr_ny<R, 64>(g.nz / 2); break;
+      default: set_plane_attr_ny<R, 128>(g.nz / 2); break;
+    }
+  }
   set_pencil_attr<R, 16>();
   set_pencil_attr<R, 32>();
   set_pencil_attr<R, 64>();
@@ -488,29 +694,38 @@ void fft_plan_free(FFTPlan<R> &p) {
 
 template <typename R>
 void fft_r2c(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s) {
-  launch_rows(p, fb, false, s);
-  launch_pencils(p, fb, 1, false, s);
-  launch_pencils(p, fb, 0, false, s);
+  fft_pass(p, fb, 0, s);
+  fft_pass(p, fb, 1, s);
 }
 
 template <typename R>
 void fft_c2r(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s) {
-  launch_herm(p, fb, s);
-  launch_pencils(p, fb, 0, true, s);
-  launch_pencils(p, fb, 1, true, s);
-  launch_rows(p, fb, true, s);
+  fft_pass(p, fb, 2, s);
+  fft_pass(p, fb, 3, s);
 }
 
 template <typename R>
 void fft_pass(const FFTPlan<R> &p, const FieldBatch<R> &fb, int pass, cudaStream_t s) {
+  const bool plane = use_plane<R>(p.g);
   switch (pass) {
-    case 0: launch_rows(p, fb, false, s); break;
-    case 1: launch_pencils(p, fb, 1, false, s); break;
-    case 2: launch_pencils(p, fb, 0, false, s); break;
-    case 3: launch_herm(p, fb, s); break;
-    case 4: launch_pencils(p, fb, 0, true, s); break;
-    case 5: launch_pencils(p, fb, 1, true, s); break;
-    default: launch_rows(p, fb, true, s); break;
+    case 0:  // z rows + y pencils, forward
+      if (plane) {
+        launch_plane(p, fb, false, s);
+      } else {
+        launch_rows(p, fb, false, s);
+        launch_pencils(p, fb, 1, false, s);
+      }
+      break;
+    case 1: launch_pencils(p, fb, 0, false, s); break;  // x pencils, forward
+    case 2: launch_pencils(p, fb, 0, true, s); break;   // x pencils, inverse
+    default:                                            // y pencils + z rows, inverse
+      if (plane) {
+        launch_plane(p, fb, true, s);
+      } else {
+        launch_herm_columns(p, fb, s);
+        launch_pencils(p, fb, 1, true, s);
+        launch_rows(p, fb, true, s);
+      }
   }
 }
 

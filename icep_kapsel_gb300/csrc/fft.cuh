@@ -34,9 +34,9 @@ void fft_r2c(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s);
 template <typename R>
 void fft_c2r(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s);
 
-// Single passes of the 3D transforms, for timing: 0 = z rows forward,
-// 1 = y pencils forward, 2 = x pencils forward, 3 = Hermitian completion,
-// 4 = x pencils inverse, 5 = y pencils inverse, 6 = z rows inverse.
+// Single passes of the 3D transforms: 0 = z rows + y pencils forward (one
+// plane kernel when an x-plane fits in shared memory), 1 = x pencils forward,
+// 2 = x pencils inverse, 3 = y pencils + z rows inverse.
 template <typename R>
 void fft_pass(const FFTPlan<R> &p, const FieldBatch<R> &fb, int pass, cudaStream_t s);
 

@@ -175,6 +175,10 @@ int icep_step_timed(icep_ctx *c, int nsteps, double *ms) {
   *ms = (double)t;
   return wrap(c, st);
 }
+int icep_phase_times(icep_ctx *c, double *ms, int n) {
+  if (!ok(c) || !ms) return ICEP_ERR_ARG;
+  return wrap(c, c->e->phase_times(ms, n));
+}
 unsigned long long icep_kernel_launches(void) { return __atomic_load_n(&icep::g_kernel_launches, __ATOMIC_RELAXED); }
 int icep_pin_host(void *p, size_t bytes) {
   return (p && cudaHostRegister(p, bytes, cudaHostRegisterDefault) == cudaSuccess) ? ICEP_OK : ICEP_ERR_CUDA;

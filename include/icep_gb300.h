@@ -148,14 +148,23 @@ int icep_call(icep_ctx *ctx, int fn);
 
 /* ---- measurement helpers (no reference counterpart) --------------------- */
 /* Average device time of `reps` launches of one kernel group on the
- * context's stream (CUDA events): which 0..6 = one pass of the 3D FFT (z rows
- * forward, y forward, x forward, Hermitian completion, x inverse, y inverse,
- * z rows inverse), 7 = forward 3D FFT, 8 = inverse 3D FFT, 9 = Ax. batch:
- * fields per launch (1..5). bytes: algorithmic bytes per launch. */
+ * context's stream (CUDA events): which 0..3 = one pass of the 3D FFT
+ * (0: z rows + y pencils forward, 1: x pencils forward, 2: x pencils inverse,
+ * 3: y pencils + z rows inverse), 7 = forward 3D FFT, 8 = inverse 3D FFT,
+ * 9 = Ax. batch: fields per launch (1..5). bytes: algorithmic bytes per
+ * launch (one field read and written per transform or pass). */
 int icep_time_kernel(icep_ctx *ctx, int which, int batch, int reps, double *ms, double *bytes);
 /* icep_step with CUDA events recorded on the context's stream around it;
  * ms receives the device time of the nsteps steps. */
 int icep_step_timed(icep_ctx *ctx, int nsteps, double *ms);
+/* Device time accumulated per phase of the step when the context was
+ * created with the environment variable ICEP_PHASE_PROFILE=1 (events at
+ * phase boundaries): 0 fluid/solute update, 1 velocity + particle positions
+ * + profile, 2 hydrodynamic force + permittivity + free charge, 3 Poisson
+ * solve, 4 Maxwell stress, 5 Maxwell force on the fluid + projection,
+ * 6 particle forces and velocities, 7 rigidity force, 8 back to vorticity,
+ * 9 unused. Returns ICEP_ERR_STATE when profiling is off. */
+int icep_phase_times(icep_ctx *ctx, double *ms, int n);
 /* Kernels launched by this library so far (all contexts). */
 unsigned long long icep_kernel_launches(void);
 /* Page-lock / release a caller's host buffer for the drop-in transfers. */

@@ -13,6 +13,7 @@
 #include "engine.cuh"
 #include "fields.cuh"
 #include "krylov.cuh"
+#include "kspace.cuh"
 
 namespace icep {
 
@@ -451,6 +452,86 @@ class Engine : public EngineBase {
     return ICEP_OK;
   }
 
+  // B = A M^-1 on a k-space vector p into v (the k-space form of A applied
+  // to the preconditioned direction; 6 FFTs)
+  void apply_B(const R *p, R *v, double eps_ref) {
+    kgrad_pre<R>(g, p, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], eps_ref, s);
+    c2r(f[F_WV3_0], f[F_WV3_1], f[F_WV3_2]);
+    eps_face_mul<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EPS], s);
+    r2c(f[F_WV3_0], f[F_WV3_1], f[F_WV3_2]);
+    kdiv_post<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], v, s);
+    matvecs++;
+  }
+
+  /*
+   * Right-preconditioned BiCGSTAB held in k-space, from a zero guess: solves
+   * A x = b (b: real field in F_KB, its mean removed) and leaves x in F_KX.
+   * Same iteration as bicgstab(spectral = true) in exact arithmetic (the
+   * vectors are the transforms of the real-space ones and the dot products
+   * agree by Parseval), with the preconditioner folded into the operator, so
+   * an iteration costs 12 FFTs instead of 20. Stops on the recursive
+   * residual; the caller checks the true residual.
+   */
+  int bicgstab_k(double tol, int maxit, double eps_ref, int *iters, double *rel_err) {
+    R *r = f[F_KR], *r0 = f[F_KR0], *p = f[F_KP], *v = f[F_KV];
+    R *sv = f[F_KS], *t = f[F_KT], *xt = f[F_KY];
+    copy_real<R>(g, f[F_KB], r, s);
+    r2c(r);
+    cudaMemsetAsync(r, 0, 2 * sizeof(R), s);  // k = 0: the mean
+    cudaMemcpyAsync(r0, r, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+    kdots<R>(g, r, r, r, r, 1, partials, scal, S_RR, s);
+    int st = read_scal();
+    if (st) return st;
+    const double bsq = hscal[S_RR];
+    zero(F_KY);
+    if (!(bsq > 0.0)) {
+      zero(F_KX);
+      *iters = 0;
+      *rel_err = 0.0;
+      return ICEP_OK;
+    }
+    zero(F_KV);
+    zero(F_KP);
+    double rho = 1, alpha = 1, w = 1;
+    const double tol2 = tol * tol * bsq, eps2 = DBL_EPSILON * DBL_EPSILON;
+    double r0sq = bsq, rr = bsq, rho_new = bsq;
+    int i = 0;
+    while (i < maxit && rr > tol2) {
+      const double rho_old = rho;
+      rho = rho_new;
+      if (fabs(rho) < eps2 * r0sq) {  // restart on the current residual
+        cudaMemcpyAsync(r0, r, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+        rho = r0sq = rr;
+        zero(F_KV);
+        zero(F_KP);
+        alpha = w = 1;
+        if (!(rho > 0.0)) break;
+        rho_new = rho;
+      }
+      const double beta = (rho / rho_old) * (alpha / w);
+      kbicg_p<R>(g, p, r, v, beta, w, s);
+      apply_B(p, v, eps_ref);
+      kdots<R>(g, r0, v, r0, v, 1, partials, scal, S_R0V, s);
+      kbicg_s<R>(g, sv, r, v, rho, scal, s);
+      apply_B(sv, t, eps_ref);
+      kdots<R>(g, t, t, t, sv, 2, partials, scal, S_TT, s);
+      kbicg_xr<R>(g, xt, r, p, sv, t, rho, scal, s);
+      kdots<R>(g, r0, r, r, r, 2, partials, scal, S_R0R, s);
+      if ((st = read_scal())) return st;
+      alpha = rho / hscal[S_R0V];
+      w = (hscal[S_TT] > 0.0) ? hscal[S_TS] / hscal[S_TT] : 0.0;
+      rho_new = hscal[S_R0R];
+      rr = hscal[S_RR];
+      ++i;
+      if (!std::isfinite(rr)) break;
+    }
+    kprecond<R>(g, xt, f[F_KX], eps_ref, s);
+    c2r(f[F_KX]);
+    *iters = i;
+    *rel_err = sqrt(rr / bsq);
+    return ICEP_OK;
+  }
+
   double mean_eps() {
     sum_real<R>(g, f[F_EPS], partials, scal, S_AUX1, s);
     if (read_scal()) return 1.0;
@@ -522,7 +603,7 @@ class Engine : public EngineBase {
         if (inner_tol > 0.5) inner_tol = 0.5;
         int it = 0;
         double er = 0.0;
-        if ((st = bicgstab(inner_tol, P.potential_iter, true, eref, &it, &er))) return st;
+        if ((st = bicgstab_k(inner_tol, P.potential_iter, eref, &it, &er))) return st;
         total_inner += it;
         add_f2d(G, (const float *)f[F_KX], d64[D_X], rn, s);
       }

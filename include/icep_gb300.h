@@ -115,6 +115,27 @@ int icep_Calc_f_Lennard_Jones(icep_ctx *ctx);
 /* The neighbour visits of the linked-cell scan: pairs (i, j), i > j, one
  * entry per visit. *n_pairs receives the total (may exceed max_pairs). */
 int icep_lj_pairs(icep_ctx *ctx, int *pairs, int max_pairs, int *n_pairs);
+/* Calc_f_Lennard_Jones on a caller-owned device array of n_particles
+ * icep_particle (positions x in [0, L)), allocating nothing: no counterpart
+ * in the reference, whose force routine (md_force.cxx:16-171) runs on host
+ * arrays. Needs no context: the Lennard-Jones constants come from params
+ * (mesh, DX, A, LJ_epsilon, LJ_powers, LJ_truncate) and fr of every particle
+ * is overwritten with its Lennard-Jones force, the same values
+ * icep_Calc_f_Lennard_Jones gives. For callers that hold their particles in
+ * their own device memory and may not allocate during a step (a fixed device
+ * memory budget, or no device-wide synchronisation from cudaMalloc/cudaFree
+ * allowed mid-step). Work is queued on stream (cudaStream_t as void*; NULL:
+ * the default stream) and the call does not wait for it.
+ * Cell-list scratch is one fixed device array per device, shared by every
+ * call: calls that may overlap in time race on it and must be serialised by
+ * the caller. The first call on each device looks the array up
+ * (cudaGetSymbolAddress, which may initialise the CUDA runtime); make that
+ * first call before any stream capture. At most
+ * ICEP_LJ_NOALLOC_MAX_PARTICLES particles and meshes up to 256^3; larger
+ * inputs return ICEP_ERR_UNSUPPORTED with a message on stderr. */
+#define ICEP_LJ_NOALLOC_MAX_PARTICLES 65536
+int icep_Calc_f_Lennard_Jones_noalloc(const icep_params *params, icep_particle *d_particles, int n_particles,
+                                      void *stream);
 /* MD_solver_position_Euler/_AB2 (particle_solver.cxx:39-91) */
 int icep_MD_solver_position(icep_ctx *ctx, int ab2);
 /* MD_solver_velocity_Euler/_AB2_hydro (particle_solver.cxx:109-150, 252-295) */

@@ -39,6 +39,10 @@ struct Grid {
   int trn[3];      // 2/3-rule limits (N+2)/3
   double wave[3];  // 2 pi / L
   double dx;
+  // staggered-grid shifts exp(i dx k_d / 2) as (cos, sin), indexed by the
+  // wavenumber index along axis d (i, j or kz); FP64 and FP32 copies
+  const double2 *shd[3];
+  const float2 *shf[3];
   __host__ __device__ long nf() const { return (long)nx * ny * nzp; }
   __host__ __device__ long nreal() const { return (long)nx * ny * nz; }
   __host__ __device__ long nmodes() const { return (long)nx * ny * hnz; }
@@ -53,6 +57,35 @@ __host__ __device__ inline bool in_two_third(const Grid &g, int i, int j, int kz
   int ax = (i <= g.nx / 2) ? i : g.nx - i;
   int ay = (j <= g.ny / 2) ? j : g.ny - j;
   return ax < g.trn[0] && ay < g.trn[1] && kz < g.trn[2];
+}
+
+__device__ __forceinline__ void shift_of(const Grid &g, int d, int idx, double &c, double &s) {
+  const double2 v = g.shd[d][idx];
+  c = v.x;
+  s = v.y;
+}
+__device__ __forceinline__ void shift_of(const Grid &g, int d, int idx, float &c, float &s) {
+  const float2 v = g.shf[d][idx];
+  c = v.x;
+  s = v.y;
+}
+
+// Weight of k-space mode (i, j, kz) in a real-space inner product taken by
+// Parseval over the half spectrum: 0 for the kz = 0 / NZ/2 entries the
+// reference's inverse FFT does not read (their values follow by Hermitian
+// symmetry), 1 at self-conjugate points (only the real part is read), 2 for
+// every other mode.
+__host__ __device__ inline int read_weight(const Grid &g, int i, int j, int kz) {
+  const int h = g.nz / 2;
+  if (kz != 0 && kz != h) return 2;
+  const int mi = (g.nx - i) % g.nx, mj = (g.ny - j) % g.ny;
+  if (mi == i && mj == j) return 1;
+  bool kept;
+  if (j >= 1 && j <= g.ny / 2 - 1) kept = true;
+  else if (j == 0 || j == g.ny / 2) kept = (i <= g.nx / 2);
+  else kept = false;
+  if (kz == h) kept = !kept;
+  return kept ? 2 : 0;
 }
 
 inline unsigned div_up(long a, long b) { return (unsigned)((a + b - 1) / b); }
@@ -70,6 +103,8 @@ enum FieldId {
   F_WV1, F_WV3_0, F_WV3_1, F_WV3_2,
   // Krylov work vectors (padded fields)
   F_KR, F_KR0, F_KP, F_KV, F_KS, F_KT, F_KX, F_KB, F_KY, F_KZ,
+  // face permittivities of the fused k-space operator
+  F_EF0, F_EF1, F_EF2,
   F_COUNT
 };
 

@@ -13,7 +13,9 @@
 #include "engine.cuh"
 #include "fields.cuh"
 #include "krylov.cuh"
+#include "kop.cuh"
 #include "kspace.cuh"
+#include <type_traits>
 
 namespace icep {
 
@@ -40,6 +42,10 @@ class Engine : public EngineBase {
   double *e_ext_n = nullptr; // device double[3]: E_ext * NX*NY*NZ
   double *partials = nullptr;
   double *scal = nullptr;
+  void *shift_tab = nullptr;  // staggered-shift tables referenced by g
+  double *kpart = nullptr;    // dot partials of the fused k-space iteration
+  double *hkpart = nullptr;   // pinned
+  int kop_npb = 0;
   double *hscal = nullptr;  // pinned
   int *ljwork = nullptr;
   int ljwork_ints = 0;
@@ -78,6 +84,9 @@ class Engine : public EngineBase {
     cudaFree(e_ext_n);
     cudaFree(partials);
     cudaFree(scal);
+    cudaFree(shift_tab);
+    cudaFree(kpart);
+    cudaFreeHost(hkpart);
     cudaFreeHost(hscal);
     cudaFree(ljwork);
     cudaFree(dpairs_n);
@@ -125,6 +134,9 @@ class Engine : public EngineBase {
       g.wave[d] = 2.0 * M_PI / (N[d] * p.dx);
     }
     g.dx = p.dx;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+      return fail(ICEP_ERR_CUDA, "cudaStreamCreate failed (no GPU?)");
+    if (make_shift_tables() != ICEP_OK) return fail(ICEP_ERR_CUDA, "shift tables");
     radius = p.a * p.dx;
     xi = p.a_xi * p.dx;
     hxi = 0.5 * xi;
@@ -133,8 +145,6 @@ class Engine : public EngineBase {
     valency_e[1] = p.valency_neg * p.elementary_charge;
     onsager[0] = p.onsager_pos;
     onsager[1] = p.onsager_neg;
-    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
-      return fail(ICEP_ERR_CUDA, "cudaStreamCreate failed (no GPU?)");
     const size_t fb = sizeof(R) * g.nf();
     for (int i = 0; i < F_COUNT; i++) {
       if (cudaMalloc(&f[i], fb) != cudaSuccess) return fail(ICEP_ERR_CUDA, "cudaMalloc of fields failed");
@@ -234,6 +244,12 @@ class Engine : public EngineBase {
       cudaStreamSynchronize(s);
     }
     cudaMalloc(&partials, sizeof(double) * 2 * DOT_BLOCKS);
+    if (mixed && electrolyte && kop_supported(g)) {
+      kop_npb = kop_pencil_blocks(g);
+      const size_t nk = 2 * (2 * (size_t)kop_npb + DOT_BLOCKS);
+      if (cudaMalloc(&kpart, sizeof(double) * nk) != cudaSuccess || cudaMallocHost(&hkpart, sizeof(double) * nk) != cudaSuccess)
+        return fail(ICEP_ERR_CUDA, "allocation of the k-space dot partials failed");
+    }
     cudaMalloc(&scal, sizeof(double) * S_COUNT);
     cudaMemsetAsync(scal, 0, sizeof(double) * S_COUNT, s);
     cudaMallocHost(&hscal, sizeof(double) * S_COUNT);
@@ -248,6 +264,41 @@ class Engine : public EngineBase {
     }
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("setup");
     return cuda_status("setup");
+  }
+
+  // exp(i dx k_d / 2) per wavenumber index, the staggered shifts of the
+  // reference's Shift_* tables (fft_wrapper.h:841-900), computed in FP64 on
+  // the host; the FP32 copy is the rounded FP64 value
+  int make_shift_tables() {
+    const int n[3] = {g.nx, g.ny, g.hnz};
+    const int tot = n[0] + n[1] + n[2];
+    std::vector<double> hd(2 * (size_t)tot);
+    std::vector<float> hf(2 * (size_t)tot);
+    int off = 0;
+    for (int d = 0; d < 3; d++)
+      for (int q = 0; q < n[d]; q++, off++) {
+        const int kint = (d == 0) ? kx_of(g, q) : (d == 1) ? ky_of(g, q) : q;
+        const double a = 0.5 * g.dx * g.wave[d] * kint;
+        hd[2 * off] = cos(a);
+        hd[2 * off + 1] = sin(a);
+        hf[2 * off] = (float)hd[2 * off];
+        hf[2 * off + 1] = (float)hd[2 * off + 1];
+      }
+    const size_t bd = sizeof(double) * hd.size(), bf = sizeof(float) * hf.size();
+    if (cudaMalloc(&shift_tab, bd + bf) != cudaSuccess) return ICEP_ERR_CUDA;
+    char *base = static_cast<char *>(shift_tab);
+    cudaMemcpyAsync(base, hd.data(), bd, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(base + bd, hf.data(), bf, cudaMemcpyHostToDevice, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return ICEP_ERR_CUDA;
+    const double2 *dd = reinterpret_cast<const double2 *>(base);
+    const float2 *ff = reinterpret_cast<const float2 *>(base + bd);
+    g.shd[0] = dd;
+    g.shd[1] = dd + n[0];
+    g.shd[2] = dd + n[0] + n[1];
+    g.shf[0] = ff;
+    g.shf[1] = ff + n[0];
+    g.shf[2] = ff + n[0] + n[1];
+    return ICEP_OK;
   }
 
   // ---------------------------------------------------------------- helpers
@@ -532,6 +583,92 @@ class Engine : public EngineBase {
     return ICEP_OK;
   }
 
+  /*
+   * bicgstab_k with the operator and the vector updates fused into FFT
+   * passes (kop.cuh): per iteration 3 passes per operator application plus
+   * one update kernel, one host synchronisation. FP32 engine on grids whose
+   * x-planes fit in shared memory.
+   */
+  int bicgstab_kf(double tol, int maxit, double eps_ref, int *iters, double *rel_err) {
+    if constexpr (!std::is_same<R, float>::value) {
+      return bicgstab_k(tol, maxit, eps_ref, iters, rel_err);
+    } else {
+      float *r = f[F_KR], *r0 = f[F_KR0], *p = f[F_KP], *v = f[F_KV];
+      float *sv = f[F_KS], *t = f[F_KT], *xt = f[F_KY];
+      float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2];
+      const int nb = kop_npb;
+      double *P1 = kpart, *P2 = kpart + 2 * nb, *P3 = kpart + 4 * nb;
+      const size_t nk = 2 * (2 * (size_t)nb + DOT_BLOCKS);
+      copy_real<R>(g, f[F_KB], r, s);
+      r2c(r);
+      cudaMemsetAsync(r, 0, 2 * sizeof(R), s);  // k = 0: the mean
+      cudaMemcpyAsync(r0, r, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+      kdots<R>(g, r, r, r, r, 1, partials, scal, S_RR, s);
+      int st = read_scal();
+      if (st) return st;
+      const double bsq = hscal[S_RR];
+      zero(F_KY);
+      if (!(bsq > 0.0)) {
+        zero(F_KX);
+        *iters = 0;
+        *rel_err = 0.0;
+        return ICEP_OK;
+      }
+      zero(F_KV);
+      zero(F_KP);
+      kop_eps_faces(g, f[F_EPS], f[F_EF0], f[F_EF1], f[F_EF2], s);
+      double rho = 1, alpha = 1, w = 1;
+      const double tol2 = tol * tol * bsq, eps2 = DBL_EPSILON * DBL_EPSILON;
+      double r0sq = bsq, rr = bsq, rho_new = bsq;
+      int i = 0;
+      while (i < maxit && rr > tol2) {
+        const double rho_old = rho;
+        rho = rho_new;
+        if (fabs(rho) < eps2 * r0sq) {  // restart on the current residual
+          cudaMemcpyAsync(r0, r, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+          rho = r0sq = rr;
+          zero(F_KV);
+          zero(F_KP);
+          alpha = w = 1;
+          if (!(rho > 0.0)) break;
+          rho_new = rho;
+        }
+        const double beta = (rho / rho_old) * (alpha / w);
+        kop_xinv(fft, KOP_P, p, r, v, beta, w, 0.0, nullptr, 0, eps_ref, w0, w1, w2, s);
+        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], s);
+        kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, s);
+        kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, rho, P1, nb, eps_ref, w0, w1, w2, s);
+        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], s);
+        kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, s);
+        kop_xr(g, xt, r, p, sv, t, r0, rho, P1, P2, nb, P3, s);
+        matvecs += 2;
+        cudaMemcpyAsync(hkpart, kpart, sizeof(double) * nk, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fused k-space iteration");
+        double r0v = 0, tt = 0, ts = 0, r0r = 0;
+        rr = 0;
+        for (int b = 0; b < nb; b++) {
+          r0v += hkpart[2 * b];
+          tt += hkpart[2 * nb + 2 * b];
+          ts += hkpart[2 * nb + 2 * b + 1];
+        }
+        for (int b = 0; b < DOT_BLOCKS; b++) {
+          r0r += hkpart[4 * nb + 2 * b];
+          rr += hkpart[4 * nb + 2 * b + 1];
+        }
+        alpha = rho / r0v;
+        w = (tt > 0.0) ? ts / tt : 0.0;
+        rho_new = r0r;
+        ++i;
+        if (!std::isfinite(rr)) break;
+      }
+      kprecond<R>(g, xt, f[F_KX], eps_ref, s);
+      c2r(f[F_KX]);
+      *iters = i;
+      *rel_err = sqrt(rr / bsq);
+      return ICEP_OK;
+    }
+  }
+
   double mean_eps() {
     sum_real<R>(g, f[F_EPS], partials, scal, S_AUX1, s);
     if (read_scal()) return 1.0;
@@ -603,7 +740,9 @@ class Engine : public EngineBase {
         if (inner_tol > 0.5) inner_tol = 0.5;
         int it = 0;
         double er = 0.0;
-        if ((st = bicgstab_k(inner_tol, P.potential_iter, eref, &it, &er))) return st;
+        if ((st = kpart ? bicgstab_kf(inner_tol, P.potential_iter, eref, &it, &er)
+                        : bicgstab_k(inner_tol, P.potential_iter, eref, &it, &er)))
+          return st;
         total_inner += it;
         add_f2d(G, (const float *)f[F_KX], d64[D_X], rn, s);
       }

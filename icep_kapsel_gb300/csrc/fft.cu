@@ -1,12 +1,6 @@
 // fft.cu -- batched 3D real FFT kernels (see fft.cuh).
 //
-// Every 1D transform is a Stockham autosort FFT with radix-8/4/2 stages held
-// in registers (block_fft): a pencil of N complex values is split into N/8
-// work items per stage, each one radix-8 (or two radix-4, four radix-2)
-// butterflies; the items of all pencils a block owns are spread over its
-// threads, and stages exchange data through padded shared-memory tiles
-// (element e of pencil w at tile[e*sw + w], conflict-free). The inverse is
-// conj(FFT(conj(x))), so only forward butterflies and twiddles exist.
+// The 1D transforms and the x-plane cores are in fft_blocks.cuh.
 //
 // A 3D transform is two passes when an x-plane fits in shared memory:
 //   forward: plane pass (z rows real->complex, then y pencils) + x pass;
@@ -21,230 +15,13 @@
 #include <vector>
 
 #include "fft.cuh"
+#include "fft_blocks.cuh"
 
 namespace icep {
 
 namespace {
 
-template <typename R>
-__device__ __forceinline__ cplx<R> cadd(cplx<R> a, cplx<R> b) { return cplx<R>{a.x + b.x, a.y + b.y}; }
-template <typename R>
-__device__ __forceinline__ cplx<R> csub(cplx<R> a, cplx<R> b) { return cplx<R>{a.x - b.x, a.y - b.y}; }
-template <typename R>
-__device__ __forceinline__ cplx<R> cmul(cplx<R> a, cplx<R> b) {
-  return cplx<R>{a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x};
-}
-template <typename R>
-__device__ __forceinline__ cplx<R> cconj(cplx<R> a) { return cplx<R>{a.x, -a.y}; }
-template <typename R>
-__device__ __forceinline__ cplx<R> mul_mi(cplx<R> a) { return cplx<R>{a.y, -a.x}; }  // * (-i)
-template <typename R>
-__device__ __forceinline__ cplx<R> conj_if(cplx<R> a, bool c) { return c ? cplx<R>{a.x, -a.y} : a; }
-
-// In-register DFTs, forward kernel exp(-2 pi i nk / r), natural order.
-template <typename R>
-__device__ __forceinline__ void dft2(cplx<R> *v) {
-  const cplx<R> a = v[0];
-  v[0] = cadd(a, v[1]);
-  v[1] = csub(a, v[1]);
-}
-template <typename R>
-__device__ __forceinline__ void dft4(cplx<R> *v) {
-  const cplx<R> a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
-  const cplx<R> a2 = cadd(v[1], v[3]), a3 = mul_mi(csub(v[1], v[3]));
-  v[0] = cadd(a0, a2);
-  v[2] = csub(a0, a2);
-  v[1] = cadd(a1, a3);
-  v[3] = csub(a1, a3);
-}
-template <typename R>
-__device__ __forceinline__ void dft8(cplx<R> *v) {
-  cplx<R> e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
-  dft4(e);
-  dft4(o);
-  const R h = (R)0.70710678118654752440084436210484903928;
-  // W8^1 = (1 - i)/sqrt2, W8^2 = -i, W8^3 = -(1 + i)/sqrt2
-  const cplx<R> t1 = cplx<R>{h * (o[1].x + o[1].y), h * (o[1].y - o[1].x)};
-  const cplx<R> t2 = mul_mi(o[2]);
-  const cplx<R> t3 = cplx<R>{h * (o[3].y - o[3].x), -h * (o[3].x + o[3].y)};
-  v[0] = cadd(e[0], o[0]);
-  v[4] = csub(e[0], o[0]);
-  v[1] = cadd(e[1], t1);
-  v[5] = csub(e[1], t1);
-  v[2] = cadd(e[2], t2);
-  v[6] = csub(e[2], t2);
-  v[3] = cadd(e[3], t3);
-  v[7] = csub(e[3], t3);
-}
-template <typename R, int RAD>
-__device__ __forceinline__ void dftr(cplx<R> *v) {
-  if (RAD == 8) dft8(v);
-  else if (RAD == 4) dft4(v);
-  else dft2(v);
-}
-
-// Radix of stage s for a length-N transform: radix-8 stages first, then the
-// remainder (N = 8: 8; 16: 8,2; 32: 8,4; 64: 8,8; 128: 8,8,2; 256: 8,8,4).
-template <int N>
-struct Plan {
-  static constexpr int nstages = (N == 8) ? 1 : (N <= 64) ? 2 : 3;
-  __host__ __device__ static constexpr int radix(int s) {
-    return (N == 8) ? 8
-         : (N == 16) ? (s == 0 ? 8 : 2)
-         : (N == 32) ? (s == 0 ? 8 : 4)
-         : (N == 64) ? 8
-         : (N == 128) ? (s < 2 ? 8 : 2)
-         : (s < 2 ? 8 : 4);
-  }
-};
-
-// ---- stage sources and sinks --------------------------------------------
-template <typename R>
-struct SmemT {  // shared tile, element e of pencil w at t[e*sw + w]
-  cplx<R> *t;
-  int sw;
-  __device__ __forceinline__ cplx<R> load(int w, int e) const { return t[e * sw + w]; }
-  __device__ __forceinline__ void store(int w, int e, cplx<R> v) const { t[e * sw + w] = v; }
-};
-
-template <typename R>
-struct GPencils {  // global pencils: element e of pencil w at data[base + w*pstride + e*estride]
-  cplx<R> *data;
-  long base, pstride, estride;
-  int nvalid;
-  __device__ __forceinline__ cplx<R> load(int w, int e) const {
-    return (w < nvalid) ? data[base + w * pstride + e * estride] : cplx<R>{0, 0};
-  }
-  __device__ __forceinline__ void store(int w, int e, cplx<R> v) const {
-    if (w < nvalid) data[base + w * pstride + e * estride] = v;
-  }
-};
-
-// x pencils of the inverse transform. The pencils (j, kz) with j in {0, NY/2}
-// and kz in {0, NZ/2} get the i-direction half of the reference's Hermitian
-// completion as they are read: kz = 0 keeps i <= NX/2, kz = NZ/2 keeps
-// i > NX/2, the other entries read conj(X(NX - i)); i in {0, NX/2} keep their
-// real part. Reads come straight from global memory, and the pass writes
-// its output only after the first stage has finished everywhere.
-template <typename R>
-struct GPencilsXInv {
-  GPencils<R> g;
-  int ny, hnz, nx;
-  __device__ __forceinline__ cplx<R> load(int w, int e) const {
-    if (w >= g.nvalid) return cplx<R>{0, 0};
-    const long q = g.base + w;  // pencil index j*hnz + kz
-    const int j = (int)(q / hnz), kz = (int)(q - (long)j * hnz);
-    const cplx<R> v = g.data[q + e * g.estride];
-    if ((j == 0 || j == ny / 2) && (kz == 0 || kz == hnz - 1)) {
-      if (e == 0 || e == nx / 2) return cplx<R>{v.x, R(0)};
-      const bool kept = (kz == 0) ? (e <= nx / 2) : (e > nx / 2);
-      if (!kept) return cconj(g.data[q + (nx - e) * g.estride]);
-    }
-    return v;
-  }
-  __device__ __forceinline__ void store(int w, int e, cplx<R> v) const { g.store(w, e, v); }
-};
-
-// One Stockham stage of radix RAD over Wp pencils. Ls: product of the
-// previous radices. Item jb of pencil w reads elements jb + q*N/RAD, applies
-// twiddles exp(-2 pi i p q/(Ls RAD)), and writes k*Ls*RAD + p + Ls*q
-// (jb = k*Ls + p). Items are distributed over all threads of the block, the
-// pencil index fastest (coalesced global access for adjacent pencils).
-template <typename R, int N, int RAD, int WP, class Src, class Dst>
-__device__ __forceinline__ void stage(const Src &src, const Dst &dst, int Ls, const cplx<R> *__restrict__ tws,
-                                      bool conj_in, bool conj_out) {
-  constexpr int T = N / 8;
-  constexpr int NB = 8 / RAD;
-  const int nthr = blockDim.x * blockDim.y;
-  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
-  constexpr int items = WP * T;
-  for (int it = lin; it < items; it += nthr) {
-    const int w = it % WP, tid = it / WP;
-#pragma unroll
-    for (int m = 0; m < NB; m++) {
-      const int jb = tid + T * m;
-      const int p = jb & (Ls - 1);
-      const int k = jb / Ls;
-      cplx<R> v[RAD];
-#pragma unroll
-      for (int q = 0; q < RAD; q++) v[q] = conj_if(src.load(w, jb + q * (N / RAD)), conj_in);
-      if (Ls > 1) {
-        const int step = N / (Ls * RAD);
-#pragma unroll
-        for (int q = 1; q < RAD; q++) v[q] = cmul(v[q], tws[(p * q * step) & (N - 1)]);
-      }
-      dftr<R, RAD>(v);
-#pragma unroll
-      for (int q = 0; q < RAD; q++) dst.store(w, k * Ls * RAD + p + Ls * q, conj_if(v[q], conj_out));
-    }
-  }
-}
-
-// Length-N transforms of Wp pencils. The first stage reads `in`, the last
-// writes `out`; intermediate stages alternate between tiles a and b (both of
-// stride sw). A __syncthreads follows every stage.
-template <typename R, int N, int WP, class In, class Out>
-__device__ __forceinline__ void block_fft(const In &in, const Out &out, cplx<R> *a, cplx<R> *b, int sw,
-                                          const cplx<R> *tws, bool inverse) {
-  SmemT<R> ta{a, sw}, tb{b, sw};
-  int Ls = 1;
-#pragma unroll
-  for (int s = 0; s < Plan<N>::nstages; s++) {
-    const int rad = Plan<N>::radix(s);
-    const bool first = (s == 0), last = (s == Plan<N>::nstages - 1);
-    const bool ci = first && inverse, co = last && inverse;
-    const SmemT<R> &tsrc = (s & 1) ? tb : ta;
-    const SmemT<R> &tdst = (s & 1) ? ta : tb;
-    if (first && last) {
-      if (rad == 8) stage<R, N, 8, WP>(in, out, Ls, tws, ci, co);
-    } else if (first) {
-      if (rad == 8) stage<R, N, 8, WP>(in, tb, Ls, tws, ci, co);
-      else if (rad == 4) stage<R, N, 4, WP>(in, tb, Ls, tws, ci, co);
-      else stage<R, N, 2, WP>(in, tb, Ls, tws, ci, co);
-    } else if (last) {
-      if (rad == 8) stage<R, N, 8, WP>(tsrc, out, Ls, tws, ci, co);
-      else if (rad == 4) stage<R, N, 4, WP>(tsrc, out, Ls, tws, ci, co);
-      else stage<R, N, 2, WP>(tsrc, out, Ls, tws, ci, co);
-    } else {
-      if (rad == 8) stage<R, N, 8, WP>(tsrc, tdst, Ls, tws, ci, co);
-      else if (rad == 4) stage<R, N, 4, WP>(tsrc, tdst, Ls, tws, ci, co);
-      else stage<R, N, 2, WP>(tsrc, tdst, Ls, tws, ci, co);
-    }
-    Ls *= rad;
-    __syncthreads();
-  }
-}
-
-template <typename R>
-__device__ __forceinline__ void load_table(cplx<R> *dst, const cplx<R> *__restrict__ src, int n) {
-  const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  for (int q = lin; q < n; q += nthr) dst[q] = src[q];
-}
-
-// z row split/merge of the real transform (H = NZ/2):
-//   forward  X[k] = E[k] + exp(-2 pi i k/NZ) O[k],  E, O from Z[k], conj Z[H-k]
-//   inverse  Z[k] = (X[k] + conj X[H-k]) + i exp(+2 pi i k/NZ)(X[k] - conj X[H-k])
-template <typename R>
-__device__ __forceinline__ cplx<R> split_fwd(cplx<R> z, cplx<R> c /* conj Z[H-k] */, cplx<R> pw) {
-  const R er = R(0.5) * (z.x + c.x), ei = R(0.5) * (z.y + c.y);
-  const R orr = R(0.5) * (z.y - c.y), oi = R(-0.5) * (z.x - c.x);
-  return cplx<R>{er + (pw.x * orr - pw.y * oi), ei + (pw.x * oi + pw.y * orr)};
-}
-template <typename R>
-__device__ __forceinline__ cplx<R> merge_inv(cplx<R> x, cplx<R> c /* conj X[H-k] */, cplx<R> pw) {
-  const R sr = x.x + c.x, si = x.y + c.y;
-  const R dr = x.x - c.x, di = x.y - c.y;
-  const R wr = pw.x, wi = -pw.y;  // exp(+2 pi i k/NZ)
-  const R tr = wr * dr - wi * di, ti = wr * di + wi * dr;
-  return cplx<R>{sr - ti, si + tr};
-}
-
 // ---- plane kernels (one block per x-plane and field) ---------------------
-// smem: tw_y[NY] | tw_z[H] | post[H+1] | A | B, A/B of plane_tile() complex.
-__host__ __device__ constexpr int plane_tile(int ny, int h) {
-  return (h * (ny + 1) > ny * (h + 2)) ? h * (ny + 1) : ny * (h + 2);
-}
-
 template <typename R, int NY, int H>
 __global__ void __launch_bounds__(1024) k_plane_fwd(FieldBatch<R> fb, Grid g, const cplx<R> *__restrict__ twy,
                                                     const cplx<R> *__restrict__ twz, const cplx<R> *__restrict__ post) {
@@ -269,23 +46,8 @@ __global__ void __launch_bounds__(1024) k_plane_fwd(FieldBatch<R> fb, Grid g, co
     A[e * rsw + j] = cplx<R>{rp[2 * e], rp[2 * e + 1]};
   }
   __syncthreads();
-  // z transforms: A -> (B, ...); with an even number of stages the result is in A
-  constexpr int zst = Plan<H>::nstages;
-  cplx<R> *zres = (zst & 1) ? B : A;
-  cplx<R> *ybuf = (zst & 1) ? A : B;
-  block_fft<R, H, NY>(SmemT<R>{A, rsw}, SmemT<R>{zres, rsw}, A, B, rsw, stz, false);
-  // split into the half spectrum, y-pencil layout: element j of pencil k at ybuf[j*ysw + k]
-  constexpr int ysw = H + 2;
-  for (int q = lin; q < NY * (H + 1); q += nthr) {
-    const int j = q / (H + 1), k = q - j * (H + 1);
-    const int k1 = (k == H) ? 0 : k, k2 = (k == 0) ? 0 : H - k;
-    ybuf[j * ysw + k] = split_fwd(zres[k1 * rsw + j], cconj(zres[k2 * rsw + j]), spost[k]);
-  }
-  __syncthreads();
-  // y transforms of the H+1 columns, last stage to global (coalesced over kz)
   GPencils<R> outp{reinterpret_cast<cplx<R> *>(data), (long)i * NY * g.hnz, 1, g.hnz, H + 1};
-  cplx<R> *other = (ybuf == A) ? B : A;
-  block_fft<R, NY, H + 1>(SmemT<R>{ybuf, ysw}, outp, ybuf, other, ysw, sty, false);
+  plane_fwd_core<R, NY, H>(A, B, sty, stz, spost, outp);
 }
 
 template <typename R, int NY, int H>
@@ -311,36 +73,8 @@ __global__ void __launch_bounds__(1024) k_plane_inv(FieldBatch<R> fb, Grid g, co
     A[j * ysw + k] = cplane[q];
   }
   __syncthreads();
-  // j-direction half of the Hermitian completion on the kz = 0 and kz = NZ/2
-  // columns: kz = 0 keeps rows 1..NY/2-1, kz = NZ/2 keeps rows NY/2+1..NY-1.
-  for (int j = 1 + lin; j < NY / 2; j += nthr) {
-    A[(NY - j) * ysw + 0] = cconj(A[j * ysw + 0]);
-    A[j * ysw + H] = cconj(A[(NY - j) * ysw + H]);
-  }
-  __syncthreads();
-  // y inverse transforms of the H+1 columns
-  constexpr int yst = Plan<NY>::nstages;
-  cplx<R> *yres = (yst & 1) ? B : A;
-  cplx<R> *zbuf = (yst & 1) ? A : B;
-  block_fft<R, NY, H + 1>(SmemT<R>{A, ysw}, SmemT<R>{yres, ysw}, A, B, ysw, sty, true);
-  // merge into H-point complex rows (element-major, pencil = row j); the
-  // imaginary parts of kz = 0 and kz = NZ/2 are ignored
+  const cplx<R> *zres = plane_inv_core<R, NY, H>(A, B, sty, stz, spost);
   constexpr int rsw = NY + 1;
-  for (int q = lin; q < NY * H; q += nthr) {
-    const int j = q / H, k = q - j * H;
-    cplx<R> x = yres[j * ysw + k];
-    cplx<R> c = yres[j * ysw + (H - k)];
-    if (k == 0) {
-      x.y = R(0);
-      c.y = R(0);
-    }
-    zbuf[k * rsw + j] = merge_inv(x, cconj(c), spost[k]);
-  }
-  __syncthreads();
-  constexpr int zst = Plan<H>::nstages;
-  cplx<R> *other = (zbuf == A) ? B : A;
-  cplx<R> *zres = (zst & 1) ? other : zbuf;
-  block_fft<R, H, NY>(SmemT<R>{zbuf, rsw}, SmemT<R>{zres, rsw}, zbuf, other, rsw, stz, true);
   R *plane = data + (long)i * NY * g.nzp;
   for (int q = lin; q < NY * (H + 1); q += nthr) {
     const int j = q / (H + 1), m = q - j * (H + 1);

@@ -59,8 +59,6 @@ __device__ __forceinline__ void kvec(const Grid &g, const Mode &m, R *k) {
 template <typename R>
 __device__ __forceinline__ R k2_of(const R *k) { return k[0] * k[0] + k[1] * k[1] + k[2] * k[2]; }
 
-__device__ __forceinline__ void sincos_t(double a, double *s, double *c) { sincos(a, s, c); }
-__device__ __forceinline__ void sincos_t(float a, float *s, float *c) { sincosf(a, s, c); }
 __device__ __forceinline__ double exp_t(double a) { return exp(a); }
 __device__ __forceinline__ float exp_t(float a) { return expf(a); }
 
@@ -214,14 +212,14 @@ __global__ void k_grad(Grid g, const R *a, R *d0, R *d1, R *d2, R scale, int shi
   R k[3];
   kvec(g, m, k);
   const R re = scale * a[m.im], im = scale * a[m.im + 1];
-  const R hdx = (R)(0.5 * g.dx);
+  const int idx[3] = {m.i, m.j, m.kz};
   R *d[3] = {d0, d1, d2};
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     R gr = -k[c] * im, gi = k[c] * re;
     if (shift) {
       R sn, cs;
-      sincos_t(hdx * k[c], &sn, &cs);
+      shift_of(g, c, idx[c], cs, sn);
       const R tr = gr * cs - gi * sn, ti = gr * sn + gi * cs;
       gr = tr;
       gi = ti;
@@ -251,11 +249,11 @@ __global__ void k_div(Grid g, const R *u0, const R *u1, const R *u2, R *div, int
     div[m.im + 1] = b;
     return;
   }
-  const R hdx = (R)(0.5 * g.dx);
+  const int idx[3] = {m.i, m.j, m.kz};
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     R sn, cs;
-    sincos_t(hdx * k[c], &sn, &cs);
+    shift_of(g, c, idx[c], cs, sn);
     const R ksr = k[c] * cs, ksi = -k[c] * sn;
     const R ur = u[c][m.im], ui = u[c][m.im + 1];
     sr += ur * ksr - ui * ksi;

@@ -1,0 +1,428 @@
+// kop.cu -- see kop.cuh.
+#include "fft_blocks.cuh"
+#include "kop.cuh"
+#include "krylov.cuh"
+
+namespace icep {
+
+namespace {
+
+constexpr int KW = 16;  // x pencils per block
+typedef cplx<float> cf;
+
+__device__ __forceinline__ void kvec3(const Grid &g, int i, int j, int kz, float *k) {
+  k[0] = (float)g.wave[0] * (float)kx_of(g, i);
+  k[1] = (float)g.wave[1] * (float)ky_of(g, j);
+  k[2] = (float)g.wave[2] * (float)kz;
+}
+
+// m(k) i k_D exp(i dx k_D / 2) p, m = -1/(eps_ref |k|^2), m(0) = 0
+template <int D>
+__device__ __forceinline__ cf grad_mult(const Grid &g, int i, int j, int kz, cf p, float ieps) {
+  float k[3];
+  kvec3(g, i, j, kz, k);
+  const float k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
+  const float mm = (k2 > 0.f) ? -ieps / k2 : 0.f;
+  const float re = p.x * mm, im = p.y * mm;
+  float cs, sn;
+  shift_of(g, D, (D == 0) ? i : (D == 1) ? j : kz, cs, sn);
+  const float gr = -k[D] * im, gi = k[D] * re;
+  return cf{gr * cs - gi * sn, gr * sn + gi * cs};
+}
+
+// Sum of a[2b + off], b < n, in a fixed order; every thread of the block
+// calls it and gets the same value.
+__device__ double block_sum_partials(const double *a, int n, int off, double *sh) {
+  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
+  if (lin < 32) {
+    double s = 0.0;
+    for (int b = lin; b < n; b += 32) s += a[2 * b + off];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lin == 0) *sh = s;
+  }
+  __syncthreads();
+  return *sh;
+}
+
+// Block reduction of (s0, s1) into partials[2*blockIdx.x + c].
+__device__ void block_partials(double s0, double s1, double *partials) {
+  __shared__ double red[2][32];
+  const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  const int lane = lin & 31, wid = lin >> 5;
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+  }
+  if (lane == 0) {
+    red[0][wid] = s0;
+    red[1][wid] = s1;
+  }
+  __syncthreads();
+  if (lin < 2) {
+    double v = 0.0;
+    for (int w = 0; w < nthr / 32; w++) v += red[lin][w];
+    partials[2 * blockIdx.x + lin] = v;
+  }
+}
+
+__device__ __forceinline__ cf ldw(const float *a, long idx, int wt) {
+  const float2 v = reinterpret_cast<const float2 *>(a)[idx];
+  return cf{v.x, wt == 1 ? 0.f : v.y};
+}
+
+// First-stage source of the inverse x transforms: the gradient multiplier of
+// component d applied to the updated vector held in shared memory (`raw`,
+// element e of pencil w at raw[e*sw + w]), with the i-direction half of the
+// reference's Hermitian completion on the pencils (j, kz), j in {0, NY/2},
+// kz in {0, NZ/2} (as GPencilsXInv in the plain passes).
+template <int D>
+struct SrcGradXInv {
+  const cf *raw;
+  int sw, q0, nvalid;
+  Grid g;
+  float ieps;
+  __device__ __forceinline__ cf load(int w, int e) const {
+    if (w >= nvalid) return cf{0.f, 0.f};
+    const int q = q0 + w;
+    const int j = q / g.hnz, kz = q - j * g.hnz;
+    if ((j == 0 || j == g.ny / 2) && (kz == 0 || kz == g.hnz - 1)) {
+      if (e == 0 || e == g.nx / 2) {
+        const cf v = grad_mult<D>(g, e, j, kz, cf{raw[e * sw + w].x, 0.f}, ieps);
+        return cf{v.x, 0.f};
+      }
+      const bool kept = (kz == 0) ? (e <= g.nx / 2) : (e > g.nx / 2);
+      if (!kept) {
+        const int m = g.nx - e;
+        return cconj(grad_mult<D>(g, m, j, kz, raw[m * sw + w], ieps));
+      }
+    }
+    return grad_mult<D>(g, e, j, kz, raw[e * sw + w], ieps);
+  }
+};
+
+template <int N>
+__global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, const float *r, const float *v,
+                                                  float beta, float omega, double rho, const double *part, int npart,
+                                                  float ieps, float *w0, float *w1, float *w2,
+                                                  const cf *__restrict__ twx) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ double sh;
+  const int sw = KW + 1;
+  cf *tws = reinterpret_cast<cf *>(smem_raw);
+  cf *raw = tws + N;
+  cf *ta = raw + N * sw;
+  cf *tb = ta + N * sw;
+  const int nq = g.ny * g.hnz;
+  const int q0 = blockIdx.x * KW;
+  const int nvalid = nq - q0 < KW ? nq - q0 : KW;
+  const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  load_table(tws, twx, N);
+  float alpha = 0.f;
+  if (mode == KOP_S) alpha = (float)(rho / block_sum_partials(part, npart, 0, &sh));
+  // vector update at the read modes of this block's pencils
+  for (int it = lin; it < N * KW; it += nthr) {
+    const int w = it % KW, e = it / KW;
+    if (w >= nvalid) {
+      raw[e * sw + w] = cf{0.f, 0.f};
+      continue;
+    }
+    const int q = q0 + w;
+    const int j = q / g.hnz, kz = q - j * g.hnz;
+    const long idx = (long)e * nq + q;
+    const int wt = read_weight(g, e, j, kz);
+    const cf rr = ldw(r, idx, wt), vv = ldw(v, idx, wt);
+    cf nv;
+    if (mode == KOP_P) {
+      const cf pp = ldw(vec, idx, wt);
+      nv = cf{rr.x + beta * (pp.x - omega * vv.x), rr.y + beta * (pp.y - omega * vv.y)};
+    } else {
+      nv = cf{rr.x - alpha * vv.x, rr.y - alpha * vv.y};
+    }
+    raw[e * sw + w] = nv;
+    if (wt > 0) reinterpret_cast<float2 *>(vec)[idx] = make_float2(nv.x, nv.y);
+  }
+  __syncthreads();
+  block_fft<float, N, KW>(SrcGradXInv<0>{raw, sw, q0, nvalid, g, ieps},
+                          GPencils<float>{reinterpret_cast<cf *>(w0), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
+                          tws, true);
+  block_fft<float, N, KW>(SrcGradXInv<1>{raw, sw, q0, nvalid, g, ieps},
+                          GPencils<float>{reinterpret_cast<cf *>(w1), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
+                          tws, true);
+  block_fft<float, N, KW>(SrcGradXInv<2>{raw, sw, q0, nvalid, g, ieps},
+                          GPencils<float>{reinterpret_cast<cf *>(w2), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
+                          tws, true);
+}
+
+template <int NY, int H>
+__global__ void __launch_bounds__(1024) k_kop_plane(Grid g, float *w0, float *w1, float *w2, const float *ef0,
+                                                    const float *ef1, const float *ef2, const cf *__restrict__ twy,
+                                                    const cf *__restrict__ twz, const cf *__restrict__ post,
+                                                    float scale) {
+  extern __shared__ unsigned char smem_raw[];
+  cf *sty = reinterpret_cast<cf *>(smem_raw);
+  cf *stz = sty + NY;
+  cf *spost = stz + H;
+  cf *A = spost + (H + 1);
+  cf *B = A + plane_tile(NY, H);
+  const int i = blockIdx.x, d = blockIdx.y;
+  float *data = (d == 0) ? w0 : (d == 1) ? w1 : w2;
+  const float *ef = (d == 0) ? ef0 : (d == 1) ? ef1 : ef2;
+  const int nthr = blockDim.x * blockDim.y, lin = threadIdx.y * blockDim.x + threadIdx.x;
+  load_table(sty, twy, NY);
+  load_table(stz, twz, H);
+  load_table(spost, post, H + 1);
+  const cf *cplane = reinterpret_cast<const cf *>(data) + (long)i * NY * g.hnz;
+  constexpr int ysw = H + 2;
+  for (int q = lin; q < NY * (H + 1); q += nthr) {
+    const int j = q / (H + 1), k = q - j * (H + 1);
+    A[j * ysw + k] = cplane[q];
+  }
+  __syncthreads();
+  cf *rows = plane_inv_core<float, NY, H>(A, B, sty, stz, spost);
+  // the real field times the face permittivity (C2R scaling first, as the
+  // plain path stores the scaled field before multiplying)
+  constexpr int rsw = NY + 1;
+  const float *efp = ef + (long)i * NY * g.nzp;
+  for (int q = lin; q < NY * H; q += nthr) {
+    const int j = q / H, e = q - j * H;
+    const float2 f = reinterpret_cast<const float2 *>(efp + (long)j * g.nzp)[e];
+    cf x = rows[e * rsw + j];
+    x.x = (x.x * scale) * f.x;
+    x.y = (x.y * scale) * f.y;
+    rows[e * rsw + j] = x;
+  }
+  __syncthreads();
+  cf *other = (rows == A) ? B : A;
+  GPencils<float> outp{reinterpret_cast<cf *>(data), (long)i * NY * g.hnz, 1, g.hnz, H + 1};
+  plane_fwd_core<float, NY, H>(rows, other, sty, stz, spost, outp);
+}
+
+// Last-stage sink of the forward x transforms: acc += k_D exp(-i dx k_D/2) X_D
+template <int D>
+struct DivAcc {
+  cf *acc;
+  int sw, q0, nvalid;
+  Grid g;
+  __device__ __forceinline__ void store(int w, int e, cf v) const {
+    if (w >= nvalid) return;
+    const int q = q0 + w;
+    const int j = q / g.hnz, kz = q - j * g.hnz;
+    float k[3];
+    kvec3(g, e, j, kz, k);
+    float cs, sn;
+    shift_of(g, D, (D == 0) ? e : (D == 1) ? j : kz, cs, sn);
+    const float ksr = k[D] * cs, ksi = -k[D] * sn;
+    cf a = (D == 0) ? cf{0.f, 0.f} : acc[e * sw + w];
+    a.x += v.x * ksr - v.y * ksi;
+    a.y += v.x * ksi + v.y * ksr;
+    acc[e * sw + w] = a;
+  }
+};
+
+template <int N>
+__global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const float *w1, const float *w2,
+                                                  float *out, int mode, const float *other, double *partials,
+                                                  const cf *__restrict__ twx) {
+  extern __shared__ unsigned char smem_raw[];
+  const int sw = KW + 1;
+  cf *tws = reinterpret_cast<cf *>(smem_raw);
+  cf *acc = tws + N;
+  cf *ta = acc + N * sw;
+  cf *tb = ta + N * sw;
+  const int nq = g.ny * g.hnz;
+  const int q0 = blockIdx.x * KW;
+  const int nvalid = nq - q0 < KW ? nq - q0 : KW;
+  const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  load_table(tws, twx, N);
+  __syncthreads();
+  block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w0)), (long)q0, 1, (long)nq, nvalid},
+                          DivAcc<0>{acc, sw, q0, nvalid, g}, ta, tb, sw, tws, false);
+  block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w1)), (long)q0, 1, (long)nq, nvalid},
+                          DivAcc<1>{acc, sw, q0, nvalid, g}, ta, tb, sw, tws, false);
+  block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w2)), (long)q0, 1, (long)nq, nvalid},
+                          DivAcc<2>{acc, sw, q0, nvalid, g}, ta, tb, sw, tws, false);
+  double s0 = 0.0, s1 = 0.0;
+  for (int it = lin; it < N * KW; it += nthr) {
+    const int w = it % KW, e = it / KW;
+    if (w >= nvalid) continue;
+    const int q = q0 + w;
+    const int j = q / g.hnz, kz = q - j * g.hnz;
+    const int wt = read_weight(g, e, j, kz);
+    if (wt == 0) continue;
+    const long idx = (long)e * nq + q;
+    const cf a = acc[e * sw + w];
+    const cf val{-a.y, a.x};  // i * acc
+    reinterpret_cast<float2 *>(out)[idx] = make_float2(val.x, val.y);
+    const double vr = val.x, vi = (wt == 1) ? 0.0 : (double)val.y;
+    const cf o = ldw(other, idx, wt);
+    if (mode == KOP_P) {
+      s0 += (double)wt * ((double)o.x * vr + (double)o.y * vi);
+    } else {
+      s0 += (double)wt * (vr * vr + vi * vi);
+      s1 += (double)wt * (vr * (double)o.x + vi * (double)o.y);
+    }
+  }
+  const double inv = 1.0 / (double)g.nreal();
+  block_partials(s0 * inv, s1 * inv, partials);
+}
+
+__global__ void k_kop_xr(Grid g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
+                         double rho, const double *part1, const double *part2, int npart, double *part3) {
+  __shared__ double sh[3];
+  const double r0v = block_sum_partials(part1, npart, 0, &sh[0]);
+  const double tt = block_sum_partials(part2, npart, 0, &sh[1]);
+  const double ts = block_sum_partials(part2, npart, 1, &sh[2]);
+  const float alpha = (float)(rho / r0v);
+  const float w = (float)((tt > 0.0) ? ts / tt : 0.0);
+  double s0 = 0.0, s1 = 0.0;
+  const unsigned nm = (unsigned)g.nmodes();
+  const unsigned plane = (unsigned)g.ny * (unsigned)g.hnz;
+  for (unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x; t0 < nm; t0 += gridDim.x * blockDim.x) {
+    const int i = (int)(t0 / plane);
+    const unsigned rem = t0 - (unsigned)i * plane;
+    const int j = (int)(rem / (unsigned)g.hnz), kz = (int)(rem - (unsigned)j * (unsigned)g.hnz);
+    const int wt = read_weight(g, i, j, kz);
+    if (wt == 0) continue;
+    const long idx = t0;
+    const cf pp = ldw(p, idx, wt), ss = ldw(sv, idx, wt), tv = ldw(t, idx, wt), xx = ldw(xt, idx, wt);
+    const cf nx{xx.x + alpha * pp.x + w * ss.x, xx.y + alpha * pp.y + w * ss.y};
+    const cf nr{ss.x - w * tv.x, ss.y - w * tv.y};
+    reinterpret_cast<float2 *>(xt)[idx] = make_float2(nx.x, nx.y);
+    reinterpret_cast<float2 *>(r)[idx] = make_float2(nr.x, nr.y);
+    const cf a = ldw(r0, idx, wt);
+    s0 += (double)wt * ((double)a.x * (double)nr.x + (double)a.y * (double)nr.y);
+    s1 += (double)wt * ((double)nr.x * (double)nr.x + (double)nr.y * (double)nr.y);
+  }
+  const double inv = 1.0 / (double)g.nreal();
+  block_partials(s0 * inv, s1 * inv, part3);
+}
+
+__global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2) {
+  const long tl = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tl >= g.nreal()) return;
+  const unsigned t = (unsigned)tl;
+  const unsigned plane = (unsigned)g.ny * (unsigned)g.nz;
+  const int i = (int)(t / plane);
+  const unsigned rem = t - (unsigned)i * plane;
+  const int j = (int)(rem / (unsigned)g.nz), k = (int)(rem - (unsigned)j * (unsigned)g.nz);
+  const long im = gidx(g, i, j, k);
+  const float e0 = eps[im];
+  ef0[im] = 0.5f * (eps[gidx(g, (i + 1) % g.nx, j, k)] + e0);
+  ef1[im] = 0.5f * (eps[gidx(g, i, (j + 1) % g.ny, k)] + e0);
+  ef2[im] = 0.5f * (eps[gidx(g, i, j, (k + 1) % g.nz)] + e0);
+}
+
+size_t xpass_smem(int n) { return ((size_t)n + 3 * (size_t)n * (KW + 1)) * sizeof(cf); }
+size_t plane_smem_f(int ny, int h) { return ((size_t)ny + h + (h + 1) + 2 * (size_t)plane_tile(ny, h)) * sizeof(cf); }
+constexpr size_t KOP_PLANE_SMEM_MAX = 200 * 1024;
+
+dim3 xblock(int n) { return dim3(KW, n / 8 < 512 / KW ? n / 8 : 512 / KW); }
+
+template <int N>
+void set_x_attr() {
+  static bool attr = false;  // one attribute call per instantiation
+  if (attr) return;
+  cudaFuncSetAttribute(k_kop_xinv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xpass_smem(N));
+  cudaFuncSetAttribute(k_kop_xfwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xpass_smem(N));
+  attr = true;
+}
+
+template <int NY, int H>
+void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
+                     const float *ef2, cudaStream_t s) {
+  const size_t sm = plane_smem_f(NY, H);
+  static bool attr = false;  // one attribute call per instantiation
+  if (!attr) {
+    cudaFuncSetAttribute(k_kop_plane<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  const float scale = (float)(1.0 / ((double)p.g.nx * p.g.ny * p.g.nz));
+  count_launch();
+  k_kop_plane<NY, H><<<dim3(p.g.nx, 3), 1024, sm, s>>>(p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z,
+                                                             p.tw_post, scale);
+}
+
+template <int NY>
+void launch_plane_n(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
+                    const float *ef2, cudaStream_t s) {
+  switch (p.g.nz / 2) {
+    case 8: launch_plane_nh<NY, 8>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+    case 16: launch_plane_nh<NY, 16>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+    case 32: launch_plane_nh<NY, 32>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+    default: launch_plane_nh<NY, 64>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+  }
+}
+
+}  // namespace
+
+bool kop_supported(const Grid &g) {
+  return g.ny <= 128 && g.nz <= 128 && plane_smem_f(g.ny, g.nz / 2) <= KOP_PLANE_SMEM_MAX;
+}
+
+int kop_pencil_blocks(const Grid &g) { return (int)div_up((long)g.ny * g.hnz, KW); }
+
+void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, float *ef2, cudaStream_t s) {
+  count_launch();
+  k_kop_eps_faces<<<div_up(g.nreal(), 256), 256, 0, s>>>(g, eps, ef0, ef1, ef2);
+}
+
+void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
+              double omega, double rho, const double *part, int npart, double eps_ref, float *w0, float *w1,
+              float *w2, cudaStream_t s) {
+  const Grid &g = p.g;
+  const unsigned nb = (unsigned)kop_pencil_blocks(g);
+  const float ieps = (float)(1.0 / eps_ref);
+  count_launch();
+#define KOP_XINV(N)                                                                                        \
+  case N:                                                                                                  \
+    set_x_attr<N>();                                                                                       \
+    k_kop_xinv<N><<<nb, xblock(N), xpass_smem(N), s>>>(g, mode, vec, r, v, (float)beta, (float)omega, rho, \
+                                                       part, npart, ieps, w0, w1, w2, p.tw_x);             \
+    break;
+  switch (g.nx) {
+    KOP_XINV(16)
+    KOP_XINV(32)
+    KOP_XINV(64)
+    KOP_XINV(128)
+    KOP_XINV(256)
+  }
+#undef KOP_XINV
+}
+
+void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
+               const float *ef2, cudaStream_t s) {
+  switch (p.g.ny) {
+    case 16: launch_plane_n<16>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+    case 32: launch_plane_n<32>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+    case 64: launch_plane_n<64>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+    default: launch_plane_n<128>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+  }
+}
+
+void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
+              const float *other, double *partials, cudaStream_t s) {
+  const Grid &g = p.g;
+  const unsigned nb = (unsigned)kop_pencil_blocks(g);
+  count_launch();
+#define KOP_XFWD(N)                                                                                                 \
+  case N:                                                                                                           \
+    set_x_attr<N>();                                                                                                \
+    k_kop_xfwd<N><<<nb, xblock(N), xpass_smem(N), s>>>(g, w0, w1, w2, out, mode, other, partials, p.tw_x); \
+    break;
+  switch (g.nx) {
+    KOP_XFWD(16)
+    KOP_XFWD(32)
+    KOP_XFWD(64)
+    KOP_XFWD(128)
+    KOP_XFWD(256)
+  }
+#undef KOP_XFWD
+}
+
+void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
+            double rho, const double *part1, const double *part2, int npart, double *part3, cudaStream_t s) {
+  count_launch();
+  k_kop_xr<<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, xt, r, p, sv, t, r0, rho, part1, part2, npart, part3);
+}
+
+}  // namespace icep

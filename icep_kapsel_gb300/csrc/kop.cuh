@@ -1,0 +1,48 @@
+// kop.cuh -- the k-space Poisson iteration's operator B = A M^-1 fused into
+// three FFT passes, with the BiCGSTAB vector updates and dot products folded
+// into them (FP32, the inner solver of MIXED precision).
+//
+//   kop_xinv : vector update (p or s) at the read modes, then for d = 0..2 the
+//              gradient multiplier m(k) i k_d exp(i dx k_d/2) and the inverse
+//              x transform, into w_d (one read of the vector, three writes)
+//   kop_plane: per x-plane and field: inverse y/z transform, multiplication
+//              by the face permittivity eps_face_d (the reference's
+//              0.5 (eps + eps shifted along d), operate_dielectric.cxx:485-522),
+//              forward z/y transform -- the real field never leaves shared memory
+//   kop_xfwd : forward x transforms of w_0..2 and the staggered divergence
+//              sum_d i k_d exp(-i dx k_d/2) w_d into the output vector, with the
+//              dot products the iteration needs next as per-block partials
+//   kop_xr   : x~ += alpha p + omega s, r = s - omega t and the dot products
+//              (r0, r), (r, r)
+// Vectors follow kspace.cuh (read modes only). Dot partials are FP64, one or
+// two per block, scaled by 1/N; sums over blocks are taken in block order.
+#pragma once
+#include "fft.cuh"
+
+namespace icep {
+
+enum { KOP_P = 0, KOP_S = 1 };
+
+// true if the fused passes cover this grid (an x-plane fits in shared memory)
+bool kop_supported(const Grid &g);
+// number of x-pencil blocks (= partial sums written by kop_xfwd)
+int kop_pencil_blocks(const Grid &g);
+// ef_d = 0.5 (eps + eps at the next point along d), real points
+void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, float *ef2, cudaStream_t s);
+// mode KOP_P: vec = p <- P(r) + beta (P(p) - omega P(v));
+// mode KOP_S: vec = s <- P(r) - alpha P(v), alpha = rho / sum_b part[2b].
+void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
+              double omega, double rho, const double *part, int npart, double eps_ref, float *w0, float *w1,
+              float *w2, cudaStream_t s);
+void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
+               const float *ef2, cudaStream_t s);
+// mode KOP_P: partials[2b] = (other, out) with other = r0;
+// mode KOP_S: partials[2b] = (out, out), partials[2b+1] = (out, other) with other = s.
+void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
+              const float *other, double *partials, cudaStream_t s);
+// alpha = rho / sum part1[2b]; omega = sum part2[2b+1] / sum part2[2b];
+// part3[2b] = (r0, r), part3[2b+1] = (r, r) over DOT_BLOCKS blocks.
+void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
+            double rho, const double *part1, const double *part2, int npart, double *part3, cudaStream_t s);
+
+}  // namespace icep

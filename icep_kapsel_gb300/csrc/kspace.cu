@@ -24,21 +24,7 @@ __device__ __forceinline__ bool kmode(const Grid &g, unsigned t, KMode &m) {
   return true;
 }
 
-// Weight of mode m in the real-space inner product (Parseval over the half
-// spectrum): 0 for the kz = 0 / NZ/2 entries the inverse transform does not
-// read, 1 at self-conjugate points, 2 for every other mode.
-__device__ __forceinline__ int kweight(const Grid &g, const KMode &m) {
-  const int h = g.nz / 2;
-  if (m.kz != 0 && m.kz != h) return 2;
-  const int mi = (g.nx - m.i) % g.nx, mj = (g.ny - m.j) % g.ny;
-  if (mi == m.i && mj == m.j) return 1;
-  bool kept;
-  if (m.j >= 1 && m.j <= g.ny / 2 - 1) kept = true;
-  else if (m.j == 0 || m.j == g.ny / 2) kept = (m.i <= g.nx / 2);
-  else kept = false;
-  if (m.kz == h) kept = !kept;
-  return kept ? 2 : 0;
-}
+__device__ __forceinline__ int kweight(const Grid &g, const KMode &m) { return read_weight(g, m.i, m.j, m.kz); }
 
 // Value of vector a at a read mode (weight > 0) as the inverse transform
 // sees it: the stored entry, real part only at self-conjugate points.
@@ -55,8 +41,6 @@ __device__ __forceinline__ void kvec(const Grid &g, const KMode &m, R *k) {
   k[2] = (R)g.wave[2] * (R)m.kz;
 }
 
-__device__ __forceinline__ void sincos_t(double a, double *s, double *c) { sincos(a, s, c); }
-__device__ __forceinline__ void sincos_t(float a, float *s, float *c) { sincosf(a, s, c); }
 
 #define KTID ((unsigned)(blockIdx.x * blockDim.x + threadIdx.x))
 
@@ -193,14 +177,14 @@ __global__ void k_kgrad_pre(Grid g, const R *p, R *g0, R *g1, R *g2, R ieps) {
   ld(p, m, wt, re, im);
   re *= mm;
   im *= mm;
-  const R hdx = (R)(0.5 * g.dx);
+  const int idx[3] = {m.i, m.j, m.kz};
   R *out[3] = {g0, g1, g2};
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     // i k_c (re + i im) = (-k_c im, k_c re), then * exp(i dx k_c / 2)
     const R gr = -k[c] * im, gi = k[c] * re;
     R sn, cs;
-    sincos_t(hdx * k[c], &sn, &cs);
+    shift_of(g, c, idx[c], cs, sn);
     out[c][m.im] = gr * cs - gi * sn;
     out[c][m.im + 1] = gr * sn + gi * cs;
   }
@@ -213,13 +197,13 @@ __global__ void k_kdiv_post(Grid g, const R *w0, const R *w1, const R *w2, R *v)
   if (kweight(g, m) == 0) return;
   R k[3];
   kvec(g, m, k);
-  const R hdx = (R)(0.5 * g.dx);
+  const int idx[3] = {m.i, m.j, m.kz};
   const R *w[3] = {w0, w1, w2};
   R sr = R(0), si = R(0);
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     R sn, cs;
-    sincos_t(hdx * k[c], &sn, &cs);
+    shift_of(g, c, idx[c], cs, sn);
     const R ksr = k[c] * cs, ksi = -k[c] * sn;  // k_c conj(s_c)
     const R ur = w[c][m.im], ui = w[c][m.im + 1];
     sr += ur * ksr - ui * ksi;

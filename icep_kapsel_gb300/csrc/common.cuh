@@ -78,7 +78,7 @@ __device__ __forceinline__ void shift_of(const Grid &g, int d, int idx, float &c
 __host__ __device__ inline int read_weight(const Grid &g, int i, int j, int kz) {
   const int h = g.nz / 2;
   if (kz != 0 && kz != h) return 2;
-  const int mi = (g.nx - i) % g.nx, mj = (g.ny - j) % g.ny;
+  const int mi = (g.nx - i) & (g.nx - 1), mj = (g.ny - j) & (g.ny - 1);  // sizes are powers of two
   if (mi == i && mj == j) return 1;
   bool kept;
   if (j >= 1 && j <= g.ny / 2 - 1) kept = true;

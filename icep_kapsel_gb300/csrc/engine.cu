@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <cstdio>
+#include <utility>
 #include <vector>
 
 #include "engine.cuh"
@@ -55,7 +56,7 @@ class Engine : public EngineBase {
   bool electrolyte;
   // FP64 shadow of the Poisson problem (MIXED precision only): permittivity,
   // potential, right-hand side, residual and operator work fields.
-  enum { D_EPS = 0, D_X, D_B, D_R, D_W3_0, D_W3_1, D_W3_2, D_COUNT };
+  enum { D_EPS = 0, D_X, D_B, D_R, D_W3_0, D_W3_1, D_W3_2, D_XP, D_COUNT };
   bool mixed = false;
   // optional per-phase device timing of the step (CUDA events at phase
   // boundaries, accumulated in ms)
@@ -69,6 +70,7 @@ class Engine : public EngineBase {
   FFTPlan<double> fft64;
   double *d64[D_COUNT] = {nullptr};
   bool x64_valid = false;
+  bool xp_valid = false;  // D_XP holds the potential of the previous solve
 
   ~Engine() override {
     if (s) cudaStreamSynchronize(s);
@@ -390,7 +392,12 @@ class Engine : public EngineBase {
   // Build_rhs (operate_dielectric.cxx:524-540)
   void build_rhs(int rhs_id, int rho_id) {
     eps_face_E<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EPS], P.e_ext[0], P.e_ext[1], P.e_ext[2], s);
-    r2c(f[F_WV3_0], f[F_WV3_1], f[F_WV3_2]);
+    FieldBatch<R> nz{};  // zero components of E_ext: cleared (with their padding), not transformed
+    for (int d = 0; d < 3; d++) {
+      if (P.e_ext[d] != 0.0) nz.p[nz.n++] = f[F_WV3_0 + d];
+      else zero(F_WV3_0 + d);
+    }
+    if (nz.n) fft_r2c(fft, nz, s);
     div_k<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[rhs_id], true, s);
     c2r(f[rhs_id]);
     axpby_real<R>(g, f[rho_id], f[rhs_id], R(-1), R(1), s);
@@ -703,11 +710,30 @@ class Engine : public EngineBase {
     if (!x64_valid) {
       convert_f2d(G.nf(), (const float *)f[pot_id], d64[D_X], s);
       x64_valid = true;
+      xp_valid = false;
     }
+    // initial guess: the potential extrapolated linearly in time from the
+    // last two solves (the reference starts from the last potential; both
+    // are converged to the same true-residual tolerance)
+    if (xp_valid) {
+      axpby_real<double>(G, d64[D_X], d64[D_XP], 2.0, -1.0, s);
+      std::swap(d64[D_X], d64[D_XP]);
+    } else {
+      cudaMemcpyAsync(d64[D_XP], d64[D_X], sizeof(double) * G.nf(), cudaMemcpyDeviceToDevice, s);
+    }
+    xp_valid = true;
     convert_f2d(G.nf(), (const float *)f[F_EPS], d64[D_EPS], s);
     // b64
     eps_face_E<double>(G, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_EPS], P.e_ext[0], P.e_ext[1], P.e_ext[2], s);
-    fft_r2c(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
+    {  // components of E_ext that are zero give zero fields: cleared (with
+       // their padding) instead of transformed
+      FieldBatch<double> nz{};
+      for (int d = 0; d < 3; d++) {
+        if (P.e_ext[d] != 0.0) nz.p[nz.n++] = d64[D_W3_0 + d];
+        else cudaMemsetAsync(d64[D_W3_0 + d], 0, sizeof(double) * G.nf(), s);
+      }
+      if (nz.n) fft_r2c(fft64, nz, s);
+    }
     div_k<double>(G, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_B], true, s);
     fft_c2r(fft64, batch(d64[D_B]), s);
     convert_f2d(G.nf(), (const float *)f[rho_id], d64[D_R], s);
@@ -977,7 +1003,7 @@ class Engine : public EngineBase {
   }
   int set_field(int id, const double *host) override {
     if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
-    if (id == F_POT) x64_valid = false;
+    if (id == F_POT) x64_valid = xp_valid = false;
     if (sizeof(R) == sizeof(double)) {
       cudaMemcpyAsync(f[id], host, sizeof(double) * g.nf(), cudaMemcpyHostToDevice, s);
     } else {

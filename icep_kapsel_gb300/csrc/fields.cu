@@ -42,10 +42,11 @@ __device__ __forceinline__ bool pt_of(const Grid &g, long tl, Pt &p) {
   return true;
 }
 
+// periodic wrap (mesh sizes are powers of two)
 __device__ __forceinline__ long wrapi(const Grid &g, int i, int j, int k) {
-  i = (i + g.nx) % g.nx;
-  j = (j + g.ny) % g.ny;
-  k = (k + g.nz) % g.nz;
+  i &= g.nx - 1;
+  j &= g.ny - 1;
+  k &= g.nz - 1;
   return gidx(g, i, j, k);
 }
 

@@ -65,6 +65,16 @@ __device__ void block_partials(double s0, double s1, double *partials) {
   }
 }
 
+// (j, kz) of pencils q0 .. q0 + KW - 1 into shared arrays (synchronised by the caller)
+__device__ __forceinline__ void pencil_coords(const Grid &g, int q0, int *pj, int *pkz) {
+  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
+  if (lin < KW) {
+    const int q = q0 + lin;
+    pj[lin] = q / g.hnz;
+    pkz[lin] = q - (q / g.hnz) * g.hnz;
+  }
+}
+
 __device__ __forceinline__ cf ldw(const float *a, long idx, int wt) {
   const float2 v = reinterpret_cast<const float2 *>(a)[idx];
   return cf{v.x, wt == 1 ? 0.f : v.y};
@@ -78,13 +88,13 @@ __device__ __forceinline__ cf ldw(const float *a, long idx, int wt) {
 template <int D>
 struct SrcGradXInv {
   const cf *raw;
-  int sw, q0, nvalid;
+  const int *pj, *pkz;  // (j, kz) of the block's pencils
+  int sw, nvalid;
   Grid g;
   float ieps;
   __device__ __forceinline__ cf load(int w, int e) const {
     if (w >= nvalid) return cf{0.f, 0.f};
-    const int q = q0 + w;
-    const int j = q / g.hnz, kz = q - j * g.hnz;
+    const int j = pj[w], kz = pkz[w];
     if ((j == 0 || j == g.ny / 2) && (kz == 0 || kz == g.hnz - 1)) {
       if (e == 0 || e == g.nx / 2) {
         const cf v = grad_mult<D>(g, e, j, kz, cf{raw[e * sw + w].x, 0.f}, ieps);
@@ -116,7 +126,10 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
   const int q0 = blockIdx.x * KW;
   const int nvalid = nq - q0 < KW ? nq - q0 : KW;
   const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  __shared__ int pj[KW], pkz[KW];
   load_table(tws, twx, N);
+  pencil_coords(g, q0, pj, pkz);
+  __syncthreads();
   float alpha = 0.f;
   if (mode == KOP_S) alpha = (float)(rho / block_sum_partials(part, npart, 0, &sh));
   // vector update at the read modes of this block's pencils
@@ -127,7 +140,7 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
       continue;
     }
     const int q = q0 + w;
-    const int j = q / g.hnz, kz = q - j * g.hnz;
+    const int j = pj[w], kz = pkz[w];
     const long idx = (long)e * nq + q;
     const int wt = read_weight(g, e, j, kz);
     const cf rr = ldw(r, idx, wt), vv = ldw(v, idx, wt);
@@ -142,13 +155,13 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
     if (wt > 0) reinterpret_cast<float2 *>(vec)[idx] = make_float2(nv.x, nv.y);
   }
   __syncthreads();
-  block_fft<float, N, KW>(SrcGradXInv<0>{raw, sw, q0, nvalid, g, ieps},
+  block_fft<float, N, KW>(SrcGradXInv<0>{raw, pj, pkz, sw, nvalid, g, ieps},
                           GPencils<float>{reinterpret_cast<cf *>(w0), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
-  block_fft<float, N, KW>(SrcGradXInv<1>{raw, sw, q0, nvalid, g, ieps},
+  block_fft<float, N, KW>(SrcGradXInv<1>{raw, pj, pkz, sw, nvalid, g, ieps},
                           GPencils<float>{reinterpret_cast<cf *>(w1), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
-  block_fft<float, N, KW>(SrcGradXInv<2>{raw, sw, q0, nvalid, g, ieps},
+  block_fft<float, N, KW>(SrcGradXInv<2>{raw, pj, pkz, sw, nvalid, g, ieps},
                           GPencils<float>{reinterpret_cast<cf *>(w2), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
 }
@@ -201,12 +214,12 @@ __global__ void __launch_bounds__(1024) k_kop_plane(Grid g, float *w0, float *w1
 template <int D>
 struct DivAcc {
   cf *acc;
-  int sw, q0, nvalid;
+  const int *pj, *pkz;
+  int sw, nvalid;
   Grid g;
   __device__ __forceinline__ void store(int w, int e, cf v) const {
     if (w >= nvalid) return;
-    const int q = q0 + w;
-    const int j = q / g.hnz, kz = q - j * g.hnz;
+    const int j = pj[w], kz = pkz[w];
     float k[3];
     kvec3(g, e, j, kz, k);
     float cs, sn;
@@ -233,23 +246,24 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
   const int q0 = blockIdx.x * KW;
   const int nvalid = nq - q0 < KW ? nq - q0 : KW;
   const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+  __shared__ int pj[KW], pkz[KW];
   load_table(tws, twx, N);
+  pencil_coords(g, q0, pj, pkz);
   __syncthreads();
   block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w0)), (long)q0, 1, (long)nq, nvalid},
-                          DivAcc<0>{acc, sw, q0, nvalid, g}, ta, tb, sw, tws, false);
+                          DivAcc<0>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
   block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w1)), (long)q0, 1, (long)nq, nvalid},
-                          DivAcc<1>{acc, sw, q0, nvalid, g}, ta, tb, sw, tws, false);
+                          DivAcc<1>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
   block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w2)), (long)q0, 1, (long)nq, nvalid},
-                          DivAcc<2>{acc, sw, q0, nvalid, g}, ta, tb, sw, tws, false);
+                          DivAcc<2>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
   double s0 = 0.0, s1 = 0.0;
   for (int it = lin; it < N * KW; it += nthr) {
     const int w = it % KW, e = it / KW;
     if (w >= nvalid) continue;
-    const int q = q0 + w;
-    const int j = q / g.hnz, kz = q - j * g.hnz;
+    const int j = pj[w], kz = pkz[w];
     const int wt = read_weight(g, e, j, kz);
     if (wt == 0) continue;
-    const long idx = (long)e * nq + q;
+    const long idx = (long)e * nq + q0 + w;
     const cf a = acc[e * sw + w];
     const cf val{-a.y, a.x};  // i * acc
     reinterpret_cast<float2 *>(out)[idx] = make_float2(val.x, val.y);

@@ -1293,7 +1293,8 @@ static long bicgstab_spectral(ko_ctx *c, double *b, double *x, double tol, long 
       for (int k = 0; k < c->nz; k++) eref += c->f[F_EPS][IDX(c, i, j, k)];
   eref /= (double)n;
   double *r = (double *)malloc(sizeof(double) * n), *r0 = (double *)malloc(sizeof(double) * n);
-  double *v = (double *)calloc((size_t)n, sizeof(double)), *p = (double *)calloc((size_t)n, sizeof(double));
+  const size_t nn = (size_t)c->nu;
+  double *v = (double *)calloc(nn, sizeof(double)), *p = (double *)calloc(nn, sizeof(double));
   double *s = (double *)malloc(sizeof(double) * n), *t = (double *)malloc(sizeof(double) * n);
   double *y = (double *)malloc(sizeof(double) * n), *z = (double *)malloc(sizeof(double) * n);
   apply_A(c, x, t);
@@ -1779,6 +1780,8 @@ void ko_apply_A(ko_ctx *c, const double *x, double *y) { apply_A(c, x, y); }
 long ko_last_iterations(const ko_ctx *c) { return c->last_iters; }
 double ko_last_error(const ko_ctx *c) { return c->last_error; }
 long ko_matvec_count(const ko_ctx *c) { return c->matvecs; }
+/* MaxIter_potential of later solves (lets a timing harness cap a solve) */
+void ko_set_potential_iter(ko_ctx *c, int maxit) { c->P.potential_iter = maxit; }
 long ko_lj_pairs(ko_ctx *c, int *pairs, long max_pairs) {
   for (int n = 0; n < c->np; n++)
     for (int d = 0; d < DIM; d++) c->p[n].fr[d] = 0.0;

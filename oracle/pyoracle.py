@@ -45,9 +45,11 @@ def build_oracle(force=False):
     src = os.path.join(HERE, "icep_oracle.c")
     if not force and os.path.exists(ORACLE_SO) and os.path.getmtime(ORACLE_SO) >= os.path.getmtime(src):
         return ORACLE_SO
+    tmp = ORACLE_SO + ".tmp"
     cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-ffp-contract=off",
-           "-o", ORACLE_SO, src, "-lm"]
+           "-o", tmp, src, "-lm"]
     subprocess.check_call(cmd)
+    os.replace(tmp, ORACLE_SO)  # atomic: processes that loaded the old file keep it
     return ORACLE_SO
 
 
@@ -111,6 +113,7 @@ class Oracle(_Base):
         L.ko_last_error.argtypes = [C.c_void_p]
         L.ko_matvec_count.restype = C.c_long
         L.ko_matvec_count.argtypes = [C.c_void_p]
+        L.ko_set_potential_iter.argtypes = [C.c_void_p, C.c_int]
         L.ko_np_domain.argtypes = [C.c_void_p]
         L.ko_sekibun.argtypes = [C.c_void_p, C.POINTER(C.c_int)]
         L.ko_lj_pairs.restype = C.c_long
@@ -189,6 +192,9 @@ class Oracle(_Base):
 
     def matvecs(self):
         return self.lib.ko_matvec_count(self.ctx)
+
+    def set_potential_iter(self, maxit):
+        self.lib.ko_set_potential_iter(self.ctx, int(maxit))
 
     def sekibun(self):
         n = self.lib.ko_np_domain(self.ctx)

@@ -37,6 +37,14 @@ import numpy as np  # noqa: E402
 METRIC = "ICEP steps/s at 128^3, learned-precond vs plain on GB300 at 1e-8 residual; HBM %"
 UNIT = "steps/s"
 
+# Dominant kernel of the step (largest share of device time in the ncu launch
+# list of this bench, profiles/launches_icep_step_128.txt) and its probe id.
+PROBE_KERNEL = "k_kop_plane<128,64> (fused plane pass of the k-space Poisson operator, 3 fields)"
+PROBE_KIND = 1
+# DRAM bytes (read + write) per launch of that kernel from one ncu capture
+# (profiles/k_kop_plane_128.txt), keyed by (grid, precision, kernel).
+TRAFFIC = {(128, "mixed", PROBE_KERNEL): 51.19e6}
+
 
 def workload(args, precision, solver):
     import cases
@@ -257,9 +265,9 @@ def run_gpu(args, world, rank, local, dist):
     from icep_kapsel_gb300.runtime import Simulation, load_library
     lib = load_library()
     lib.icep_step_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
-    lib.icep_time_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double),
-                                     C.POINTER(C.c_double)]
     lib.icep_kernel_launches.restype = C.c_ulonglong
+    lib.icep_probe_start.argtypes = [C.c_int, C.c_int]
+    lib.icep_probe_stop.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
     lib.icep_pin_host.argtypes = [C.c_void_p, C.c_size_t]
     lib.icep_unpin_host.argtypes = [C.c_void_p]
     precision = abi.MIXED if args.precision == "mixed" else abi.FP64
@@ -273,22 +281,25 @@ def run_gpu(args, world, rank, local, dist):
         dist.barrier()
     ms = C.c_double(0)
     launches0 = lib.icep_kernel_launches()
+    # the dominant kernel's launches are timed with CUDA events on their
+    # stream while the timed steps run
+    lib.icep_probe_start(PROBE_KIND, 1 << 16)
     with ClockSampler(0) as clk:
         st = lib.icep_step_timed(sim.ctx, args.steps, C.byref(ms))
     if st != 0:
         raise RuntimeError("timed steps failed: %d" % st)
+    pms, pn, pbytes = C.c_double(0), C.c_longlong(0), C.c_double(0)
+    lib.icep_probe_stop(C.byref(pms), C.byref(pn), C.byref(pbytes))
     launches = int(lib.icep_kernel_launches() - launches0)
     iters, err, _ = sim.solver_stats()
     t_ms = reduce_max(dist, ms.value)
     if dist is not None:
         dist.barrier()
     value = world * args.steps / (t_ms / 1000.0)
-
-    # roofline of the dominant kernel: the x-pencil FFT pass (batch of 3 fields)
-    kms, kbytes = C.c_double(0), C.c_double(0)
-    lib.icep_time_kernel(sim.ctx, 1, 3, 50, C.byref(kms), C.byref(kbytes))
     peak, peak_kind = measured_peaks()
-    achieved = kbytes.value / (kms.value * 1e-3) / 1e9
+    achieved = pbytes.value / (pms.value * 1e-3) / 1e9 if pms.value > 0 else None
+    per_launch_bytes = pbytes.value / pn.value if pn.value else None
+    traffic = TRAFFIC.get((args.n, args.precision, PROBE_KERNEL))
 
     # end to end: the drop-in Time_evolution call on pinned host arrays
     shp = (p.nx, p.ny, 2 * (p.nz // 2 + 1))
@@ -328,10 +339,11 @@ def run_gpu(args, world, rank, local, dist):
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes},
             "gpu_launches": launches,
-            "roofline": {"bound": "hbm", "kernel": "k_pencils (x pass, 3 fields)", "achieved": achieved,
-                         "peak": peak, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                         "traffic": args.traffic, "ms_per_launch": kms.value,
-                         "bytes_per_launch": kbytes.value},
+            "roofline": {"bound": "hbm", "kernel": PROBE_KERNEL, "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind + " (hbm_gbs, copy)", "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None, "traffic": traffic,
+                         "launches_timed": pn.value, "ms_per_launch": pms.value / pn.value if pn.value else None,
+                         "bytes_per_launch": per_launch_bytes},
             "cpu_baseline": base}
     print(json.dumps(line), flush=True)
 
@@ -347,7 +359,6 @@ def main():
     ap.add_argument("--np", type=int, default=512)
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--maxit", type=int, default=1000)
-    ap.add_argument("--traffic", type=float, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()

@@ -2,6 +2,7 @@
 #include "fft_blocks.cuh"
 #include "kop.cuh"
 #include "krylov.cuh"
+#include "probe.cuh"
 
 namespace icep {
 
@@ -352,8 +353,11 @@ void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, c
   }
   const float scale = (float)(1.0 / ((double)p.g.nx * p.g.ny * p.g.nz));
   count_launch();
+  probe_begin(PROBE_KOP_PLANE, s);
   k_kop_plane<NY, H><<<dim3(p.g.nx, 3), 1024, sm, s>>>(p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z,
                                                              p.tw_post, scale);
+  // algorithmic bytes: per field the half spectrum in and out and eps_face_d in
+  probe_end(PROBE_KOP_PLANE, 3.0 * 3.0 * sizeof(float) * (double)p.g.nreal(), s);
 }
 
 template <int NY>
@@ -387,6 +391,7 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
   const unsigned nb = (unsigned)kop_pencil_blocks(g);
   const float ieps = (float)(1.0 / eps_ref);
   count_launch();
+  probe_begin(PROBE_KOP_XINV, s);
 #define KOP_XINV(N)                                                                                        \
   case N:                                                                                                  \
     set_x_attr<N>();                                                                                       \
@@ -401,6 +406,8 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
     KOP_XINV(256)
   }
 #undef KOP_XINV
+  // algorithmic bytes: r, v (and p) in, the updated vector and 3 fields out
+  probe_end(PROBE_KOP_XINV, (mode == KOP_P ? 7.0 : 6.0) * sizeof(float) * (double)g.nreal(), s);
 }
 
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
@@ -418,6 +425,7 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const f
   const Grid &g = p.g;
   const unsigned nb = (unsigned)kop_pencil_blocks(g);
   count_launch();
+  probe_begin(PROBE_KOP_XFWD, s);
 #define KOP_XFWD(N)                                                                                                 \
   case N:                                                                                                           \
     set_x_attr<N>();                                                                                                \
@@ -431,6 +439,8 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const f
     KOP_XFWD(256)
   }
 #undef KOP_XFWD
+  // algorithmic bytes: 3 fields and the dot operand in, the output vector out
+  probe_end(PROBE_KOP_XFWD, 5.0 * sizeof(float) * (double)g.nreal(), s);
 }
 
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,

@@ -198,6 +198,16 @@ void *icep_stream(icep_ctx *ctx);
 /* Block until the context's queued work has finished. */
 int icep_synchronize(icep_ctx *ctx);
 
+/* Measurement hook (no counterpart in the reference): time every launch of
+ * one kernel class with CUDA events on its stream until icep_probe_stop.
+ * kind: 1 fused plane pass of the k-space Poisson operator, 2 its fused
+ * inverse x pass, 3 its fused forward x pass. At most max_launches launches
+ * are timed. Process-wide; not for concurrent use. */
+int icep_probe_start(int kind, int max_launches);
+/* Ends the probe: total device time (ms), launches timed and their total
+ * algorithmic bytes (the kernel's external inputs and outputs). */
+int icep_probe_stop(double *ms_total, long long *launches_timed, double *bytes_total);
+
 #ifdef __cplusplus
 }
 #endif

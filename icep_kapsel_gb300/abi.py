@@ -17,6 +17,7 @@ FP64 = 0
 MIXED = 1
 SOLVER_REF = 0
 SOLVER_SPECTRAL = 1
+SOLVER_LEARNED = 2
 
 
 class Params(C.Structure):

@@ -7,7 +7,9 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <cstdio>
+#include <random>
 #include <utility>
 #include <vector>
 
@@ -16,6 +18,7 @@
 #include "krylov.cuh"
 #include "kop.cuh"
 #include "kspace.cuh"
+#include "unet.cuh"
 #include <type_traits>
 
 namespace icep {
@@ -47,6 +50,14 @@ class Engine : public EngineBase {
   double *kpart = nullptr;    // dot partials of the fused k-space iteration
   double *hkpart = nullptr;   // pinned
   int kop_npb = 0;
+  // learned preconditioner and its flexible GMRES (solver LEARNED)
+  static constexpr int FG_M = 20;  // restart length
+  bool learned = false;
+  UNet net;
+  bool net_trained = false, net_use = true;
+  float *fgV[FG_M + 1] = {nullptr}, *fgZ[FG_M] = {nullptr};
+  double *kcoef = nullptr, *hcoef = nullptr, *mpart = nullptr;
+  enum { KC_H1 = 0, KC_H2 = KVEC_MAX, KC_NRM = 2 * KVEC_MAX, KC_Y = 2 * KVEC_MAX + 1, KC_COUNT = 3 * KVEC_MAX + 1 };
   double *hscal = nullptr;  // pinned
   int *ljwork = nullptr;
   int ljwork_ints = 0;
@@ -89,6 +100,12 @@ class Engine : public EngineBase {
     cudaFree(shift_tab);
     cudaFree(kpart);
     cudaFreeHost(hkpart);
+    if (learned) net.free_all();
+    for (int i = 0; i <= FG_M; i++) cudaFree(fgV[i]);
+    for (int i = 0; i < FG_M; i++) cudaFree(fgZ[i]);
+    cudaFree(kcoef);
+    cudaFreeHost(hcoef);
+    cudaFree(mpart);
     cudaFreeHost(hscal);
     cudaFree(ljwork);
     cudaFree(dpairs_n);
@@ -251,6 +268,21 @@ class Engine : public EngineBase {
       const size_t nk = 2 * (2 * (size_t)kop_npb + DOT_BLOCKS);
       if (cudaMalloc(&kpart, sizeof(double) * nk) != cudaSuccess || cudaMallocHost(&hkpart, sizeof(double) * nk) != cudaSuccess)
         return fail(ICEP_ERR_CUDA, "allocation of the k-space dot partials failed");
+    }
+    if (p.solver == ICEP_SOLVER_LEARNED) {
+      if (!mixed || !electrolyte || !kpart || p.nx != p.ny || p.nx != p.nz || p.nx < 32)
+        return fail(ICEP_ERR_UNSUPPORTED,
+                    "solver LEARNED needs precision MIXED, Electrolyte, a cubic mesh of 32..128 per axis");
+      learned = true;
+      if (net.init(p.nx / 2, 0x1ce9u, s) != ICEP_OK) return fail(ICEP_ERR_CUDA, "network setup failed");
+      for (int i = 0; i <= FG_M; i++)
+        if (cudaMalloc(&fgV[i], sizeof(R) * g.nf()) != cudaSuccess) return fail(ICEP_ERR_CUDA, "GMRES vectors");
+      for (int i = 0; i < FG_M; i++)
+        if (cudaMalloc(&fgZ[i], sizeof(R) * g.nf()) != cudaSuccess) return fail(ICEP_ERR_CUDA, "GMRES vectors");
+      if (cudaMalloc(&kcoef, sizeof(double) * KC_COUNT) != cudaSuccess ||
+          cudaMallocHost(&hcoef, sizeof(double) * KC_COUNT) != cudaSuccess ||
+          cudaMalloc(&mpart, sizeof(double) * DOT_BLOCKS * KVEC_MAX) != cudaSuccess)
+        return fail(ICEP_ERR_CUDA, "GMRES scalars");
     }
     cudaMalloc(&scal, sizeof(double) * S_COUNT);
     cudaMemsetAsync(scal, 0, sizeof(double) * S_COUNT, s);
@@ -676,6 +708,377 @@ class Engine : public EngineBase {
     }
   }
 
+  // ---- learned preconditioner ------------------------------------------
+  // P(v) = M^-1 (v + c), c = rms(v) prolong(net(eps, v)) the network's
+  // correction of the residual (for the unit-norm k-space vector v); in the
+  // x~ form of the fused operator: x~ = v^ + c^, B x~ = A P(v).
+  void learned_precond(const float *vhat, float *xt, double eref) {
+    if constexpr (std::is_same<R, float>::value) {
+      if (!(net_trained && net_use)) {
+        cudaMemcpyAsync(xt, vhat, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+        return;
+      }
+      const double rms = 1.0 / sqrt((double)g.nreal());  // v has unit norm
+      cudaMemcpyAsync(f[F_KZ], vhat, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+      c2r(f[F_KZ]);
+      unet_input(g, f[F_EPS], f[F_KZ], eref, rms, net.x, s);
+      net.forward(s);
+      zero(F_WV1);
+      unet_prolong_add(g, net.y, rms, f[F_WV1], s);
+      r2c(f[F_WV1]);
+      kadd(g, vhat, f[F_WV1], xt, s);
+    }
+  }
+  // out = B x~ through the fused passes (no vector update, no dots)
+  void apply_Bk(float *xt, float *out) {
+    if constexpr (std::is_same<R, float>::value) {
+      kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, 0, mean_eps_cached, f[F_WV3_0], f[F_WV3_1],
+               f[F_WV3_2], s);
+      kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], s);
+      kop_xfwd(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], out, KOP_NONE, nullptr, nullptr, s);
+      matvecs++;
+    }
+  }
+  double mean_eps_cached = 1.0;
+  // |w|^2 (Parseval) into kcoef[slot] on the device
+  void knorm2(const float *w, int slot) {
+    KVecs one{};
+    one.p[0] = w;
+    kmdot(g, one, 1, w, mpart, s);
+    kmdot_final(mpart, 1, kcoef + slot, s);
+  }
+
+  /*
+   * Flexible GMRES(FG_M) in k-space on B x~ = b^ (b: F_KB, real, mean
+   * removed), right-preconditioned by learned_precond; classical Gram-Schmidt
+   * applied twice, FP64 dot products, one host synchronisation per
+   * iteration. Converges on the GMRES residual estimate; returns false in
+   * *ok when the residual stagnates across a restart or maxit is reached
+   * (the caller falls back to the plain solver). Leaves x = M^-1 x~ in F_KX.
+   */
+  int fgmres(double tol, int maxit, double eref, int *iters, double *rel_err, bool *ok) {
+    if constexpr (!std::is_same<R, float>::value) {
+      return ICEP_ERR_UNSUPPORTED;
+    } else {
+      float *bhat = f[F_KR0], *r = f[F_KR], *xt = f[F_KY];
+      copy_real<R>(g, f[F_KB], r, s);
+      r2c(r);
+      cudaMemsetAsync(r, 0, 2 * sizeof(R), s);
+      cudaMemcpyAsync(bhat, r, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+      kop_eps_faces(g, f[F_EPS], f[F_EF0], f[F_EF1], f[F_EF2], s);
+      mean_eps_cached = eref;
+      knorm2(r, KC_NRM);
+      cudaMemcpyAsync(hcoef, kcoef, sizeof(double) * KC_COUNT, cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fgmres");
+      double beta = sqrt(hcoef[KC_NRM]);
+      const double b0 = beta;
+      zero(F_KY);
+      *ok = true;
+      if (!(beta > 0.0)) {
+        zero(F_KX);
+        *iters = 0;
+        *rel_err = 0.0;
+        return ICEP_OK;
+      }
+      double H[FG_M + 1][FG_M], cs[FG_M], sn[FG_M], gv[FG_M + 1], y[FG_M];
+      int total = 0, apps = 0;
+      bool conv = false;
+      double resid = beta, prev_beta = beta;
+      while (total < maxit && !conv) {
+        kscale_by_norm(g, r, fgV[0], kcoef + KC_NRM, s);
+        for (int i = 0; i <= FG_M; i++) gv[i] = 0.0;
+        gv[0] = beta;
+        int j = 0;
+        for (; j < FG_M && total < maxit; j++) {
+          learned_precond(fgV[j], fgZ[j], eref);
+          apps++;
+          apply_Bk(fgZ[j], fgV[j + 1]);
+          KVecs Vs{};
+          for (int i = 0; i <= j; i++) Vs.p[i] = fgV[i];
+          kmdot(g, Vs, j + 1, fgV[j + 1], mpart, s);
+          kmdot_final(mpart, j + 1, kcoef + KC_H1, s);
+          kmaxpy(g, fgV[j + 1], Vs, j + 1, kcoef + KC_H1, -1.0, s);
+          kmdot(g, Vs, j + 1, fgV[j + 1], mpart, s);
+          kmdot_final(mpart, j + 1, kcoef + KC_H2, s);
+          kmaxpy(g, fgV[j + 1], Vs, j + 1, kcoef + KC_H2, -1.0, s);
+          knorm2(fgV[j + 1], KC_NRM);
+          kscale_by_norm(g, fgV[j + 1], fgV[j + 1], kcoef + KC_NRM, s);
+          cudaMemcpyAsync(hcoef, kcoef, sizeof(double) * KC_Y, cudaMemcpyDeviceToHost, s);
+          if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fgmres iteration");
+          for (int i = 0; i <= j; i++) H[i][j] = hcoef[KC_H1 + i] + hcoef[KC_H2 + i];
+          H[j + 1][j] = sqrt(std::max(hcoef[KC_NRM], 0.0));
+          for (int i = 0; i < j; i++) {  // previous rotations
+            const double a = H[i][j], b = H[i + 1][j];
+            H[i][j] = cs[i] * a + sn[i] * b;
+            H[i + 1][j] = -sn[i] * a + cs[i] * b;
+          }
+          const double a = H[j][j], b = H[j + 1][j];
+          const double rr = std::hypot(a, b);
+          cs[j] = (rr > 0) ? a / rr : 1.0;
+          sn[j] = (rr > 0) ? b / rr : 0.0;
+          H[j][j] = rr;
+          H[j + 1][j] = 0.0;
+          gv[j + 1] = -sn[j] * gv[j];
+          gv[j] = cs[j] * gv[j];
+          total++;
+          resid = fabs(gv[j + 1]);
+          if (!std::isfinite(resid)) {
+            *ok = false;
+            break;
+          }
+          if (resid <= tol * b0) {
+            j++;
+            conv = true;
+            break;
+          }
+        }
+        if (!*ok) break;
+        for (int i = j - 1; i >= 0; i--) {  // H y = g
+          double t = gv[i];
+          for (int k2 = i + 1; k2 < j; k2++) t -= H[i][k2] * y[k2];
+          y[i] = (H[i][i] != 0.0) ? t / H[i][i] : 0.0;
+        }
+        for (int i = 0; i < j; i++) hcoef[KC_Y + i] = y[i];
+        cudaMemcpyAsync(kcoef + KC_Y, hcoef + KC_Y, sizeof(double) * j, cudaMemcpyHostToDevice, s);
+        KVecs Zs{};
+        for (int i = 0; i < j; i++) Zs.p[i] = fgZ[i];
+        kmaxpy(g, xt, Zs, j, kcoef + KC_Y, 1.0, s);
+        if (conv) break;
+        // restart from the true k-space residual
+        apply_Bk(xt, fgV[0]);
+        ksub(g, bhat, fgV[0], r, s);
+        knorm2(r, KC_NRM);
+        cudaMemcpyAsync(hcoef, kcoef, sizeof(double) * KC_Y, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fgmres restart");
+        beta = sqrt(std::max(hcoef[KC_NRM], 0.0));
+        resid = beta;
+        if (!(beta < 0.9 * prev_beta)) {  // stagnation across a restart
+          *ok = false;
+          break;
+        }
+        prev_beta = beta;
+        if (beta <= tol * b0) conv = true;
+      }
+      if (!conv) *ok = false;
+      kprecond<R>(g, xt, f[F_KX], eref, s);
+      c2r(f[F_KX]);
+      *iters = total;
+      *rel_err = resid / b0;
+      last_precond_apps += apps;
+      return ICEP_OK;
+    }
+  }
+
+  // random sphere centres in [0, L)^3 with periodic separation >= dmin
+  bool random_positions(std::mt19937_64 &rng, double dmin) {
+    const double L[3] = {g.nx * P.dx, g.ny * P.dx, g.nz * P.dx};
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    std::vector<double> c;
+    for (int q = 0; q < np; q++) {
+      bool placed = false;
+      for (int tries = 0; tries < 20000 && !placed; tries++) {
+        double x[3];
+        for (int d = 0; d < 3; d++) x[d] = u(rng) * L[d];
+        placed = true;
+        for (int o = 0; o < q && placed; o++) {
+          double r2 = 0;
+          for (int d = 0; d < 3; d++) {
+            double dd = fabs(x[d] - c[3 * o + d]);
+            dd = std::min(dd, L[d] - dd);
+            r2 += dd * dd;
+          }
+          placed = r2 >= dmin * dmin;
+        }
+        if (placed) {
+          for (int d = 0; d < 3; d++) {
+            c.push_back(x[d]);
+            hp[q].x[d] = hp[q].x_nopbc[d] = x[d];
+          }
+        }
+      }
+      if (!placed) return false;
+    }
+    return true;
+  }
+
+  // z = P(r) for the unit-norm real residual r (F_KR) into F_KZ: the spectral
+  // inverse of r plus, with use_net, the network's correction of r
+  void learned_precond_real(double eref, bool use_net) {
+    const double rms = 1.0 / sqrt((double)g.nreal());
+    copy_real<R>(g, f[F_KR], f[F_KZ], s);
+    if (use_net) {
+      if constexpr (std::is_same<R, float>::value) {
+        unet_input(g, f[F_EPS], f[F_KR], eref, rms, net.x, s);
+        net.forward(s);
+        unet_prolong_add(g, net.y, rms, f[F_KZ], s);
+      }
+    }
+    precond(f[F_KZ], f[F_KZ], eref);
+  }
+
+  // one training step on the unit-norm residual in F_KR (real):
+  // loss = |r - A P(r)|^2; dL/dc = -2 M^-1 A (r - A P(r)) for the correction c.
+  // Leaves the normalised next residual (r - A P(r))/|.| in F_KR.
+  int train_step(double eref, float lr, double *loss) {
+    if constexpr (std::is_same<R, float>::value) {
+      const double rms = 1.0 / sqrt((double)g.nreal());
+      learned_precond_real(eref, true);
+      apply_A(f[F_KZ], f[F_KT]);
+      sub_real<R>(g, f[F_KR], f[F_KT], f[F_KS], s);
+      dots<R>(g, f[F_KS], f[F_KS], f[F_KS], f[F_KS], 1, partials, scal, S_AUX0, s);
+      apply_A(f[F_KS], f[F_KT]);
+      precond(f[F_KT], f[F_KT], eref);
+      unet_prolong_adjoint(g, f[F_KT], -2.0 * rms, net.gy, s);
+      net.backward(s);
+      net.adam_step(lr, s);
+      int st = read_scal();
+      if (st) return st;
+      *loss = hscal[S_AUX0];
+      const double nrm = sqrt(*loss);
+      scale_copy<R>(g, f[F_KS], f[F_KR], (R)(nrm > 0 ? 1.0 / nrm : 0.0), s);
+    }
+    return ICEP_OK;
+  }
+
+  // Mean one-step loss |r - A P(r)|^2 of the spectral-only and the learned
+  // preconditioner on the same residuals: the context's right-hand side
+  // (normalised) and the next chain-1 residuals of the spectral iteration.
+  int learned_eval(int chain, double *loss_spectral, double *loss_learned) override {
+    if (!learned) return unsupported_learned();
+    if (chain < 1) return fail(ICEP_ERR_ARG, "learned_eval chain");
+    const double eref = mean_eps();
+    build_rhs(F_KB, F_RHO);
+    dots<R>(g, f[F_KB], f[F_KB], f[F_KB], f[F_KB], 1, partials, scal, S_AUX0, s);
+    sum_real<R>(g, f[F_KB], partials, scal, S_AUX1, s);
+    int st = read_scal();
+    if (st) return st;
+    sub_mean<R>(g, f[F_KB], scal, S_AUX1, s);
+    dots<R>(g, f[F_KB], f[F_KB], f[F_KB], f[F_KB], 1, partials, scal, S_AUX0, s);
+    if ((st = read_scal())) return st;
+    scale_copy<R>(g, f[F_KB], f[F_KB], (R)(1.0 / sqrt(hscal[S_AUX0])), s);
+    double ls = 0, ll = 0;
+    for (int k = 0; k < chain; k++) {
+      double l[2];
+      for (int use = 1; use >= 0; use--) {
+        copy_real<R>(g, f[F_KB], f[F_KR], s);
+        learned_precond_real(eref, use == 1 && net_trained);
+        apply_A(f[F_KZ], f[F_KT]);
+        sub_real<R>(g, f[F_KR], f[F_KT], f[F_KS], s);
+        dots<R>(g, f[F_KS], f[F_KS], f[F_KS], f[F_KS], 1, partials, scal, S_AUX0, s);
+        if ((st = read_scal())) return st;
+        l[use] = hscal[S_AUX0];
+      }
+      ls += l[0];
+      ll += l[1];
+      // next residual of the spectral chain (F_KS holds it after use = 0)
+      scale_copy<R>(g, f[F_KS], f[F_KB], (R)(1.0 / sqrt(l[0])), s);
+    }
+    *loss_spectral = ls / chain;
+    *loss_learned = ll / chain;
+    return ICEP_OK;
+  }
+
+  int learned_train(int configs, int steps, unsigned seed, double lr, double *loss_first, double *loss_last) override {
+    if (!learned) return unsupported_learned();
+    if (configs < 1 || steps < 1 || !(lr > 0)) return fail(ICEP_ERR_ARG, "learned_train arguments");
+    std::vector<icep_particle> keep(np > 0 ? np : 1);
+    cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
+    memcpy(keep.data(), hp, sizeof(icep_particle) * np);
+    const double e_keep[3] = {P.e_ext[0], P.e_ext[1], P.e_ext[2]};
+    double emag = sqrt(e_keep[0] * e_keep[0] + e_keep[1] * e_keep[1] + e_keep[2] * e_keep[2]);
+    if (!(emag > 0)) emag = 0.1;
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<double> nd(0.0, 1.0);
+    std::uniform_real_distribution<double> u(0.0, 1.0);
+    int st = ICEP_OK;
+    double loss = 0.0;
+    for (int c = 0; c < configs && st == ICEP_OK; c++) {
+      if (!random_positions(rng, 2.0 * P.a * P.dx + P.dx)) {
+        st = fail(ICEP_ERR_ARG, "cannot place the training particles");
+        break;
+      }
+      for (int q = 0; q < np; q++) hp[q].eps_p = P.per_particle_eps ? 1.0 + 9.0 * u(rng) : P.eps_particle_top;
+      cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
+      double e[3] = {nd(rng), nd(rng), nd(rng)};
+      const double en = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
+      for (int d = 0; d < 3; d++) P.e_ext[d] = emag * e[d] / en;
+      make_dielectric_field(F_WORK, F_WV1);
+      const double eref = mean_eps();
+      zero(F_KT);
+      build_rhs(F_KR, F_KT);  // b = D^-(eps_face E), no free charge
+      dots<R>(g, f[F_KR], f[F_KR], f[F_KR], f[F_KR], 1, partials, scal, S_AUX0, s);
+      if ((st = read_scal())) break;
+      scale_copy<R>(g, f[F_KR], f[F_KR], (R)(1.0 / sqrt(hscal[S_AUX0])), s);
+      for (int k = 0; k < steps && st == ICEP_OK; k++) {
+        st = train_step(eref, (float)lr, &loss);
+        if (c == 0 && k == 0 && loss_first) *loss_first = loss;
+      }
+    }
+    if (loss_last) *loss_last = loss;
+    // the context's own state back
+    for (int d = 0; d < 3; d++) P.e_ext[d] = e_keep[d];
+    memcpy(hp, keep.data(), sizeof(icep_particle) * np);
+    cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
+    make_dielectric_field(F_WORK, F_WV1);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
+    if (st == ICEP_OK) net_trained = true;
+    return st;
+  }
+  int learned_enable(int on) override {
+    if (!learned) return unsupported_learned();
+    net_use = on != 0;
+    if (on) net_trained = true;  // parameters set by the caller count as trained
+    return ICEP_OK;
+  }
+  long learned_nparams() override { return learned ? net.nparams : 0; }
+  int learned_params(double *buf, bool get) override {
+    if (!learned) return unsupported_learned();
+    std::vector<float> h(net.nparams);
+    if (get) {
+      cudaMemcpyAsync(h.data(), net.params, sizeof(float) * net.nparams, cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_params");
+      for (long q = 0; q < net.nparams; q++) buf[q] = h[q];
+    } else {
+      for (long q = 0; q < net.nparams; q++) h[q] = (float)buf[q];
+      cudaMemcpyAsync(net.params, h.data(), sizeof(float) * net.nparams, cudaMemcpyHostToDevice, s);
+      net.pack(s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_params");
+    }
+    return ICEP_OK;
+  }
+  // network on host fine fields (padded layout): y (coarse n^3)
+  int learned_forward(const double *eps, const double *r, double eps_ref, double *y) override {
+    if (!learned) return unsupported_learned();
+    int st;
+    if ((st = set_field(F_WORK, eps)) || (st = set_field(F_KR, r))) return st;
+    if constexpr (std::is_same<R, float>::value) {
+      dots<R>(g, f[F_KR], f[F_KR], f[F_KR], f[F_KR], 1, partials, scal, S_AUX0, s);
+      if ((st = read_scal())) return st;
+      const double rms = sqrt(hscal[S_AUX0] / (double)g.nreal());
+      unet_input(g, f[F_WORK], f[F_KR], eps_ref, rms, net.x, s);
+      net.forward(s);
+      const long nc = (long)net.n * net.n * net.n;
+      std::vector<float> h(nc);
+      cudaMemcpyAsync(h.data(), net.y, sizeof(float) * nc, cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_forward");
+      for (long q = 0; q < nc; q++) y[q] = h[q];
+    }
+    return ICEP_OK;
+  }
+  int learned_backward(const double *gy, double *grad) override {
+    if (!learned) return unsupported_learned();
+    const long nc = (long)net.n * net.n * net.n;
+    std::vector<float> h(std::max(nc, net.nparams));
+    for (long q = 0; q < nc; q++) h[q] = (float)gy[q];
+    cudaMemcpyAsync(net.gy, h.data(), sizeof(float) * nc, cudaMemcpyHostToDevice, s);
+    net.backward(s);
+    cudaMemcpyAsync(h.data(), net.grads, sizeof(float) * net.nparams, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_backward");
+    for (long q = 0; q < net.nparams; q++) grad[q] = h[q];
+    return ICEP_OK;
+  }
+
   double mean_eps() {
     sum_real<R>(g, f[F_EPS], partials, scal, S_AUX1, s);
     if (read_scal()) return 1.0;
@@ -747,6 +1150,8 @@ class Engine : public EngineBase {
     const double eref = mean_eps();
     int total_inner = 0;
     double rel = 0.0;
+    last_fallbacks = 0;
+    last_precond_apps = 0;
     if (bb > 0.0) {
       const double tol2 = P.potential_tol * P.potential_tol * bb;
       for (int outer = 0; outer < 30; outer++) {
@@ -766,9 +1171,19 @@ class Engine : public EngineBase {
         if (inner_tol > 0.5) inner_tol = 0.5;
         int it = 0;
         double er = 0.0;
-        if ((st = kpart ? bicgstab_kf(inner_tol, P.potential_iter, eref, &it, &er)
-                        : bicgstab_k(inner_tol, P.potential_iter, eref, &it, &er)))
+        if (learned) {
+          bool ok = true;
+          if ((st = fgmres(inner_tol, P.potential_iter, eref, &it, &er, &ok))) return st;
+          if (!ok) {  // stagnation: the plain solver from a zero guess
+            last_fallbacks++;
+            int it2 = 0;
+            if ((st = bicgstab_kf(inner_tol, P.potential_iter, eref, &it2, &er))) return st;
+            it += it2;
+          }
+        } else if ((st = kpart ? bicgstab_kf(inner_tol, P.potential_iter, eref, &it, &er)
+                               : bicgstab_k(inner_tol, P.potential_iter, eref, &it, &er))) {
           return st;
+        }
         total_inner += it;
         add_f2d(G, (const float *)f[F_KX], d64[D_X], rn, s);
       }

@@ -33,6 +33,24 @@ struct EngineBase {
   virtual int time_kernel(int which, int batch, int reps, double *ms, double *bytes) = 0;
   // accumulated device time per step phase (ICEP_PHASE_PROFILE=1 at create)
   virtual int phase_times(double *ms, int n) = 0;
+  // learned preconditioner (MIXED precision with solver ICEP_SOLVER_LEARNED)
+  virtual int learned_train(int configs, int steps, unsigned seed, double lr, double *loss_first, double *loss_last) {
+    return unsupported_learned();
+  }
+  virtual int learned_enable(int on) { return unsupported_learned(); }
+  virtual int learned_eval(int chain, double *loss_spectral, double *loss_learned) { return unsupported_learned(); }
+  virtual long learned_nparams() { return 0; }
+  virtual int learned_params(double *buf, bool get) { return unsupported_learned(); }
+  virtual int learned_forward(const double *eps, const double *r, double eps_ref, double *y) {
+    return unsupported_learned();
+  }
+  virtual int learned_backward(const double *gy, double *grad) { return unsupported_learned(); }
+  int unsupported_learned() {
+    err = "the learned preconditioner needs precision MIXED and solver LEARNED";
+    return ICEP_ERR_UNSUPPORTED;
+  }
+  int last_fallbacks = 0;      // plain-solver fallbacks of the last learned solve
+  int last_precond_apps = 0;   // preconditioner applications of the last learned solve
   int ts = 0;
   double time = 0.0;
   int last_iters = 0;

@@ -188,4 +188,34 @@ int icep_unpin_host(void *p) { return (p && cudaHostUnregister(p) == cudaSuccess
 /* generic dispatch used by the Python layer (same numbering as the oracle) */
 int icep_call(icep_ctx *c, int fn) { return ok(c) ? wrap(c, c->e->call(fn)) : ICEP_ERR_ARG; }
 
+/* learned preconditioner */
+int icep_learned_train(icep_ctx *c, int configs, int steps_per_config, unsigned seed, double lr, double *loss_first,
+                       double *loss_last) {
+  return ok(c) ? wrap(c, c->e->learned_train(configs, steps_per_config, seed, lr, loss_first, loss_last)) : ICEP_ERR_ARG;
+}
+int icep_learned_enable(icep_ctx *c, int on) { return ok(c) ? wrap(c, c->e->learned_enable(on)) : ICEP_ERR_ARG; }
+int icep_learned_eval(icep_ctx *c, int chain, double *loss_spectral, double *loss_learned) {
+  return ok(c) && loss_spectral && loss_learned ? wrap(c, c->e->learned_eval(chain, loss_spectral, loss_learned))
+                                                : ICEP_ERR_ARG;
+}
+long icep_learned_nparams(icep_ctx *c) { return ok(c) ? c->e->learned_nparams() : 0; }
+int icep_learned_get_params(icep_ctx *c, double *params) {
+  return ok(c) && params ? wrap(c, c->e->learned_params(params, true)) : ICEP_ERR_ARG;
+}
+int icep_learned_set_params(icep_ctx *c, const double *params) {
+  return ok(c) && params ? wrap(c, c->e->learned_params(const_cast<double *>(params), false)) : ICEP_ERR_ARG;
+}
+int icep_learned_forward(icep_ctx *c, const double *eps, const double *r, double eps_ref, double *y) {
+  return ok(c) && eps && r && y ? wrap(c, c->e->learned_forward(eps, r, eps_ref, y)) : ICEP_ERR_ARG;
+}
+int icep_learned_backward(icep_ctx *c, const double *gy, double *grad) {
+  return ok(c) && gy && grad ? wrap(c, c->e->learned_backward(gy, grad)) : ICEP_ERR_ARG;
+}
+int icep_learned_stats(icep_ctx *c, int *fallbacks, int *precond_apps) {
+  if (!ok(c)) return ICEP_ERR_ARG;
+  if (fallbacks) *fallbacks = c->e->last_fallbacks;
+  if (precond_apps) *precond_apps = c->e->last_precond_apps;
+  return ICEP_OK;
+}
+
 }  // extern "C"

@@ -144,6 +144,10 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
     const int j = pj[w], kz = pkz[w];
     const long idx = (long)e * nq + q;
     const int wt = read_weight(g, e, j, kz);
+    if (mode == KOP_NONE) {
+      raw[e * sw + w] = ldw(vec, idx, wt);
+      continue;
+    }
     const cf rr = ldw(r, idx, wt), vv = ldw(v, idx, wt);
     cf nv;
     if (mode == KOP_P) {
@@ -268,6 +272,7 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
     const cf a = acc[e * sw + w];
     const cf val{-a.y, a.x};  // i * acc
     reinterpret_cast<float2 *>(out)[idx] = make_float2(val.x, val.y);
+    if (mode == KOP_NONE) continue;
     const double vr = val.x, vi = (wt == 1) ? 0.0 : (double)val.y;
     const cf o = ldw(other, idx, wt);
     if (mode == KOP_P) {
@@ -278,7 +283,7 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
     }
   }
   const double inv = 1.0 / (double)g.nreal();
-  block_partials(s0 * inv, s1 * inv, partials);
+  if (mode != KOP_NONE) block_partials(s0 * inv, s1 * inv, partials);
 }
 
 __global__ void k_kop_xr(Grid g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
@@ -407,7 +412,7 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
   }
 #undef KOP_XINV
   // algorithmic bytes: r, v (and p) in, the updated vector and 3 fields out
-  probe_end(PROBE_KOP_XINV, (mode == KOP_P ? 7.0 : 6.0) * sizeof(float) * (double)g.nreal(), s);
+  probe_end(PROBE_KOP_XINV, (mode == KOP_P ? 7.0 : mode == KOP_S ? 6.0 : 4.0) * sizeof(float) * (double)g.nreal(), s);
 }
 
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
@@ -440,7 +445,7 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const f
   }
 #undef KOP_XFWD
   // algorithmic bytes: 3 fields and the dot operand in, the output vector out
-  probe_end(PROBE_KOP_XFWD, 5.0 * sizeof(float) * (double)g.nreal(), s);
+  probe_end(PROBE_KOP_XFWD, (mode == KOP_NONE ? 4.0 : 5.0) * sizeof(float) * (double)g.nreal(), s);
 }
 
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,

@@ -21,7 +21,7 @@
 
 namespace icep {
 
-enum { KOP_P = 0, KOP_S = 1 };
+enum { KOP_P = 0, KOP_S = 1, KOP_NONE = 2 };
 
 // true if the fused passes cover this grid (an x-plane fits in shared memory)
 bool kop_supported(const Grid &g);
@@ -30,14 +30,16 @@ int kop_pencil_blocks(const Grid &g);
 // ef_d = 0.5 (eps + eps at the next point along d), real points
 void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, float *ef2, cudaStream_t s);
 // mode KOP_P: vec = p <- P(r) + beta (P(p) - omega P(v));
-// mode KOP_S: vec = s <- P(r) - alpha P(v), alpha = rho / sum_b part[2b].
+// mode KOP_S: vec = s <- P(r) - alpha P(v), alpha = rho / sum_b part[2b];
+// mode KOP_NONE: vec is used as it is (r, v unused).
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
               double omega, double rho, const double *part, int npart, double eps_ref, float *w0, float *w1,
               float *w2, cudaStream_t s);
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
                const float *ef2, cudaStream_t s);
 // mode KOP_P: partials[2b] = (other, out) with other = r0;
-// mode KOP_S: partials[2b] = (out, out), partials[2b+1] = (out, other) with other = s.
+// mode KOP_S: partials[2b] = (out, out), partials[2b+1] = (out, other) with other = s;
+// mode KOP_NONE: no dot products (other, partials unused).
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
               const float *other, double *partials, cudaStream_t s);
 // alpha = rho / sum part1[2b]; omega = sum part2[2b+1] / sum part2[2b];

@@ -34,6 +34,14 @@ __device__ __forceinline__ void ld(const R *__restrict__ a, const KMode &m, int 
   im = (w == 1) ? R(0) : a[m.im + 1];
 }
 
+struct R2 {
+  float x, y;
+};
+__device__ __forceinline__ void ldv(const float *a, const KMode &m, int wt, R2 &v) {
+  v.x = a[m.im];
+  v.y = (wt == 1) ? 0.f : a[m.im + 1];
+}
+
 template <typename R>
 __device__ __forceinline__ void kvec(const Grid &g, const KMode &m, R *k) {
   k[0] = (R)g.wave[0] * (R)kx_of(g, m.i);
@@ -228,6 +236,117 @@ __global__ void k_kprecond(Grid g, const R *x, R *y, R ieps) {
   y[m.im + 1] = mm * im;
 }
 
+// groups of four vectors per pass keep the accumulators in registers
+__global__ void k_kmdot(Grid g, KVecs V, int nv, const float *w, double *partials) {
+  __shared__ double red[4][32];
+  const unsigned N = (unsigned)g.nmodes();
+  const double inv = 1.0 / (double)g.nreal();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i0 = 0; i0 < nv; i0 += 4) {
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+      KMode m;
+      kmode(g, t, m);
+      const int wt = kweight(g, m);
+      if (wt == 0) continue;
+      R2 wv;
+      ldv(w, m, wt, wv);
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        if (i0 + q < nv) {
+          R2 a;
+          ldv(V.p[i0 + q], m, wt, a);
+          acc[q] += (double)wt * ((double)a.x * (double)wv.x + (double)a.y * (double)wv.y);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      double v = acc[q] * inv;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (lane == 0) red[q][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && i0 + (int)threadIdx.x < nv) {
+      double t2 = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); q++) t2 += red[threadIdx.x][q];
+      partials[(long)blockIdx.x * nv + i0 + threadIdx.x] = t2;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_kmdot_final(const double *partials, int nblocks, int nv, double *out) {
+  const int i = blockIdx.x;
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(long)b * nv + i];
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if (lane == 0) red[wid] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t2 = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t2 += red[q];
+    out[i] = t2;
+  }
+}
+
+__global__ void k_kmaxpy(Grid g, float *w, KVecs V, int nv, const double *coef, float sign) {
+  KMode m;
+  if (!kmode(g, KTID, m)) return;
+  const int wt = kweight(g, m);
+  if (wt == 0) return;
+  R2 a;
+  ldv(w, m, wt, a);
+  for (int i = 0; i < nv; i++) {
+    R2 v;
+    ldv(V.p[i], m, wt, v);
+    const float c = sign * (float)coef[i];
+    a.x += c * v.x;
+    a.y += c * v.y;
+  }
+  w[m.im] = a.x;
+  w[m.im + 1] = a.y;
+}
+
+__global__ void k_kscale_by_norm(Grid g, const float *w, float *out, const double *nrm2) {
+  KMode m;
+  if (!kmode(g, KTID, m)) return;
+  const int wt = kweight(g, m);
+  if (wt == 0) return;
+  const double n2 = *nrm2;
+  const float f = (n2 > 0.0) ? (float)(1.0 / sqrt(n2)) : 0.f;
+  R2 a;
+  ldv(w, m, wt, a);
+  out[m.im] = f * a.x;
+  out[m.im + 1] = f * a.y;
+}
+
+__global__ void k_kadd(Grid g, const float *v, const float *z, float *xt) {
+  KMode m;
+  if (!kmode(g, KTID, m)) return;
+  const int wt = kweight(g, m);
+  if (wt == 0) return;
+  R2 a, b;
+  ldv(v, m, wt, a);
+  ldv(z, m, wt, b);
+  xt[m.im] = a.x + b.x;
+  xt[m.im + 1] = a.y + b.y;
+}
+
+__global__ void k_ksub(Grid g, const float *b, const float *w, float *r) {
+  KMode m;
+  if (!kmode(g, KTID, m)) return;
+  const int wt = kweight(g, m);
+  if (wt == 0) return;
+  R2 x, y;
+  ldv(b, m, wt, x);
+  ldv(w, m, wt, y);
+  r[m.im] = x.x - y.x;
+  r[m.im + 1] = x.y - y.y;
+}
+
 inline unsigned nblk(const Grid &g) { return div_up(g.nmodes(), TPB); }
 
 }  // namespace
@@ -270,6 +389,31 @@ template <typename R>
 void kprecond(const Grid &g, const R *x, R *y, double eps_ref, cudaStream_t s) {
   count_launch();
   k_kprecond<R><<<nblk(g), TPB, 0, s>>>(g, x, y, (R)(1.0 / eps_ref));
+}
+
+void kmdot(const Grid &g, const KVecs &V, int nv, const float *w, double *partials, cudaStream_t s) {
+  count_launch();
+  k_kmdot<<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, V, nv, w, partials);
+}
+void kmdot_final(const double *partials, int nv, double *out, cudaStream_t s) {
+  count_launch();
+  k_kmdot_final<<<nv, 256, 0, s>>>(partials, DOT_BLOCKS, nv, out);
+}
+void kmaxpy(const Grid &g, float *w, const KVecs &V, int nv, const double *coef, double sign, cudaStream_t s) {
+  count_launch();
+  k_kmaxpy<<<nblk(g), TPB, 0, s>>>(g, w, V, nv, coef, (float)sign);
+}
+void kscale_by_norm(const Grid &g, const float *w, float *out, const double *nrm2, cudaStream_t s) {
+  count_launch();
+  k_kscale_by_norm<<<nblk(g), TPB, 0, s>>>(g, w, out, nrm2);
+}
+void kadd(const Grid &g, const float *v, const float *z, float *xt, cudaStream_t s) {
+  count_launch();
+  k_kadd<<<nblk(g), TPB, 0, s>>>(g, v, z, xt);
+}
+void ksub(const Grid &g, const float *b, const float *w, float *r, cudaStream_t s) {
+  count_launch();
+  k_ksub<<<nblk(g), TPB, 0, s>>>(g, b, w, r);
 }
 
 #define KS_INST(R)                                                                                                 \

@@ -46,4 +46,22 @@ void kdiv_post(const Grid &g, const R *w0, const R *w1, const R *w2, R *v, cudaS
 template <typename R>
 void kprecond(const Grid &g, const R *x, R *y, double eps_ref, cudaStream_t s);
 
+// ---- vectors of the flexible GMRES (k-space, read modes) ------------------
+constexpr int KVEC_MAX = 34;
+struct KVecs {
+  const float *p[KVEC_MAX];
+};
+// partials[b * nv + i] = block b's part of (V_i, w), DOT_BLOCKS blocks
+void kmdot(const Grid &g, const KVecs &V, int nv, const float *w, double *partials, cudaStream_t s);
+// out[i] = sum over blocks of partials[b * nv + i] (block order)
+void kmdot_final(const double *partials, int nv, double *out, cudaStream_t s);
+// w += sign * sum_i coef[i] V_i (coef on the device)
+void kmaxpy(const Grid &g, float *w, const KVecs &V, int nv, const double *coef, double sign, cudaStream_t s);
+// out = w / sqrt(*nrm2)
+void kscale_by_norm(const Grid &g, const float *w, float *out, const double *nrm2, cudaStream_t s);
+// xt = v + z
+void kadd(const Grid &g, const float *v, const float *z, float *xt, cudaStream_t s);
+// r = b - w
+void ksub(const Grid &g, const float *b, const float *w, float *r, cudaStream_t s);
+
 }  // namespace icep

@@ -85,6 +85,16 @@ def load_library(path=None):
     L.icep_time_evolution.argtypes = [V, _DP, _DP, _DP, _DP, _DP, _DP, V, I]
     L.icep_stream.restype = V
     L.icep_stream.argtypes = [V]
+    L.icep_learned_train.argtypes = [V, I, I, C.c_uint, C.c_double, _DP, _DP]
+    L.icep_learned_enable.argtypes = [V, I]
+    L.icep_learned_eval.argtypes = [V, I, _DP, _DP]
+    L.icep_learned_nparams.restype = C.c_long
+    L.icep_learned_nparams.argtypes = [V]
+    L.icep_learned_get_params.argtypes = [V, _DP]
+    L.icep_learned_set_params.argtypes = [V, _DP]
+    L.icep_learned_forward.argtypes = [V, _DP, _DP, C.c_double, _DP]
+    L.icep_learned_backward.argtypes = [V, _DP, _DP]
+    L.icep_learned_stats.argtypes = [V, C.POINTER(I), C.POINTER(I)]
     _lib = L
     return L
 
@@ -199,6 +209,50 @@ class Simulation:
 
     def last_error(self):
         return self.solver_stats()[1]
+
+    # learned preconditioner (solver LEARNED)
+    def learned_train(self, configs, steps, seed=1, lr=1e-3):
+        l0, l1 = C.c_double(0), C.c_double(0)
+        self._check(self.lib.icep_learned_train(self.ctx, configs, steps, seed, lr, C.byref(l0), C.byref(l1)),
+                    "learned_train")
+        return l0.value, l1.value
+
+    def learned_eval(self, chain=4):
+        a, b = C.c_double(0), C.c_double(0)
+        self._check(self.lib.icep_learned_eval(self.ctx, chain, C.byref(a), C.byref(b)), "learned_eval")
+        return a.value, b.value
+
+    def learned_enable(self, on):
+        self._check(self.lib.icep_learned_enable(self.ctx, 1 if on else 0), "learned_enable")
+
+    def learned_params(self):
+        out = np.zeros(self.lib.icep_learned_nparams(self.ctx))
+        self._check(self.lib.icep_learned_get_params(self.ctx, _dp(out)), "learned_get_params")
+        return out
+
+    def set_learned_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        self._check(self.lib.icep_learned_set_params(self.ctx, _dp(p)), "learned_set_params")
+
+    def learned_forward(self, eps, r, eps_ref):
+        """Network output on the half-resolution grid for fine real fields eps, r."""
+        n = self.params.nx // 2
+        y = np.zeros(n * n * n)
+        e = np.ascontiguousarray(eps, dtype=np.float64).reshape(self._shape())
+        rr = np.ascontiguousarray(r, dtype=np.float64).reshape(self._shape())
+        self._check(self.lib.icep_learned_forward(self.ctx, _dp(e), _dp(rr), eps_ref, _dp(y)), "learned_forward")
+        return y.reshape(n, n, n)
+
+    def learned_backward(self, gy):
+        g = np.zeros(self.lib.icep_learned_nparams(self.ctx))
+        gy = np.ascontiguousarray(gy, dtype=np.float64)
+        self._check(self.lib.icep_learned_backward(self.ctx, _dp(gy), _dp(g)), "learned_backward")
+        return g
+
+    def learned_stats(self):
+        fb, ap = C.c_int(0), C.c_int(0)
+        self._check(self.lib.icep_learned_stats(self.ctx, C.byref(fb), C.byref(ap)), "learned_stats")
+        return fb.value, ap.value
 
     def lj_pairs(self, max_pairs=1 << 20):
         buf = np.zeros(2 * max_pairs, dtype=np.int32)

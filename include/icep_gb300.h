@@ -167,6 +167,43 @@ int icep_solver_stats(icep_ctx *ctx, int *iterations, double *error, long *matve
  * checker used by the tests). */
 int icep_call(icep_ctx *ctx, int fn);
 
+/* ---- learned Poisson preconditioner (no reference counterpart) -----------
+ * Contexts created with precision ICEP_MIXED and solver ICEP_SOLVER_LEARNED
+ * (cubic mesh 32..128) solve the inner correction systems of
+ * Charge_field2potential_dielectric with flexible GMRES whose preconditioner
+ * is the spectral one applied to the residual plus a U-Net correction of it
+ * (computed on the half-resolution grid, BF16 tensor cores); the spectral BiCGSTAB is the fallback when the
+ * flexible iteration stagnates, and the FP64 true residual decides
+ * convergence as for the plain solver. Before training (or with
+ * icep_learned_enable(ctx, 0)) the network is not applied. */
+/* Train on the GPU: `configs` random particle configurations (the context's
+ * particle count and radius, new positions, eps_p uniform in [1, 10] when
+ * per-particle permittivity is on, a random direction of E_ext), each for
+ * `steps_per_config` Adam steps along the chain of residuals r -> r - A P(r)
+ * starting from the right-hand side; loss |r - A P(r)|^2 / |r|^2 with
+ * P(r) = M^-1 (r + rms(r) prolong(net(eps, r))). The
+ * context's particles and field are restored afterwards. */
+int icep_learned_train(icep_ctx *ctx, int configs, int steps_per_config, unsigned seed, double lr, double *loss_first,
+                       double *loss_last);
+/* 1: apply the network in the preconditioner, 0: spectral part only. */
+int icep_learned_enable(icep_ctx *ctx, int on);
+/* Mean one-step loss |r - A P(r)|^2 / |r|^2 of the spectral-only and of the
+ * learned preconditioner P on the same residuals: the context's current
+ * right-hand side and the next chain-1 residuals of the spectral iteration. */
+int icep_learned_eval(icep_ctx *ctx, int chain, double *loss_spectral, double *loss_learned);
+/* Number of network parameters (FP32 master copy) and their exchange. */
+long icep_learned_nparams(icep_ctx *ctx);
+int icep_learned_get_params(icep_ctx *ctx, double *params);
+int icep_learned_set_params(icep_ctx *ctx, const double *params);
+/* The network alone, for checks: input from the fine-grid permittivity and
+ * residual (real fields, reference layout), output y on the half-resolution
+ * grid ((NX/2)^3 values, z fastest); the backward pass after it gives the
+ * parameter gradient for dL/dy = gy. */
+int icep_learned_forward(icep_ctx *ctx, const double *eps, const double *r, double eps_ref, double *y);
+int icep_learned_backward(icep_ctx *ctx, const double *gy, double *grad);
+/* Plain-solver fallbacks and preconditioner applications of the last solve. */
+int icep_learned_stats(icep_ctx *ctx, int *fallbacks, int *precond_apps);
+
 /* ---- measurement helpers (no reference counterpart) --------------------- */
 /* Average device time of `reps` launches of one kernel group on the
  * context's stream (CUDA events): which 0..3 = one pass of the 3D FFT

@@ -34,8 +34,10 @@ enum icep_precision { ICEP_FP64 = 0, ICEP_MIXED = 1 };
 /* Poisson solver: REF = identity-preconditioned BiCGSTAB with the
  * reference's (Eigen's) stopping and restart rules; SPECTRAL = BiCGSTAB
  * right-preconditioned by the inverse constant-permittivity operator,
- * stopping on the true residual. */
-enum icep_solver { ICEP_SOLVER_REF = 0, ICEP_SOLVER_SPECTRAL = 1 };
+ * stopping on the true residual; LEARNED (MIXED precision only) = flexible
+ * GMRES whose preconditioner adds a trained U-Net correction to the spectral
+ * one, with SPECTRAL as the fallback on stagnation. */
+enum icep_solver { ICEP_SOLVER_REF = 0, ICEP_SOLVER_SPECTRAL = 1, ICEP_SOLVER_LEARNED = 2 };
 
 /*
  * Simulation parameters. Field names follow the reference's input.udf keys

@@ -323,6 +323,7 @@ def run_gpu(args, world, rank, local, dist):
     lib.icep_unpin_host(C.addressof(hparts))
     e2e = world * args.steps / e2e_s
     sim.close()
+    learned = None if (args.no_learned or args.precision != "mixed") else run_learned(args, lib, value)
     if rank != 0:
         return
     base = None
@@ -345,7 +346,44 @@ def run_gpu(args, world, rank, local, dist):
                          "launches_timed": pn.value, "ms_per_launch": pms.value / pn.value if pn.value else None,
                          "bytes_per_launch": per_launch_bytes},
             "cpu_baseline": base}
+    if learned is not None:
+        line["learned"] = learned
     print(json.dumps(line), flush=True)
+
+
+def run_learned(args, lib, plain_value):
+    """The same workload with the learned preconditioner (solver LEARNED):
+    the network is trained on the GPU first (outside the timed region), then
+    K steps are timed as for the plain solver; also timed with the network
+    switched off (flexible GMRES with the spectral preconditioner only)."""
+    from icep_kapsel_gb300 import abi
+    from icep_kapsel_gb300.runtime import Simulation
+    p, parts = workload(args, abi.MIXED, abi.SOLVER_LEARNED)
+    sim = Simulation(p, parts)
+    sim.init_state()
+    t0 = time.perf_counter()
+    l0, l1 = sim.learned_train(configs=40, steps=50, seed=3, lr=1e-3)
+    sim.synchronize()
+    t_train = time.perf_counter() - t0
+    ls, ll = sim.learned_eval(4)
+    out = {"train": {"adam_steps": 2000, "configurations": 40, "seconds": t_train, "loss_first": l0,
+                     "loss_last": l1},
+           "one_step_loss_on_step_residuals": {"spectral": ls, "learned": ll}}
+    for key, on in (("with_network", 1), ("network_off", 0)):
+        sim.learned_enable(on)
+        for _ in range(args.warmup):
+            sim.step(1)
+        ms = C.c_double(0)
+        if lib.icep_step_timed(sim.ctx, args.steps, C.byref(ms)) != 0:
+            raise RuntimeError("learned timed steps failed")
+        it, err, _ = sim.solver_stats()
+        fb, apps = sim.learned_stats()
+        v = args.steps / (ms.value / 1000.0)
+        out[key] = {"value": v, "unit": UNIT, "ms_per_step": ms.value / args.steps, "vs_plain": v / plain_value,
+                    "inner_iterations_last_solve": it, "network_applications_last_solve": apps if on else 0,
+                    "fallbacks_last_solve": fb, "relative_true_residual": err}
+    sim.close()
+    return out
 
 
 def main():
@@ -360,6 +398,7 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--maxit", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":

@@ -1147,6 +1147,7 @@ class Engine : public EngineBase {
     int st = read_scal();
     if (st) return st;
     const double bb = hscal[S_BB];
+    if (!std::isfinite(bb)) return fail(ICEP_ERR_NOT_CONVERGED, "Poisson solve: non-finite right-hand side");
     const double eref = mean_eps();
     int total_inner = 0;
     double rel = 0.0;
@@ -1161,7 +1162,8 @@ class Engine : public EngineBase {
         if ((st = read_scal())) return st;
         const double rr = hscal[S_RR];
         rel = sqrt(rr / bb);
-        if (!(rr > tol2) || !std::isfinite(rr)) break;
+        if (!std::isfinite(rr)) return fail(ICEP_ERR_NOT_CONVERGED, "Poisson solve: non-finite residual");
+        if (!(rr > tol2)) break;
         // FP32 correction solve on the normalised residual
         const double rn = sqrt(rr / (double)G.nreal());
         scale_d2f(G, d64[D_R], (float *)f[F_KB], 1.0 / rn, s);
@@ -1213,6 +1215,7 @@ class Engine : public EngineBase {
     }
     last_iters = it;
     last_error = er;
+    if (!std::isfinite(er)) return fail(ICEP_ERR_NOT_CONVERGED, "Poisson solve: non-finite residual");
     copy_real<R>(g, f[F_KX], f[pot_id], s);
     return ICEP_OK;
   }

@@ -67,6 +67,10 @@ int icep_init_state(icep_ctx *ctx);
  * nsteps of the time loop body (sp_3d_ns.cxx:524-525): Time_evolution_hydro
  * (sp_3d_ns.cxx:24-186), the function the reference calls through the
  * pointer Time_evolution (sp_3d_ns.cxx:10), then jikan.time += dt.
+ * A Poisson solve that meets a non-finite right-hand side or residual stops
+ * the step with ICEP_ERR_NOT_CONVERGED (the reference keeps going); reaching
+ * MaxIter is not an error, as in the reference (retry from a zero guess,
+ * operate_dielectric.cxx:563-570).
  */
 int icep_step(icep_ctx *ctx, int nsteps);
 

@@ -324,6 +324,7 @@ def run_gpu(args, world, rank, local, dist):
     e2e = world * args.steps / e2e_s
     sim.close()
     learned = None if (args.no_learned or args.precision != "mixed") else run_learned(args, lib, value)
+    batched = None if (args.no_batch or args.precision != "mixed") else run_batch(args)
     if rank != 0:
         return
     base = None
@@ -348,7 +349,42 @@ def run_gpu(args, world, rank, local, dist):
             "cpu_baseline": base}
     if learned is not None:
         line["learned"] = learned
+    if batched is not None:
+        line["batched"] = batched
     print(json.dumps(line), flush=True)
+
+
+def run_batch(args, n_replicas=64, seed=4242):
+    """The batched ensemble: independent replicas with meshes drawn from
+    {32^3, 64^3} (the path supports power-of-two meshes, as the reference),
+    8-16 spheres at 32^3 and 8-64 at 64^3 (a = 4, xi = 2, seeded positions,
+    eps_p uniform in [1, 5]), |E0| uniform in [0.05, 0.2], advanced together
+    by icep_batch_step. Value: replica-steps per second over the batch."""
+    import cases
+    from icep_kapsel_gb300 import abi
+    from icep_kapsel_gb300.runtime import Batch
+    rng = np.random.default_rng(seed)
+    reps, points = [], 0
+    for i in range(n_replicas):
+        n = int(rng.choice([32, 64]))
+        npart = int(rng.integers(8, 17 if n == 32 else 65))
+        ez = float(rng.uniform(0.05, 0.2))
+        reps.append(cases.icep_case(n=n, npart=npart, minsep=10.0, seed=seed + i, a=4.0, eps_f=80.0, eps_p=3.0,
+                                    e_ext=(0.0, 0.0, ez), tol=args.tol, maxit=args.maxit, dt=0.01,
+                                    per_particle_eps=(1.0, 5.0), solver=abi.SOLVER_SPECTRAL,
+                                    precision=abi.MIXED))
+        points += n ** 3
+    b = Batch(reps)
+    b.init_state()
+    b.step(args.warmup)
+    t0 = time.perf_counter()
+    b.step(args.steps)
+    dt = time.perf_counter() - t0
+    b.close()
+    return {"replicas": n_replicas, "meshes": "32^3 / 64^3", "value": n_replicas * args.steps / dt,
+            "unit": "replica-steps/s", "grid_point_steps_per_s": points * args.steps / dt,
+            "ms_per_batch_step": 1000.0 * dt / args.steps, "timing": "host wall clock around icep_batch_step "
+            "(returns after every replica's stream has finished)"}
 
 
 def run_learned(args, lib, plain_value):
@@ -399,6 +435,7 @@ def main():
     ap.add_argument("--maxit", type=int, default=1000)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
     if args.impl == "reference":

@@ -1,7 +1,10 @@
 // icep_abi.cu -- the extern "C" entry points declared in include/icep_gb300.h.
 #include <string.h>
 
+#include <algorithm>
+#include <atomic>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/icep_gb300.h"
@@ -216,6 +219,87 @@ int icep_learned_stats(icep_ctx *c, int *fallbacks, int *precond_apps) {
   if (fallbacks) *fallbacks = c->e->last_fallbacks;
   if (precond_apps) *precond_apps = c->e->last_precond_apps;
   return ICEP_OK;
+}
+
+/* ---- batches of independent replicas ------------------------------------ */
+}  // extern "C"
+
+struct icep_batch {
+  std::vector<icep_ctx *> ctx;
+  std::string err;
+};
+
+namespace {
+// Runs fn(i) for every replica on a pool of host threads; each replica's
+// work goes to its own CUDA stream, so the replicas run concurrently on the
+// GPU. Returns the first error (its text in b->err).
+template <class F>
+int batch_run(icep_batch *b, F fn) {
+  const int n = (int)b->ctx.size();
+  unsigned hw = std::thread::hardware_concurrency();
+  const int nt = std::max(1, std::min(n, (int)std::min(hw ? hw : 4u, 32u)));
+  std::atomic<int> next{0}, first_err{0}, err_idx{-1};
+  auto worker = [&]() {
+    for (;;) {
+      const int i = next.fetch_add(1);
+      if (i >= n) break;
+      const int st = fn(b->ctx[i]);
+      int expected = 0;
+      if (st != ICEP_OK && first_err.compare_exchange_strong(expected, st)) err_idx = i;
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; t++) th.emplace_back(worker);
+  for (auto &t : th) t.join();
+  if (first_err) {
+    const int i = err_idx;
+    b->err = "replica " + std::to_string(i) + ": " + (i >= 0 ? b->ctx[i]->err : std::string());
+  }
+  return first_err;
+}
+}  // namespace
+
+extern "C" {
+
+icep_batch *icep_batch_create(int n, const icep_params *params, const icep_particle *const *particles, int *status) {
+  if (n < 1 || !params || !particles) {
+    if (status) *status = ICEP_ERR_ARG;
+    return nullptr;
+  }
+  icep_batch *b = new icep_batch();
+  for (int i = 0; i < n; i++) {
+    int st = ICEP_OK;
+    icep_ctx *c = icep_create(&params[i], particles[i], params[i].n_particles, &st);
+    if (!c) {
+      for (icep_ctx *o : b->ctx) icep_destroy(o);
+      delete b;
+      if (status) *status = st;
+      return nullptr;
+    }
+    b->ctx.push_back(c);
+  }
+  if (status) *status = ICEP_OK;
+  return b;
+}
+void icep_batch_destroy(icep_batch *b) {
+  if (!b) return;
+  for (icep_ctx *c : b->ctx) icep_destroy(c);
+  delete b;
+}
+int icep_batch_size(const icep_batch *b) { return b ? (int)b->ctx.size() : 0; }
+icep_ctx *icep_batch_context(icep_batch *b, int i) {
+  return (b && i >= 0 && i < (int)b->ctx.size()) ? b->ctx[i] : nullptr;
+}
+const char *icep_batch_last_error(const icep_batch *b) { return b ? b->err.c_str() : "null batch"; }
+int icep_batch_init_state(icep_batch *b) {
+  return b ? batch_run(b, [](icep_ctx *c) { return icep_init_state(c); }) : ICEP_ERR_ARG;
+}
+int icep_batch_step(icep_batch *b, int nsteps) {
+  if (!b || nsteps < 0) return ICEP_ERR_ARG;
+  return batch_run(b, [nsteps](icep_ctx *c) {
+    const int st = icep_step(c, nsteps);
+    return st != ICEP_OK ? st : icep_synchronize(c);
+  });
 }
 
 }  // extern "C"

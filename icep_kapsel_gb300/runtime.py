@@ -85,6 +85,16 @@ def load_library(path=None):
     L.icep_time_evolution.argtypes = [V, _DP, _DP, _DP, _DP, _DP, _DP, V, I]
     L.icep_stream.restype = V
     L.icep_stream.argtypes = [V]
+    L.icep_batch_create.restype = V
+    L.icep_batch_create.argtypes = [I, V, V, C.POINTER(I)]
+    L.icep_batch_destroy.argtypes = [V]
+    L.icep_batch_size.argtypes = [V]
+    L.icep_batch_context.restype = V
+    L.icep_batch_context.argtypes = [V, I]
+    L.icep_batch_last_error.restype = C.c_char_p
+    L.icep_batch_last_error.argtypes = [V]
+    L.icep_batch_init_state.argtypes = [V]
+    L.icep_batch_step.argtypes = [V, I]
     L.icep_learned_train.argtypes = [V, I, I, C.c_uint, C.c_double, _DP, _DP]
     L.icep_learned_enable.argtypes = [V, I]
     L.icep_learned_eval.argtypes = [V, I, _DP, _DP]
@@ -112,9 +122,9 @@ class Simulation:
             raise IcepError("icep_create failed with status %d" % st.value)
 
     def close(self):
-        if getattr(self, "ctx", None):
+        if getattr(self, "ctx", None) and getattr(self, "_owned", True):
             self.lib.icep_destroy(self.ctx)
-            self.ctx = None
+        self.ctx = None
 
     def __del__(self):
         try:
@@ -268,3 +278,53 @@ class Simulation:
         self._check(self.lib.icep_time_evolution(self.ctx, _dp(zeta0), _dp(zeta1), _dp(uk_dc), ptr(conc0),
                                                  ptr(conc1), ptr(potential), particles, nsteps),
                     "time_evolution")
+
+
+class Batch:
+    """Independent replicas advanced together (icep_batch_*, include/icep_gb300.h).
+    replica(i) gives a Simulation view on replica i's context."""
+
+    def __init__(self, replicas):
+        """replicas: list of (params, particles) pairs."""
+        self.lib = load_library()
+        n = len(replicas)
+        self._params = (abi.Params * n)(*[p for p, _ in replicas])
+        self._parts = [parts for _, parts in replicas]
+        ptrs = (C.c_void_p * n)(*[C.addressof(pp) for pp in self._parts])
+        st = C.c_int(0)
+        self.handle = self.lib.icep_batch_create(n, self._params, ptrs, C.byref(st))
+        if not self.handle:
+            raise IcepError("icep_batch_create failed with status %d" % st.value)
+        self.n = n
+
+    def _check(self, st, what):
+        if st != 0:
+            msg = self.lib.icep_batch_last_error(self.handle)
+            raise IcepError("%s failed (%d): %s" % (what, st, msg.decode() if msg else ""))
+
+    def init_state(self):
+        self._check(self.lib.icep_batch_init_state(self.handle), "batch_init_state")
+
+    def step(self, n=1):
+        self._check(self.lib.icep_batch_step(self.handle, n), "batch_step")
+
+    def replica(self, i):
+        v = Simulation.__new__(Simulation)
+        v.lib = self.lib
+        v.params = self._params[i]
+        v.np = v.params.n_particles
+        v.ctx = self.lib.icep_batch_context(self.handle, i)
+        v._owned = False
+        return v
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.icep_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

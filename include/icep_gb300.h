@@ -171,6 +171,24 @@ int icep_solver_stats(icep_ctx *ctx, int *iterations, double *error, long *matve
  * checker used by the tests). */
 int icep_call(icep_ctx *ctx, int fn);
 
+/* ---- batches of independent replicas (no reference counterpart) ---------
+ * The reference runs one system per process; an ensemble there is many
+ * processes. A batch holds n contexts (any mix of meshes, particle counts and
+ * parameters), each with its own CUDA stream; icep_batch_step advances all of
+ * them from a pool of host threads so that their kernels run concurrently on
+ * the GPU, and returns when every replica has finished. */
+typedef struct icep_batch icep_batch;
+/* params[i], particles[i] (params[i].n_particles entries) for replica i. */
+icep_batch *icep_batch_create(int n, const icep_params *params, const icep_particle *const *particles, int *status);
+void icep_batch_destroy(icep_batch *batch);
+int icep_batch_size(const icep_batch *batch);
+/* The context of replica i, for the per-replica calls (get/set fields, ...). */
+icep_ctx *icep_batch_context(icep_batch *batch, int i);
+/* Text of the first error of the last batch call ("replica i: ..."). */
+const char *icep_batch_last_error(const icep_batch *batch);
+int icep_batch_init_state(icep_batch *batch);
+int icep_batch_step(icep_batch *batch, int nsteps);
+
 /* ---- learned Poisson preconditioner (no reference counterpart) -----------
  * Contexts created with precision ICEP_MIXED and solver ICEP_SOLVER_LEARNED
  * (cubic mesh 32..128) solve the inner correction systems of

@@ -628,7 +628,7 @@ class Engine : public EngineBase {
    * one update kernel, one host synchronisation. FP32 engine on grids whose
    * x-planes fit in shared memory.
    */
-  int bicgstab_kf(double tol, int maxit, double eps_ref, int *iters, double *rel_err) {
+  int bicgstab_kf(double tol, int maxit, double eps_ref, int *iters, double *rel_err, bool kspace_io = false) {
     if constexpr (!std::is_same<R, float>::value) {
       return bicgstab_k(tol, maxit, eps_ref, iters, rel_err);
     } else {
@@ -638,8 +638,10 @@ class Engine : public EngineBase {
       const int nb = kop_npb;
       double *P1 = kpart, *P2 = kpart + 2 * nb, *P3 = kpart + 4 * nb;
       const size_t nk = 2 * (2 * (size_t)nb + DOT_BLOCKS);
-      copy_real<R>(g, f[F_KB], r, s);
-      r2c(r);
+      if (!kspace_io) {  // right-hand side from the real field F_KB, else already in F_KR
+        copy_real<R>(g, f[F_KB], r, s);
+        r2c(r);
+      }
       cudaMemsetAsync(r, 0, 2 * sizeof(R), s);  // k = 0: the mean
       cudaMemcpyAsync(r0, r, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
       kdots<R>(g, r, r, r, r, 1, partials, scal, S_RR, s);
@@ -701,7 +703,7 @@ class Engine : public EngineBase {
         if (!std::isfinite(rr)) break;
       }
       kprecond<R>(g, xt, f[F_KX], eps_ref, s);
-      c2r(f[F_KX]);
+      if (!kspace_io) c2r(f[F_KX]);
       *iters = i;
       *rel_err = sqrt(rr / bsq);
       return ICEP_OK;
@@ -1108,10 +1110,35 @@ class Engine : public EngineBase {
    * spectral-preconditioned BiCGSTAB to a relative tolerance that leaves a
    * margin below the target, then x64 += d.
    */
+  // A64 x^ in k-space: the FP64 operator (Ax, operate_dielectric.cxx:485-522)
+  // from a half spectrum to a half spectrum (6 FFTs instead of 8)
+  void apply_A64_k(const double *xk, double *yk) {
+    grad_k<double>(g, xk, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], 1.0, true, nullptr, s);
+    fft_c2r(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
+    eps_face_mul<double>(g, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_EPS], s);
+    fft_r2c(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
+    div_k<double>(g, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], yk, true, s);
+    matvecs++;
+  }
+
+  /*
+   * MIXED precision Charge_field2potential_dielectric: iterative refinement
+   * held in k-space. The FP64 system is A64 x = b64 with A64 the reference
+   * operator on the permittivity (double)eps and
+   * b64 = D^-.(eps_face E) - (double)rho with its mean (the k = 0 mode)
+   * removed. The potential's half spectrum x^ (FP64) is state kept between
+   * steps. Each outer step forms the true residual r^ = b^ - A64 x^ in FP64
+   * (its norm by Parseval) and, while |r| > tol |b|, solves A d = r/|r| in
+   * FP32 with the k-space BiCGSTAB to a tolerance that leaves a factor-4
+   * margin, then x^ += |r| d^. The real FP32 potential is one FP32 inverse
+   * transform of x^ at the end.
+   */
   int solve_potential_mixed(int rho_id, int pot_id) {
     const Grid &G = g;
+    const long nf = G.nf();
     if (!x64_valid) {
-      convert_f2d(G.nf(), (const float *)f[pot_id], d64[D_X], s);
+      convert_f2d(nf, (const float *)f[pot_id], d64[D_X], s);
+      fft_r2c(fft64, batch(d64[D_X]), s);
       x64_valid = true;
       xp_valid = false;
     }
@@ -1119,31 +1146,30 @@ class Engine : public EngineBase {
     // last two solves (the reference starts from the last potential; both
     // are converged to the same true-residual tolerance)
     if (xp_valid) {
-      axpby_real<double>(G, d64[D_X], d64[D_XP], 2.0, -1.0, s);
+      axpby_all(nf, d64[D_X], d64[D_XP], 2.0, -1.0, s);
       std::swap(d64[D_X], d64[D_XP]);
     } else {
-      cudaMemcpyAsync(d64[D_XP], d64[D_X], sizeof(double) * G.nf(), cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(d64[D_XP], d64[D_X], sizeof(double) * nf, cudaMemcpyDeviceToDevice, s);
     }
     xp_valid = true;
-    convert_f2d(G.nf(), (const float *)f[F_EPS], d64[D_EPS], s);
-    // b64
+    convert_f2d(nf, (const float *)f[F_EPS], d64[D_EPS], s);
+    // b^64
     eps_face_E<double>(G, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_EPS], P.e_ext[0], P.e_ext[1], P.e_ext[2], s);
     {  // components of E_ext that are zero give zero fields: cleared (with
        // their padding) instead of transformed
       FieldBatch<double> nz{};
       for (int d = 0; d < 3; d++) {
         if (P.e_ext[d] != 0.0) nz.p[nz.n++] = d64[D_W3_0 + d];
-        else cudaMemsetAsync(d64[D_W3_0 + d], 0, sizeof(double) * G.nf(), s);
+        else cudaMemsetAsync(d64[D_W3_0 + d], 0, sizeof(double) * nf, s);
       }
       if (nz.n) fft_r2c(fft64, nz, s);
     }
     div_k<double>(G, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_B], true, s);
-    fft_c2r(fft64, batch(d64[D_B]), s);
-    convert_f2d(G.nf(), (const float *)f[rho_id], d64[D_R], s);
-    axpby_real<double>(G, d64[D_R], d64[D_B], -1.0, 1.0, s);
-    sum_real<double>(G, d64[D_B], partials, scal, S_AUX0, s);
-    sub_mean<double>(G, d64[D_B], scal, S_AUX0, s);
-    dots<double>(G, d64[D_B], d64[D_B], d64[D_B], d64[D_B], 1, partials, scal, S_BB, s);
+    convert_f2d(nf, (const float *)f[rho_id], d64[D_R], s);
+    fft_r2c(fft64, batch(d64[D_R]), s);
+    axpby_all(nf, d64[D_R], d64[D_B], -1.0, 1.0, s);
+    cudaMemsetAsync(d64[D_B], 0, 2 * sizeof(double), s);  // k = 0: the mean
+    kdots<double>(G, d64[D_B], d64[D_B], d64[D_B], d64[D_B], 1, partials, scal, S_BB, s);
     int st = read_scal();
     if (st) return st;
     const double bb = hscal[S_BB];
@@ -1156,9 +1182,9 @@ class Engine : public EngineBase {
     if (bb > 0.0) {
       const double tol2 = P.potential_tol * P.potential_tol * bb;
       for (int outer = 0; outer < 30; outer++) {
-        apply_A64(d64[D_X], d64[D_R]);
-        sub_real<double>(G, d64[D_B], d64[D_R], d64[D_R], s);
-        dots<double>(G, d64[D_R], d64[D_R], d64[D_R], d64[D_R], 1, partials, scal, S_RR, s);
+        apply_A64_k(d64[D_X], d64[D_R]);
+        axpby_all(nf, d64[D_B], d64[D_R], 1.0, -1.0, s);  // r^ = b^ - A x^
+        kdots<double>(G, d64[D_R], d64[D_R], d64[D_R], d64[D_R], 1, partials, scal, S_RR, s);
         if ((st = read_scal())) return st;
         const double rr = hscal[S_RR];
         rel = sqrt(rr / bb);
@@ -1166,31 +1192,38 @@ class Engine : public EngineBase {
         if (!(rr > tol2)) break;
         // FP32 correction solve on the normalised residual
         const double rn = sqrt(rr / (double)G.nreal());
-        scale_d2f(G, d64[D_R], (float *)f[F_KB], 1.0 / rn, s);
-        zero(F_KX);
+        scale_d2f_all(nf, d64[D_R], (float *)f[F_KR], 1.0 / rn, s);
         double inner_tol = 0.25 * P.potential_tol * sqrt(bb / rr);
         if (inner_tol < 2e-5) inner_tol = 2e-5;
         if (inner_tol > 0.5) inner_tol = 0.5;
         int it = 0;
         double er = 0.0;
-        if (learned) {
-          bool ok = true;
-          if ((st = fgmres(inner_tol, P.potential_iter, eref, &it, &er, &ok))) return st;
-          if (!ok) {  // stagnation: the plain solver from a zero guess
-            last_fallbacks++;
-            int it2 = 0;
-            if ((st = bicgstab_kf(inner_tol, P.potential_iter, eref, &it2, &er))) return st;
-            it += it2;
+        if (kpart && !learned) {
+          if ((st = bicgstab_kf(inner_tol, P.potential_iter, eref, &it, &er, true))) return st;
+        } else {  // solvers with a real-space interface
+          copy(F_KB, F_KR);
+          c2r(f[F_KB]);
+          zero(F_KX);
+          if (learned) {
+            bool ok = true;
+            if ((st = fgmres(inner_tol, P.potential_iter, eref, &it, &er, &ok))) return st;
+            if (!ok) {  // stagnation: the plain solver from a zero guess
+              last_fallbacks++;
+              int it2 = 0;
+              if ((st = bicgstab_kf(inner_tol, P.potential_iter, eref, &it2, &er))) return st;
+              it += it2;
+            }
+          } else if ((st = bicgstab_k(inner_tol, P.potential_iter, eref, &it, &er))) {
+            return st;
           }
-        } else if ((st = kpart ? bicgstab_kf(inner_tol, P.potential_iter, eref, &it, &er)
-                               : bicgstab_k(inner_tol, P.potential_iter, eref, &it, &er))) {
-          return st;
+          r2c(f[F_KX]);
         }
         total_inner += it;
-        add_f2d(G, (const float *)f[F_KX], d64[D_X], rn, s);
+        add_f2d_all(nf, (const float *)f[F_KX], d64[D_X], rn, s);
       }
     }
-    scale_d2f(G, d64[D_X], (float *)f[pot_id], 1.0, s);
+    scale_d2f_all(nf, d64[D_X], (float *)f[pot_id], 1.0, s);
+    c2r(f[pot_id]);
     last_iters = total_inner;
     last_error = rel;
     return ICEP_OK;
@@ -1405,8 +1438,10 @@ class Engine : public EngineBase {
 
   int get_field(int id, double *host) override {
     if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
-    if (id == F_POT && mixed && x64_valid) {  // the potential is FP64 state
-      cudaMemcpyAsync(host, d64[D_X], sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
+    if (id == F_POT && mixed && x64_valid) {  // the potential is FP64 state (its half spectrum)
+      cudaMemcpyAsync(d64[D_R], d64[D_X], sizeof(double) * g.nf(), cudaMemcpyDeviceToDevice, s);
+      fft_c2r(fft64, batch(d64[D_R]), s);
+      cudaMemcpyAsync(host, d64[D_R], sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
       if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_field");
       return ICEP_OK;
     }

@@ -153,6 +153,20 @@ __global__ void k_d2f(long n, const double *x, float *y) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) y[t] = (float)x[t];
 }
+// element-wise over all n values (k-space arrays included)
+__global__ void k_scale_d2f_all(long n, const double *x, float *y, double a) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] = (float)(a * x[t]);
+}
+__global__ void k_add_f2d_all(long n, const float *x, double *y, double a) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] += a * (double)x[t];
+}
+__global__ void k_axpby_all(long n, const double *x, double *y, double a, double b) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] = a * x[t] + b * y[t];
+}
+
 __global__ void k_add_f2d(Grid g, const float *x, double *y, double a) {
   const unsigned t = RTID;
   if (t >= (unsigned)g.nreal()) return;
@@ -221,6 +235,18 @@ void convert_f2d(long n, const float *x, double *y, cudaStream_t s) {
 void convert_d2f(long n, const double *x, float *y, cudaStream_t s) {
   count_launch();
   k_d2f<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y);
+}
+void scale_d2f_all(long n, const double *x, float *y, double a, cudaStream_t s) {
+  count_launch();
+  k_scale_d2f_all<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y, a);
+}
+void add_f2d_all(long n, const float *x, double *y, double a, cudaStream_t s) {
+  count_launch();
+  k_add_f2d_all<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y, a);
+}
+void axpby_all(long n, const double *x, double *y, double a, double b, cudaStream_t s) {
+  count_launch();
+  k_axpby_all<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y, a, b);
 }
 void add_f2d(const Grid &g, const float *x, double *y, double a, cudaStream_t s) {
   count_launch();

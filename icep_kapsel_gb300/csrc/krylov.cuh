@@ -45,6 +45,11 @@ void sum_real(const Grid &g, const R *a, double *partials, double *scal, int slo
 // type conversion over all NX*NY*NZ_ values
 void convert_f2d(long n, const float *x, double *y, cudaStream_t s);
 void convert_d2f(long n, const double *x, float *y, cudaStream_t s);
+// element-wise over all n values (real or k-space arrays): y = (float)(a x);
+// y += a (double)x; y = a x + b y
+void scale_d2f_all(long n, const double *x, float *y, double a, cudaStream_t s);
+void add_f2d_all(long n, const float *x, double *y, double a, cudaStream_t s);
+void axpby_all(long n, const double *x, double *y, double a, double b, cudaStream_t s);
 // y (double) += a * x (float) on real points
 void add_f2d(const Grid &g, const float *x, double *y, double a, cudaStream_t s);
 // y (float) = a * x (double) on real points, padding zero

@@ -8,7 +8,8 @@
   plain FP64 oracle: 3e-2 on the output.
 * A solve with the learned preconditioner reaches the same FP64 true
   residual as the plain solver and gives the same fields within the MIXED
-  tolerances; training lowers its loss. The iteration counts of the flexible
+  tolerances; the trained correction does not raise the one-step loss of the
+  spectral preconditioner. The iteration counts of the flexible
   GMRES with and without the network and of the plain BiCGSTAB are printed
   (run with -s to see them).
 """

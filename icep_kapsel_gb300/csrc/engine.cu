@@ -49,6 +49,7 @@ class Engine : public EngineBase {
   void *shift_tab = nullptr;  // staggered-shift tables referenced by g
   double *kpart = nullptr;    // dot partials of the fused k-space iteration
   double *hkpart = nullptr;   // pinned
+  int *kerr = nullptr;        // error word of the fused plane passes (inside kpart)
   int kop_npb = 0;
   // learned preconditioner and its flexible GMRES (solver LEARNED)
   static constexpr int FG_M = 20;  // restart length
@@ -265,9 +266,12 @@ class Engine : public EngineBase {
     cudaMalloc(&partials, sizeof(double) * 2 * DOT_BLOCKS);
     if (mixed && electrolyte && kop_supported(g)) {
       kop_npb = kop_pencil_blocks(g);
-      const size_t nk = 2 * (2 * (size_t)kop_npb + DOT_BLOCKS);
+      // the dot partials, then one word for the plane passes' error flag
+      const size_t nk = 2 * (2 * (size_t)kop_npb + DOT_BLOCKS) + 1;
       if (cudaMalloc(&kpart, sizeof(double) * nk) != cudaSuccess || cudaMallocHost(&hkpart, sizeof(double) * nk) != cudaSuccess)
         return fail(ICEP_ERR_CUDA, "allocation of the k-space dot partials failed");
+      cudaMemsetAsync(kpart, 0, sizeof(double) * nk, s);
+      kerr = reinterpret_cast<int *>(kpart + nk - 1);
     }
     if (p.solver == ICEP_SOLVER_LEARNED) {
       if (!mixed || !electrolyte || !kpart || p.nx != p.ny || p.nx != p.nz || p.nx < 32)
@@ -637,7 +641,7 @@ class Engine : public EngineBase {
       float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2];
       const int nb = kop_npb;
       double *P1 = kpart, *P2 = kpart + 2 * nb, *P3 = kpart + 4 * nb;
-      const size_t nk = 2 * (2 * (size_t)nb + DOT_BLOCKS);
+      const size_t nk = 2 * (2 * (size_t)nb + DOT_BLOCKS) + 1;  // with the error word
       if (!kspace_io) {  // right-hand side from the real field F_KB, else already in F_KR
         copy_real<R>(g, f[F_KB], r, s);
         r2c(r);
@@ -676,15 +680,17 @@ class Engine : public EngineBase {
         }
         const double beta = (rho / rho_old) * (alpha / w);
         kop_xinv(fft, KOP_P, p, r, v, beta, w, 0.0, nullptr, 0, eps_ref, w0, w1, w2, s);
-        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], s);
+        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
         kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, s);
         kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, rho, P1, nb, eps_ref, w0, w1, w2, s);
-        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], s);
+        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
         kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, s);
         kop_xr(g, xt, r, p, sv, t, r0, rho, P1, P2, nb, P3, s);
         matvecs += 2;
         cudaMemcpyAsync(hkpart, kpart, sizeof(double) * nk, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fused k-space iteration");
+        if (*reinterpret_cast<const int *>(hkpart + nk - 1))
+          return fail(ICEP_ERR_CUDA, "fused plane pass: a bulk copy did not complete within the wait limit");
         double r0v = 0, tt = 0, ts = 0, r0r = 0;
         rr = 0;
         for (int b = 0; b < nb; b++) {
@@ -736,7 +742,7 @@ class Engine : public EngineBase {
     if constexpr (std::is_same<R, float>::value) {
       kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, 0, mean_eps_cached, f[F_WV3_0], f[F_WV3_1],
                f[F_WV3_2], s);
-      kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], s);
+      kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
       kop_xfwd(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], out, KOP_NONE, nullptr, nullptr, s);
       matvecs++;
     }
@@ -862,6 +868,12 @@ class Engine : public EngineBase {
         if (beta <= tol * b0) conv = true;
       }
       if (!conv) *ok = false;
+      {
+        int herr = 0;
+        cudaMemcpyAsync(&herr, kerr, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fgmres");
+        if (herr) return fail(ICEP_ERR_CUDA, "fused plane pass: a bulk copy did not complete within the wait limit");
+      }
       kprecond<R>(g, xt, f[F_KX], eref, s);
       c2r(f[F_KX]);
       *iters = total;

@@ -229,6 +229,109 @@ __device__ __forceinline__ cplx<R> merge_inv(cplx<R> x, cplx<R> c /* conj X[H-k]
   return cplx<R>{sr - ti, si + tr};
 }
 
+// ---- warp-local transforms --------------------------------------------------
+// Shared tile with an XOR swizzle: element e of pencil w at
+// t[e*sw + (w ^ ((e ^ (e >> 3)) & 15))], sw a multiple of 16. The lane groups
+// of group_fft read elements 1 apart and write elements up to 8 apart within
+// one pencil; the swizzle spreads both patterns over all banks.
+__host__ __device__ __forceinline__ int swz(int e, int w, int sw) { return e * sw + (w ^ ((e ^ (e >> 3)) & 15)); }
+template <typename R>
+struct SmemX {
+  cplx<R> *t;
+  int sw;
+  __device__ __forceinline__ cplx<R> load(int w, int e) const { return t[swz(e, w, sw)]; }
+  __device__ __forceinline__ void store(int w, int e, cplx<R> v) const { t[swz(e, w, sw)] = v; }
+};
+
+// One Stockham stage of pencil w done by lane tl of its group of T = N/8
+// lanes (the same butterflies as stage(), distributed over the group).
+template <typename R, int N, int RAD, class Src, class Dst>
+__device__ __forceinline__ void gstage(const Src &src, const Dst &dst, int w, int tl, int Ls,
+                                       const cplx<R> *__restrict__ tws, bool conj_in, bool conj_out) {
+  constexpr int T = N / 8;
+  constexpr int NB = 8 / RAD;
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    const int jb = tl + T * m;
+    const int p = jb & (Ls - 1);
+    const int k = jb / Ls;
+    cplx<R> v[RAD];
+#pragma unroll
+    for (int q = 0; q < RAD; q++) v[q] = conj_if(src.load(w, jb + q * (N / RAD)), conj_in);
+    if (Ls > 1) {
+      const int step = N / (Ls * RAD);
+#pragma unroll
+      for (int q = 1; q < RAD; q++) v[q] = cmul(v[q], tws[(p * q * step) & (N - 1)]);
+    }
+    dftr<R, RAD>(v);
+#pragma unroll
+    for (int q = 0; q < RAD; q++) dst.store(w, k * Ls * RAD + p + Ls * q, conj_if(v[q], conj_out));
+  }
+}
+
+// Length-N transforms of NPEN pencils with every pencil on one lane group of
+// T = N/8 lanes inside a warp, so that consecutive stages are ordered by
+// __syncwarp alone. Groups take pencils in rounds that every lane runs (idle
+// lanes included). First stage reads `in`, last writes `out`; intermediate
+// stages alternate between tiles a and b (stride sw).
+// Intermediate tiles are swizzled (SmemX); the groups that share a half-warp
+// get pencils T apart, so a half-warp's accesses never collide.
+// The caller synchronises the block around the call where other groups'
+// pencils are read or written.
+template <typename R, int N, int NPEN, class In, class Out>
+__device__ __forceinline__ void group_fft(const In &in, const Out &out, cplx<R> *a, cplx<R> *b, int sw,
+                                          const cplx<R> *tws, bool inverse) {
+  constexpr int T = N / 8;
+  static_assert(T >= 1 && T <= 32 && (32 % T) == 0, "a pencil's lane group must fit in a warp");
+  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
+  const int ngroups = (blockDim.x * blockDim.y) / T;
+  const int tl = lin % T;
+  int w0;  // this group's pencil in round 0
+  if (T >= 32) {
+    w0 = lin / 32;
+  } else {
+    const int wi = lin >> 5, g = (lin & 31) / T;   // warp, group within the warp
+    const int per = 16 / (T < 16 ? T : 16);        // groups per half-warp
+    const int h = g / per, c = g - h * per;        // half-warp, position in it
+    const int wpg = (T >= 2) ? T / 2 : 1;          // warps per 16 pencils
+    w0 = (wi / wpg) * 16 + (wi % wpg) * 2 + c * T + h;
+  }
+  const int rounds = (NPEN + ngroups - 1) / ngroups;
+  SmemX<R> ta{a, sw}, tb{b, sw};
+  for (int r = 0; r < rounds; r++) {
+    const int w = w0 + r * ngroups;
+    const bool act = w < NPEN;
+    int Ls = 1;
+#pragma unroll
+    for (int s = 0; s < Plan<N>::nstages; s++) {
+      const int rad = Plan<N>::radix(s);
+      const bool first = (s == 0), last = (s == Plan<N>::nstages - 1);
+      const bool ci = first && inverse, co = last && inverse;
+      const SmemX<R> &tsrc = (s & 1) ? tb : ta;
+      const SmemX<R> &tdst = (s & 1) ? ta : tb;
+      if (act) {
+        if (first && last) {
+          if (rad == 8) gstage<R, N, 8>(in, out, w, tl, Ls, tws, ci, co);
+        } else if (first) {
+          if (rad == 8) gstage<R, N, 8>(in, tb, w, tl, Ls, tws, ci, co);
+          else if (rad == 4) gstage<R, N, 4>(in, tb, w, tl, Ls, tws, ci, co);
+          else gstage<R, N, 2>(in, tb, w, tl, Ls, tws, ci, co);
+        } else if (last) {
+          if (rad == 8) gstage<R, N, 8>(tsrc, out, w, tl, Ls, tws, ci, co);
+          else if (rad == 4) gstage<R, N, 4>(tsrc, out, w, tl, Ls, tws, ci, co);
+          else gstage<R, N, 2>(tsrc, out, w, tl, Ls, tws, ci, co);
+        } else {
+          if (rad == 8) gstage<R, N, 8>(tsrc, tdst, w, tl, Ls, tws, ci, co);
+          else if (rad == 4) gstage<R, N, 4>(tsrc, tdst, w, tl, Ls, tws, ci, co);
+          else gstage<R, N, 2>(tsrc, tdst, w, tl, Ls, tws, ci, co);
+        }
+      }
+      Ls *= rad;
+      __syncwarp();
+    }
+  }
+}
+
 // ---- x-plane cores (one block per x-plane) -------------------------------
 // smem: tw_y[NY] | tw_z[H] | post[H+1] | A | B, A/B of plane_tile() complex.
 __host__ __device__ constexpr int plane_tile(int ny, int h) {

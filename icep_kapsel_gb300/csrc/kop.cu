@@ -171,48 +171,207 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
                           tws, true);
 }
 
+// Last-stage sink of the inverse z transforms: the real row values times the
+// C2R scaling and the face permittivity (FP32, rows of the x-plane).
+struct MulSink {
+  cf *t;
+  int sw;
+  const float *efp;  // eps_face_d of this x-plane (shared memory)
+  int nzp;
+  float scale;
+  __device__ __forceinline__ void store(int w, int e, cf v) const {
+    const float2 f = reinterpret_cast<const float2 *>(efp + w * nzp)[e];
+    t[swz(e, w, sw)] = cf{(v.x * scale) * f.x, (v.y * scale) * f.y};
+  }
+};
+
+// Row strides of the plane kernel's swizzled tiles (multiples of 16 complex
+// values covering the pencil indices, see SmemX): the y layout holds columns
+// 0..H-1 (the kz = NZ/2 column travels packed into column 0), the z layout
+// rows 0..NY-1. A tile also holds one raw plane (NY x (H+1)) on arrival.
+__host__ __device__ constexpr int kplane_ysw(int h) { return ((h + 15) / 16) * 16; }
+__host__ __device__ constexpr int kplane_rsw(int ny) { return ((ny + 15) / 16) * 16; }
+__host__ __device__ constexpr int kmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int kplane_tile(int ny, int h) {
+  return kmax(kmax(h * kplane_rsw(ny), ny * kplane_ysw(h)), ny * (h + 1));
+}
+// bytes of the plane kernel's shared memory: eps_face plane (NY x NZ_ floats),
+// two tiles, twiddles (NY + H + H+1), packed column, kz = NZ/2 column, 2 mbarriers
+__host__ __device__ constexpr size_t kplane_smem(int ny, int h) {
+  return (size_t)ny * (2 * h + 2) * sizeof(float) + 2 * (size_t)kplane_tile(ny, h) * sizeof(cf) +
+         ((size_t)ny + h + (h + 1) + 2 * ny) * sizeof(cf) + 2 * sizeof(unsigned long long);
+}
+
+// ---- bulk asynchronous copies (1D TMA) with mbarrier completion ------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+// global -> shared copy of `bytes` (multiple of 16, both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(mbar)
+               : "memory");
+}
+// Wait for phase `parity` of the mbarrier, at most `limit` polls; on timeout
+// the error word is set (the host reports it) and the caller goes on.
+__device__ __forceinline__ void mbar_wait(uint32_t mbar, uint32_t parity, int *err) {
+  for (int it = 0; it < (1 << 16); it++) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return;
+  }
+  atomicExch(err, 1);
+}
+
+// First-stage source of the y transforms with the kz = 0 and kz = NZ/2
+// columns packed into pencil 0 (p holds that pencil's elements).
+struct SrcPacked {
+  const cf *t;
+  int sw;
+  const cf *p;
+  __device__ __forceinline__ cf load(int w, int e) const { return w == 0 ? p[e] : t[swz(e, w, sw)]; }
+};
+
+// One block per (x-plane, component): the plane's y/z inverse transform, the
+// product with the face permittivity and the z/y forward transform. The raw
+// k-space plane and the eps_face plane arrive by bulk asynchronous copies
+// (the latter overlapping the y phase). Every 1D transform runs on one lane
+// group of a warp (group_fft); the block synchronises only where a phase
+// reads other groups' pencils (the two y <-> z re-layouts, the real
+// merge/split and the global load/store). The kz = 0 and kz = NZ/2 columns
+// are Hermitian in j on the way in and real in j on the way out, so they
+// travel as one complex column (Z = X0 + i XH), leaving H y transforms.
 template <int NY, int H>
 __global__ void __launch_bounds__(1024) k_kop_plane(Grid g, float *w0, float *w1, float *w2, const float *ef0,
                                                     const float *ef1, const float *ef2, const cf *__restrict__ twy,
                                                     const cf *__restrict__ twz, const cf *__restrict__ post,
-                                                    float scale) {
-  extern __shared__ unsigned char smem_raw[];
-  cf *sty = reinterpret_cast<cf *>(smem_raw);
+                                                    float scale, int *err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int ysw = kplane_ysw(H), rsw = kplane_rsw(NY), TILE = kplane_tile(NY, H);
+  constexpr int NZP = 2 * H + 2;
+  float *efs = reinterpret_cast<float *>(smem_raw);  // eps_face_d of the plane, [j][NZ_]
+  cf *A = reinterpret_cast<cf *>(efs + NY * NZP);
+  cf *B = A + TILE;
+  cf *sty = B + TILE;
   cf *stz = sty + NY;
   cf *spost = stz + H;
-  cf *A = spost + (H + 1);
-  cf *B = A + plane_tile(NY, H);
+  cf *pk = spost + (H + 1);  // the packed column
+  cf *colh = pk + NY;        // the kz = NZ/2 column as loaded
+  unsigned long long *mb = reinterpret_cast<unsigned long long *>(colh + NY);
   const int i = blockIdx.x, d = blockIdx.y;
   float *data = (d == 0) ? w0 : (d == 1) ? w1 : w2;
   const float *ef = (d == 0) ? ef0 : (d == 1) ? ef1 : ef2;
   const int nthr = blockDim.x * blockDim.y, lin = threadIdx.y * blockDim.x + threadIdx.x;
+  cf *cplane = reinterpret_cast<cf *>(data) + (long)i * NY * (H + 1);
+  const float *efp = ef + (long)i * NY * NZP;
+  constexpr uint32_t PLANE_BYTES = NY * (H + 1) * sizeof(cf), EF_BYTES = NY * NZP * sizeof(float);
+  const uint32_t mb0 = smem_addr(&mb[0]), mb1 = smem_addr(&mb[1]);
+  if (lin == 0) {
+    mbar_init(mb0, 1);
+    mbar_init(mb1, 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (lin == 0) {
+    mbar_expect_tx(mb0, PLANE_BYTES);
+    bulk_g2s(smem_addr(B), cplane, PLANE_BYTES, mb0);
+    mbar_expect_tx(mb1, EF_BYTES);
+    bulk_g2s(smem_addr(efs), efp, EF_BYTES, mb1);
+  }
   load_table(sty, twy, NY);
   load_table(stz, twz, H);
   load_table(spost, post, H + 1);
-  const cf *cplane = reinterpret_cast<const cf *>(data) + (long)i * NY * g.hnz;
-  constexpr int ysw = H + 2;
+  mbar_wait(mb0, 0, err);
+  // raw plane [j][k] (in B) -> swizzled y layout (columns 0..H-1) + column H
   for (int q = lin; q < NY * (H + 1); q += nthr) {
     const int j = q / (H + 1), k = q - j * (H + 1);
-    A[j * ysw + k] = cplane[q];
+    const cf v = B[q];
+    if (k < H) A[swz(j, k, ysw)] = v;
+    else colh[j] = v;
   }
   __syncthreads();
-  cf *rows = plane_inv_core<float, NY, H>(A, B, sty, stz, spost);
-  // the real field times the face permittivity (C2R scaling first, as the
-  // plain path stores the scaled field before multiplying)
-  constexpr int rsw = NY + 1;
-  const float *efp = ef + (long)i * NY * g.nzp;
+  // the j-direction half of the Hermitian completion (kz = 0 keeps rows
+  // 1..NY/2-1, kz = NZ/2 keeps rows NY/2+1..NY-1; rows 0, NY/2 are complete)
+  // and the packing Z = X0 + i XH of the two completed columns
+  for (int j = lin; j < NY; j += nthr) {
+    const int m = (NY - j) & (NY - 1);
+    const bool low = (j >= 1 && j < NY / 2), high = (j > NY / 2);
+    const cf x0 = high ? cconj(A[swz(m, 0, ysw)]) : A[swz(j, 0, ysw)];
+    const cf xh = low ? cconj(colh[m]) : colh[j];
+    pk[j] = cf{x0.x - xh.y, x0.y + xh.x};
+  }
+  __syncthreads();
+  // y inverse of the H columns (pencil 0 packed)
+  constexpr int yst = Plan<NY>::nstages;
+  cf *yres = (yst & 1) ? B : A;
+  cf *zbuf = (yst & 1) ? A : B;
+  group_fft<float, NY, H>(SrcPacked{A, ysw, pk}, SmemX<float>{yres, ysw}, A, B, ysw, sty, true);
+  __syncthreads();
+  // merge into H-point complex rows; column 0 holds x0 + i xh (both real)
   for (int q = lin; q < NY * H; q += nthr) {
-    const int j = q / H, e = q - j * H;
-    const float2 f = reinterpret_cast<const float2 *>(efp + (long)j * g.nzp)[e];
-    cf x = rows[e * rsw + j];
-    x.x = (x.x * scale) * f.x;
-    x.y = (x.y * scale) * f.y;
-    rows[e * rsw + j] = x;
+    const int j = q / H, k = q - j * H;
+    cf x, c;
+    if (k == 0) {
+      const cf z = yres[swz(j, 0, ysw)];
+      x = cf{z.x, 0.f};
+      c = cf{z.y, 0.f};
+    } else {
+      x = yres[swz(j, k, ysw)];
+      c = yres[swz(j, H - k, ysw)];
+    }
+    zbuf[swz(k, j, rsw)] = merge_inv(x, cconj(c), spost[k]);
   }
   __syncthreads();
-  cf *other = (rows == A) ? B : A;
-  GPencils<float> outp{reinterpret_cast<cf *>(data), (long)i * NY * g.hnz, 1, g.hnz, H + 1};
-  plane_fwd_core<float, NY, H>(rows, other, sty, stz, spost, outp);
+  mbar_wait(mb1, 0, err);
+  // z inverse, times the scaled face permittivity, z forward: row j stays on
+  // the same lane group throughout, so no block synchronisation in between
+  constexpr int zst = Plan<H>::nstages;
+  cf *other = (zbuf == A) ? B : A;
+  cf *rows = (zst & 1) ? other : zbuf;
+  MulSink ms{rows, rsw, efs, NZP, scale};
+  group_fft<float, H, NY>(SmemX<float>{zbuf, rsw}, ms, zbuf, other, rsw, stz, true);
+  cf *rother = (rows == A) ? B : A;
+  cf *zf = (zst & 1) ? rother : rows;
+  group_fft<float, H, NY>(SmemX<float>{rows, rsw}, SmemX<float>{zf, rsw}, rows, rother, rsw, stz, false);
+  __syncthreads();
+  // split into the half spectrum (y-pencil layout); the real kz = 0 and
+  // kz = NZ/2 values are packed into column 0
+  cf *ybuf = (zf == A) ? B : A;
+  for (int q = lin; q < NY * H; q += nthr) {
+    const int j = q / H, k = q - j * H;
+    if (k == 0) {
+      const cf z0 = zf[swz(0, j, rsw)], c0 = cconj(z0);
+      const float x0 = split_fwd(z0, c0, spost[0]).x, xh = split_fwd(z0, c0, spost[H]).x;
+      ybuf[swz(j, 0, ysw)] = cf{x0, xh};
+    } else {
+      ybuf[swz(j, k, ysw)] = split_fwd(zf[swz(k, j, rsw)], cconj(zf[swz(H - k, j, rsw)]), spost[k]);
+    }
+  }
+  __syncthreads();
+  // y forward of the H columns, then the unpacking of column 0 and a
+  // coalesced store
+  cf *yo = (ybuf == A) ? B : A;
+  cf *yout = (yst & 1) ? yo : ybuf;
+  group_fft<float, NY, H>(SmemX<float>{ybuf, ysw}, SmemX<float>{yout, ysw}, ybuf, yo, ysw, sty, false);
+  __syncthreads();
+  for (int q = lin; q < NY * (H + 1); q += nthr) {
+    const int j = q / (H + 1), k = q - j * (H + 1);
+    if (k == 0 || k == H) {
+      const cf z = yout[swz(j, 0, ysw)], zm = cconj(yout[swz((NY - j) & (NY - 1), 0, ysw)]);
+      cplane[q] = (k == 0) ? cf{0.5f * (z.x + zm.x), 0.5f * (z.y + zm.y)}
+                           : cf{0.5f * (z.y - zm.y), -0.5f * (z.x - zm.x)};
+    } else {
+      cplane[q] = yout[swz(j, k, ysw)];
+    }
+  }
 }
 
 // Last-stage sink of the forward x transforms: acc += k_D exp(-i dx k_D/2) X_D
@@ -333,8 +492,8 @@ __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1
 }
 
 size_t xpass_smem(int n) { return ((size_t)n + 3 * (size_t)n * (KW + 1)) * sizeof(cf); }
-size_t plane_smem_f(int ny, int h) { return ((size_t)ny + h + (h + 1) + 2 * (size_t)plane_tile(ny, h)) * sizeof(cf); }
-constexpr size_t KOP_PLANE_SMEM_MAX = 200 * 1024;
+size_t plane_smem_f(int ny, int h) { return kplane_smem(ny, h); }
+constexpr size_t KOP_PLANE_SMEM_MAX = 220 * 1024;
 
 dim3 xblock(int n) { return dim3(KW, n / 8 < 512 / KW ? n / 8 : 512 / KW); }
 
@@ -349,7 +508,7 @@ void set_x_attr() {
 
 template <int NY, int H>
 void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-                     const float *ef2, cudaStream_t s) {
+                     const float *ef2, int *err, cudaStream_t s) {
   const size_t sm = plane_smem_f(NY, H);
   static bool attr = false;  // one attribute call per instantiation
   if (!attr) {
@@ -360,19 +519,19 @@ void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, c
   count_launch();
   probe_begin(PROBE_KOP_PLANE, s);
   k_kop_plane<NY, H><<<dim3(p.g.nx, 3), 1024, sm, s>>>(p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z,
-                                                             p.tw_post, scale);
+                                                             p.tw_post, scale, err);
   // algorithmic bytes: per field the half spectrum in and out and eps_face_d in
   probe_end(PROBE_KOP_PLANE, 3.0 * 3.0 * sizeof(float) * (double)p.g.nreal(), s);
 }
 
 template <int NY>
 void launch_plane_n(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-                    const float *ef2, cudaStream_t s) {
+                    const float *ef2, int *err, cudaStream_t s) {
   switch (p.g.nz / 2) {
-    case 8: launch_plane_nh<NY, 8>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
-    case 16: launch_plane_nh<NY, 16>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
-    case 32: launch_plane_nh<NY, 32>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
-    default: launch_plane_nh<NY, 64>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+    case 8: launch_plane_nh<NY, 8>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
+    case 16: launch_plane_nh<NY, 16>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
+    case 32: launch_plane_nh<NY, 32>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
+    default: launch_plane_nh<NY, 64>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
   }
 }
 
@@ -416,12 +575,12 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
 }
 
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-               const float *ef2, cudaStream_t s) {
+               const float *ef2, int *err, cudaStream_t s) {
   switch (p.g.ny) {
-    case 16: launch_plane_n<16>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
-    case 32: launch_plane_n<32>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
-    case 64: launch_plane_n<64>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
-    default: launch_plane_n<128>(p, w0, w1, w2, ef0, ef1, ef2, s); break;
+    case 16: launch_plane_n<16>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
+    case 32: launch_plane_n<32>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
+    case 64: launch_plane_n<64>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
+    default: launch_plane_n<128>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
   }
 }
 

@@ -35,8 +35,10 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
               double omega, double rho, const double *part, int npart, double eps_ref, float *w0, float *w1,
               float *w2, cudaStream_t s);
+// err: device word set to 1 if a bulk copy into shared memory did not
+// complete within the kernel's wait limit (checked by the caller)
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-               const float *ef2, cudaStream_t s);
+               const float *ef2, int *err, cudaStream_t s);
 // mode KOP_P: partials[2b] = (other, out) with other = r0;
 // mode KOP_S: partials[2b] = (out, out), partials[2b+1] = (out, other) with other = s;
 // mode KOP_NONE: no dot products (other, partials unused).

@@ -122,6 +122,162 @@ __global__ void __launch_bounds__(CONV_WARPS * 32) k_conv_mma(int lg, const bf16
   }
 }
 
+// ---- tcgen05 convolution (forward) ------------------------------------------
+// out[v][co] = act(bias[co] + sum_t sum_ci in[v + s_t][ci] Wk[t][co][ci]) as an
+// implicit GEMM on the 5th-generation tensor cores: a CTA owns 128 voxels
+// (M = 128), N = COUT, and walks the 27 taps; per tap the 128 x CIN operand
+// rows (the tap's neighbours, cat/up-sampled sources as in k_conv_mma) and
+// the COUT x CIN weights are staged in shared memory in the K-major
+// no-swizzle core-matrix layout (8 rows x 16 bytes per core matrix), and one
+// thread issues CIN/16 tcgen05.mma (kind::f16, BF16 x BF16 -> FP32) into a
+// TMEM accumulator. Operand buffers are double-buffered; a tcgen05.commit per
+// tap arrives on that buffer's mbarrier, which the threads wait on (bounded)
+// before refilling it. The epilogue reads the accumulator with tcgen05.ld.
+constexpr int TC_M = 128;
+__device__ __forceinline__ uint32_t sh_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+// byte offset of element (row, k) of a K-major no-swizzle tile with KG k-groups
+__device__ __forceinline__ int tc_off(int row, int k, int KG) {
+  return (((row >> 3) * KG + (k >> 3)) << 7) + ((row & 7) << 4) + ((k & 7) << 1);
+}
+// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets between core matrices, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | ((uint64_t)1 << 46);
+}
+// instruction descriptor of kind::f16: FP32 accumulate, BF16 A and B, both K-major
+template <int M, int N>
+__host__ __device__ constexpr uint32_t tc_idesc() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void tc_wait(uint32_t mbar, uint32_t parity, int *err) {
+  for (int it = 0; it < (1 << 16); it++) {
+    uint32_t done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                 : "=r"(done)
+                 : "r"(mbar), "r"(parity)
+                 : "memory");
+    if (done) return;
+  }
+  atomicExch(err, 1);
+}
+
+template <int CINA, int CINB, int COUT, bool RELU>
+__global__ void __launch_bounds__(128) k_conv_tc(int lg, const bf16 *__restrict__ a, const bf16 *__restrict__ b,
+                                                 const bf16 *__restrict__ W, const float *__restrict__ bias, bf16 *out,
+                                                 int *err) {
+  constexpr int CIN = CINA + CINB, KG = CIN / 8, KSTEPS = CIN / 16;
+  constexpr int NCOL = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
+  constexpr int ABYTES = TC_M * CIN * 2, BBYTES = COUT * CIN * 2;
+  static_assert(CINA % 16 == 0 && CINB % 16 == 0 && COUT % 16 == 0 && COUT <= 128, "tcgen05 shapes");
+  extern __shared__ __align__(128) unsigned char tsm[];
+  // operand buffers: A[buf] at tsm + buf*ABYTES, B[buf] at tsm + 2*ABYTES + buf*BBYTES
+  __shared__ __align__(8) unsigned long long mbar[2];
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int V = 1 << (3 * lg), m = (1 << lg) - 1;
+  const int v = blockIdx.x * TC_M + tid;  // this thread's voxel row
+  const bool valid = v < V;
+  int x0 = 0, y0 = 0, z0 = 0;
+  if (valid) vcoord(lg, v, x0, y0, z0);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sh_addr(&mbar[0])) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(sh_addr(&mbar[1])) : "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sh_addr(&tmem_base)),
+                 "r"(NCOL)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  for (int t = 0; t < 27; t++) {
+    const int buf = t & 1;
+    if (t >= 2) tc_wait(sh_addr(&mbar[buf]), ((t - 2) >> 1) & 1, err);  // the MMAs of tap t-2 read this buffer
+    // operand rows: this thread's voxel neighbour at tap t, CIN channels in 16-byte chunks
+    int dx, dy, dz;
+    tap(t, dx, dy, dz);
+    const int nx = (x0 + dx) & m, ny = (y0 + dy) & m, nz = (z0 + dz) & m;
+#pragma unroll
+    for (int c = 0; c < KG; c++) {
+      uint4 val = make_uint4(0, 0, 0, 0);
+      if (valid) {
+        if (c * 8 < CINA)
+          val = *reinterpret_cast<const uint4 *>(a + (long)vox(lg, nx, ny, nz) * CINA + c * 8);
+        else
+          val = *reinterpret_cast<const uint4 *>(b + (long)vox(lg - 1, nx >> 1, ny >> 1, nz >> 1) * CINB +
+                                                 (c * 8 - CINA));
+      }
+      *reinterpret_cast<uint4 *>(tsm + buf * ABYTES + tc_off(tid, c * 8, KG)) = val;
+    }
+    // weights of tap t, Wk[t][co][ci]
+    for (int q = tid; q < COUT * KG; q += 128) {
+      const int co = q / KG, c = q - co * KG;
+      *reinterpret_cast<uint4 *>(tsm + 2 * ABYTES + buf * BBYTES + tc_off(co, c * 8, KG)) =
+          *reinterpret_cast<const uint4 *>(W + ((long)t * COUT + co) * CIN + c * 8);
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < KSTEPS; kk++) {
+        const uint64_t ad = tc_desc(sh_addr(tsm + buf * ABYTES) + kk * 256, 128, KG * 128);
+        const uint64_t bd = tc_desc(sh_addr(tsm + 2 * ABYTES + buf * BBYTES) + kk * 256, 128, KG * 128);
+        const uint32_t acc = (t > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+                tmem),
+            "l"(ad), "l"(bd), "r"(tc_idesc<TC_M, COUT>()), "r"(acc)
+            : "memory");
+      }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       sh_addr(&mbar[buf]))
+                   : "memory");
+    }
+  }
+  // the last commit (tap 26, buffer 0, its 14th) follows every MMA
+  tc_wait(sh_addr(&mbar[0]), 13 & 1, err);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // epilogue: warp w holds rows 32w..32w+31 of the accumulator
+#pragma unroll
+  for (int c0 = 0; c0 < COUT; c0 += 16) {
+    uint32_t r[16];
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+    const int row = warp * 32 + lane;
+    const int vr = blockIdx.x * TC_M + row;
+    if (vr < V) {
+      __nv_bfloat162 o[8];
+#pragma unroll
+      for (int j = 0; j < 16; j += 2) {
+        float d0 = __uint_as_float(r[j]) + bias[c0 + j], d1 = __uint_as_float(r[j + 1]) + bias[c0 + j + 1];
+        if (RELU) {
+          d0 = fmaxf(d0, 0.f);
+          d1 = fmaxf(d1, 0.f);
+        }
+        o[j / 2] = __floats2bfloat162_rn(d0, d1);
+      }
+      uint4 *dst = reinterpret_cast<uint4 *>(out + (long)vr * COUT + c0);
+      dst[0] = *reinterpret_cast<uint4 *>(&o[0]);
+      dst[1] = *reinterpret_cast<uint4 *>(&o[4]);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOL) : "memory");
+}
+
 // ---- CUDA-core layers ------------------------------------------------------
 // first layer: 2 FP32 input channels -> 16 (bias, relu, BF16 out)
 __global__ void k_conv_in(int lg, const float *__restrict__ x, const float *__restrict__ W,
@@ -410,6 +566,21 @@ void conv_mma(int lg, const bf16 *a, const bf16 *b, const bf16 *W, const float *
       <<<(unsigned)((V / 16 + CONV_WARPS - 1) / CONV_WARPS), CONV_WARPS * 32, 0, s>>>(lg, a, b, W, bias, out);
 }
 
+template <int CINA, int CINB, int COUT, bool RELU>
+void conv_tc(int lg, const bf16 *a, const bf16 *b, const bf16 *W, const float *bias, bf16 *out, int *err,
+             cudaStream_t s) {
+  const long V = 1L << (3 * lg);
+  constexpr int CIN = CINA + CINB;
+  const size_t sm = 2 * (size_t)(TC_M * CIN + COUT * CIN) * sizeof(bf16);
+  static bool attr = false;  // one attribute call per instantiation
+  if (!attr) {
+    cudaFuncSetAttribute(k_conv_tc<CINA, CINB, COUT, RELU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr = true;
+  }
+  count_launch();
+  k_conv_tc<CINA, CINB, COUT, RELU><<<(unsigned)((V + TC_M - 1) / TC_M), 128, sm, s>>>(lg, a, b, W, bias, out, err);
+}
+
 template <typename TA, typename TZ, int CINA, int CINB, int COUT>
 void conv_wgrad(int lg, const TA *a, const TA *b, const TZ *gz, float *dW, float *db, cudaStream_t s) {
   const long V = 1L << (3 * lg);
@@ -471,7 +642,9 @@ int UNet::init(int n_coarse, unsigned long long seed, cudaStream_t s) {
   fal(&g1, 32 * V1);
   bal(&gz, 16 * V0);
   bal(&gz2, 16 * V0);
+  ok = ok && cudaMalloc(&err, sizeof(int)) == cudaSuccess;
   if (!ok) return ICEP_ERR_CUDA;
+  cudaMemsetAsync(err, 0, sizeof(int), s);
   // He-normal initial weights (zero biases), drawn on the host
   std::vector<float> h(nparams, 0.f);
   std::mt19937_64 rng(seed);
@@ -493,6 +666,7 @@ void UNet::free_all() {
   for (float *p : fs) cudaFree(p);
   bf16 *bs[] = {wf, wb, e0a, e0, p1, e1a, e1, p2, e2a, e2, d1, d0, gz, gz2};
   for (bf16 *p : bs) cudaFree(p);
+  cudaFree(err);
   params = nullptr;
 }
 
@@ -509,17 +683,17 @@ void UNet::forward(cudaStream_t s) {
   const long V0 = (long)n * n * n, V1 = V0 / 8, V2 = V0 / 64;
   count_launch();
   k_conv_in<<<nb256(V0), 256, 0, s>>>(lg, x, params + woff[L_C0A], params + boff[L_C0A], e0a);
-  conv_mma<16, 0, 16, false, true>(lg, e0a, nullptr, wf + wbf_off[L_C0B], params + boff[L_C0B], e0, s);
+  conv_tc<16, 0, 16, true>(lg, e0a, nullptr, wf + wbf_off[L_C0B], params + boff[L_C0B], e0, err, s);
   count_launch();
   k_pool<<<nb256(V1 * 16), 256, 0, s>>>(lg, 16, e0, p1);
-  conv_mma<16, 0, 32, false, true>(lg - 1, p1, nullptr, wf + wbf_off[L_C1A], params + boff[L_C1A], e1a, s);
-  conv_mma<32, 0, 32, false, true>(lg - 1, e1a, nullptr, wf + wbf_off[L_C1B], params + boff[L_C1B], e1, s);
+  conv_tc<16, 0, 32, true>(lg - 1, p1, nullptr, wf + wbf_off[L_C1A], params + boff[L_C1A], e1a, err, s);
+  conv_tc<32, 0, 32, true>(lg - 1, e1a, nullptr, wf + wbf_off[L_C1B], params + boff[L_C1B], e1, err, s);
   count_launch();
   k_pool<<<nb256(V2 * 32), 256, 0, s>>>(lg - 1, 32, e1, p2);
-  conv_mma<32, 0, 64, false, true>(lg - 2, p2, nullptr, wf + wbf_off[L_C2A], params + boff[L_C2A], e2a, s);
-  conv_mma<64, 0, 64, false, true>(lg - 2, e2a, nullptr, wf + wbf_off[L_C2B], params + boff[L_C2B], e2, s);
-  conv_mma<32, 64, 32, false, true>(lg - 1, e1, e2, wf + wbf_off[L_C1U], params + boff[L_C1U], d1, s);
-  conv_mma<16, 32, 16, false, true>(lg, e0, d1, wf + wbf_off[L_C0U], params + boff[L_C0U], d0, s);
+  conv_tc<32, 0, 64, true>(lg - 2, p2, nullptr, wf + wbf_off[L_C2A], params + boff[L_C2A], e2a, err, s);
+  conv_tc<64, 0, 64, true>(lg - 2, e2a, nullptr, wf + wbf_off[L_C2B], params + boff[L_C2B], e2, err, s);
+  conv_tc<32, 64, 32, true>(lg - 1, e1, e2, wf + wbf_off[L_C1U], params + boff[L_C1U], d1, err, s);
+  conv_tc<16, 32, 16, true>(lg, e0, d1, wf + wbf_off[L_C0U], params + boff[L_C0U], d0, err, s);
   count_launch();
   k_conv_out<<<nb256(V0), 256, 0, s>>>(lg, d0, params + woff[L_OUT], params + boff[L_OUT], y);
 }

@@ -10,9 +10,11 @@
 //   up 0    d0 = relu(c0u(cat(e0, up d1)))               16 ch, n^3
 //   output  y  = out(d0)                                 1 ch,  n^3 (FP32)
 //
-// The 16..96-channel convolutions are implicit GEMMs on the tensor cores
-// (BF16 mma, FP32 accumulation); the 2-channel input and 1-channel output
-// layers run on the CUDA cores in FP32. The flat FP32 parameter vector and
+// The 16..96-channel convolutions are implicit GEMMs on the tensor cores with
+// FP32 accumulation: tcgen05.mma with a TMEM accumulator in the forward pass
+// (inference and training), mma.sync for the data gradients of the backward
+// pass; the 2-channel input and 1-channel output layers and the weight
+// gradients run on the CUDA cores in FP32. The flat FP32 parameter vector and
 // the tap/channel conventions are those of the CPU oracle (oracle/unet_ref.py).
 #pragma once
 #include <cuda_bf16.h>
@@ -39,6 +41,7 @@ struct UNet {
   // backward work
   float *gy = nullptr, *tmp = nullptr, *g0 = nullptr, *g1 = nullptr;
   bf16 *gz = nullptr, *gz2 = nullptr;
+  int *err = nullptr;  // set by a tensor-core convolution whose completion wait ran out
   int adam_t = 0;
 
   int init(int n_coarse, unsigned long long seed, cudaStream_t s);

@@ -25,12 +25,13 @@ __device__ __forceinline__ long stencil_point(const PartParams &pp, const double
     const int xi = (int)v;
     const double res = (v - (double)xi) * pp.dx;
     const int cell = sek[3 * m + d];
-    // wrap in 64-bit: a non-finite or huge coordinate (a diverged run) still
-    // yields an index inside the grid
-    rm[d] = (int)((((long long)xi % pp.N[d]) + cell + 2LL * pp.N[d]) % pp.N[d]);
+    // periodic wrap (N a power of two): unsigned arithmetic keeps the index
+    // inside the grid for any coordinate, a non-finite or huge one included
+    rm[d] = (int)(((unsigned)xi + (unsigned)cell) & (unsigned)(pp.N[d] - 1));
     r[d] = (double)cell * pp.dx - res;
     double x12 = xp[d] - rm[d] * pp.dx;
-    x12 -= (double)nint_d(x12 / pp.L[d]) * pp.L[d];
+    // minimum image: nint(x12/L) is 0 while |x12| < L/2
+    if (!(fabs(x12) < 0.5 * pp.L[d])) x12 -= (double)nint_d(x12 / pp.L[d]) * pp.L[d];
     s += x12 * x12;
   }
   *dist = sqrt(s);
@@ -250,49 +251,62 @@ __global__ void k_lj_cells(PartParams pp, CellGeom cg, const icep_particle *__re
 // Per-particle gather over the 27-cell scan with the reference's wrap rule
 // (md_force.cxx:60-82): with one or two cells along an axis a neighbour cell
 // is visited more than once and each visit adds the pair force again.
+// One warp per particle: lane l < 27 scans neighbour cell l of the 27-cell
+// block (the reference's wrap rule, md_force.cxx:60-82: with one or two cells
+// along an axis a neighbour cell is visited more than once and each visit
+// adds the pair force again); the FP64 force is reduced over the warp. Pairs
+// farther than the cutoff are skipped on the squared distance with a margin
+// before any division; for the others the arithmetic is the reference's
+// (the minimum-image division can only be non-zero where |dx| >= L/2).
 __global__ void k_lj_gather(PartParams pp, CellGeom cg, icep_particle *p, const int *__restrict__ start,
                             const int *__restrict__ list, int *pairs, int max_pairs, int *n_pairs) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
-  if (a >= pp.np) return;
+  const int a = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (a >= pp.np) return;  // whole warps leave together
   double xa[3];
   for (int d = 0; d < 3; d++) xa[d] = p[a].x[d];
-  int ic[3];
-  for (int d = 0; d < 3; d++) ic[d] = cell_coord(cg, xa[d], d);
   double f[3] = {0, 0, 0};
-  for (int o0 = -1; o0 <= 1; o0++)
-    for (int o1 = -1; o1 <= 1; o1++)
-      for (int o2 = -1; o2 <= 1; o2++) {
-        int cl[3] = {ic[0] + o0, ic[1] + o1, ic[2] + o2};
-        for (int d = 0; d < 3; d++) {
-          if (cl[d] < 0) cl[d] = cg.lc[d] - 1;
-          if (cl[d] > cg.lc[d] - 1) cl[d] = 0;
-        }
-        const int c = (cl[0] * cg.lc[1] + cl[1]) * cg.lc[2] + cl[2];
-        for (int q = start[c]; q < start[c + 1]; q++) {
-          const int j = list[q];
-          if (j == a) continue;
-          double rv[3], s = 0.0;
-          for (int d = 0; d < 3; d++) {
-            rv[d] = p[j].x[d] - xa[d];
-            rv[d] -= (double)nint_d(rv[d] / pp.L[d]) * pp.L[d];
-            s += rv[d] * rv[d];
-          }
-          const double rij = sqrt(s);
-          if (rij < pp.r_cutoff) {
-            const double va = DBL_MAX / rij, vb = lj_f(pp, rij);
-            const double fr = (va < vb) ? va : vb;
-            for (int d = 0; d < 3; d++) f[d] += fr * (-rv[d]);
-            if (pairs && j < a) {
-              const int k = atomicAdd(n_pairs, 1);
-              if (k < max_pairs) {
-                pairs[2 * k] = a;
-                pairs[2 * k + 1] = j;
-              }
-            }
+  const double rc = pp.r_cutoff, rc2 = rc * rc * (1.0 + 1e-9);
+  if (lane < 27) {
+    int ic[3];
+    for (int d = 0; d < 3; d++) ic[d] = cell_coord(cg, xa[d], d);
+    const int o[3] = {lane / 9 - 1, (lane / 3) % 3 - 1, lane % 3 - 1};
+    int cl[3];
+    for (int d = 0; d < 3; d++) {
+      cl[d] = ic[d] + o[d];
+      if (cl[d] < 0) cl[d] = cg.lc[d] - 1;
+      if (cl[d] > cg.lc[d] - 1) cl[d] = 0;
+    }
+    const int c = (cl[0] * cg.lc[1] + cl[1]) * cg.lc[2] + cl[2];
+    for (int q = start[c]; q < start[c + 1]; q++) {
+      const int j = list[q];
+      if (j == a) continue;
+      double rv[3], s = 0.0;
+      for (int d = 0; d < 3; d++) {
+        rv[d] = p[j].x[d] - xa[d];
+        if (!(fabs(rv[d]) < 0.5 * pp.L[d])) rv[d] -= (double)nint_d(rv[d] / pp.L[d]) * pp.L[d];
+        s += rv[d] * rv[d];
+      }
+      if (s > rc2) continue;
+      const double rij = sqrt(s);
+      if (rij < rc) {
+        const double va = DBL_MAX / rij, vb = lj_f(pp, rij);
+        const double fr = (va < vb) ? va : vb;
+        for (int d = 0; d < 3; d++) f[d] += fr * (-rv[d]);
+        if (pairs && j < a) {
+          const int k = atomicAdd(n_pairs, 1);
+          if (k < max_pairs) {
+            pairs[2 * k] = a;
+            pairs[2 * k + 1] = j;
           }
         }
       }
-  for (int d = 0; d < 3; d++) p[a].fr[d] += f[d];
+    }
+  }
+  for (int d = 0; d < 3; d++)
+    for (int off = 16; off > 0; off >>= 1) f[d] += __shfl_down_sync(0xffffffffu, f[d], off);
+  if (lane == 0)
+    for (int d = 0; d < 3; d++) p[a].fr[d] += f[d];
 }
 
 // quaternion helpers (quaternion.h:173-213, rigid_body.cxx:10-24)
@@ -436,7 +450,7 @@ int lj_force(const PartParams &pp, icep_particle *p, int *work, int work_ints, i
   count_launch();
   k_lj_cells<<<1, 1024, 0, s>>>(pp, cg, p, start, fill, list, ncell);
   count_launch();
-  k_lj_gather<<<div_up(pp.np, 128), 128, 0, s>>>(pp, cg, p, start, list, pairs, max_pairs, n_pairs);
+  k_lj_gather<<<div_up((long)pp.np * 32, 128), 128, 0, s>>>(pp, cg, p, start, list, pairs, max_pairs, n_pairs);
   return ICEP_OK;
 }
 

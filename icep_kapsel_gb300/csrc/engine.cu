@@ -267,7 +267,7 @@ class Engine : public EngineBase {
     if (mixed && electrolyte && kop_supported(g)) {
       kop_npb = kop_pencil_blocks(g);
       // the dot partials, then one word for the plane passes' error flag
-      const size_t nk = 2 * (2 * (size_t)kop_npb + DOT_BLOCKS) + 1;
+      const size_t nk = 2 * (2 * (size_t)kop_npb + kop_xr_blocks(g)) + 1;
       if (cudaMalloc(&kpart, sizeof(double) * nk) != cudaSuccess || cudaMallocHost(&hkpart, sizeof(double) * nk) != cudaSuccess)
         return fail(ICEP_ERR_CUDA, "allocation of the k-space dot partials failed");
       cudaMemsetAsync(kpart, 0, sizeof(double) * nk, s);
@@ -641,7 +641,8 @@ class Engine : public EngineBase {
       float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2];
       const int nb = kop_npb;
       double *P1 = kpart, *P2 = kpart + 2 * nb, *P3 = kpart + 4 * nb;
-      const size_t nk = 2 * (2 * (size_t)nb + DOT_BLOCKS) + 1;  // with the error word
+      const int nxr = kop_xr_blocks(g);
+      const size_t nk = 2 * (2 * (size_t)nb + nxr) + 1;  // with the error word
       if (!kspace_io) {  // right-hand side from the real field F_KB, else already in F_KR
         copy_real<R>(g, f[F_KB], r, s);
         r2c(r);
@@ -698,7 +699,7 @@ class Engine : public EngineBase {
           tt += hkpart[2 * nb + 2 * b];
           ts += hkpart[2 * nb + 2 * b + 1];
         }
-        for (int b = 0; b < DOT_BLOCKS; b++) {
+        for (int b = 0; b < nxr; b++) {
           r0r += hkpart[4 * nb + 2 * b];
           rr += hkpart[4 * nb + 2 * b + 1];
         }

@@ -168,7 +168,8 @@ __global__ void k_advection_combine(Grid g, R *u0, R *u1, R *u2, R *a0, R *a1) {
 }
 
 template <typename R>
-__global__ void k_ns_slaved(Grid g, R *z0, R *z1, const R *a0, const R *a1, double nu, double dt) {
+// mnudt = -nu dt and inu = 1/nu come from the host (no FP64 arithmetic per thread)
+__global__ void k_ns_slaved(Grid g, R *z0, R *z1, const R *a0, const R *a1, R mnudt, R inu) {
   Mode m;
   if (!mode_of(g, TID, m)) return;
   if (!in_two_third(g, m.i, m.j, m.kz)) return;
@@ -176,8 +177,7 @@ __global__ void k_ns_slaved(Grid g, R *z0, R *z1, const R *a0, const R *a1, doub
   kvec(g, m, k);
   const R k2 = k2_of(k);
   const R ik2 = (k2 > R(0)) ? R(1) / k2 : R(0);
-  const R f = exp_t((R)(-nu * dt) * k2) - R(1);
-  const R inu = (R)(1. / nu);
+  const R f = exp_t(mnudt * k2) - R(1);
 #pragma unroll
   for (int c = 0; c < 2; c++) {
     const long im = m.im + c;
@@ -265,15 +265,14 @@ __global__ void k_div(Grid g, const R *u0, const R *u1, const R *u2, R *div, int
 }
 
 template <typename R>
-__global__ void k_euler(Grid g, R *z0, R *z1, R *r0, R *r1, R *c0, R *c1, const R *cr0, const R *cr1, double nu,
-                        double dt) {
+__global__ void k_euler(Grid g, R *z0, R *z1, R *r0, R *r1, R *c0, R *c1, const R *cr0, const R *cr1, R nu, R dt) {
   Mode m;
   if (!mode_of(g, TID, m)) return;
   if (!in_two_third(g, m.i, m.j, m.kz)) return;
   R k[3];
   kvec(g, m, k);
   const R k2 = k2_of(k);
-  const R nuk2 = (R)nu * k2, rdt = (R)dt;
+  const R nuk2 = nu * k2, rdt = dt;
 #pragma unroll
   for (int c = 0; c < 2; c++) {
     const long im = m.im + c;
@@ -350,11 +349,12 @@ __global__ void k_add_vec(Grid g, V3<R> u, V3<R> f, R a) {
 }
 
 template <typename R>
-__global__ void k_eps_from_profile(Grid g, R *eps, const R *phis, const R *epsw, double ef, double ep, double dc) {
+// efdc = eps_f dc, dc, epdc = (eps_p - eps_f) dc from the host
+__global__ void k_eps_from_profile(Grid g, R *eps, const R *phis, const R *epsw, R efdc, R dc, R epdc) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
-  if (epsw) eps[p.im] = (R)(ef * dc) + (R)dc * epsw[p.im];
-  else eps[p.im] = (R)(ef * dc) + (R)((ep - ef) * dc) * phis[p.im];
+  if (epsw) eps[p.im] = efdc + dc * epsw[p.im];
+  else eps[p.im] = efdc + epdc * phis[p.im];
 }
 
 template <typename R>
@@ -504,7 +504,7 @@ template <typename R> void advection_combine(const Grid &g, R *u0, R *u1, R *u2,
 }
 template <typename R> void ns_slaved_update(const Grid &g, R *z0, R *z1, const R *a0, const R *a1, double nu, double dt, cudaStream_t s) {
   count_launch();
-  k_ns_slaved<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, a0, a1, nu, dt);
+  k_ns_slaved<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, a0, a1, (R)(-nu * dt), (R)(1. / nu));
 }
 template <typename R> void solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s) {
   count_launch();
@@ -520,7 +520,7 @@ template <typename R> void div_k(const Grid &g, const R *u0, const R *u1, const 
 }
 template <typename R> void euler_update(const Grid &g, R *z0, R *z1, R *r0, R *r1, R *c0, R *c1, const R *cr0, const R *cr1, double nu, double dt, cudaStream_t s) {
   count_launch();
-  k_euler<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, r0, r1, c0, c1, cr0, cr1, nu, dt);
+  k_euler<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, r0, r1, c0, c1, cr0, cr1, (R)nu, (R)dt);
 }
 template <typename R> void inv_laplace_k(const Grid &g, R *a, double eps_ref, cudaStream_t s) {
   count_launch();
@@ -548,7 +548,7 @@ template <typename R> void add_vec(const Grid &g, R *const *u, R *const *f, R a,
 }
 template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_sin, const R *eps_w, double ef, double ep, double dc, cudaStream_t s) {
   count_launch();
-  k_eps_from_profile<R><<<nblk_real(g), TPB, 0, s>>>(g, eps, phi_sin, eps_w, ef, ep, dc);
+  k_eps_from_profile<R><<<nblk_real(g), TPB, 0, s>>>(g, eps, phi_sin, eps_w, (R)(ef * dc), (R)dc, (R)((ep - ef) * dc));
 }
 template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s) {
   count_launch();

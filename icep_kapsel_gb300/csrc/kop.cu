@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
                           DivAcc<1>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
   block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w2)), (long)q0, 1, (long)nq, nvalid},
                           DivAcc<2>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
-  double s0 = 0.0, s1 = 0.0;
+  float s0 = 0.f, s1 = 0.f;  // the thread's few terms in FP32; blocks and their sum in FP64
   for (int it = lin; it < N * KW; it += nthr) {
     const int w = it % KW, e = it / KW;
     if (w >= nvalid) continue;
@@ -432,48 +432,70 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
     const cf val{-a.y, a.x};  // i * acc
     reinterpret_cast<float2 *>(out)[idx] = make_float2(val.x, val.y);
     if (mode == KOP_NONE) continue;
-    const double vr = val.x, vi = (wt == 1) ? 0.0 : (double)val.y;
+    const float vr = val.x, vi = (wt == 1) ? 0.f : val.y, fw = (float)wt;
     const cf o = ldw(other, idx, wt);
     if (mode == KOP_P) {
-      s0 += (double)wt * ((double)o.x * vr + (double)o.y * vi);
+      s0 += fw * (o.x * vr + o.y * vi);
     } else {
-      s0 += (double)wt * (vr * vr + vi * vi);
-      s1 += (double)wt * (vr * (double)o.x + vi * (double)o.y);
+      s0 += fw * (vr * vr + vi * vi);
+      s1 += fw * (vr * o.x + vi * o.y);
     }
   }
   const double inv = 1.0 / (double)g.nreal();
-  if (mode != KOP_NONE) block_partials(s0 * inv, s1 * inv, partials);
+  if (mode != KOP_NONE) block_partials((double)s0 * inv, (double)s1 * inv, partials);
 }
 
-__global__ void k_kop_xr(Grid g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
-                         double rho, const double *part1, const double *part2, int npart, double *part3) {
+// Update kernel: KOP_XR_MPT modes per thread (independent loads), the block's
+// modes contiguous in memory; mode t = row*(H+1) + kz with a compile-time row
+// length. alpha and omega come from the pass partials, summed by three warps
+// at once.
+constexpr int KOP_XR_TPB = 256, KOP_XR_MPT = 4;
+template <int H>
+__global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float *r, const float *p, const float *sv,
+                                                     const float *t, const float *r0, double rho,
+                                                     const double *part1, const double *part2, int npart,
+                                                     double *part3) {
   __shared__ double sh[3];
-  const double r0v = block_sum_partials(part1, npart, 0, &sh[0]);
-  const double tt = block_sum_partials(part2, npart, 0, &sh[1]);
-  const double ts = block_sum_partials(part2, npart, 1, &sh[2]);
+  const int lin = threadIdx.x, warp = lin >> 5, lane = lin & 31;
+  if (warp < 3) {
+    const double *a = (warp == 0) ? part1 : part2;
+    const int off = (warp == 2) ? 1 : 0;
+    double v = 0.0;
+    for (int b = lane; b < npart; b += 32) v += a[2 * b + off];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp] = v;
+  }
+  __syncthreads();
+  const double r0v = sh[0], tt = sh[1], ts = sh[2];
   const float alpha = (float)(rho / r0v);
   const float w = (float)((tt > 0.0) ? ts / tt : 0.0);
-  double s0 = 0.0, s1 = 0.0;
-  const unsigned nm = (unsigned)g.nmodes();
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.hnz;
-  for (unsigned t0 = blockIdx.x * blockDim.x + threadIdx.x; t0 < nm; t0 += gridDim.x * blockDim.x) {
-    const int i = (int)(t0 / plane);
-    const unsigned rem = t0 - (unsigned)i * plane;
-    const int j = (int)(rem / (unsigned)g.hnz), kz = (int)(rem - (unsigned)j * (unsigned)g.hnz);
+  constexpr int RL = H + 1;  // modes per z row
+  const long nm = g.nmodes();
+  const long base = (long)blockIdx.x * (KOP_XR_TPB * KOP_XR_MPT);
+  const int lny = __ffs(g.ny) - 1;  // NY is a power of two
+  // the thread's few terms are summed in FP32 (FP64 arithmetic is scarce on
+  // this GPU); blocks and the final sum over blocks are FP64
+  float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+  for (int k = 0; k < KOP_XR_MPT; k++) {
+    const long idx = base + k * KOP_XR_TPB + lin;
+    if (idx >= nm) break;
+    const int row = (int)(idx / RL), kz = (int)(idx - (long)row * RL);
+    const int i = row >> lny, j = row & (g.ny - 1);
     const int wt = read_weight(g, i, j, kz);
     if (wt == 0) continue;
-    const long idx = t0;
     const cf pp = ldw(p, idx, wt), ss = ldw(sv, idx, wt), tv = ldw(t, idx, wt), xx = ldw(xt, idx, wt);
+    const cf a = ldw(r0, idx, wt);
     const cf nx{xx.x + alpha * pp.x + w * ss.x, xx.y + alpha * pp.y + w * ss.y};
     const cf nr{ss.x - w * tv.x, ss.y - w * tv.y};
     reinterpret_cast<float2 *>(xt)[idx] = make_float2(nx.x, nx.y);
     reinterpret_cast<float2 *>(r)[idx] = make_float2(nr.x, nr.y);
-    const cf a = ldw(r0, idx, wt);
-    s0 += (double)wt * ((double)a.x * (double)nr.x + (double)a.y * (double)nr.y);
-    s1 += (double)wt * ((double)nr.x * (double)nr.x + (double)nr.y * (double)nr.y);
+    const float fw = (float)wt;
+    s0 += fw * (a.x * nr.x + a.y * nr.y);
+    s1 += fw * (nr.x * nr.x + nr.y * nr.y);
   }
   const double inv = 1.0 / (double)g.nreal();
-  block_partials(s0 * inv, s1 * inv, part3);
+  block_partials((double)s0 * inv, (double)s1 * inv, part3);
 }
 
 __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2) {
@@ -607,10 +629,24 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const f
   probe_end(PROBE_KOP_XFWD, (mode == KOP_NONE ? 4.0 : 5.0) * sizeof(float) * (double)g.nreal(), s);
 }
 
+int kop_xr_blocks(const Grid &g) { return (int)div_up(g.nmodes(), KOP_XR_TPB * KOP_XR_MPT); }
+
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
             double rho, const double *part1, const double *part2, int npart, double *part3, cudaStream_t s) {
+  const unsigned nb = (unsigned)kop_xr_blocks(g);
   count_launch();
-  k_kop_xr<<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, xt, r, p, sv, t, r0, rho, part1, part2, npart, part3);
+#define KOP_XR(HH)                                                                                            \
+  case HH:                                                                                                    \
+    k_kop_xr<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, sv, t, r0, rho, part1, part2, npart, part3); \
+    break;
+  switch (g.nz / 2) {
+    KOP_XR(8)
+    KOP_XR(16)
+    KOP_XR(32)
+    KOP_XR(64)
+    KOP_XR(128)
+  }
+#undef KOP_XR
 }
 
 }  // namespace icep

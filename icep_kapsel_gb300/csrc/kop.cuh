@@ -45,7 +45,8 @@ void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const f
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
               const float *other, double *partials, cudaStream_t s);
 // alpha = rho / sum part1[2b]; omega = sum part2[2b+1] / sum part2[2b];
-// part3[2b] = (r0, r), part3[2b+1] = (r, r) over DOT_BLOCKS blocks.
+// part3[2b] = (r0, r), part3[2b+1] = (r, r) over kop_xr_blocks(g) blocks.
+int kop_xr_blocks(const Grid &g);
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
             double rho, const double *part1, const double *part2, int npart, double *part3, cudaStream_t s);
 

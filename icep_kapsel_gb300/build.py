@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libicep_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["fft.cu", "fields.cu", "particles.cu", "krylov.cu", "kspace.cu", "kop.cu", "unet.cu", "engine.cu", "icep_abi.cu", "lj_noalloc.cu", "probe.cu"]
+SOURCES = ["fft_df.cu", "fft.cu", "fields.cu", "particles.cu", "krylov.cu", "kspace.cu", "kop.cu", "unet.cu", "engine.cu", "icep_abi.cu", "lj_noalloc.cu", "probe.cu", "refine.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

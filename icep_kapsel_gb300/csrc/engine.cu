@@ -18,6 +18,7 @@
 #include "krylov.cuh"
 #include "kop.cuh"
 #include "kspace.cuh"
+#include "refine.cuh"
 #include "unet.cuh"
 #include <type_traits>
 
@@ -66,9 +67,11 @@ class Engine : public EngineBase {
   double radius, xi, hxi, nu;
   double valency_e[2], onsager[2];
   bool electrolyte;
-  // FP64 shadow of the Poisson problem (MIXED precision only): permittivity,
-  // potential, right-hand side, residual and operator work fields.
-  enum { D_EPS = 0, D_X, D_B, D_R, D_W3_0, D_W3_1, D_W3_2, D_XP, D_COUNT };
+  // FP64-accurate shadow of the Poisson problem (MIXED precision only), as
+  // float-float vectors (8 bytes per number, the FP64 layout): potential
+  // spectrum, right-hand side, residual, operator work fields and the
+  // previous potential spectrum.
+  enum { D_X = 0, D_B, D_R, D_W3_0, D_W3_1, D_W3_2, D_XP, D_COUNT };
   bool mixed = false;
   // optional per-phase device timing of the step (CUDA events at phase
   // boundaries, accumulated in ms)
@@ -79,8 +82,10 @@ class Engine : public EngineBase {
   void mark(int k) {
     if (phase_on) cudaEventRecord(ph_ev[k], s);
   }
-  FFTPlan<double> fft64;
+  FFTPlan<dfl> fftdf;
+  RefineTables rtab;
   double *d64[D_COUNT] = {nullptr};
+  dfl *df(int i) { return reinterpret_cast<dfl *>(d64[i]); }
   bool x64_valid = false;
   bool xp_valid = false;  // D_XP holds the potential of the previous solve
 
@@ -89,7 +94,8 @@ class Engine : public EngineBase {
     for (int i = 0; i < F_COUNT; i++) cudaFree(f[i]);
     fft_plan_free(fft);
     for (int i = 0; i < D_COUNT; i++) cudaFree(d64[i]);
-    if (mixed) fft_plan_free(fft64);
+    if (mixed) fft_plan_free(fftdf);
+    rtab.free_all();
     cudaFree(stage);
     cudaFree(dp);
     cudaFreeHost(hp);
@@ -180,7 +186,8 @@ class Engine : public EngineBase {
           return fail(ICEP_ERR_CUDA, "cudaMalloc of FP64 Poisson fields failed");
         cudaMemsetAsync(d64[i], 0, sizeof(double) * g.nf(), s);
       }
-      if (fft_plan_init(fft64, g, s) != ICEP_OK) return fail(ICEP_ERR_CUDA, "FP64 FFT plan setup failed");
+      if (fft_plan_init(fftdf, g, s) != ICEP_OK) return fail(ICEP_ERR_CUDA, "float-float FFT plan setup failed");
+      if (rtab.init(g, s) != ICEP_OK) return fail(ICEP_ERR_CUDA, "float-float operator tables");
     }
     // Particle_domain (profile.cxx:25-74)
     std::vector<int> sek;
@@ -1100,47 +1107,29 @@ class Engine : public EngineBase {
     return hscal[S_AUX1] / (double)g.nreal();
   }
 
-  // ---- FP64 Poisson operator of the MIXED path (same dataflow as apply_A)
-  void apply_A64(const double *x, double *y) {
-    copy_real<double>(g, x, y, s);
-    fft_r2c(fft64, batch(y), s);
-    grad_k<double>(g, y, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], 1.0, true, nullptr, s);
-    fft_c2r(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
-    eps_face_mul<double>(g, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_EPS], s);
-    fft_r2c(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
-    div_k<double>(g, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], y, true, s);
-    fft_c2r(fft64, batch(y), s);
-    matvecs++;
-  }
-
-  /*
-   * MIXED precision Charge_field2potential_dielectric: iterative refinement.
-   * The FP64 system is A64 x = b64 with A64 the reference operator on the
-   * permittivity (double)eps and b64 = D^-.(eps_face E) - (double)rho
-   * projected to mean zero. The potential x64 is FP64 state kept between
-   * steps. Each outer step computes the true residual r = b64 - A64 x64 in
-   * FP64 and, while |r| > tol |b64|, solves A d = r in FP32 with the
-   * spectral-preconditioned BiCGSTAB to a relative tolerance that leaves a
-   * margin below the target, then x64 += d.
-   */
-  // A64 x^ in k-space: the FP64 operator (Ax, operate_dielectric.cxx:485-522)
-  // from a half spectrum to a half spectrum (6 FFTs instead of 8)
-  void apply_A64_k(const double *xk, double *yk) {
-    grad_k<double>(g, xk, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], 1.0, true, nullptr, s);
-    fft_c2r(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
-    eps_face_mul<double>(g, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_EPS], s);
-    fft_r2c(fft64, batch(d64[D_W3_0], d64[D_W3_1], d64[D_W3_2]), s);
-    div_k<double>(g, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], yk, true, s);
+  // r^ = b^ - A x^ in float-float and |r^|^2 / N into hscal[S_RR] after the
+  // next read_scal (A: Ax, operate_dielectric.cxx:485-522, on the FP32
+  // permittivity; 6 float-float FFTs)
+  void residual_df(float prescale) {
+    const bool all[3] = {true, true, true};
+    dfl *w0 = df(D_W3_0), *w1 = df(D_W3_1), *w2 = df(D_W3_2);
+    rf_grad(g, rtab, df(D_X), w0, w1, w2, s);
+    fft_c2r(fftdf, batch(w0, w1, w2), s);
+    rf_eps_face_mul(g, w0, w1, w2, (const float *)f[F_EPS], s);
+    fft_r2c(fftdf, batch(w0, w1, w2), s);
+    rf_div_combine(g, rtab, w0, w1, w2, all, df(D_B), df(D_R), RF_RESIDUAL, prescale, false, partials, scal, S_RR,
+                   s);
     matvecs++;
   }
 
   /*
    * MIXED precision Charge_field2potential_dielectric: iterative refinement
-   * held in k-space. The FP64 system is A64 x = b64 with A64 the reference
-   * operator on the permittivity (double)eps and
-   * b64 = D^-.(eps_face E) - (double)rho with its mean (the k = 0 mode)
-   * removed. The potential's half spectrum x^ (FP64) is state kept between
-   * steps. Each outer step forms the true residual r^ = b^ - A64 x^ in FP64
+   * held in k-space. The accurate system is A x = b with A the reference
+   * operator on the permittivity eps and b = D^-.(eps_face E) - rho with its
+   * mean (the k = 0 mode) removed, both evaluated in float-float arithmetic
+   * (48-bit significands) on the FP32 pipes: GB300's FP64 rate is 1/64 of its
+   * FP32 rate. The potential's half spectrum x^ is float-float state kept
+   * between steps. Each outer step forms the true residual r^ = b^ - A x^
    * (its norm by Parseval) and, while |r| > tol |b|, solves A d = r/|r| in
    * FP32 with the k-space BiCGSTAB to a tolerance that leaves a factor-4
    * margin, then x^ += |r| d^. The real FP32 potential is one FP32 inverse
@@ -1150,8 +1139,8 @@ class Engine : public EngineBase {
     const Grid &G = g;
     const long nf = G.nf();
     if (!x64_valid) {
-      convert_f2d(nf, (const float *)f[pot_id], d64[D_X], s);
-      fft_r2c(fft64, batch(d64[D_X]), s);
+      rf_from_f32(nf, (const float *)f[pot_id], df(D_X), s);
+      fft_r2c(fftdf, batch(df(D_X)), s);
       x64_valid = true;
       xp_valid = false;
     }
@@ -1159,30 +1148,26 @@ class Engine : public EngineBase {
     // last two solves (the reference starts from the last potential; both
     // are converged to the same true-residual tolerance)
     if (xp_valid) {
-      axpby_all(nf, d64[D_X], d64[D_XP], 2.0, -1.0, s);
+      rf_extrapolate(nf, df(D_X), df(D_XP), s);
       std::swap(d64[D_X], d64[D_XP]);
     } else {
       cudaMemcpyAsync(d64[D_XP], d64[D_X], sizeof(double) * nf, cudaMemcpyDeviceToDevice, s);
     }
     xp_valid = true;
-    convert_f2d(nf, (const float *)f[F_EPS], d64[D_EPS], s);
-    // b^64
-    eps_face_E<double>(G, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_EPS], P.e_ext[0], P.e_ext[1], P.e_ext[2], s);
-    {  // components of E_ext that are zero give zero fields: cleared (with
-       // their padding) instead of transformed
-      FieldBatch<double> nz{};
-      for (int d = 0; d < 3; d++) {
-        if (P.e_ext[d] != 0.0) nz.p[nz.n++] = d64[D_W3_0 + d];
-        else cudaMemsetAsync(d64[D_W3_0 + d], 0, sizeof(double) * nf, s);
-      }
-      if (nz.n) fft_r2c(fft64, nz, s);
+    // b^: components of E_ext that are zero give zero fields and are skipped
+    const bool use[3] = {P.e_ext[0] != 0.0, P.e_ext[1] != 0.0, P.e_ext[2] != 0.0};
+    {
+      dfl *w[3] = {df(D_W3_0), df(D_W3_1), df(D_W3_2)};
+      rf_eps_face_e(G, w[0], w[1], w[2], (const float *)f[F_EPS], P.e_ext, use, s);
+      FieldBatch<dfl> nz{};
+      for (int d = 0; d < 3; d++)
+        if (use[d]) nz.p[nz.n++] = w[d];
+      if (nz.n) fft_r2c(fftdf, nz, s);
     }
-    div_k<double>(G, d64[D_W3_0], d64[D_W3_1], d64[D_W3_2], d64[D_B], true, s);
-    convert_f2d(nf, (const float *)f[rho_id], d64[D_R], s);
-    fft_r2c(fft64, batch(d64[D_R]), s);
-    axpby_all(nf, d64[D_R], d64[D_B], -1.0, 1.0, s);
-    cudaMemsetAsync(d64[D_B], 0, 2 * sizeof(double), s);  // k = 0: the mean
-    kdots<double>(G, d64[D_B], d64[D_B], d64[D_B], d64[D_B], 1, partials, scal, S_BB, s);
+    rf_from_f32(nf, (const float *)f[rho_id], df(D_R), s);
+    fft_r2c(fftdf, batch(df(D_R)), s);
+    rf_div_combine(G, rtab, df(D_W3_0), df(D_W3_1), df(D_W3_2), use, df(D_R), df(D_B), RF_RHS, 1.f, true, partials,
+                   scal, S_BB, s);
     int st = read_scal();
     if (st) return st;
     const double bb = hscal[S_BB];
@@ -1194,10 +1179,11 @@ class Engine : public EngineBase {
     last_precond_apps = 0;
     if (bb > 0.0) {
       const double tol2 = P.potential_tol * P.potential_tol * bb;
+      // residual norms are summed in FP32 after scaling by a power of two
+      // that brings sum_k |b^_k|^2 to order 1
+      const float prescale = (float)ldexp(1.0, -ilogb(sqrt((double)G.nreal() * bb)));
       for (int outer = 0; outer < 30; outer++) {
-        apply_A64_k(d64[D_X], d64[D_R]);
-        axpby_all(nf, d64[D_B], d64[D_R], 1.0, -1.0, s);  // r^ = b^ - A x^
-        kdots<double>(G, d64[D_R], d64[D_R], d64[D_R], d64[D_R], 1, partials, scal, S_RR, s);
+        residual_df(prescale);
         if ((st = read_scal())) return st;
         const double rr = hscal[S_RR];
         rel = sqrt(rr / bb);
@@ -1205,7 +1191,7 @@ class Engine : public EngineBase {
         if (!(rr > tol2)) break;
         // FP32 correction solve on the normalised residual
         const double rn = sqrt(rr / (double)G.nreal());
-        scale_d2f_all(nf, d64[D_R], (float *)f[F_KR], 1.0 / rn, s);
+        rf_to_f32(nf, df(D_R), (float *)f[F_KR], 1.0 / rn, s);
         double inner_tol = 0.25 * P.potential_tol * sqrt(bb / rr);
         if (inner_tol < 2e-5) inner_tol = 2e-5;
         if (inner_tol > 0.5) inner_tol = 0.5;
@@ -1232,10 +1218,10 @@ class Engine : public EngineBase {
           r2c(f[F_KX]);
         }
         total_inner += it;
-        add_f2d_all(nf, (const float *)f[F_KX], d64[D_X], rn, s);
+        rf_add_f32(nf, (const float *)f[F_KX], df(D_X), rn, s);
       }
     }
-    scale_d2f_all(nf, d64[D_X], (float *)f[pot_id], 1.0, s);
+    rf_to_f32(nf, df(D_X), (float *)f[pot_id], 1.0, s);
     c2r(f[pot_id]);
     last_iters = total_inner;
     last_error = rel;
@@ -1451,10 +1437,11 @@ class Engine : public EngineBase {
 
   int get_field(int id, double *host) override {
     if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
-    if (id == F_POT && mixed && x64_valid) {  // the potential is FP64 state (its half spectrum)
+    if (id == F_POT && mixed && x64_valid) {  // the potential is float-float state (its half spectrum)
       cudaMemcpyAsync(d64[D_R], d64[D_X], sizeof(double) * g.nf(), cudaMemcpyDeviceToDevice, s);
-      fft_c2r(fft64, batch(d64[D_R]), s);
-      cudaMemcpyAsync(host, d64[D_R], sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
+      fft_c2r(fftdf, batch(df(D_R)), s);
+      rf_to_f64(g.nf(), df(D_R), stage, s);
+      cudaMemcpyAsync(host, stage, sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
       if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_field");
       return ICEP_OK;
     }
@@ -1561,7 +1548,7 @@ class Engine : public EngineBase {
       if (which <= 3) fft_pass(fft, fb, which, s);
       else if (which == 7) fft_r2c(fft, fb, s);
       else if (which == 8) fft_c2r(fft, fb, s);
-      else if (which == 10 && mixed && d64[D_X]) apply_A64(d64[D_X], d64[D_R]);
+      else if (which == 10 && mixed && d64[D_X]) residual_df(1.f);
       else apply_A(f[F_KP], f[F_KV]);
     };
     one();  // warm-up

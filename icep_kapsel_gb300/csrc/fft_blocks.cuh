@@ -11,6 +11,7 @@
 // (element e of pencil w at tile[e*sw + w], conflict-free). The inverse is
 // conj(FFT(conj(x))), so only forward butterflies and twiddles exist.
 #pragma once
+#include "dfloat.cuh"
 #include "fft.cuh"
 
 namespace icep {
@@ -52,7 +53,7 @@ __device__ __forceinline__ void dft8(cplx<R> *v) {
   cplx<R> e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
   dft4(e);
   dft4(o);
-  const R h = (R)0.70710678118654752440084436210484903928;
+  const R h = sqrt_half<R>();
   // W8^1 = (1 - i)/sqrt2, W8^2 = -i, W8^3 = -(1 + i)/sqrt2
   const cplx<R> t1 = cplx<R>{h * (o[1].x + o[1].y), h * (o[1].y - o[1].x)};
   const cplx<R> t2 = mul_mi(o[2]);
@@ -216,8 +217,8 @@ __device__ __forceinline__ void load_table(cplx<R> *dst, const cplx<R> *__restri
 //   inverse  Z[k] = (X[k] + conj X[H-k]) + i exp(+2 pi i k/NZ)(X[k] - conj X[H-k])
 template <typename R>
 __device__ __forceinline__ cplx<R> split_fwd(cplx<R> z, cplx<R> c /* conj Z[H-k] */, cplx<R> pw) {
-  const R er = R(0.5) * (z.x + c.x), ei = R(0.5) * (z.y + c.y);
-  const R orr = R(0.5) * (z.y - c.y), oi = R(-0.5) * (z.x - c.x);
+  const R er = half_of(z.x + c.x), ei = half_of(z.y + c.y);
+  const R orr = half_of(z.y - c.y), oi = half_of(c.x - z.x);
   return cplx<R>{er + (pw.x * orr - pw.y * oi), ei + (pw.x * oi + pw.y * orr)};
 }
 template <typename R>

@@ -351,6 +351,11 @@ inline unsigned nblk(const Grid &g) { return div_up(g.nmodes(), TPB); }
 
 }  // namespace
 
+void kdots_finish(const double *partials, int nblocks, int n, double *scal, int slot, cudaStream_t s) {
+  count_launch();
+  k_kdots_final<<<1, 256, 0, s>>>(partials, nblocks, n, scal, slot);
+}
+
 template <typename R>
 void kdots(const Grid &g, const R *a0, const R *b0, const R *a1, const R *b1, int n, double *partials, double *scal,
            int slot, cudaStream_t s) {

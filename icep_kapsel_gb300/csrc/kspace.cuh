@@ -22,6 +22,8 @@
 
 namespace icep {
 
+// scal[slot + c] = sum over blocks of partials[2 b + c], c < n (block order)
+void kdots_finish(const double *partials, int nblocks, int n, double *scal, int slot, cudaStream_t s);
 // scal[slot + c] = real-space dot of k-space vectors (a_c, b_c), c < n <= 2
 template <typename R>
 void kdots(const Grid &g, const R *a0, const R *b0, const R *a1, const R *b1, int n, double *partials, double *scal,

@@ -231,8 +231,10 @@ int icep_learned_stats(icep_ctx *ctx, int *fallbacks, int *precond_apps);
  * context's stream (CUDA events): which 0..3 = one pass of the 3D FFT
  * (0: z rows + y pencils forward, 1: x pencils forward, 2: x pencils inverse,
  * 3: y pencils + z rows inverse), 7 = forward 3D FFT, 8 = inverse 3D FFT,
- * 9 = Ax. batch: fields per launch (1..5). bytes: algorithmic bytes per
- * launch (one field read and written per transform or pass). */
+ * 9 = Ax, 10 = the MIXED solve's float-float true residual b^ - A x^ (a
+ * MIXED context with an electrolyte, after a step). batch: fields per
+ * launch (1..5). bytes: algorithmic bytes per launch (one field read and
+ * written per transform or pass). */
 int icep_time_kernel(icep_ctx *ctx, int which, int batch, int reps, double *ms, double *bytes);
 /* icep_step with CUDA events recorded on the context's stream around it;
  * ms receives the device time of the nsteps steps. */

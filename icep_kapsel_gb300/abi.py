@@ -18,6 +18,7 @@ MIXED = 1
 SOLVER_REF = 0
 SOLVER_SPECTRAL = 1
 SOLVER_LEARNED = 2
+JANUS_NONE, JANUS_X, JANUS_Y, JANUS_Z = 0, 1, 2, 3
 
 
 class Params(C.Structure):
@@ -56,7 +57,8 @@ class Params(C.Structure):
         ("precision", C.c_int),
         ("solver", C.c_int),
         ("per_particle_eps", C.c_int),
-        ("reserved", C.c_int * 5),
+        ("janus_axis", C.c_int * MAX_SPECIES),
+        ("reserved", C.c_int * 1),
     ]
 
 
@@ -90,12 +92,14 @@ def make_params(**kw):
     jf = kw.pop("janus_force", [[0.0] * 3] * MAX_SPECIES)
     jt = kw.pop("janus_torque", [[0.0] * 3] * MAX_SPECIES)
     e_ext = kw.pop("e_ext", [0.0, 0.0, 0.0])
+    jax = kw.pop("janus_axis", [JANUS_NONE] * MAX_SPECIES)
     defaults.update(kw)
     for k, v in defaults.items():
         setattr(p, k, v)
     for i in range(MAX_SPECIES):
         p.mass_ratio[i] = mass_ratio[i] if i < len(mass_ratio) else 1.0
         p.janus_propulsion[i] = prop[i] if i < len(prop) else NO_PROPULSION
+        p.janus_axis[i] = jax[i] if i < len(jax) else JANUS_NONE
         for d in range(3):
             p.janus_force[i][d] = jf[i][d] if i < len(jf) else 0.0
             p.janus_torque[i][d] = jt[i][d] if i < len(jt) else 0.0
@@ -115,9 +119,10 @@ def params_dict(p):
     return out
 
 
-def make_particles(x, v=None, spec=None, eps_p=None):
-    """Particle array with positions x (n,3), optional velocities, species and
-    per-particle permittivity; every other field zero, q = identity."""
+def make_particles(x, v=None, spec=None, eps_p=None, q=None):
+    """Particle array with positions x (n,3), optional velocities, species,
+    per-particle permittivity and orientation quaternions q (n,4) as
+    (s, v0, v1, v2); every other field zero, q = identity by default."""
     x = np.asarray(x, dtype=np.float64)
     n = x.shape[0]
     arr = (Particle * max(n, 1))()
@@ -129,8 +134,10 @@ def make_particles(x, v=None, spec=None, eps_p=None):
             p.x_nopbc[d] = x[i, d]
             if v is not None:
                 p.v[d] = v[i, d]
-        p.q[0] = 1.0
-        p.q_old[0] = 1.0
+        qq = (1.0, 0.0, 0.0, 0.0) if q is None else q[i]
+        for a in range(4):
+            p.q[a] = float(qq[a])
+            p.q_old[a] = float(qq[a])
         p.eps_p = 0.0 if eps_p is None else float(eps_p[i])
     return arr
 

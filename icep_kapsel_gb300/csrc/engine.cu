@@ -73,6 +73,7 @@ class Engine : public EngineBase {
   // previous potential spectrum.
   enum { D_X = 0, D_B, D_R, D_W3_0, D_W3_1, D_W3_2, D_XP, D_COUNT };
   bool mixed = false;
+  bool janus = false;  // Janus permittivity field (particle 0's species has an axis)
   // optional per-phase device timing of the step (CUDA events at phase
   // boundaries, accumulated in ms)
   static constexpr int NPH = 10;
@@ -147,6 +148,19 @@ class Engine : public EngineBase {
     if (p.dt <= 0 || p.dx <= 0 || p.rho <= 0 || p.eta <= 0) return fail(ICEP_ERR_ARG, "non-positive dt/dx/rho/eta");
     for (int q = 0; q < n; q++)
       if (parts[q].spec < 0 || parts[q].spec >= p.n_species) return fail(ICEP_ERR_ARG, "particle species out of range");
+    // Janus field when particle 0's species has an axis (operate_dielectric.cxx:
+    // 276-280); the reference exits when another particle's species has none
+    // (operate_dielectric.cxx:195-198)
+    for (int q = 0; q < ICEP_MAX_SPECIES; q++)
+      if (p.janus_axis[q] < ICEP_JANUS_NONE || p.janus_axis[q] > ICEP_JANUS_Z)
+        return fail(ICEP_ERR_ARG, "janus_axis out of range");
+    janus = n > 0 && p.janus_axis[parts[0].spec] != ICEP_JANUS_NONE;
+    if (janus) {
+      if (p.per_particle_eps) return fail(ICEP_ERR_ARG, "Janus particles with per-particle permittivity");
+      for (int q = 0; q < n; q++)
+        if (p.janus_axis[parts[q].spec] == ICEP_JANUS_NONE)
+          return fail(ICEP_ERR_ARG, "Janus field: a particle's species has no Janus axis");
+    }
     electrolyte = (p.sw_eq == ICEP_ELECTROLYTE);
     if (electrolyte && !p.dielectric)
       return fail(ICEP_ERR_UNSUPPORTED, "Electrolyte requires Dielectric_property ON on this path");
@@ -260,6 +274,10 @@ class Engine : public EngineBase {
     }
     pp.g = p.g;
     pp.g_direction = p.g_direction;
+    for (int q = 0; q < ICEP_MAX_SPECIES; q++) pp.janus_axis[q] = p.janus_axis[q] - 1;  // x, y, z -> 0, 1, 2
+    pp.eps_ave = 0.5 * (p.eps_particle_top + p.eps_particle_bottom) * p.dielectric_cst;
+    pp.eps_delta = 0.5 * (p.eps_particle_top - p.eps_particle_bottom) * p.dielectric_cst;
+    pp.sharp = 1.0 / p.dx;
     cudaMalloc(&ukdc, sizeof(double) * 3);
     cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
     cudaMalloc(&e_ext_n, sizeof(double) * 3);
@@ -404,6 +422,12 @@ class Engine : public EngineBase {
   // phi_id; per-particle permittivity (extension) accumulates into aux_id.
   void make_dielectric_field(int phi_id, int aux_id) {
     zero(phi_id);
+    if (janus) {  // Make_janus_permittivity_dielectric (operate_dielectric.cxx:208-267)
+      zero(aux_id);
+      scatter_profile<R>(pp, dp, dsek, f[phi_id], f[aux_id], PROF_JANUS, s);
+      eps_janus<R>(g, f[F_EPS], f[phi_id], f[aux_id], P.eps_fluid, P.dielectric_cst, s);
+      return;
+    }
     R *aux = nullptr;
     if (P.per_particle_eps) {
       zero(aux_id);
@@ -1473,6 +1497,14 @@ class Engine : public EngineBase {
     return ICEP_OK;
   }
   int set_particles(const icep_particle *h) override {
+    // species in range; the field stays Janus (every species with an axis) or
+    // not (particle 0's species without one), as the context was created
+    for (int q = 0; q < np; q++) {
+      if (h[q].spec < 0 || h[q].spec >= P.n_species) return fail(ICEP_ERR_ARG, "particle species out of range");
+      const bool ax = P.janus_axis[h[q].spec] != ICEP_JANUS_NONE;
+      if ((janus && !ax) || (!janus && q == 0 && ax))
+        return fail(ICEP_ERR_ARG, "set_particles: species Janus axes do not match the context's permittivity field");
+    }
     cudaStreamSynchronize(s);
     memcpy(hp, h, sizeof(icep_particle) * np);
     if (!P.per_particle_eps)

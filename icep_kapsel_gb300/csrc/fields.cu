@@ -357,6 +357,15 @@ __global__ void k_eps_from_profile(Grid g, R *eps, const R *phis, const R *epsw,
   else eps[p.im] = efdc + epdc * phis[p.im];
 }
 
+// Janus: eps = sum_n phi (eps_ave + eps_delta tanh) + eps_f (1 - phi_p) Dc
+// (operate_dielectric.cxx:282-292)
+template <typename R>
+__global__ void k_eps_janus(Grid g, R *eps, const R *phis, const R *epsj, R ef, R dc) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  eps[p.im] = epsj[p.im] + ef * (R(1) - phis[p.im]) * dc;
+}
+
 template <typename R>
 __global__ void k_charge_add(Grid g, R *rho, const R *c, const R *phi, double ze, int first) {
   Pt p;
@@ -550,6 +559,10 @@ template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_
   count_launch();
   k_eps_from_profile<R><<<nblk_real(g), TPB, 0, s>>>(g, eps, phi_sin, eps_w, (R)(ef * dc), (R)dc, (R)((ep - ef) * dc));
 }
+template <typename R> void eps_janus(const Grid &g, R *eps, const R *phi_sin, const R *eps_j, double ef, double dc, cudaStream_t s) {
+  count_launch();
+  k_eps_janus<R><<<nblk_real(g), TPB, 0, s>>>(g, eps, phi_sin, eps_j, (R)ef, (R)dc);
+}
 template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s) {
   count_launch();
   k_charge_add<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c, phi, ze, first ? 1 : 0);
@@ -613,6 +626,7 @@ template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s) {
   template void f_nonsole<R>(const Grid &, R *const *, R *const *, const R *, R *const *, cudaStream_t);               \
   template void add_vec<R>(const Grid &, R *const *, R *const *, R, cudaStream_t);                                     \
   template void eps_from_profile<R>(const Grid &, R *, const R *, const R *, double, double, double, cudaStream_t);    \
+  template void eps_janus<R>(const Grid &, R *, const R *, const R *, double, double, cudaStream_t);                   \
   template void charge_add<R>(const Grid &, R *, const R *, const R *, double, bool, cudaStream_t);                    \
   template void eps_face_mul<R>(const Grid &, R *, R *, R *, const R *, cudaStream_t);                                 \
   template void eps_face_E<R>(const Grid &, R *, R *, R *, const R *, double, double, double, cudaStream_t);           \

@@ -45,6 +45,9 @@ template <typename R> void add_vec(const Grid &g, R *const *u, R *const *f, R a,
 // eps = ef*dc + (ep - ef)*dc*phi_sin, or eps = ef*dc + dc*eps_w (per particle)
 // (Make_dielectric_field, operate_dielectric.cxx:298-307)
 template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_sin, const R *eps_w, double ef, double ep, double dc, cudaStream_t s);
+// Janus: eps = eps_j + eps_f (1 - phi_sin) Dc, eps_j the scattered particle
+// term (operate_dielectric.cxx:276-292)
+template <typename R> void eps_janus(const Grid &g, R *eps, const R *phi_sin, const R *eps_j, double ef, double dc, cudaStream_t s);
 // rho += ze c (1 - phi) (Conc_k2charge_field_no_surfase_charge, operate_dielectric.cxx:135-160)
 template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s);
 // w_d *= 0.5 (eps(i+e_d) + eps(i)) (Ax, operate_dielectric.cxx:494-510)

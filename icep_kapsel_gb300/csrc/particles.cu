@@ -71,6 +71,31 @@ __device__ __forceinline__ R prof_phi_sin(const PartParams &pp, R x) {
 }
 
 template <typename R>
+__device__ __forceinline__ R tanh_t(R a);
+template <>
+__device__ __forceinline__ double tanh_t<double>(double a) { return tanh(a); }
+template <>
+__device__ __forceinline__ float tanh_t<float>(float a) { return tanhf(a); }
+
+// Janus axis e3 of the particle's species rotated to the space frame and
+// normalised (Make_janus_normal_dielectric, operate_dielectric.cxx:173-205;
+// BODY2SPACE: q (0, e3) q*, rigid_body.cxx:10-24, quaternion.h:205-213)
+// (in the field type R: FP32 arithmetic in MIXED precision)
+template <typename R>
+__device__ __forceinline__ void janus_normal(const double *qd64, int axis, R *nrm) {
+  const R q[4] = {(R)qd64[0], (R)qd64[1], (R)qd64[2], (R)qd64[3]};
+  const R e[3] = {R(axis == 0 ? 1 : 0), R(axis == 1 ? 1 : 0), R(axis == 2 ? 1 : 0)};
+  const R qs2 = q[0] * q[0] - (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  const R qd = q[1] * e[0] + q[2] * e[1] + q[3] * e[2];
+  R v[3];
+  v[0] = qs2 * e[0] + R(2) * (qd * q[1] + q[0] * (q[2] * e[2] - q[3] * e[1]));
+  v[1] = qs2 * e[1] + R(2) * (qd * q[2] + q[0] * (q[3] * e[0] - q[1] * e[2]));
+  v[2] = qs2 * e[2] + R(2) * (qd * q[3] + q[0] * (q[1] * e[1] - q[2] * e[0]));
+  const R in = R(1) / sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  for (int d = 0; d < 3; d++) nrm[d] = v[d] * in;
+}
+
+template <typename R>
 __global__ void k_scatter_profile(PartParams pp, const icep_particle *__restrict__ p, const int *__restrict__ sek, R *out,
                                   R *aux, int kind) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -81,11 +106,22 @@ __global__ void k_scatter_profile(PartParams pp, const icep_particle *__restrict
   if (kind == PROF_PHI) {
     const R v = prof_phi<R>(pp, (R)dist);
     if (v != R(0)) atomicAdd(out + im, v);
-  } else {
+  } else if (kind == PROF_PHI_SIN) {
     const R v = prof_phi_sin<R>(pp, (R)dist);
     if (v != R(0)) {
       atomicAdd(out + im, v);
       if (aux) atomicAdd(aux + im, (R)(p[n].eps_p - pp.eps_f) * v);
+    }
+  } else {
+    const R v = prof_phi_sin<R>(pp, (R)dist);
+    if (v != R(0)) {
+      R nrm[3];
+      janus_normal<R>(p[n].q, pp.janus_axis[p[n].spec], nrm);
+      R jr = R(0);
+      for (int d = 0; d < 3; d++) jr += (R)r[d] * nrm[d];
+      const R th = tanh_t<R>((R)pp.sharp * jr);
+      atomicAdd(out + im, v);
+      atomicAdd(aux + im, v * ((R)pp.eps_ave + (R)pp.eps_delta * th));
     }
   }
 }

@@ -26,6 +26,12 @@ struct PartParams {
   double g;
   int g_direction;
   int lj_on;
+  // Janus permittivity (Make_janus_permittivity_dielectric,
+  // operate_dielectric.cxx:208-267): per species the body axis e3 (0, 1, 2
+  // for x, y, z; -1 none), eps_ave/eps_delta = (top +- bottom)/2 * Dc and
+  // the tanh sharpness 1/DX
+  int janus_axis[ICEP_MAX_SPECIES];
+  double eps_ave, eps_delta, sharp;
 };
 
 // Profile scatters over the integration stencil (Particle_domain stencil,
@@ -33,7 +39,11 @@ struct PartParams {
 //   PROF_PHI:     out += Phi (Make_phi_particle_sum, make_phi.cxx:229-275)
 //   PROF_PHI_SIN: out += Phi_compact_sin; if aux: aux += (eps_p - eps_f) Phi_compact_sin
 //                 (Make_phi_sin_primitive, operate_dielectric.cxx:78-120)
-enum { PROF_PHI = 0, PROF_PHI_SIN = 1 };
+//   PROF_JANUS:   out += Phi_compact_sin; aux += Phi_compact_sin (eps_ave +
+//                 eps_delta tanh(sharp r.n)), n the particle's Janus axis in
+//                 the space frame (Make_janus_permittivity_dielectric,
+//                 operate_dielectric.cxx:173-267)
+enum { PROF_PHI = 0, PROF_PHI_SIN = 1, PROF_JANUS = 2 };
 template <typename R>
 void scatter_profile(const PartParams &pp, const icep_particle *p, const int *sek, R *out, R *aux, int kind,
                      cudaStream_t s);

@@ -39,6 +39,11 @@ enum icep_precision { ICEP_FP64 = 0, ICEP_MIXED = 1 };
  * one, with SPECTRAL as the fallback on stagnation. */
 enum icep_solver { ICEP_SOLVER_REF = 0, ICEP_SOLVER_SPECTRAL = 1, ICEP_SOLVER_LEARNED = 2 };
 
+/* Janus axis of a species: the body-frame axis e3 whose rotation by the
+ * particle's quaternion separates the eps_particle_top (e3 side) and
+ * eps_particle_bottom halves (JAX {x_axis, y_axis, z_axis, no_axis}). */
+enum icep_janus_axis { ICEP_JANUS_NONE = 0, ICEP_JANUS_X = 1, ICEP_JANUS_Y = 2, ICEP_JANUS_Z = 3 };
+
 /*
  * Simulation parameters. Field names follow the reference's input.udf keys
  * and globals (input.cxx:286-440 derives the rest):
@@ -89,7 +94,14 @@ typedef struct icep_params {
   int precision;      /* enum icep_precision */
   int solver;         /* enum icep_solver */
   int per_particle_eps; /* 1: use icep_particle.eps_p instead of eps_particle_top */
-  int reserved[5];
+  /* Janus dielectric particles (Make_janus_permittivity_dielectric,
+   * operate_dielectric.cxx:208-267): per species the body axis of the Janus
+   * cap, enum icep_janus_axis (the reference's JAX, input.h:55, renumbered so
+   * that a zero-initialised struct means no Janus particles). The field is
+   * Janus when particle 0's species has an axis (operate_dielectric.cxx:
+   * 276-280); then every particle's species needs one. */
+  int janus_axis[ICEP_MAX_SPECIES];
+  int reserved[1];
 } icep_params;
 
 /*

@@ -1078,11 +1078,61 @@ static inline long wrap_idx(const ko_ctx *c, int i, int j, int k) {
   return IDX(c, i, j, k);
 }
 
+/* Make_janus_normal_dielectric (operate_dielectric.cxx:173-205): the body
+ * axis e3 of the species (x, y or z) in the space frame, normalised. */
+static void janus_normal(const ko_ctx *c, const icep_particle *p, double *nrm) {
+  const int ax = c->P.janus_axis[p->spec];
+  const double e3[3] = {ax == ICEP_JANUS_X ? 1.0 : 0.0, ax == ICEP_JANUS_Y ? 1.0 : 0.0, ax == ICEP_JANUS_Z ? 1.0 : 0.0};
+  qrot(nrm, p->q, e3, 0);
+  const double n = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+  const double in = 1.0 / n;
+  for (int d = 0; d < DIM; d++) nrm[d] *= in;
+}
+
+/* Make_dielectric_field, Janus branch (operate_dielectric.cxx:208-292): per
+ * particle and stencil point phi = Phi_compact_sin, phi_p += phi,
+ * eps += phi (eps_ave + eps_delta tanh(r.n / DX)); then
+ * eps += eps_f (1 - phi_p) Dc. */
+static void make_janus_eps(ko_ctx *c, double *eps, double *phi_p) {
+  const double dc = c->P.dielectric_cst;
+  const double eps_ave = 0.5 * (c->P.eps_particle_top + c->P.eps_particle_bottom) * dc;
+  const double eps_delta = 0.5 * (c->P.eps_particle_top - c->P.eps_particle_bottom) * dc;
+  const double sharp = 1 / c->dx;
+  zero_real(c, phi_p);
+  zero_real(c, eps);
+  for (int n = 0; n < c->np; n++) {
+    double nrm[3];
+    janus_normal(c, &c->p[n], nrm);
+    pcell pc;
+    particle_cell(c, c->p[n].x, &pc);
+    for (int m = 0; m < c->np_domain; m++) {
+      double r[3], dist, jr = 0.0;
+      long im = stencil_point(c, &pc, c->p[n].x, m, r, &dist);
+      for (int d = 0; d < DIM; d++) jr += r[d] * nrm[d];
+      double v = prof_phi_sin(c, dist, c->radius);
+      phi_p[im] += v;
+      eps[im] += v * (eps_ave + eps_delta * tanh(sharp * jr));
+    }
+  }
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      for (int k = 0; k < c->nz; k++) {
+        long im = IDX(c, i, j, k);
+        eps[im] += c->P.eps_fluid * (1 - phi_p[im]) * dc;
+      }
+}
+
 /* Make_dielectric_field, non-Janus branch (operate_dielectric.cxx:270-309):
  * phi_sin into phi_p; eps = eps_f*Dc + (eps_p - eps_f)*Dc*phi_sin. With
- * per_particle_eps the particle term is summed per particle (extension). */
+ * per_particle_eps the particle term is summed per particle (extension).
+ * The field is Janus when particle 0's species has an axis (:276-280). */
 static void make_dielectric_field(ko_ctx *c, double *eps, double *phi_p) {
   const double dc = c->P.dielectric_cst, ef = c->P.eps_fluid;
+  if (c->np > 0 && c->P.janus_axis[c->p[0].spec] != ICEP_JANUS_NONE) {
+    make_janus_eps(c, eps, phi_p);
+    return;
+  }
   if (!c->P.per_particle_eps) {
     make_phi_sin(c, phi_p, NULL);
     const double de = c->P.eps_particle_top - ef;

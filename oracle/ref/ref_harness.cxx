@@ -165,7 +165,13 @@ static void set_globals(const icep_params *q) {
     double mass = RHO_particle[i] * 4. / 3. * M_PI * POW3(RADIUS);
     IMASS[i] = 1. / mass;
     IMOI[i] = 1. / (2. / 5. * mass * SQ(RADIUS));
-    janus_axis[i] = no_axis;
+    // icep_janus_axis (0 none, 1..3 x..z) -> the reference's JAX (input.h:55)
+    switch (q->janus_axis[i]) {
+      case ICEP_JANUS_X: janus_axis[i] = x_axis; break;
+      case ICEP_JANUS_Y: janus_axis[i] = y_axis; break;
+      case ICEP_JANUS_Z: janus_axis[i] = z_axis; break;
+      default: janus_axis[i] = no_axis;
+    }
     janus_propulsion[i] = (q->janus_propulsion[i] == ICEP_MOTOR) ? motor : no_propulsion;
     if (janus_propulsion[i] == motor) SW_JANUS_MOTOR = 1;
     janus_force[i] = (double *)calloc(DIM, sizeof(double));

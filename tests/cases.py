@@ -73,6 +73,30 @@ def icep_case(n=32, npart=4, minsep=12.0, seed=2, a=4.0, eps_f=1.0, eps_p=10.0, 
     return p, abi.make_particles(x, eps_p=eps)
 
 
+def unit_quaternions(n, seed):
+    """n orientations uniform on the rotation group (normalised Gaussian 4-vectors)."""
+    q = np.random.default_rng(seed).standard_normal((n, 4))
+    return q / np.linalg.norm(q, axis=1, keepdims=True)
+
+
+def janus_case(n=32, npart=4, minsep=12.0, seed=4, axes=(abi.JANUS_Z,), eps_top=10.0, eps_bottom=2.0,
+               eps_f=80.0, e_ext=(0.0, 0.0, 0.1), tol=1e-8, maxit=2000, solver=abi.SOLVER_REF,
+               precision=abi.FP64):
+    """Janus dielectric particles (Make_janus_permittivity_dielectric): one
+    species per entry of `axes` (particles assigned round-robin), the cap
+    eps_top on the +e3 side and eps_bottom on the other, random orientations."""
+    p, _ = icep_case(n=n, npart=npart, minsep=minsep, seed=seed, eps_f=eps_f, eps_p=eps_top, e_ext=e_ext,
+                     tol=tol, maxit=maxit, solver=solver, precision=precision)
+    p.n_species = len(axes)
+    for i, a in enumerate(axes):
+        p.janus_axis[i] = a
+        p.mass_ratio[i] = 1.0
+    p.eps_particle_bottom = eps_bottom
+    x = positions(npart, n, minsep, seed)
+    spec = [i % len(axes) for i in range(npart)]
+    return p, abi.make_particles(x, spec=spec, q=unit_quaternions(npart, seed + 500))
+
+
 def lj_dense_case(n=32, npart=24, seed=7, minsep=7.2):
     """Particles closer than the WCA cutoff (2^(1/6) * 8 = 8.98) so that the
     cell-list scan and its multiplicity at 32^3 (2 cells per side) matter."""

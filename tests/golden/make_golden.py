@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32"]
+CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32", "janus32"]
 
 
 def small_case():
@@ -194,6 +194,26 @@ def run_case(name, out):
         r.call("dielectric_field")
         x = np.random.default_rng(31).standard_normal(32 * 32 * 32)
         data["ax"] = r.apply_A(x)
+    elif name == "janus32":
+        # two species with different Janus axes, random orientations; a
+        # moderate permittivity contrast so that the reference's
+        # unpreconditioned BiCGSTAB converges within its iteration limit
+        p, parts = cases.janus_case(npart=6, axes=(abi.JANUS_Z, abi.JANUS_X), eps_f=4.0, tol=1e-7)
+        r = pyoracle.RefKapsel(p, parts)
+        r.call("dielectric_field")
+        data["eps_field"] = r.get("eps")[:, :, :32]
+        data["phi_p"] = r.get("work")[:, :, :32]
+        r.init_state()
+        meta["init_iterations"] = int(r.last_iterations())
+        r.step(2)
+        meta["step_iterations"] = int(r.last_iterations())
+        meta["step_error"] = float(r.last_error())
+        for k in ("zeta0", "zeta1", "c0", "c1"):
+            data[k] = r.get(k)
+        data["pot"] = r.get("pot")[:, :, :32]
+        data["eps"] = r.get("eps")[:, :, :32]
+        for k, v in abi.particles_to_numpy(r.particles(), p.n_particles).items():
+            data["p_" + k] = v
     else:
         raise ValueError(name)
     meta["params"] = abi.params_dict(p)

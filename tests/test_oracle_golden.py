@@ -175,3 +175,28 @@ def test_ax32(oracle_so):
     o.call("dielectric_field")
     x = np.random.default_rng(31).standard_normal(32 * 32 * 32)
     assert rel(o.apply_A(x), g["ax"]) < 1e-13
+
+
+def test_janus32(oracle_so):
+    """Janus dielectric particles (two species, Janus axes z and x, random
+    orientations): the permittivity field and two ICEP steps."""
+    g, _ = load("janus32")
+    p, parts = cases.janus_case(npart=6, axes=(abi.JANUS_Z, abi.JANUS_X), eps_f=4.0, tol=1e-7)
+    o = pyoracle.Oracle(p, parts, so=oracle_so)
+    o.call("dielectric_field")
+    assert rel(o.get("eps")[:, :, :32], g["eps_field"]) < 1e-13
+    assert rel(o.get("work")[:, :, :32], g["phi_p"]) < 1e-13
+    # the tanh cap really splits the particles: both eps_top and eps_bottom regions occur
+    e = g["eps_field"]
+    assert e.max() > 9.0 and e.min() < 2.5
+    o.init_state()
+    o.step(2)
+    for k in ("zeta0", "zeta1"):
+        assert rel(o.get(k), g[k]) < 2e-5, k
+    for k in ("c0", "c1"):
+        assert rel(o.get(k), g[k]) < 1e-9, k
+    a = o.get("pot")[:, :, :32]
+    assert rel(a - a.mean(), g["pot"] - g["pot"].mean()) < 2e-5
+    assert rel(o.get("eps")[:, :, :32], g["eps"]) < 1e-13
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    assert rel(pa["x"], g["p_x"]) < 1e-12

@@ -1490,6 +1490,144 @@ class Engine : public EngineBase {
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_field");
     return ICEP_OK;
   }
+  // ---- checkpoint / restart (Save_Restart_udf / Force_restore_parameters,
+  // resume.cxx:10-78, 308-398, plus the potential) -----------------------
+  // Binary, host byte order:
+  //   "ICEPCKP1", int32 nx ny nz n_particles precision electrolyte nfield spec
+  //   int64 ts, double time, double uk_dc[3]
+  //   nfield x (int32 field id, NX*NY*NZ_ doubles)
+  //   n_particles x icep_particle
+  //   spec != 0: int32 xp_valid, then the float-float potential spectrum and
+  //   the previous one (MIXED electrolyte; NX*NY*NZ_ x 8 bytes each)
+  // FP32 fields are stored as doubles (exact both ways).
+  static constexpr char CKPT_MAGIC[9] = "ICEPCKP1";
+  void ckpt_fields(int *ids, int *n) const {
+    *n = 0;
+    ids[(*n)++] = F_ZETA0;
+    ids[(*n)++] = F_ZETA1;
+    if (electrolyte) {
+      ids[(*n)++] = F_C0;
+      ids[(*n)++] = F_C1;
+      ids[(*n)++] = F_POT;
+    }
+  }
+  int save_checkpoint(const char *path) override {
+    if (!path) return fail(ICEP_ERR_ARG, "checkpoint path");
+    int ids[8], nfld;
+    ckpt_fields(ids, &nfld);
+    const long nf = g.nf();
+    std::vector<double> buf((size_t)nf);
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return fail(ICEP_ERR_IO, "cannot open the checkpoint file for writing");
+    const int spec = (mixed && electrolyte && x64_valid) ? 1 : 0;
+    const int32_t hdr[8] = {g.nx, g.ny, g.nz, np, mixed ? ICEP_MIXED : ICEP_FP64, electrolyte ? 1 : 0, nfld, spec};
+    const int64_t ts64 = ts;
+    double ukh[3];
+    bool okw = get_uk_dc(ukh) == ICEP_OK;
+    okw = okw && fwrite(CKPT_MAGIC, 1, 8, fp) == 8 && fwrite(hdr, sizeof(hdr), 1, fp) == 1 &&
+          fwrite(&ts64, sizeof(ts64), 1, fp) == 1 && fwrite(&time, sizeof(time), 1, fp) == 1 &&
+          fwrite(ukh, sizeof(ukh), 1, fp) == 1;
+    for (int q = 0; q < nfld && okw; q++) {
+      const int32_t id = ids[q];
+      if (sizeof(R) == sizeof(double)) {
+        cudaMemcpyAsync(buf.data(), f[id], sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
+      } else {
+        convert_f2d(nf, (const float *)f[id], stage, s);
+        cudaMemcpyAsync(buf.data(), stage, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
+      }
+      okw = cudaStreamSynchronize(s) == cudaSuccess && fwrite(&id, sizeof(id), 1, fp) == 1 &&
+            fwrite(buf.data(), sizeof(double), (size_t)nf, fp) == (size_t)nf;
+    }
+    if (okw && np > 0) {
+      cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
+      okw = cudaStreamSynchronize(s) == cudaSuccess && fwrite(hp, sizeof(icep_particle), (size_t)np, fp) == (size_t)np;
+    }
+    if (okw && spec) {
+      const int32_t xpv = xp_valid ? 1 : 0;
+      okw = fwrite(&xpv, sizeof(xpv), 1, fp) == 1;
+      const int ds[2] = {D_X, D_XP};
+      for (int q = 0; q < 2 && okw; q++) {
+        cudaMemcpyAsync(buf.data(), d64[ds[q]], sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
+        okw = cudaStreamSynchronize(s) == cudaSuccess &&
+              fwrite(buf.data(), sizeof(double), (size_t)nf, fp) == (size_t)nf;
+      }
+    }
+    if (fclose(fp) != 0) okw = false;
+    if (!okw) return fail(ICEP_ERR_IO, "writing the checkpoint failed");
+    return cuda_status("save_checkpoint");
+  }
+  int load_checkpoint(const char *path) override {
+    if (!path) return fail(ICEP_ERR_ARG, "checkpoint path");
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return fail(ICEP_ERR_IO, "cannot open the checkpoint file");
+    const long nf = g.nf();
+    char magic[8];
+    int32_t hdr[8];
+    int64_t ts64 = 0;
+    double tm = 0.0, ukh[3];
+    int st = ICEP_OK;
+    std::string why;
+    if (fread(magic, 1, 8, fp) != 8 || memcmp(magic, CKPT_MAGIC, 8) != 0 || fread(hdr, sizeof(hdr), 1, fp) != 1 ||
+        fread(&ts64, sizeof(ts64), 1, fp) != 1 || fread(&tm, sizeof(tm), 1, fp) != 1 ||
+        fread(ukh, sizeof(ukh), 1, fp) != 1) {
+      st = ICEP_ERR_IO;
+      why = "not a checkpoint file or truncated header";
+    } else if (hdr[0] != g.nx || hdr[1] != g.ny || hdr[2] != g.nz || hdr[3] != np ||
+               hdr[4] != (mixed ? ICEP_MIXED : ICEP_FP64) || hdr[5] != (electrolyte ? 1 : 0) || hdr[6] < 0 ||
+               hdr[6] > 8 || hdr[7] < 0 || hdr[7] > 1) {
+      st = ICEP_ERR_ARG;
+      why = "checkpoint does not match the context (mesh, particle count, precision or model)";
+    }
+    // read everything into host memory first: a failed load leaves the context unchanged
+    std::vector<int32_t> ids;
+    std::vector<double> data;
+    std::vector<icep_particle> parts;
+    std::vector<double> spec;
+    int32_t xpv = 0;
+    if (st == ICEP_OK) {
+      ids.resize((size_t)hdr[6]);
+      data.resize((size_t)hdr[6] * (size_t)nf);
+      for (int q = 0; q < hdr[6] && st == ICEP_OK; q++) {
+        if (fread(&ids[q], sizeof(int32_t), 1, fp) != 1 ||
+            fread(data.data() + (size_t)q * nf, sizeof(double), (size_t)nf, fp) != (size_t)nf) {
+          st = ICEP_ERR_IO;
+          why = "truncated checkpoint (fields)";
+        } else if (ids[q] < 0 || ids[q] >= F_COUNT) {
+          st = ICEP_ERR_ARG;
+          why = "checkpoint field id out of range";
+        }
+      }
+      parts.resize((size_t)(np > 0 ? np : 1));
+      if (st == ICEP_OK && np > 0 && fread(parts.data(), sizeof(icep_particle), (size_t)np, fp) != (size_t)np) {
+        st = ICEP_ERR_IO;
+        why = "truncated checkpoint (particles)";
+      }
+      if (st == ICEP_OK && hdr[7]) {
+        spec.resize(2 * (size_t)nf);
+        if (fread(&xpv, sizeof(xpv), 1, fp) != 1 ||
+            fread(spec.data(), sizeof(double), 2 * (size_t)nf, fp) != 2 * (size_t)nf) {
+          st = ICEP_ERR_IO;
+          why = "truncated checkpoint (potential spectrum)";
+        }
+      }
+    }
+    fclose(fp);
+    if (st != ICEP_OK) return fail(st, why.c_str());
+    if ((st = set_particles(parts.data())) != ICEP_OK) return st;
+    for (size_t q = 0; q < ids.size(); q++)
+      if ((st = set_field(ids[q], data.data() + q * nf)) != ICEP_OK) return st;
+    if ((st = set_uk_dc(ukh)) != ICEP_OK) return st;
+    if (hdr[7]) {  // after set_field(F_POT), which invalidates the spectrum
+      cudaMemcpyAsync(d64[D_X], spec.data(), sizeof(double) * nf, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(d64[D_XP], spec.data() + nf, sizeof(double) * nf, cudaMemcpyHostToDevice, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("load_checkpoint");
+      x64_valid = true;
+      xp_valid = xpv != 0;
+    }
+    ts = (int)ts64;
+    time = tm;
+    return ICEP_OK;
+  }
   int get_particles(icep_particle *h) override {
     cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_particles");

@@ -33,6 +33,9 @@ struct EngineBase {
   virtual int time_kernel(int which, int batch, int reps, double *ms, double *bytes) = 0;
   // accumulated device time per step phase (ICEP_PHASE_PROFILE=1 at create)
   virtual int phase_times(double *ms, int n) = 0;
+  // checkpoint / restart of the step state (fields, particles, time)
+  virtual int save_checkpoint(const char *path) = 0;
+  virtual int load_checkpoint(const char *path) = 0;
   // learned preconditioner (MIXED precision with solver ICEP_SOLVER_LEARNED)
   virtual int learned_train(int configs, int steps, unsigned seed, double lr, double *loss_first, double *loss_last) {
     return unsupported_learned();

@@ -92,6 +92,13 @@ int icep_set_time(icep_ctx *c, int ts, double time) {
   return ICEP_OK;
 }
 
+int icep_save_checkpoint(icep_ctx *c, const char *path) {
+  return ok(c) && path ? wrap(c, c->e->save_checkpoint(path)) : ICEP_ERR_ARG;
+}
+int icep_load_checkpoint(icep_ctx *c, const char *path) {
+  return ok(c) && path ? wrap(c, c->e->load_checkpoint(path)) : ICEP_ERR_ARG;
+}
+
 int icep_time_evolution(icep_ctx *c, double *zeta0, double *zeta1, double *uk_dc, double *conc0, double *conc1,
                         double *potential, icep_particle *particles, int nsteps) {
   if (!ok(c) || !zeta0 || !zeta1 || !uk_dc || !particles || nsteps < 0) return ICEP_ERR_ARG;

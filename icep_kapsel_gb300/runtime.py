@@ -74,6 +74,8 @@ def load_library(path=None):
     L.icep_set_uk_dc.argtypes = [V, _DP]
     L.icep_get_time.argtypes = [V, C.POINTER(I), _DP]
     L.icep_set_time.argtypes = [V, I, C.c_double]
+    L.icep_save_checkpoint.argtypes = [V, C.c_char_p]
+    L.icep_load_checkpoint.argtypes = [V, C.c_char_p]
     L.icep_A2a_k.argtypes = [V, _DP]
     L.icep_A_k2a.argtypes = [V, _DP]
     L.icep_Ax.argtypes = [V, _DP, _DP]
@@ -182,6 +184,19 @@ class Simulation:
 
     def set_ts(self, ts, time):
         self._check(self.lib.icep_set_time(self.ctx, ts, time), "set_time")
+
+    def time(self):
+        ts, t = C.c_int(), C.c_double()
+        self._check(self.lib.icep_get_time(self.ctx, C.byref(ts), C.byref(t)), "get_time")
+        return ts.value, t.value
+
+    def save_checkpoint(self, path):
+        """Write the step state (Save_Restart_udf + potential) to `path`."""
+        self._check(self.lib.icep_save_checkpoint(self.ctx, os.fsencode(path)), "save_checkpoint")
+
+    def load_checkpoint(self, path):
+        """Restore the step state written by save_checkpoint."""
+        self._check(self.lib.icep_load_checkpoint(self.ctx, os.fsencode(path)), "load_checkpoint")
 
     # reference-named phases
     def fft_r2c(self, a):

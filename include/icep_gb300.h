@@ -30,6 +30,7 @@ extern "C" {
 #define ICEP_ERR_UNSUPPORTED 3
 #define ICEP_ERR_NOT_CONVERGED 4
 #define ICEP_ERR_STATE 5
+#define ICEP_ERR_IO 6
 
 typedef struct icep_ctx icep_ctx;
 
@@ -93,6 +94,18 @@ int icep_get_uk_dc(icep_ctx *ctx, double *uk_dc);
 int icep_set_uk_dc(icep_ctx *ctx, const double *uk_dc);
 int icep_get_time(icep_ctx *ctx, int *ts, double *time);
 int icep_set_time(icep_ctx *ctx, int ts, double time);
+/* Checkpoint / restart (replaces Save_Restart_udf, resume.cxx:10-78, and
+ * Force_restore_parameters, resume.cxx:308-398, with a binary file instead of
+ * the UDF "resume" record). Saved: zeta, uk_dc, the particle array, ts and
+ * time as in the reference, plus for electrolytes the concentrations' spectra
+ * and the potential (and, in MIXED precision, the potential's float-float
+ * spectrum and the previous one that the next solve extrapolates from), so
+ * that a restarted run continues as the uninterrupted one. The load checks
+ * mesh, particle count, precision and model against the context and leaves
+ * the context unchanged when the file does not match (ICEP_ERR_ARG) or is
+ * unreadable or truncated (ICEP_ERR_IO). */
+int icep_save_checkpoint(icep_ctx *ctx, const char *path);
+int icep_load_checkpoint(icep_ctx *ctx, const char *path);
 
 /* ---- phase entry points (operate on the context's device state) -------- */
 

@@ -58,7 +58,7 @@ class Params(C.Structure):
         ("solver", C.c_int),
         ("per_particle_eps", C.c_int),
         ("janus_axis", C.c_int * MAX_SPECIES),
-        ("reserved", C.c_int * 1),
+        ("fix_cell", C.c_int),
     ]
 
 

@@ -2,7 +2,9 @@
 
 Each CUDA translation unit under csrc/ is compiled by its own nvcc process
 (in parallel), then linked into one shared library with the CUDA runtime
-linked statically. Objects go to icep_kapsel_gb300/_build/.
+linked statically; the command-line driver icep_kapsel_gb300/icep_kapsel
+(csrc/kapsel_main.cpp) links against it. Objects go to
+icep_kapsel_gb300/_build/.
 
     python -m icep_kapsel_gb300.build [--force]
 """
@@ -16,8 +18,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libicep_gb300.so")
+BIN = os.path.join(HERE, "icep_kapsel")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["fft_df.cu", "fft.cu", "fields.cu", "particles.cu", "krylov.cu", "kspace.cu", "kop.cu", "unet.cu", "engine.cu", "icep_abi.cu", "lj_noalloc.cu", "probe.cu", "refine.cu"]
+SOURCES = ["fft_df.cu", "fft.cu", "fields.cu", "particles.cu", "krylov.cu", "kspace.cu", "kop.cu", "unet.cu", "engine.cu", "icep_abi.cu", "lj_noalloc.cu", "probe.cu", "refine.cu", "udf.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -38,7 +41,8 @@ def _newest_dep():
 
 
 def build(force=False, verbose=False):
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_dep():
+    if (not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _newest_dep() and os.path.exists(BIN)
+            and os.path.getmtime(BIN) >= _newest_dep()):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     nv = nvcc()
@@ -61,6 +65,14 @@ def build(force=False, verbose=False):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
     os.replace(tmp, LIB)
+    # the command-line driver (kapsel -I input.udf), linked against the library
+    main = os.path.join(CSRC, "kapsel_main.cpp")
+    tmpb = BIN + ".tmp"
+    cmd = [nv, "-O2", "-std=c++17", main, "-o", tmpb, "-L" + HERE, "-licep_gb300", "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(tmpb, BIN)
     return LIB
 
 

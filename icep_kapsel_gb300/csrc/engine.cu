@@ -1349,6 +1349,8 @@ class Engine : public EngineBase {
     mark(0);
     if (!electrolyte) ns_solver_slaved_euler();
     else nssolute_solver_euler();
+    for (int d = 0; d < 3; d++)  // FIX_CELL: time-dependent mean pressure gradient (sp_3d_ns.cxx:30-36)
+      if ((P.fix_cell >> d) & 1) cudaMemsetAsync(ukdc + d, 0, sizeof(double), s);
     mark(1);
     truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
     zeta_k2u();

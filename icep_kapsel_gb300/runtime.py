@@ -75,6 +75,8 @@ def load_library(path=None):
     L.icep_get_time.argtypes = [V, C.POINTER(I), _DP]
     L.icep_set_time.argtypes = [V, I, C.c_double]
     L.icep_save_checkpoint.argtypes = [V, C.c_char_p]
+    L.icep_udf_read.argtypes = [C.c_char_p, V, V, I, C.POINTER(I), C.POINTER(I), C.POINTER(I), C.c_char_p, I]
+    L.icep_udf_value.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, I]
     L.icep_load_checkpoint.argtypes = [V, C.c_char_p]
     L.icep_A2a_k.argtypes = [V, _DP]
     L.icep_A_k2a.argtypes = [V, _DP]
@@ -110,6 +112,34 @@ def load_library(path=None):
     _lib = L
     return L
 
+
+
+def udf_read(path):
+    """Parameters, initial particles, GTS and Num_snap of a kapsel input UDF
+    file (icep_udf_read; no GPU needed)."""
+    L = load_library()
+    p = abi.Params()
+    n, gts, nsnap = C.c_int(), C.c_int(), C.c_int()
+    err = C.create_string_buffer(512)
+    st = L.icep_udf_read(os.fsencode(path), C.byref(p), None, 0, C.byref(n), C.byref(gts), C.byref(nsnap), err, 512)
+    if st:
+        raise IcepError("icep_udf_read failed (%d): %s" % (st, err.value.decode()))
+    parts = (abi.Particle * max(n.value, 1))()
+    st = L.icep_udf_read(os.fsencode(path), C.byref(p), parts, n.value, C.byref(n), C.byref(gts), C.byref(nsnap),
+                         err, 512)
+    if st:
+        raise IcepError("icep_udf_read failed (%d): %s" % (st, err.value.decode()))
+    return p, parts, gts.value, nsnap.value
+
+
+def udf_value(path, key):
+    """The text of one value of a UDF file by its dotted path (icep_udf_value)."""
+    L = load_library()
+    buf = C.create_string_buffer(4096)
+    st = L.icep_udf_value(os.fsencode(path), key.encode(), buf, 4096)
+    if st:
+        raise IcepError("icep_udf_value failed (%d): %s" % (st, buf.value.decode()))
+    return buf.value.decode()
 
 class Simulation:
     """One ICEP simulation on the GPU (see include/icep_gb300.h)."""

@@ -105,6 +105,29 @@ int icep_set_time(icep_ctx *ctx, int ts, double time);
  * the context unchanged when the file does not match (ICEP_ERR_ARG) or is
  * unreadable or truncated (ICEP_ERR_IO). */
 int icep_save_checkpoint(icep_ctx *ctx, const char *path);
+
+/* ---- input front end (no GPU needed) ------------------------------------- */
+/* Reads a kapsel input UDF file (and the definitions it \include's) as the
+ * reference's Gourmet_file_io (input.cxx:457-2139) does for the keys of this
+ * path, with Set_global_parameters' auto time step (input.cxx:333-398), and
+ * builds the initial particles as Init_Particle (init_particle.cxx:12-420):
+ * uniform_random (glibc rand() sequence seeded with 10, kept private) or
+ * user_specify positions; random, space_align or user orientations.
+ * params gets precision FP64 and solver REF (the reference's arithmetic);
+ * gts and num_snap are output.GTS and output.Num_snap (the run is
+ * GTS * Num_snap steps). particles may be NULL to query n_particles; else it
+ * needs max_particles >= n_particles. Returns ICEP_ERR_UNSUPPORTED (with the
+ * reason in err) for settings outside this path: shear flows, chains and
+ * rigid bodies, charged particles, Dielectric_property OFF, salt-free
+ * electrolytes, AC fields, pinned particles, lattice or random-walk
+ * initial configurations, resumed runs (use icep_load_checkpoint). */
+int icep_udf_read(const char *path, icep_params *params, icep_particle *particles, int max_particles,
+                  int *n_particles, int *gts, int *num_snap, char *err, int err_len);
+/* The text of one value of a UDF file by its dotted path, as the reference's
+ * Location names it ("mesh.NPX",
+ * "object_type.spherical_particle.Particle_spec[0].MASS_RATIO"; "<array>.size"
+ * gives a list's length). On an error, value holds the message. */
+int icep_udf_value(const char *path, const char *key, char *value, int len);
 int icep_load_checkpoint(icep_ctx *ctx, const char *path);
 
 /* ---- phase entry points (operate on the context's device state) -------- */

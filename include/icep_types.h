@@ -101,7 +101,9 @@ typedef struct icep_params {
    * Janus when particle 0's species has an axis (operate_dielectric.cxx:
    * 276-280); then every particle's species needs one. */
   int janus_axis[ICEP_MAX_SPECIES];
-  int reserved[1];
+  /* switch.FIX_CELL (input.cxx:1603-1625): bit d set keeps the mean flow
+   * uk_dc[d] at zero after every fluid update (sp_3d_ns.cxx:30-36) */
+  int fix_cell;
 } icep_params;
 
 /*

@@ -1638,6 +1638,8 @@ static void time_evolution_hydro(ko_ctx *c) {
   const int electrolyte = (c->P.sw_eq == ICEP_ELECTROLYTE);
   if (!electrolyte) ns_solver_slaved_euler(c);
   else nssolute_solver_euler(c);
+  for (int d = 0; d < DIM; d++) /* FIX_CELL (sp_3d_ns.cxx:30-36) */
+    if ((c->P.fix_cell >> d) & 1) c->uk_dc[d] = 0.0;
   truncate_23(c, zeta[0]);
   truncate_23(c, zeta[1]);
   zeta_k2u(c, zeta, c->uk_dc, u);

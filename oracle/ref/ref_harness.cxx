@@ -75,6 +75,7 @@ double EPSILON, ETA;
 double E_ext[DIM];
 double Elementary_charge = 1.;
 int External_field, Fixed_particle;
+int FIX_CELL, FIX_CELLxyz[DIM];
 double G;
 int G_direction;
 double HXI;
@@ -159,6 +160,11 @@ static void set_globals(const icep_params *q) {
   janus_force = (double **)calloc(Component_Number, sizeof(double *));
   janus_torque = (double **)calloc(Component_Number, sizeof(double *));
   SW_JANUS_MOTOR = 0;
+  FIX_CELL = 0;
+  for (int d = 0; d < DIM; d++) {  // switch.FIX_CELL (input.cxx:1603-1625)
+    FIX_CELLxyz[d] = (q->fix_cell >> d) & 1;
+    FIX_CELL |= FIX_CELLxyz[d];
+  }
   for (int i = 0; i < Component_Number; i++) {
     MASS_RATIOS[i] = q->mass_ratio[i];
     RHO_particle[i] = MASS_RATIOS[i] * RHO;
@@ -324,6 +330,10 @@ static void time_evolution_hydro() {
     NS_solver_slavedEuler(zeta, jikan, uk_dc, ijk_range, n_ijk_range, particles);
   } else {
     NSsolute_solver_Euler(zeta, jikan, uk_dc, Concentration, particles, ijk_range, n_ijk_range);
+  }
+  if (FIX_CELL) {  // sp_3d_ns.cxx:30-36
+    for (int d = 0; d < DIM; d++)
+      if (FIX_CELLxyz[d]) uk_dc[d] = 0.0;
   }
   for (int d = 0; d < (DIM - 1); d++) Truncate_two_third_rule(zeta[d]);
   Zeta_k2u(zeta, uk_dc, u);

@@ -182,6 +182,31 @@ def test_ns32_hundred_steps_against_oracle(Sim):
         assert rel(pa[k], pb[k]) < 1e-10, k
 
 
+def test_ns32_fix_cell_against_oracle(Sim):
+    """FIX_CELL (sp_3d_ns.cxx:30-36): the mean flow along the flagged axes
+    (here x and z) is reset to zero after each fluid update (the particle
+    force of the same step sets it again), against the oracle; the motor
+    particle drives a different flow than without FIX_CELL."""
+    p, parts = cases.ns_case()
+    p.fix_cell = 1 | 4
+    o = Sim(p, parts)
+    r = pyoracle.Oracle(p, parts)
+    o.init_state(); r.init_state()
+    o.step(20); r.step(20)
+    uk, ukr = o.uk_dc(), r.uk_dc()
+    assert np.linalg.norm(uk - ukr) <= 1e-10 * np.linalg.norm(ukr)
+    for k in ("zeta0", "zeta1"):
+        assert rel(o.get(k), r.get(k)) < 1e-10, k
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    pb = abi.particles_to_numpy(r.particles(), p.n_particles)
+    assert rel(pa["x"], pb["x"]) < 1e-10
+    p2, parts2 = cases.ns_case()
+    free = Sim(p2, parts2)
+    free.init_state()
+    free.step(20)
+    assert abs(free.uk_dc()[0] - uk[0]) > 1e-3 * abs(free.uk_dc()[0])
+
+
 def test_icep32_two_steps_golden(Sim):
     g = load("icep32")
     p, parts = cases.icep_case(tol=1e-7)

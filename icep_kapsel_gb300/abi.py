@@ -59,6 +59,7 @@ class Params(C.Structure):
         ("per_particle_eps", C.c_int),
         ("janus_axis", C.c_int * MAX_SPECIES),
         ("fix_cell", C.c_int),
+        ("surface_charge", C.c_double * MAX_SPECIES),
     ]
 
 
@@ -93,6 +94,7 @@ def make_params(**kw):
     jt = kw.pop("janus_torque", [[0.0] * 3] * MAX_SPECIES)
     e_ext = kw.pop("e_ext", [0.0, 0.0, 0.0])
     jax = kw.pop("janus_axis", [JANUS_NONE] * MAX_SPECIES)
+    qs = kw.pop("surface_charge", [0.0] * MAX_SPECIES)
     defaults.update(kw)
     for k, v in defaults.items():
         setattr(p, k, v)
@@ -100,6 +102,7 @@ def make_params(**kw):
         p.mass_ratio[i] = mass_ratio[i] if i < len(mass_ratio) else 1.0
         p.janus_propulsion[i] = prop[i] if i < len(prop) else NO_PROPULSION
         p.janus_axis[i] = jax[i] if i < len(jax) else JANUS_NONE
+        p.surface_charge[i] = qs[i] if i < len(qs) else 0.0
         for d in range(3):
             p.janus_force[i][d] = jf[i][d] if i < len(jf) else 0.0
             p.janus_torque[i][d] = jt[i][d] if i < len(jt) else 0.0

@@ -74,6 +74,7 @@ class Engine : public EngineBase {
   enum { D_X = 0, D_B, D_R, D_W3_0, D_W3_1, D_W3_2, D_XP, D_COUNT };
   bool mixed = false;
   bool janus = false;  // Janus permittivity field (particle 0's species has an axis)
+  bool have_sc = false;  // charged particles (Conc_k2charge_field with Make_phi_qq_particle)
   // optional per-phase device timing of the step (CUDA events at phase
   // boundaries, accumulated in ms)
   static constexpr int NPH = 10;
@@ -155,6 +156,13 @@ class Engine : public EngineBase {
       if (p.janus_axis[q] < ICEP_JANUS_NONE || p.janus_axis[q] > ICEP_JANUS_Z)
         return fail(ICEP_ERR_ARG, "janus_axis out of range");
     janus = n > 0 && p.janus_axis[parts[0].spec] != ICEP_JANUS_NONE;
+    // surface charges: all species charged or none (Init_rho_ion_dielectric,
+    // operate_electrolyte.cxx:912-930, exits otherwise)
+    have_sc = p.n_species > 0 && p.surface_charge[0] != 0.0;
+    for (int q = 0; q < p.n_species; q++)
+      if ((p.surface_charge[q] != 0.0) != have_sc)
+        return fail(ICEP_ERR_ARG, "surface charges must be non-zero for every species or for none");
+    if (have_sc && p.sw_eq != ICEP_ELECTROLYTE) return fail(ICEP_ERR_ARG, "surface charges need the Electrolyte model");
     if (janus) {
       if (p.per_particle_eps) return fail(ICEP_ERR_ARG, "Janus particles with per-particle permittivity");
       for (int q = 0; q < n; q++)
@@ -231,6 +239,8 @@ class Engine : public EngineBase {
       if (!p.per_particle_eps) hp[q].eps_p = p.eps_particle_top;
     }
     cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * n, cudaMemcpyHostToDevice, s);
+    abs_total_qe = 0.0;
+    for (int q = 0; q < n; q++) abs_total_qe += fabs(p.surface_charge[hp[q].spec] * p.elementary_charge);
     // particle parameters (Set_global_parameters, input.cxx:286-300, 404-440)
     memset(&pp, 0, sizeof(pp));
     pp.dx = p.dx; pp.radius = radius; pp.xi = xi; pp.hxi = hxi;
@@ -278,6 +288,7 @@ class Engine : public EngineBase {
     pp.eps_ave = 0.5 * (p.eps_particle_top + p.eps_particle_bottom) * p.dielectric_cst;
     pp.eps_delta = 0.5 * (p.eps_particle_top - p.eps_particle_bottom) * p.dielectric_cst;
     pp.sharp = 1.0 / p.dx;
+    for (int q = 0; q < ICEP_MAX_SPECIES; q++) pp.qe[q] = p.surface_charge[q] * p.elementary_charge;
     cudaMalloc(&ukdc, sizeof(double) * 3);
     cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
     cudaMalloc(&e_ext_n, sizeof(double) * 3);
@@ -436,14 +447,30 @@ class Engine : public EngineBase {
     scatter_profile<R>(pp, dp, dsek, f[phi_id], aux, PROF_PHI_SIN, s);
     eps_from_profile<R>(g, f[F_EPS], f[phi_id], aux, P.eps_fluid, P.eps_particle_top, P.dielectric_cst, s);
   }
-  // Conc_k2charge_field_no_surfase_charge (operate_dielectric.cxx:135-160)
-  void conc_k2charge(int rho_id, int phi_id, int tmp_id) {
+  // Conc_k2charge_field_no_surfase_charge (operate_dielectric.cxx:135-160);
+  // with surface charges Conc_k2charge_field (operate_electrolyte.cxx:45-74):
+  // phi_id becomes the sum of Phi and rho starts from the surface charge of
+  // Make_phi_qq_particle (operate_electrolyte.cxx:179-243)
+  int conc_k2charge(int rho_id, int phi_id, int tmp_id) {
+    if (have_sc) {
+      zero(phi_id);
+      zero(rho_id);
+      scatter_profile<R>(pp, dp, dsek, f[phi_id], f[rho_id], PROF_QQ, s);
+      sum_abs_real<R>(g, f[rho_id], partials, scal, S_AUX1, s);
+      int st = read_scal();
+      if (st) return st;
+      // volume of the surface section normalised to sum_n |e Q_n|
+      const double rescale = abs_total_qe / (hscal[S_AUX1] * P.dx * P.dx * P.dx);
+      scale_copy<R>(g, f[rho_id], f[rho_id], (R)rescale, s);
+    }
     for (int n = 0; n < 2; n++) {
       copy(tmp_id, F_C0 + n);
       c2r(f[tmp_id]);
-      charge_add<R>(g, f[rho_id], f[tmp_id], f[phi_id], valency_e[n], n == 0, s);
+      charge_add<R>(g, f[rho_id], f[tmp_id], f[phi_id], valency_e[n], n == 0 && !have_sc, s);
     }
+    return ICEP_OK;
   }
+  double abs_total_qe = 0.0;  // sum over particles of |e Q|
   // Ax (operate_dielectric.cxx:485-522) on padded real fields
   void apply_A(const R *x, R *y) {
     copy_real<R>(g, x, y, s);
@@ -1287,8 +1314,9 @@ class Engine : public EngineBase {
   // Make_Maxwell_force_x_on_fluid (operate_dielectric.cxx:611-764)
   int maxwell_force(int rho_id) {
     make_dielectric_field(F_F0, F_WORK);
-    conc_k2charge(rho_id, F_F0, F_F1);
-    int st = solve_potential(rho_id, F_POT, F_F2);
+    int st = conc_k2charge(rho_id, F_F0, F_F1);
+    if (st) return st;
+    st = solve_potential(rho_id, F_POT, F_F2);
     if (st) return st;
     maxwell_stress(rho_id);
     return ICEP_OK;
@@ -1364,7 +1392,7 @@ class Engine : public EngineBase {
       }
       f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], true, s);
       make_dielectric_field(F_F0, F_WORK);
-      conc_k2charge(F_UP0, F_F0, F_F1);
+      if ((st = conc_k2charge(F_UP0, F_F0, F_F1))) return st;
       mark(3);
       if ((st = solve_potential(F_UP0, F_POT, F_F2))) return st;
       mark(4);
@@ -1407,9 +1435,31 @@ class Engine : public EngineBase {
     zero(F_PHI);
     scatter_profile<R>(pp, dp, dsek, f[F_PHI], nullptr, PROF_PHI, s);
     const double z0 = P.valency_pos, z1 = P.valency_neg;
-    const double rho_inf = P.kbt * P.dielectric_cst * P.eps_fluid /
-                           ((P.elementary_charge * P.debye_length * radius) * (P.elementary_charge * P.debye_length * radius));
-    const double cp = rho_inf / (z0 * (z0 - z1)), cm = -rho_inf / (z1 * (z0 - z1));
+    double rho_inf = P.kbt * P.dielectric_cst * P.eps_fluid /
+                     ((P.elementary_charge * P.debye_length * radius) * (P.elementary_charge * P.debye_length * radius));
+    double cp = rho_inf / (z0 * (z0 - z1)), cm = -rho_inf / (z1 * (z0 - z1));
+    if (have_sc) {
+      // Init_rho_ion -> Set_uniform_ion_charge_density_salt (operate_electrolyte.cxx:
+      // 738-862, 559-620): the counterions of the surface charges spread over
+      // the fluid volume sum(1 - Phi), plus kBT Dc eps_f / (e lambda_D)^2
+      // of salt (this branch has no radius factor)
+      double pos = 0.0, neg = 0.0;
+      for (int sp = 0; sp < P.n_species; sp++) {
+        int cnt = 0;
+        for (int q = 0; q < np; q++) cnt += (hp[q].spec == sp);
+        const double qs = P.surface_charge[sp], num = (double)cnt;
+        if (qs < 0.) pos += fabs(qs * num / z0);
+        else if (qs > 0.) neg += fabs(qs * num / z1);
+      }
+      sum_real<R>(g, f[F_PHI], partials, scal, S_AUX1, s);
+      read_scal();
+      const double volume_phi = (double)g.nreal() - hscal[S_AUX1];
+      const double dx3 = P.dx * P.dx * P.dx;
+      rho_inf = P.kbt * P.dielectric_cst / ((P.elementary_charge * P.debye_length) * (P.elementary_charge * P.debye_length));
+      rho_inf *= P.eps_fluid;
+      cp = pos / (volume_phi * dx3) + rho_inf / (z0 * (z0 - z1));
+      cm = neg / (volume_phi * dx3) + -rho_inf / (z1 * (z0 - z1));
+    }
     for (int n = 0; n < 2; n++) {
       zero(F_C0 + n);
       fill_real<R>(g, f[F_C0 + n], (R)(n ? cm : cp), s);
@@ -1442,8 +1492,9 @@ class Engine : public EngineBase {
       init_ions();
       // Init_potential_dielectric (operate_dielectric.cxx:574-609)
       make_dielectric_field(F_GE2, F_WORK);
-      conc_k2charge(F_GE1, F_GE2, F_GE0);
-      int st = solve_potential(F_GE1, F_POT, F_GE2);
+      int st = conc_k2charge(F_GE1, F_GE2, F_GE0);
+      if (st) return st;
+      st = solve_potential(F_GE1, F_POT, F_GE2);
       if (st) return st;
     }
     ts = 0;
@@ -1792,7 +1843,7 @@ class Engine : public EngineBase {
         solenoidal_u(F_F0);
         break;
       case C_TRUNCATE: truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s); break;
-      case C_CHARGE_FIELD: conc_k2charge(F_RHO, F_WORK, F_UP0); break;
+      case C_CHARGE_FIELD: st = conc_k2charge(F_RHO, F_WORK, F_UP0); break;
       case C_INIT_ION: init_ions(); break;
       default: return fail(ICEP_ERR_ARG, "unknown call id");
     }

@@ -70,11 +70,13 @@ __global__ void k_dots_final(const double *partials, int nblocks, int n, double 
 }
 
 template <typename R>
-__global__ void k_sum(Grid g, const R *a, double *partials) {
+__global__ void k_sum(Grid g, const R *a, double *partials, int absval) {
   double s0 = 0.0;
   const unsigned N = (unsigned)g.nreal();
-  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x)
-    s0 += (double)a[real_index(g, t)];
+  for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
+    const double v = (double)a[real_index(g, t)];
+    s0 += absval ? fabs(v) : v;
+  }
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int o = 16; o > 0; o >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, o);
@@ -193,7 +195,14 @@ void dots(const Grid &g, const R *a0, const R *b0, const R *a1, const R *b1, int
 template <typename R>
 void sum_real(const Grid &g, const R *a, double *partials, double *scal, int slot, cudaStream_t s) {
   count_launch();
-  k_sum<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a, partials);
+  k_sum<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a, partials, 0);
+  count_launch();
+  k_dots_final<<<1, 256, 0, s>>>(partials, DOT_BLOCKS, 1, scal, slot);
+}
+template <typename R>
+void sum_abs_real(const Grid &g, const R *a, double *partials, double *scal, int slot, cudaStream_t s) {
+  count_launch();
+  k_sum<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a, partials, 1);
   count_launch();
   k_dots_final<<<1, 256, 0, s>>>(partials, DOT_BLOCKS, 1, scal, slot);
 }
@@ -261,6 +270,7 @@ void scale_d2f(const Grid &g, const double *x, float *y, double a, cudaStream_t 
   template void dots<R>(const Grid &, const R *, const R *, const R *, const R *, int, double *, double *, int, \
                         cudaStream_t);                                                                           \
   template void sum_real<R>(const Grid &, const R *, double *, double *, int, cudaStream_t);                     \
+  template void sum_abs_real<R>(const Grid &, const R *, double *, double *, int, cudaStream_t);                 \
   template void bicg_p<R>(const Grid &, R *, const R *, const R *, double, double, cudaStream_t);                \
   template void bicg_s<R>(const Grid &, R *, const R *, const R *, double, const double *, cudaStream_t);        \
   template void bicg_xr<R>(const Grid &, R *, R *, const R *, const R *, const R *, const R *, double,           \

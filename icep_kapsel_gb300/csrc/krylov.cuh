@@ -42,6 +42,9 @@ void sub_mean(const Grid &g, R *a, const double *scal, int slot, cudaStream_t s)
 // sum over real points of a (into scal[slot])
 template <typename R>
 void sum_real(const Grid &g, const R *a, double *partials, double *scal, int slot, cudaStream_t s);
+// scal[slot] = sum |a| over the real points
+template <typename R>
+void sum_abs_real(const Grid &g, const R *a, double *partials, double *scal, int slot, cudaStream_t s);
 // type conversion over all NX*NY*NZ_ values
 void convert_f2d(long n, const float *x, double *y, cudaStream_t s);
 void convert_d2f(long n, const double *x, float *y, cudaStream_t s);

@@ -95,6 +95,16 @@ __device__ __forceinline__ void janus_normal(const double *qd64, int axis, R *nr
   for (int d = 0; d < 3; d++) nrm[d] = v[d] * in;
 }
 
+// DPhi_compact_sin (profile.h:168-181)
+template <typename R>
+__device__ __forceinline__ R prof_dphi_sin(const PartParams &pp, R x) {
+  const R hxi = (R)pp.xi * R(.5);
+  const R ixi = R(1) / (R)pp.xi;
+  const R d = (R)pp.radius - x;
+  if (fabs(d) < hxi) return (R)M_PI * R(.5) * ixi * cos((R)M_PI * d * ixi);
+  return R(0);
+}
+
 template <typename R>
 __global__ void k_scatter_profile(PartParams pp, const icep_particle *__restrict__ p, const int *__restrict__ sek, R *out,
                                   R *aux, int kind) {
@@ -106,6 +116,11 @@ __global__ void k_scatter_profile(PartParams pp, const icep_particle *__restrict
   if (kind == PROF_PHI) {
     const R v = prof_phi<R>(pp, (R)dist);
     if (v != R(0)) atomicAdd(out + im, v);
+  } else if (kind == PROF_QQ) {
+    const R v = prof_phi<R>(pp, (R)dist);
+    if (v != R(0)) atomicAdd(out + im, v);
+    const R sq = (R)pp.qe[p[n].spec] * prof_dphi_sin<R>(pp, (R)dist);
+    if (sq != R(0)) atomicAdd(aux + im, sq);
   } else if (kind == PROF_PHI_SIN) {
     const R v = prof_phi_sin<R>(pp, (R)dist);
     if (v != R(0)) {

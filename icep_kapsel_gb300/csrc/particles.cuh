@@ -32,6 +32,8 @@ struct PartParams {
   // the tanh sharpness 1/DX
   int janus_axis[ICEP_MAX_SPECIES];
   double eps_ave, eps_delta, sharp;
+  // surface charge e Q of each species (Make_phi_qq_particle)
+  double qe[ICEP_MAX_SPECIES];
 };
 
 // Profile scatters over the integration stencil (Particle_domain stencil,
@@ -43,7 +45,9 @@ struct PartParams {
 //                 eps_delta tanh(sharp r.n)), n the particle's Janus axis in
 //                 the space frame (Make_janus_permittivity_dielectric,
 //                 operate_dielectric.cxx:173-267)
-enum { PROF_PHI = 0, PROF_PHI_SIN = 1, PROF_JANUS = 2 };
+//   PROF_QQ:      out += Phi; aux += e Q DPhi_compact_sin (Make_phi_qq_particle,
+//                 operate_electrolyte.cxx:179-218, before its rescaling)
+enum { PROF_PHI = 0, PROF_PHI_SIN = 1, PROF_JANUS = 2, PROF_QQ = 3 };
 template <typename R>
 void scatter_profile(const PartParams &pp, const icep_particle *p, const int *sek, R *out, R *aux, int kind,
                      cudaStream_t s);

@@ -497,8 +497,12 @@ static bool fill(Bound &b, Result &r) {
         !b.num(ps + "Surface_charge", charge) || !b.str(ps + "janus_axis", ax) || !b.str(ps + "janus_propulsion", prop))
       return bad(r, b);
     if (counts[i] < 0) return unsupported(r, "negative Particle_number");
-    if (p.sw_eq == ICEP_ELECTROLYTE && charge != 0.0)
-      return unsupported(r, "charged particles (the surface-charge electrolyte path)");
+    p.surface_charge[i] = (p.sw_eq == ICEP_ELECTROLYTE) ? charge : 0.0;
+    if (p.sw_eq == ICEP_ELECTROLYTE && (charge != 0.0) != (p.surface_charge[0] != 0.0)) {
+      r.status = ICEP_ERR_ARG;  // Init_rho_ion_dielectric (operate_electrolyte.cxx:912-930)
+      r.err = "Surface_charge must be non-zero for every species or for none";
+      return false;
+    }
     p.janus_axis[i] = ax == "X" ? ICEP_JANUS_X : ax == "Y" ? ICEP_JANUS_Y : ax == "Z" ? ICEP_JANUS_Z : ICEP_JANUS_NONE;
     if (prop == "OFF") {
       p.janus_propulsion[i] = ICEP_NO_PROPULSION;

@@ -118,7 +118,7 @@ int icep_save_checkpoint(icep_ctx *ctx, const char *path);
  * GTS * Num_snap steps). particles may be NULL to query n_particles; else it
  * needs max_particles >= n_particles. Returns ICEP_ERR_UNSUPPORTED (with the
  * reason in err) for settings outside this path: shear flows, chains and
- * rigid bodies, charged particles, Dielectric_property OFF, salt-free
+ * rigid bodies, Dielectric_property OFF, salt-free
  * electrolytes, AC fields, pinned particles, lattice or random-walk
  * initial configurations, resumed runs (use icep_load_checkpoint). */
 int icep_udf_read(const char *path, icep_params *params, icep_particle *particles, int max_particles,

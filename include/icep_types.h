@@ -104,6 +104,12 @@ typedef struct icep_params {
   /* switch.FIX_CELL (input.cxx:1603-1625): bit d set keeps the mean flow
    * uk_dc[d] at zero after every fluid update (sp_3d_ns.cxx:30-36) */
   int fix_cell;
+  /* Particle_spec[].Surface_charge (input.cxx:1038): all zero (the salt
+   * solution path) or all non-zero (Init_rho_ion_dielectric,
+   * operate_electrolyte.cxx:912-937): then the charge field adds the
+   * particles' surface charge (Conc_k2charge_field, operate_electrolyte.cxx:
+   * 45-74) and the ions start with their counterions */
+  double surface_charge[ICEP_MAX_SPECIES];
 } icep_params;
 
 /*

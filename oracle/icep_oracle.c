@@ -629,6 +629,15 @@ static inline double prof_phi_sin(const ko_ctx *c, double x, double radius) {
   return (d > c->hxi) ? 1. : 0.;
 }
 
+/* DPhi_compact_sin (profile.h:168-181): the surface profile */
+static inline double prof_dphi_sin(const ko_ctx *c, double x, double radius) {
+  const double hxi = c->xi * .5;
+  const double ixi = 1. / c->xi;
+  double d = radius - x;
+  if (fabs(d) < hxi) return M_PI * .5 * ixi * cos(M_PI * d * ixi);
+  return 0.;
+}
+
 /* Particle_domain (profile.cxx:25-74): integration stencil offsets, in the
  * reference's loop order. */
 static void build_sekibun(ko_ctx *c) {
@@ -1155,10 +1164,43 @@ static void make_dielectric_field(ko_ctx *c, double *eps, double *phi_p) {
   }
 }
 
+/* Make_phi_qq_particle (operate_electrolyte.cxx:179-243): phi += Phi and
+ * surface += Q_e DPhi_compact_sin per particle, then the surface charge
+ * rescaled so that its volume integral of |.| is sum_n |Q_e|. */
+static void make_phi_qq(ko_ctx *c, double *phi, double *surface) {
+  double abs_total = 0.;
+  for (int n = 0; n < c->np; n++) {
+    const double q = c->P.surface_charge[c->p[n].spec] * c->P.elementary_charge;
+    pcell pc;
+    particle_cell(c, c->p[n].x, &pc);
+    for (int m = 0; m < c->np_domain; m++) {
+      double r[3], dist;
+      long im = stencil_point(c, &pc, c->p[n].x, m, r, &dist);
+      phi[im] += prof_phi(c, dist, c->radius);
+      surface[im] += q * prof_dphi_sin(c, dist, c->radius);
+    }
+    abs_total += fabs(q);
+  }
+  double dmy = 0.0;
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      for (int k = 0; k < c->nz; k++) dmy += fabs(surface[IDX(c, i, j, k)]);
+  const double rescale = abs_total / (dmy * c->dx3);
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      for (int k = 0; k < c->nz; k++) surface[IDX(c, i, j, k)] *= rescale;
+}
+
 /* Conc_k2charge_field_no_surfase_charge (operate_dielectric.cxx:135-160):
- * rho = sum_n z_n e c_n (1 - phi_p); tmp is scratch. */
-static void conc_k2charge(ko_ctx *c, double *rho, const double *phi_p, double *tmp) {
+ * rho = sum_n z_n e c_n (1 - phi_p); tmp is scratch. With surface charges,
+ * Conc_k2charge_field (operate_electrolyte.cxx:45-74): phi_p is rebuilt as
+ * the sum of Phi and rho starts from the rescaled surface charge. */
+static void conc_k2charge(ko_ctx *c, double *rho, double *phi_p, double *tmp) {
   zero_real(c, rho);
+  if (c->P.surface_charge[0] != 0.0) {
+    zero_real(c, phi_p);
+    make_phi_qq(c, phi_p, rho);
+  }
   for (int n = 0; n < 2; n++) {
     memcpy(tmp, c->f[F_C0 + n], sizeof(double) * c->nf);
     fft_c2r(c, tmp);
@@ -1688,6 +1730,28 @@ static void init_ions(ko_ctx *c) {
                    SQ(c->P.elementary_charge * c->P.debye_length * c->radius);
   double cp = rho_inf / (z0 * (z0 - z1));
   double cm = -rho_inf / (z1 * (z0 - z1));
+  if (c->P.surface_charge[0] != 0.0) {
+    /* Init_rho_ion -> Set_uniform_ion_charge_density_salt
+     * (operate_electrolyte.cxx:738-862, 559-620): counterions of the surface
+     * charges spread over the fluid volume, plus the salt density
+     * kBT Dc eps_f / (e lambda_D)^2 (no radius factor on this branch) */
+    double pos = 0., neg = 0.;
+    for (int sp = 0; sp < c->P.n_species; sp++) {
+      int cnt = 0;
+      for (int n = 0; n < c->np; n++) cnt += (c->p[n].spec == sp);
+      const double q = c->P.surface_charge[sp], num = (double)cnt;
+      if (q < 0.) pos += fabs(q * num / z0);
+      else if (q > 0.) neg += fabs(q * num / z1);
+    }
+    double volume_phi = 0.;
+    for (int i = 0; i < c->nx; i++)
+      for (int j = 0; j < c->ny; j++)
+        for (int k = 0; k < c->nz; k++) volume_phi += (1. - c->f[F_PHI][IDX(c, i, j, k)]);
+    rho_inf = c->P.kbt * c->P.dielectric_cst / SQ(c->P.elementary_charge * c->P.debye_length);
+    rho_inf *= c->P.eps_fluid;
+    cp = pos / (volume_phi * c->dx3) + rho_inf / (z0 * (z0 - z1));
+    cm = neg / (volume_phi * c->dx3) + -rho_inf / (z1 * (z0 - z1));
+  }
   for (int n = 0; n < 2; n++) {
     double *cf = c->f[F_C0 + n];
     double val = n ? cm : cp;

@@ -167,6 +167,7 @@ static void set_globals(const icep_params *q) {
   }
   for (int i = 0; i < Component_Number; i++) {
     MASS_RATIOS[i] = q->mass_ratio[i];
+    Surface_charge[i] = q->surface_charge[i];
     RHO_particle[i] = MASS_RATIOS[i] * RHO;
     double mass = RHO_particle[i] * 4. / 3. * M_PI * POW3(RADIUS);
     IMASS[i] = 1. / mass;
@@ -401,6 +402,8 @@ int kref_setup(const icep_params *q, const icep_particle *p, int np) {
    * set here too so that isolated calls can use it */
   Charge_field2potential_dielectric = Charge_field2potential_dielectric_LO;
   for (int n = 0; n < Particle_Number; n++) to_particle(&p[n], &particles[n]);
+  for (int n = 0; n < Particle_Number; n++)  // Particle_Numbers per species (input.cxx:1036)
+    if (particles[n].spec >= 0 && particles[n].spec < Component_Number) Particle_Numbers[particles[n].spec]++;
   ready = true;
   return 0;
 }
@@ -547,8 +550,10 @@ int kref_call(int fn) {
     case C_F_PARTICLE_SOLE: Make_f_particle_dt_sole(f_particle, u, up, phi); break;
     case C_TRUNCATE: Truncate_two_third_rule(zeta[0]); Truncate_two_third_rule(zeta[1]); break;
     case C_CHARGE_FIELD:
-      /* rho_free from the concentrations and the compact-sine profile in work */
-      Conc_k2charge_field_no_surfase_charge(particles, Concentration, rho_free_buf, work_buf, up[0]);
+      /* rho_free from the concentrations and the compact-sine profile in work;
+       * with surface charges Conc_k2charge_field (work receives the Phi sum) */
+      if (have_surface_charge) Conc_k2charge_field(particles, Concentration, rho_free_buf, work_buf, up[0]);
+      else Conc_k2charge_field_no_surfase_charge(particles, Concentration, rho_free_buf, work_buf, up[0]);
       break;
     case C_INIT_ION: Init_rho_ion_dielectric(Concentration, particles, jikan); break;
     default: return 1;

@@ -97,6 +97,21 @@ def janus_case(n=32, npart=4, minsep=12.0, seed=4, axes=(abi.JANUS_Z,), eps_top=
     return p, abi.make_particles(x, spec=spec, q=unit_quaternions(npart, seed + 500))
 
 
+def charged_case(n=32, npart=4, seed=2, charges=(-5.0,), tol=1e-7, solver=abi.SOLVER_REF, precision=abi.FP64,
+                 eps_f=1.0, eps_p=10.0, e_ext=(0.01, 0.0, 0.0)):
+    """Charged particles in the salt solution (Init_rho_ion +
+    Conc_k2charge_field with Make_phi_qq_particle): one species per entry of
+    `charges` (particles assigned round-robin)."""
+    p, _ = icep_case(n=n, npart=npart, seed=seed, eps_f=eps_f, eps_p=eps_p, e_ext=e_ext, tol=tol, solver=solver,
+                     precision=precision)
+    p.n_species = len(charges)
+    for i, q in enumerate(charges):
+        p.surface_charge[i] = q
+        p.mass_ratio[i] = 1.0
+    x = positions(npart, n, 12.0, seed)
+    return p, abi.make_particles(x, spec=[i % len(charges) for i in range(npart)])
+
+
 def lj_dense_case(n=32, npart=24, seed=7, minsep=7.2):
     """Particles closer than the WCA cutoff (2^(1/6) * 8 = 8.98) so that the
     cell-list scan and its multiplicity at 32^3 (2 cells per side) matter."""

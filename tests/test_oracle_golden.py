@@ -200,3 +200,21 @@ def test_janus32(oracle_so):
     assert rel(o.get("eps")[:, :, :32], g["eps"]) < 1e-13
     pa = abi.particles_to_numpy(o.particles(), p.n_particles)
     assert rel(pa["x"], g["p_x"]) < 1e-12
+
+
+def test_charged32(oracle_so):
+    """Charged particles (Init_rho_ion's counterions, Conc_k2charge_field with
+    Make_phi_qq_particle) and the initial potential."""
+    g, meta = load("charged32")
+    p, parts = cases.charged_case()
+    o = pyoracle.Oracle(p, parts, so=oracle_so)
+    o.init_state()
+    for k in ("c0", "c1"):
+        assert rel(o.get(k), g[k]) < 1e-14, k
+    a = o.get("pot")[:, :, :32]
+    assert rel(a - a.mean(), g["pot"] - g["pot"].mean()) < 2e-5
+    o.call("charge_field")
+    assert rel(o.get("rho")[:, :, :32], g["rho"]) < 1e-13
+    assert rel(o.get("work")[:, :, :32], g["phi_p"]) < 1e-13
+    # the surface term is there: the charge field is far from the salt-only one
+    assert np.abs(g["rho"]).max() > 1e-3

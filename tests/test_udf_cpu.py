@@ -83,7 +83,6 @@ def rewrite(tmp_path, old, new):
     ('{"ON", {"DC", {0.0, 0.0, 0.1}', '{"ON", {"AC", {0.0, 0.0, 0.1}'),  # AC field
     ('"Uniform",', '"Poisson_Boltzmann",'),
     ('{"salt", {1.0, 7.24}', '{"saltfree", {1.0, 7.24}'),
-    ('{2,1.0,0.0,"Z","OFF"', '{2,1.0,0.5,"Z","OFF"'),  # surface charge
     ('{"user_specify",\n', '{"uniform_random",\n'),  # fine: placement by rand()
 ])
 def test_unsupported_or_changed(rt, tmp_path, old, new):
@@ -135,3 +134,19 @@ def test_reference_input_udf(rt):
     assert np.array_equal(x[0], r)
     # the rest of the file binds too (values the path does not use)
     assert rt.udf_value(REF_UDF, "output.ON.EXTENDED.Print_field.YES.Slab_z.stride") == "4"
+
+
+def test_surface_charges(rt, tmp_path):
+    """Charged species are read into surface_charge; mixing charged and
+    uncharged species is refused (ICEP_ERR_ARG), as the reference exits."""
+    both = rewrite(tmp_path, '{2,1.0,0.0,"Z","OFF"', '{2,1.0,-5.0,"Z","OFF"')
+    both2 = open(both).read().replace('{2,1.0,0.0,"X","OFF"', '{2,1.0,3.0,"X","OFF"')
+    open(both, "w").write(both2)
+    p, _, _, _ = rt.udf_read(both)
+    assert list(p.surface_charge)[:2] == [-5.0, 3.0]
+    one = rewrite(tmp_path, '{2,1.0,0.0,"Z","OFF"', '{2,1.0,-5.0,"Z","OFF"')
+    L = rt.load_library()
+    err = C.create_string_buffer(256)
+    n = C.c_int()
+    st = L.icep_udf_read(os.fsencode(one), C.byref(abi.Params()), None, 0, C.byref(n), None, None, err, 256)
+    assert st == 1 and b"Surface_charge" in err.value

@@ -37,6 +37,14 @@ class Engine : public EngineBase {
   FFTPlan<R> fft;
   R *f[F_COUNT];
   double *stage = nullptr;  // FP64 staging for get/set of FP32 fields
+  // per-field FP64 staging of the batched host I/O (MIXED), allocated on first use
+  static constexpr int NSTAGE = 6;
+  double *stage_n[NSTAGE] = {nullptr};
+  // the FP64 potential last handed to the host (MIXED): a potential passed
+  // back unchanged keeps the solver's float-float state
+  double *pot_export = nullptr;
+  bool pot_export_valid = false;
+  int *dflag = nullptr;
   icep_particle *dp = nullptr;
   icep_particle *hp = nullptr;  // pinned
   int np = 0;
@@ -99,6 +107,9 @@ class Engine : public EngineBase {
     if (mixed) fft_plan_free(fftdf);
     rtab.free_all();
     cudaFree(stage);
+    for (int i = 0; i < NSTAGE; i++) cudaFree(stage_n[i]);
+    cudaFree(pot_export);
+    cudaFree(dflag);
     cudaFree(dp);
     cudaFreeHost(hp);
     cudaFree(dsek);
@@ -1189,6 +1200,7 @@ class Engine : public EngineBase {
   int solve_potential_mixed(int rho_id, int pot_id) {
     const Grid &G = g;
     const long nf = G.nf();
+    pot_export_valid = false;
     if (!x64_valid) {
       rf_from_f32(nf, (const float *)f[pot_id], df(D_X), s);
       fft_r2c(fftdf, batch(df(D_X)), s);
@@ -1515,9 +1527,7 @@ class Engine : public EngineBase {
   int get_field(int id, double *host) override {
     if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
     if (id == F_POT && mixed && x64_valid) {  // the potential is float-float state (its half spectrum)
-      cudaMemcpyAsync(d64[D_R], d64[D_X], sizeof(double) * g.nf(), cudaMemcpyDeviceToDevice, s);
-      fft_c2r(fftdf, batch(df(D_R)), s);
-      rf_to_f64(g.nf(), df(D_R), stage, s);
+      if (export_potential(stage)) return ICEP_ERR_CUDA;
       cudaMemcpyAsync(host, stage, sizeof(double) * g.nf(), cudaMemcpyDeviceToHost, s);
       if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_field");
       return ICEP_OK;
@@ -1531,9 +1541,87 @@ class Engine : public EngineBase {
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_field");
     return ICEP_OK;
   }
+  // the FP64 potential from the float-float spectrum into out (device), kept
+  // as pot_export for the unchanged-potential test of set_field
+  int export_potential(double *out) {
+    if (!pot_export && cudaMalloc(&pot_export, sizeof(double) * g.nf()) != cudaSuccess) return 1;
+    cudaMemcpyAsync(d64[D_R], d64[D_X], sizeof(double) * g.nf(), cudaMemcpyDeviceToDevice, s);
+    fft_c2r(fftdf, batch(df(D_R)), s);
+    rf_to_f64(g.nf(), df(D_R), out, s);
+    cudaMemcpyAsync(pot_export, out, sizeof(double) * g.nf(), cudaMemcpyDeviceToDevice, s);
+    pot_export_valid = true;
+    return 0;
+  }
+  // a potential uploaded into dev (FP64) that equals the last exported one
+  // leaves the state as it is; else it replaces the potential and the
+  // solver's float-float state. Synchronises the stream.
+  int import_potential(const double *dev) {
+    bool same = false;
+    if (mixed && x64_valid && pot_export_valid) {
+      if (!dflag && cudaMalloc(&dflag, sizeof(int)) != cudaSuccess) return cuda_status("set_field");
+      rf_differs(g.nf(), dev, pot_export, dflag, s);
+      int h = 1;
+      cudaMemcpyAsync(&h, dflag, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_field");
+      same = (h == 0);
+    }
+    if (same) return ICEP_OK;
+    x64_valid = xp_valid = pot_export_valid = false;
+    if (sizeof(R) == sizeof(double)) cudaMemcpyAsync(f[F_POT], dev, sizeof(double) * g.nf(), cudaMemcpyDeviceToDevice, s);
+    else convert_d2f(g.nf(), dev, (float *)f[F_POT], s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_field");
+    return ICEP_OK;
+  }
+  double *stage_buf(int k) {
+    if (k >= NSTAGE) return nullptr;
+    if (!stage_n[k] && cudaMalloc(&stage_n[k], sizeof(double) * g.nf()) != cudaSuccess) return nullptr;
+    return stage_n[k];
+  }
+  int set_fields(const int *ids, const double *const *host, int n) override {
+    const long nf = g.nf();
+    int pot_k = -1;
+    for (int k = 0; k < n; k++) {
+      if (ids[k] < 0 || ids[k] >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
+      if (sizeof(R) == sizeof(double) && !(ids[k] == F_POT && mixed)) {
+        cudaMemcpyAsync(f[ids[k]], host[k], sizeof(double) * nf, cudaMemcpyHostToDevice, s);
+        continue;
+      }
+      double *st = stage_buf(k);
+      if (!st) return fail(ICEP_ERR_CUDA, "staging buffers");
+      cudaMemcpyAsync(st, host[k], sizeof(double) * nf, cudaMemcpyHostToDevice, s);
+      if (ids[k] == F_POT && mixed) pot_k = k;
+      else convert_d2f(nf, st, (float *)f[ids[k]], s);
+    }
+    if (pot_k >= 0) return import_potential(stage_n[pot_k]);  // synchronises
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_fields");
+    return ICEP_OK;
+  }
+  int get_fields(const int *ids, double *const *host, int n) override {
+    const long nf = g.nf();
+    for (int k = 0; k < n; k++) {
+      if (ids[k] < 0 || ids[k] >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
+      if (sizeof(R) == sizeof(double)) {
+        cudaMemcpyAsync(host[k], f[ids[k]], sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
+        continue;
+      }
+      double *st = stage_buf(k);
+      if (!st) return fail(ICEP_ERR_CUDA, "staging buffers");
+      if (ids[k] == F_POT && mixed && x64_valid) {
+        if (export_potential(st)) return fail(ICEP_ERR_CUDA, "potential export");
+      } else {
+        convert_f2d(nf, (const float *)f[ids[k]], st, s);
+      }
+      cudaMemcpyAsync(host[k], st, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
+    }
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_fields");
+    return ICEP_OK;
+  }
   int set_field(int id, const double *host) override {
     if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
-    if (id == F_POT) x64_valid = xp_valid = false;
+    if (id == F_POT && mixed) {
+      cudaMemcpyAsync(stage, host, sizeof(double) * g.nf(), cudaMemcpyHostToDevice, s);
+      return import_potential(stage);
+    }
     if (sizeof(R) == sizeof(double)) {
       cudaMemcpyAsync(f[id], host, sizeof(double) * g.nf(), cudaMemcpyHostToDevice, s);
     } else {
@@ -1670,6 +1758,7 @@ class Engine : public EngineBase {
     for (size_t q = 0; q < ids.size(); q++)
       if ((st = set_field(ids[q], data.data() + q * nf)) != ICEP_OK) return st;
     if ((st = set_uk_dc(ukh)) != ICEP_OK) return st;
+    pot_export_valid = false;
     if (hdr[7]) {  // after set_field(F_POT), which invalidates the spectrum
       cudaMemcpyAsync(d64[D_X], spec.data(), sizeof(double) * nf, cudaMemcpyHostToDevice, s);
       cudaMemcpyAsync(d64[D_XP], spec.data() + nf, sizeof(double) * nf, cudaMemcpyHostToDevice, s);

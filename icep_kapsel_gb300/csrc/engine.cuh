@@ -16,6 +16,10 @@ struct EngineBase {
   virtual int step(int n) = 0;
   virtual int get_field(int id, double *host) = 0;
   virtual int set_field(int id, const double *host) = 0;
+  // n fields at once (the drop-in call's host I/O): all copies queued, one
+  // synchronisation; host arrays should be pinned for the copies to overlap
+  virtual int set_fields(const int *ids, const double *const *host, int n) = 0;
+  virtual int get_fields(const int *ids, double *const *host, int n) = 0;
   virtual int get_particles(icep_particle *h) = 0;
   virtual int set_particles(const icep_particle *h) = 0;
   virtual int get_uk_dc(double *v) = 0;

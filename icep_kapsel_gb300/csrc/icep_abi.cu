@@ -104,19 +104,19 @@ int icep_time_evolution(icep_ctx *c, double *zeta0, double *zeta1, double *uk_dc
   if (!ok(c) || !zeta0 || !zeta1 || !uk_dc || !particles || nsteps < 0) return ICEP_ERR_ARG;
   int st;
   icep::EngineBase *e = c->e;
-  if ((st = e->set_field(icep::F_ZETA0, zeta0)) || (st = e->set_field(icep::F_ZETA1, zeta1)) ||
-      (st = e->set_uk_dc(uk_dc)) || (st = e->set_particles(particles)))
+  // the fields go as one batch each way (one synchronisation); a potential
+  // passed back as this call returned it keeps the Poisson solver's state
+  int ids[5] = {icep::F_ZETA0, icep::F_ZETA1};
+  double *ptr[5] = {zeta0, zeta1};
+  int n = 2;
+  if (conc0) { ids[n] = icep::F_C0; ptr[n++] = conc0; }
+  if (conc1) { ids[n] = icep::F_C1; ptr[n++] = conc1; }
+  if (potential) { ids[n] = icep::F_POT; ptr[n++] = potential; }
+  if ((st = e->set_uk_dc(uk_dc)) || (st = e->set_particles(particles)) || (st = e->set_fields(ids, ptr, n)))
     return wrap(c, st);
-  if (conc0 && (st = e->set_field(icep::F_C0, conc0))) return wrap(c, st);
-  if (conc1 && (st = e->set_field(icep::F_C1, conc1))) return wrap(c, st);
-  if (potential && (st = e->set_field(icep::F_POT, potential))) return wrap(c, st);
   if ((st = e->step(nsteps))) return wrap(c, st);
-  if ((st = e->get_field(icep::F_ZETA0, zeta0)) || (st = e->get_field(icep::F_ZETA1, zeta1)) ||
-      (st = e->get_uk_dc(uk_dc)) || (st = e->get_particles(particles)))
+  if ((st = e->get_fields(ids, ptr, n)) || (st = e->get_uk_dc(uk_dc)) || (st = e->get_particles(particles)))
     return wrap(c, st);
-  if (conc0 && (st = e->get_field(icep::F_C0, conc0))) return wrap(c, st);
-  if (conc1 && (st = e->get_field(icep::F_C1, conc1))) return wrap(c, st);
-  if (potential && (st = e->get_field(icep::F_POT, potential))) return wrap(c, st);
   return ICEP_OK;
 }
 

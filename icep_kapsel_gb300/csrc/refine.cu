@@ -208,6 +208,12 @@ __global__ void __launch_bounds__(DOT_TPB) k_rf_div_combine(Grid g, RfTab tab, c
   }
 }
 
+__global__ void k_rf_differs(long n, const unsigned long long *__restrict__ a,
+                             const unsigned long long *__restrict__ b, int *flag) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n && a[t] != b[t]) *flag = 1;
+}
+
 inline unsigned nblk(long n) { return div_up(n, TPB); }
 
 }  // namespace
@@ -251,6 +257,12 @@ void rf_from_f32(long n, const float *a, dfl *out, cudaStream_t s) {
 void rf_to_f32(long n, const dfl *a, float *out, double scale, cudaStream_t s) {
   count_launch();
   k_rf_to_f32<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const float2 *>(a), out, (float)scale);
+}
+void rf_differs(long n, const double *a, const double *b, int *flag, cudaStream_t s) {
+  cudaMemsetAsync(flag, 0, sizeof(int), s);
+  count_launch();
+  k_rf_differs<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const unsigned long long *>(a),
+                                       reinterpret_cast<const unsigned long long *>(b), flag);
 }
 void rf_to_f64(long n, const dfl *a, double *out, cudaStream_t s) {
   count_launch();

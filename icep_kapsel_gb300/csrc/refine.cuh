@@ -34,6 +34,8 @@ void rf_from_f32(long n, const float *a, dfl *out, cudaStream_t s);
 void rf_to_f32(long n, const dfl *a, float *out, double scale, cudaStream_t s);
 // out = (double)a
 void rf_to_f64(long n, const dfl *a, double *out, cudaStream_t s);
+// *flag = 1 if the n doubles a and b differ in any bit, else 0 (device int)
+void rf_differs(long n, const double *a, const double *b, int *flag, cudaStream_t s);
 // x += a * d (a a host double, d FP32)
 void rf_add_f32(long n, const float *d, dfl *x, double a, cudaStream_t s);
 // y = 2 x - y (linear extrapolation in time)

@@ -1,6 +1,8 @@
 // particles.cu -- see particles.cuh.
 #include <float.h>
 
+#include <type_traits>
+
 #include "particles.cuh"
 
 namespace icep {
@@ -36,6 +38,44 @@ __device__ __forceinline__ long stencil_point(const PartParams &pp, const double
   }
   *dist = sqrt(s);
   return ((long)rm[0] * pp.N[1] + rm[1]) * pp.nzp + rm[2];
+}
+
+// The particle's cell and residue (Particle_cell, make_phi.h:114-140), FP64.
+struct PCell {
+  int xi[3];
+  float res[3];
+};
+__device__ __forceinline__ void particle_cell(const PartParams &pp, const double *xp, PCell &pc) {
+  const double idx = 1. / pp.dx;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const double v = xp[d] * idx;
+    pc.xi[d] = (int)v;
+    pc.res[d] = (float)((v - (double)pc.xi[d]) * pp.dx);
+  }
+}
+// Stencil point m in the field type R. FP64: stencil_point (the reference's
+// rounding). FP32 (MIXED): r = cell dx - residue in FP32 and dist = |r|: the
+// minimum image of x_mesh - x_p is -r because the stencil is narrower than
+// half the box, so no FP64 arithmetic is needed per point.
+template <typename R>
+__device__ __forceinline__ long stencil_pt(const PartParams &pp, const double *xp, const PCell &pc, const int *sek,
+                                           int m, R *r, R *dist) {
+  if constexpr (std::is_same<R, double>::value) {
+    return stencil_point(pp, xp, sek, m, r, dist);
+  } else {
+    int rm[3];
+    float s = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const int cell = sek[3 * m + d];
+      rm[d] = (int)(((unsigned)pc.xi[d] + (unsigned)cell) & (unsigned)(pp.N[d] - 1));
+      r[d] = (float)cell * (float)pp.dx - pc.res[d];
+      s = fmaf(r[d], r[d], s);
+    }
+    *dist = sqrtf(s);
+    return ((long)rm[0] * pp.N[1] + rm[1]) * pp.nzp + rm[2];
+  }
 }
 
 template <typename R>
@@ -111,8 +151,10 @@ __global__ void k_scatter_profile(PartParams pp, const icep_particle *__restrict
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)pp.np * pp.np_domain) return;
   const int n = (int)(t / pp.np_domain), m = (int)(t - (long)n * pp.np_domain);
-  double r[3], dist;
-  const long im = stencil_point(pp, p[n].x, sek, m, r, &dist);
+  R r[3], dist;
+  PCell pc;
+  if constexpr (!std::is_same<R, double>::value) particle_cell(pp, p[n].x, pc);
+  const long im = stencil_pt<R>(pp, p[n].x, pc, sek, m, r, &dist);
   if (kind == PROF_PHI) {
     const R v = prof_phi<R>(pp, (R)dist);
     if (v != R(0)) atomicAdd(out + im, v);
@@ -133,7 +175,7 @@ __global__ void k_scatter_profile(PartParams pp, const icep_particle *__restrict
       R nrm[3];
       janus_normal<R>(p[n].q, pp.janus_axis[p[n].spec], nrm);
       R jr = R(0);
-      for (int d = 0; d < 3; d++) jr += (R)r[d] * nrm[d];
+      for (int d = 0; d < 3; d++) jr += r[d] * nrm[d];
       const R th = tanh_t<R>((R)pp.sharp * jr);
       atomicAdd(out + im, v);
       atomicAdd(aux + im, v * ((R)pp.eps_ave + (R)pp.eps_delta * th));
@@ -147,21 +189,23 @@ __global__ void k_scatter_up(PartParams pp, const icep_particle *__restrict__ p,
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)pp.np * pp.np_domain) return;
   const int n = (int)(t / pp.np_domain), m = (int)(t - (long)n * pp.np_domain);
-  double r[3], dist;
-  const long im = stencil_point(pp, p[n].x, sek, m, r, &dist);
+  R r[3], dist;
+  PCell pc;
+  if constexpr (!std::is_same<R, double>::value) particle_cell(pp, p[n].x, pc);
+  const long im = stencil_pt<R>(pp, p[n].x, pc, sek, m, r, &dist);
   const R ps = phs[im];
-  const R w = prof_phi<R>(pp, (R)dist) / ((ps > R(1)) ? ps : R(1));
+  const R w = prof_phi<R>(pp, dist) / ((ps > R(1)) ? ps : R(1));
   if (w == R(0)) return;
-  double vr[3] = {0, 0, 0};
+  R vr[3] = {0, 0, 0};
   if (pp.rotation) {
-    const double *om = p[n].omega;
+    const R om[3] = {(R)p[n].omega[0], (R)p[n].omega[1], (R)p[n].omega[2]};
     vr[0] = om[1] * r[2] - om[2] * r[1];
     vr[1] = om[2] * r[0] - om[0] * r[2];
     vr[2] = om[0] * r[1] - om[1] * r[0];
   }
-  atomicAdd(u0 + im, (R)(p[n].v[0] + vr[0]) * w);
-  atomicAdd(u1 + im, (R)(p[n].v[1] + vr[1]) * w);
-  atomicAdd(u2 + im, (R)(p[n].v[2] + vr[2]) * w);
+  atomicAdd(u0 + im, ((R)p[n].v[0] + vr[0]) * w);
+  atomicAdd(u1 + im, ((R)p[n].v[1] + vr[1]) * w);
+  atomicAdd(u2 + im, ((R)p[n].v[2] + vr[2]) * w);
 }
 
 template <typename R>
@@ -181,35 +225,40 @@ __global__ void k_scatter_normal(PartParams pp, const icep_particle *__restrict_
   }
 }
 
-// One block per particle; FP64 accumulation of force and torque.
+// One block per particle; force and torque summed per thread in the field
+// type (FP64, or FP32 with the FP32 stencil geometry in MIXED precision) and
+// across the block in FP64.
 template <typename R>
 __global__ void k_f_hydro(PartParams pp, icep_particle *p, const int *__restrict__ sek, const R *__restrict__ phs,
                           const R *__restrict__ u0, const R *__restrict__ u1, const R *__restrict__ u2, int copy1) {
   const int n = blockIdx.x;
   if (n >= pp.np) return;
   const icep_particle &q = p[n];
-  double xp[3], vp[3], om[3];
+  double xp[3];
+  R vp[3], om[3];
   for (int d = 0; d < 3; d++) {
     xp[d] = q.x[d];
-    vp[d] = q.v[d];
-    om[d] = q.omega[d];
+    vp[d] = (R)q.v[d];
+    om[d] = (R)q.omega[d];
   }
-  double acc[6] = {0, 0, 0, 0, 0, 0};
+  PCell pc;
+  if constexpr (!std::is_same<R, double>::value) particle_cell(pp, xp, pc);
+  R acc[6] = {0, 0, 0, 0, 0, 0};
   for (int m = threadIdx.x; m < pp.np_domain; m += blockDim.x) {
-    double r[3], dist;
-    const long im = stencil_point(pp, xp, sek, m, r, &dist);
+    R r[3], dist;
+    const long im = stencil_pt<R>(pp, xp, pc, sek, m, r, &dist);
     const R ps = phs[im];
-    const double w = (double)(prof_phi<R>(pp, (R)dist) / ((ps > R(1)) ? ps : R(1)));
-    if (w == 0.0) continue;
-    double vr[3] = {0, 0, 0};
+    const R w = prof_phi<R>(pp, dist) / ((ps > R(1)) ? ps : R(1));
+    if (w == R(0)) continue;
+    R vr[3] = {0, 0, 0};
     if (pp.rotation) {
       vr[0] = om[1] * r[2] - om[2] * r[1];
       vr[1] = om[2] * r[0] - om[0] * r[2];
       vr[2] = om[0] * r[1] - om[1] * r[0];
     }
-    const double f0 = ((vp[0] + vr[0]) - (double)u0[im]) * w;
-    const double f1 = ((vp[1] + vr[1]) - (double)u1[im]) * w;
-    const double f2 = ((vp[2] + vr[2]) - (double)u2[im]) * w;
+    const R f0 = ((vp[0] + vr[0]) - u0[im]) * w;
+    const R f1 = ((vp[1] + vr[1]) - u1[im]) * w;
+    const R f2 = ((vp[2] + vr[2]) - u2[im]) * w;
     acc[0] += f0;
     acc[1] += f1;
     acc[2] += f2;

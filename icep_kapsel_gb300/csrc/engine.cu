@@ -59,6 +59,8 @@ class Engine : public EngineBase {
   double *kpart = nullptr;    // dot partials of the fused k-space iteration
   double *hkpart = nullptr;   // pinned
   int *kerr = nullptr;        // error word of the fused plane passes (inside kpart)
+  double *kfin = nullptr;     // final sums of the three dot passes (inside kpart), then kerr
+  unsigned *kcnt = nullptr;   // last-block counters of the dot passes
   int kop_npb = 0;
   // learned preconditioner and its flexible GMRES (solver LEARNED)
   static constexpr int FG_M = 20;  // restart length
@@ -119,6 +121,7 @@ class Engine : public EngineBase {
     cudaFree(scal);
     cudaFree(shift_tab);
     cudaFree(kpart);
+    cudaFree(kcnt);
     cudaFreeHost(hkpart);
     if (learned) net.free_all();
     for (int i = 0; i <= FG_M; i++) cudaFree(fgV[i]);
@@ -313,11 +316,15 @@ class Engine : public EngineBase {
     cudaMalloc(&partials, sizeof(double) * 2 * DOT_BLOCKS);
     if (mixed && electrolyte && kop_supported(g)) {
       kop_npb = kop_pencil_blocks(g);
-      // the dot partials, then one word for the plane passes' error flag
-      const size_t nk = 2 * (2 * (size_t)kop_npb + kop_xr_blocks(g)) + 1;
-      if (cudaMalloc(&kpart, sizeof(double) * nk) != cudaSuccess || cudaMallocHost(&hkpart, sizeof(double) * nk) != cudaSuccess)
+      // the dot partials of the three passes, their final sums (3 pairs), then
+      // one word for the plane passes' error flag; three pass counters
+      const size_t nk = 2 * (2 * (size_t)kop_npb + kop_xr_blocks(g)) + 7;
+      if (cudaMalloc(&kpart, sizeof(double) * nk) != cudaSuccess || cudaMallocHost(&hkpart, sizeof(double) * 7) != cudaSuccess ||
+          cudaMalloc(&kcnt, sizeof(unsigned) * 4) != cudaSuccess)
         return fail(ICEP_ERR_CUDA, "allocation of the k-space dot partials failed");
       cudaMemsetAsync(kpart, 0, sizeof(double) * nk, s);
+      cudaMemsetAsync(kcnt, 0, sizeof(unsigned) * 4, s);
+      kfin = kpart + nk - 7;
       kerr = reinterpret_cast<int *>(kpart + nk - 1);
     }
     if (p.solver == ICEP_SOLVER_LEARNED) {
@@ -710,8 +717,7 @@ class Engine : public EngineBase {
       float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2];
       const int nb = kop_npb;
       double *P1 = kpart, *P2 = kpart + 2 * nb, *P3 = kpart + 4 * nb;
-      const int nxr = kop_xr_blocks(g);
-      const size_t nk = 2 * (2 * (size_t)nb + nxr) + 1;  // with the error word
+      double *F1 = kfin, *F2 = kfin + 2, *F3 = kfin + 4;  // final sums; kfin[6] holds the error word
       if (!kspace_io) {  // right-hand side from the real field F_KB, else already in F_KR
         copy_real<R>(g, f[F_KB], r, s);
         r2c(r);
@@ -749,29 +755,20 @@ class Engine : public EngineBase {
           rho_new = rho;
         }
         const double beta = (rho / rho_old) * (alpha / w);
-        kop_xinv(fft, KOP_P, p, r, v, beta, w, 0.0, nullptr, 0, eps_ref, w0, w1, w2, s);
+        kop_xinv(fft, KOP_P, p, r, v, beta, w, 0.0, nullptr, eps_ref, w0, w1, w2, s);
         kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-        kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, s);
-        kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, rho, P1, nb, eps_ref, w0, w1, w2, s);
+        kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s);
+        kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, rho, F1, eps_ref, w0, w1, w2, s);
         kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-        kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, s);
-        kop_xr(g, xt, r, p, sv, t, r0, rho, P1, P2, nb, P3, s);
+        kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s);
+        kop_xr(g, xt, r, p, sv, t, r0, rho, F1, F2, P3, F3, kcnt + 2, s);
         matvecs += 2;
-        cudaMemcpyAsync(hkpart, kpart, sizeof(double) * nk, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hkpart, kfin, sizeof(double) * 7, cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fused k-space iteration");
-        if (*reinterpret_cast<const int *>(hkpart + nk - 1))
+        if (*reinterpret_cast<const int *>(hkpart + 6))
           return fail(ICEP_ERR_CUDA, "fused plane pass: a bulk copy did not complete within the wait limit");
-        double r0v = 0, tt = 0, ts = 0, r0r = 0;
-        rr = 0;
-        for (int b = 0; b < nb; b++) {
-          r0v += hkpart[2 * b];
-          tt += hkpart[2 * nb + 2 * b];
-          ts += hkpart[2 * nb + 2 * b + 1];
-        }
-        for (int b = 0; b < nxr; b++) {
-          r0r += hkpart[4 * nb + 2 * b];
-          rr += hkpart[4 * nb + 2 * b + 1];
-        }
+        const double r0v = hkpart[0], tt = hkpart[2], ts = hkpart[3], r0r = hkpart[4];
+        rr = hkpart[5];
         alpha = rho / r0v;
         w = (tt > 0.0) ? ts / tt : 0.0;
         rho_new = r0r;
@@ -810,10 +807,10 @@ class Engine : public EngineBase {
   // out = B x~ through the fused passes (no vector update, no dots)
   void apply_Bk(float *xt, float *out) {
     if constexpr (std::is_same<R, float>::value) {
-      kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, 0, mean_eps_cached, f[F_WV3_0], f[F_WV3_1],
+      kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, mean_eps_cached, f[F_WV3_0], f[F_WV3_1],
                f[F_WV3_2], s);
       kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-      kop_xfwd(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], out, KOP_NONE, nullptr, nullptr, s);
+      kop_xfwd(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], out, KOP_NONE, nullptr, nullptr, nullptr, nullptr, s);
       matvecs++;
     }
   }

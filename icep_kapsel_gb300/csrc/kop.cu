@@ -31,20 +31,6 @@ __device__ __forceinline__ cf grad_mult(const Grid &g, int i, int j, int kz, cf 
   return cf{gr * cs - gi * sn, gr * sn + gi * cs};
 }
 
-// Sum of a[2b + off], b < n, in a fixed order; every thread of the block
-// calls it and gets the same value.
-__device__ double block_sum_partials(const double *a, int n, int off, double *sh) {
-  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
-  if (lin < 32) {
-    double s = 0.0;
-    for (int b = lin; b < n; b += 32) s += a[2 * b + off];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-    if (lin == 0) *sh = s;
-  }
-  __syncthreads();
-  return *sh;
-}
-
 // Block reduction of (s0, s1) into partials[2*blockIdx.x + c].
 __device__ void block_partials(double s0, double s1, double *partials) {
   __shared__ double red[2][32];
@@ -64,6 +50,32 @@ __device__ void block_partials(double s0, double s1, double *partials) {
     for (int w = 0; w < nthr / 32; w++) v += red[lin][w];
     partials[2 * blockIdx.x + lin] = v;
   }
+}
+
+// block_partials, then the last block to finish sums every block's pair in a
+// fixed order (lane b reads blocks b, b+32, ...; a shuffle tree combines the
+// lanes) into finals[0..1] and re-arms the counter: the next kernel reads two
+// numbers instead of all partials. Partials of other blocks are read through
+// L2 (__ldcg) after the ticket, which follows each block's fence.
+__device__ void block_partials_final(double s0, double s1, double *partials, double *finals, unsigned *counter) {
+  block_partials(s0, s1, partials);
+  __shared__ int last;
+  const int lin = threadIdx.y * blockDim.x + threadIdx.x;
+  __threadfence();
+  __syncthreads();
+  if (lin == 0) last = (atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1) ? 1 : 0;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (lin < 64) {
+    const int c = lin >> 5, lane = lin & 31;
+    const int nb = (int)(gridDim.x * gridDim.y);
+    double v = 0.0;
+    for (int b = lane; b < nb; b += 32) v += __ldcg(partials + 2 * b + c);
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) finals[c] = v;
+  }
+  if (lin == 0) *counter = 0u;
 }
 
 // (j, kz) of pencils q0 .. q0 + KW - 1 into shared arrays (synchronised by the caller)
@@ -113,11 +125,10 @@ struct SrcGradXInv {
 
 template <int N>
 __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, const float *r, const float *v,
-                                                  float beta, float omega, double rho, const double *part, int npart,
+                                                  float beta, float omega, double rho, const double *fin,
                                                   float ieps, float *w0, float *w1, float *w2,
                                                   const cf *__restrict__ twx) {
   extern __shared__ unsigned char smem_raw[];
-  __shared__ double sh;
   const int sw = KW + 1;
   cf *tws = reinterpret_cast<cf *>(smem_raw);
   cf *raw = tws + N;
@@ -132,7 +143,7 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
   pencil_coords(g, q0, pj, pkz);
   __syncthreads();
   float alpha = 0.f;
-  if (mode == KOP_S) alpha = (float)(rho / block_sum_partials(part, npart, 0, &sh));
+  if (mode == KOP_S) alpha = (float)(rho / fin[0]);
   // vector update at the read modes of this block's pencils
   for (int it = lin; it < N * KW; it += nthr) {
     const int w = it % KW, e = it / KW;
@@ -399,7 +410,7 @@ struct DivAcc {
 template <int N>
 __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const float *w1, const float *w2,
                                                   float *out, int mode, const float *other, double *partials,
-                                                  const cf *__restrict__ twx) {
+                                                  double *finals, unsigned *counter, const cf *__restrict__ twx) {
   extern __shared__ unsigned char smem_raw[];
   const int sw = KW + 1;
   cf *tws = reinterpret_cast<cf *>(smem_raw);
@@ -442,31 +453,20 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
     }
   }
   const double inv = 1.0 / (double)g.nreal();
-  if (mode != KOP_NONE) block_partials((double)s0 * inv, (double)s1 * inv, partials);
+  if (mode != KOP_NONE) block_partials_final((double)s0 * inv, (double)s1 * inv, partials, finals, counter);
 }
 
 // Update kernel: KOP_XR_MPT modes per thread (independent loads), the block's
 // modes contiguous in memory; mode t = row*(H+1) + kz with a compile-time row
-// length. alpha and omega come from the pass partials, summed by three warps
-// at once.
+// length. alpha and omega come from the final sums of the x passes.
 constexpr int KOP_XR_TPB = 256, KOP_XR_MPT = 4;
 template <int H>
 __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float *r, const float *p, const float *sv,
                                                      const float *t, const float *r0, double rho,
-                                                     const double *part1, const double *part2, int npart,
-                                                     double *part3) {
-  __shared__ double sh[3];
-  const int lin = threadIdx.x, warp = lin >> 5, lane = lin & 31;
-  if (warp < 3) {
-    const double *a = (warp == 0) ? part1 : part2;
-    const int off = (warp == 2) ? 1 : 0;
-    double v = 0.0;
-    for (int b = lane; b < npart; b += 32) v += a[2 * b + off];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[warp] = v;
-  }
-  __syncthreads();
-  const double r0v = sh[0], tt = sh[1], ts = sh[2];
+                                                     const double *fin1, const double *fin2, double *part3,
+                                                     double *fin3, unsigned *counter3) {
+  const int lin = threadIdx.x;
+  const double r0v = fin1[0], tt = fin2[0], ts = fin2[1];
   const float alpha = (float)(rho / r0v);
   const float w = (float)((tt > 0.0) ? ts / tt : 0.0);
   constexpr int RL = H + 1;  // modes per z row
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float 
     s1 += fw * (nr.x * nr.x + nr.y * nr.y);
   }
   const double inv = 1.0 / (double)g.nreal();
-  block_partials((double)s0 * inv, (double)s1 * inv, part3);
+  block_partials_final((double)s0 * inv, (double)s1 * inv, part3, fin3, counter3);
 }
 
 __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2) {
@@ -571,8 +571,8 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 }
 
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
-              double omega, double rho, const double *part, int npart, double eps_ref, float *w0, float *w1,
-              float *w2, cudaStream_t s) {
+              double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
+              cudaStream_t s) {
   const Grid &g = p.g;
   const unsigned nb = (unsigned)kop_pencil_blocks(g);
   const float ieps = (float)(1.0 / eps_ref);
@@ -582,7 +582,7 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
   case N:                                                                                                  \
     set_x_attr<N>();                                                                                       \
     k_kop_xinv<N><<<nb, xblock(N), xpass_smem(N), s>>>(g, mode, vec, r, v, (float)beta, (float)omega, rho, \
-                                                       part, npart, ieps, w0, w1, w2, p.tw_x);             \
+                                                       fin, ieps, w0, w1, w2, p.tw_x);                     \
     break;
   switch (g.nx) {
     KOP_XINV(16)
@@ -607,7 +607,7 @@ void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const f
 }
 
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
-              const float *other, double *partials, cudaStream_t s) {
+              const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s) {
   const Grid &g = p.g;
   const unsigned nb = (unsigned)kop_pencil_blocks(g);
   count_launch();
@@ -615,7 +615,8 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const f
 #define KOP_XFWD(N)                                                                                                 \
   case N:                                                                                                           \
     set_x_attr<N>();                                                                                                \
-    k_kop_xfwd<N><<<nb, xblock(N), xpass_smem(N), s>>>(g, w0, w1, w2, out, mode, other, partials, p.tw_x); \
+    k_kop_xfwd<N><<<nb, xblock(N), xpass_smem(N), s>>>(g, w0, w1, w2, out, mode, other, partials, finals, \
+                                                       counter, p.tw_x);                                    \
     break;
   switch (g.nx) {
     KOP_XFWD(16)
@@ -632,12 +633,13 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const f
 int kop_xr_blocks(const Grid &g) { return (int)div_up(g.nmodes(), KOP_XR_TPB * KOP_XR_MPT); }
 
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
-            double rho, const double *part1, const double *part2, int npart, double *part3, cudaStream_t s) {
+            double rho, const double *fin1, const double *fin2, double *part3, double *fin3, unsigned *counter3,
+            cudaStream_t s) {
   const unsigned nb = (unsigned)kop_xr_blocks(g);
   count_launch();
 #define KOP_XR(HH)                                                                                            \
   case HH:                                                                                                    \
-    k_kop_xr<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, sv, t, r0, rho, part1, part2, npart, part3); \
+    k_kop_xr<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, sv, t, r0, rho, fin1, fin2, part3, fin3, counter3); \
     break;
   switch (g.nz / 2) {
     KOP_XR(8)

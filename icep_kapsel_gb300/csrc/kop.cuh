@@ -15,7 +15,8 @@
 //   kop_xr   : x~ += alpha p + omega s, r = s - omega t and the dot products
 //              (r0, r), (r, r)
 // Vectors follow kspace.cuh (read modes only). Dot partials are FP64, one or
-// two per block, scaled by 1/N; sums over blocks are taken in block order.
+// two per block, scaled by 1/N; the last block of a pass sums them in a fixed
+// order into two final numbers.
 #pragma once
 #include "fft.cuh"
 
@@ -30,24 +31,28 @@ int kop_pencil_blocks(const Grid &g);
 // ef_d = 0.5 (eps + eps at the next point along d), real points
 void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, float *ef2, cudaStream_t s);
 // mode KOP_P: vec = p <- P(r) + beta (P(p) - omega P(v));
-// mode KOP_S: vec = s <- P(r) - alpha P(v), alpha = rho / sum_b part[2b];
-// mode KOP_NONE: vec is used as it is (r, v unused).
+// mode KOP_S: vec = s <- P(r) - alpha P(v), alpha = rho / fin[0];
+// mode KOP_NONE: vec is used as it is (r, v, fin unused).
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
-              double omega, double rho, const double *part, int npart, double eps_ref, float *w0, float *w1,
-              float *w2, cudaStream_t s);
+              double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
+              cudaStream_t s);
 // err: device word set to 1 if a bulk copy into shared memory did not
 // complete within the kernel's wait limit (checked by the caller)
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
                const float *ef2, int *err, cudaStream_t s);
 // mode KOP_P: partials[2b] = (other, out) with other = r0;
 // mode KOP_S: partials[2b] = (out, out), partials[2b+1] = (out, other) with other = s;
-// mode KOP_NONE: no dot products (other, partials unused).
+// finals[c] = sum over blocks of partials[2b + c], summed by the last block
+// to finish (counter: a device word at zero, left at zero);
+// mode KOP_NONE: no dot products (other, partials, finals unused).
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
-              const float *other, double *partials, cudaStream_t s);
-// alpha = rho / sum part1[2b]; omega = sum part2[2b+1] / sum part2[2b];
-// part3[2b] = (r0, r), part3[2b+1] = (r, r) over kop_xr_blocks(g) blocks.
+              const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s);
+// alpha = rho / fin1[0]; omega = fin2[1] / fin2[0];
+// part3[2b] = (r0, r), part3[2b+1] = (r, r) over kop_xr_blocks(g) blocks,
+// fin3 their sums (counter3 as for kop_xfwd).
 int kop_xr_blocks(const Grid &g);
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
-            double rho, const double *part1, const double *part2, int npart, double *part3, cudaStream_t s);
+            double rho, const double *fin1, const double *fin2, double *part3, double *fin3, unsigned *counter3,
+            cudaStream_t s);
 
 }  // namespace icep

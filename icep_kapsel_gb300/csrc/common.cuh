@@ -38,6 +38,7 @@ struct Grid {
   int nzp;         // NZ_ = 2*hnz doubles per z row
   int trn[3];      // 2/3-rule limits (N+2)/3
   double wave[3];  // 2 pi / L
+  float wavef[3];  // (float)wave: FP32 kernels take it without a per-thread FP64 conversion
   double dx;
   // staggered-grid shifts exp(i dx k_d / 2) as (cos, sin), indexed by the
   // wavenumber index along axis d (i, j or kz); FP64 and FP32 copies
@@ -58,6 +59,13 @@ __host__ __device__ inline bool in_two_third(const Grid &g, int i, int j, int kz
   int ay = (j <= g.ny / 2) ? j : g.ny - j;
   return ax < g.trn[0] && ay < g.trn[1] && kz < g.trn[2];
 }
+
+template <typename R>
+__host__ __device__ __forceinline__ R wave_of(const Grid &g, int d);
+template <>
+__host__ __device__ __forceinline__ double wave_of<double>(const Grid &g, int d) { return g.wave[d]; }
+template <>
+__host__ __device__ __forceinline__ float wave_of<float>(const Grid &g, int d) { return g.wavef[d]; }
 
 __device__ __forceinline__ void shift_of(const Grid &g, int d, int idx, double &c, double &s) {
   const double2 v = g.shd[d][idx];

@@ -194,6 +194,7 @@ class Engine : public EngineBase {
     for (int d = 0; d < 3; d++) {
       g.trn[d] = (N[d] + 2) / 3;
       g.wave[d] = 2.0 * M_PI / (N[d] * p.dx);
+      g.wavef[d] = (float)g.wave[d];
     }
     g.dx = p.dx;
     if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)

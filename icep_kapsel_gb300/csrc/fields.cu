@@ -52,9 +52,9 @@ __device__ __forceinline__ long wrapi(const Grid &g, int i, int j, int k) {
 
 template <typename R>
 __device__ __forceinline__ void kvec(const Grid &g, const Mode &m, R *k) {
-  k[0] = (R)g.wave[0] * (R)kx_of(g, m.i);
-  k[1] = (R)g.wave[1] * (R)ky_of(g, m.j);
-  k[2] = (R)g.wave[2] * (R)m.kz;
+  k[0] = wave_of<R>(g, 0) * (R)kx_of(g, m.i);
+  k[1] = wave_of<R>(g, 1) * (R)ky_of(g, m.j);
+  k[2] = wave_of<R>(g, 2) * (R)m.kz;
 }
 
 template <typename R>
@@ -81,7 +81,7 @@ __global__ void k_zeta_k2u_k(Grid g, const R *z0, const R *z1, const double *ukd
   Mode m;
   if (!mode_of(g, TID, m)) return;
   const int KX = kx_of(g, m.i), KY = ky_of(g, m.j);
-  R kx = (R)g.wave[0] * (R)KX, ky = (R)g.wave[1] * (R)KY, kz = (R)g.wave[2] * (R)m.kz;
+  R kx = wave_of<R>(g, 0) * (R)KX, ky = wave_of<R>(g, 1) * (R)KY, kz = wave_of<R>(g, 2) * (R)m.kz;
   const R k2 = kx * kx + ky * ky + kz * kz;
   const R ik2 = (k2 > R(0)) ? R(1) / k2 : R(0);
   const R a_r = z0[m.im], a_i = z0[m.im + 1];
@@ -367,10 +367,10 @@ __global__ void k_eps_janus(Grid g, R *eps, const R *phis, const R *epsj, R ef, 
 }
 
 template <typename R>
-__global__ void k_charge_add(Grid g, R *rho, const R *c, const R *phi, double ze, int first) {
+__global__ void k_charge_add(Grid g, R *rho, const R *c, const R *phi, R ze, int first) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
-  const R v = (R)ze * c[p.im] * (R(1) - phi[p.im]);
+  const R v = ze * c[p.im] * (R(1) - phi[p.im]);
   rho[p.im] = first ? v : rho[p.im] + v;
 }
 
@@ -385,13 +385,13 @@ __global__ void k_eps_face_mul(Grid g, R *w0, R *w1, R *w2, const R *eps) {
 }
 
 template <typename R>
-__global__ void k_eps_face_E(Grid g, R *w0, R *w1, R *w2, const R *eps, double e0, double e1, double e2) {
+__global__ void k_eps_face_E(Grid g, R *w0, R *w1, R *w2, const R *eps, R e0, R e1, R e2) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
   const R s0 = R(0.5) * eps[p.im];
-  w0[p.im] = (R(0.5) * eps[wrapi(g, p.i + 1, p.j, p.k)] + s0) * (R)e0;
-  w1[p.im] = (R(0.5) * eps[wrapi(g, p.i, p.j + 1, p.k)] + s0) * (R)e1;
-  w2[p.im] = (R(0.5) * eps[wrapi(g, p.i, p.j, p.k + 1)] + s0) * (R)e2;
+  w0[p.im] = (R(0.5) * eps[wrapi(g, p.i + 1, p.j, p.k)] + s0) * e0;
+  w1[p.im] = (R(0.5) * eps[wrapi(g, p.i, p.j + 1, p.k)] + s0) * e1;
+  w2[p.im] = (R(0.5) * eps[wrapi(g, p.i, p.j, p.k + 1)] + s0) * e2;
 }
 
 template <typename R>
@@ -411,8 +411,7 @@ __global__ void k_interp_normal(Grid g, V3<R> out, V3<R> in) {
 }
 
 template <typename R>
-__global__ void k_maxwell_e2(Grid g, const R *f0, const R *f1, const R *f2, R *w1, double e0, double e1, double e2,
-                             int ext) {
+__global__ void k_maxwell_e2(Grid g, const R *f0, const R *f1, const R *f2, R *w1, R e0, R e1, R e2, int ext) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
   R fw0 = -f0[p.im], fw1 = -f1[p.im], fw2 = -f2[p.im];
@@ -420,19 +419,18 @@ __global__ void k_maxwell_e2(Grid g, const R *f0, const R *f1, const R *f2, R *w
   R bw1 = -f1[wrapi(g, p.i, p.j - 1, p.k)];
   R bw2 = -f2[wrapi(g, p.i, p.j, p.k - 1)];
   if (ext) {
-    fw0 += (R)e0; fw1 += (R)e1; fw2 += (R)e2;
-    bw0 += (R)e0; bw1 += (R)e1; bw2 += (R)e2;
+    fw0 += e0; fw1 += e1; fw2 += e2;
+    bw0 += e0; bw1 += e1; bw2 += e2;
   }
   const R a = (fw0 + bw0) / R(2), b = (fw1 + bw1) / R(2), c = (fw2 + bw2) / R(2);
   w1[p.im] = a * a + b * b + c * c;
 }
 
 template <typename R>
-__global__ void k_maxwell_face(Grid g, V3<R> force, const R *rho, const R *w1, V3<R> ge, double e0, double e1,
-                               double e2, int ext) {
+__global__ void k_maxwell_face(Grid g, V3<R> force, const R *rho, const R *w1, V3<R> ge, R e0, R e1, R e2, int ext) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
-  const R E[3] = {(R)e0, (R)e1, (R)e2};
+  const R E[3] = {e0, e1, e2};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     const long ip = wrapi(g, p.i + (d == 0), p.j + (d == 1), p.k + (d == 2));
@@ -445,10 +443,10 @@ __global__ void k_maxwell_face(Grid g, V3<R> force, const R *rho, const R *w1, V
 }
 
 template <typename R>
-__global__ void k_np_flux_electric(Grid g, V3<R> flux, const R *c, V3<R> gp, double L_ze) {
+__global__ void k_np_flux_electric(Grid g, V3<R> flux, const R *c, V3<R> gp, R lz) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
-  const R cc = c[p.im], lz = (R)L_ze;
+  const R cc = c[p.im];
 #pragma unroll
   for (int d = 0; d < 3; d++) flux.p[d][p.im] = flux.p[d][p.im] + cc * (gp.p[d][p.im] * lz);
 }
@@ -565,7 +563,7 @@ template <typename R> void eps_janus(const Grid &g, R *eps, const R *phi_sin, co
 }
 template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s) {
   count_launch();
-  k_charge_add<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c, phi, ze, first ? 1 : 0);
+  k_charge_add<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c, phi, (R)ze, first ? 1 : 0);
 }
 template <typename R> void eps_face_mul(const Grid &g, R *w0, R *w1, R *w2, const R *eps, cudaStream_t s) {
   count_launch();
@@ -573,7 +571,7 @@ template <typename R> void eps_face_mul(const Grid &g, R *w0, R *w1, R *w2, cons
 }
 template <typename R> void eps_face_E(const Grid &g, R *w0, R *w1, R *w2, const R *eps, double e0, double e1, double e2, cudaStream_t s) {
   count_launch();
-  k_eps_face_E<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps, e0, e1, e2);
+  k_eps_face_E<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps, (R)e0, (R)e1, (R)e2);
 }
 template <typename R> void axpby_real(const Grid &g, const R *x, R *y, R a, R b, cudaStream_t s) {
   count_launch();
@@ -585,15 +583,15 @@ template <typename R> void interp_normal(const Grid &g, R *const *out, R *const 
 }
 template <typename R> void maxwell_e2(const Grid &g, const R *f0, const R *f1, const R *f2, R *w1, double e0, double e1, double e2, int ext, cudaStream_t s) {
   count_launch();
-  k_maxwell_e2<R><<<nblk_real(g), TPB, 0, s>>>(g, f0, f1, f2, w1, e0, e1, e2, ext);
+  k_maxwell_e2<R><<<nblk_real(g), TPB, 0, s>>>(g, f0, f1, f2, w1, (R)e0, (R)e1, (R)e2, ext);
 }
 template <typename R> void maxwell_face(const Grid &g, R *const *force, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s) {
   count_launch();
-  k_maxwell_face<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(force), rho, w1, v3(ge), e0, e1, e2, ext);
+  k_maxwell_face<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(force), rho, w1, v3(ge), (R)e0, (R)e1, (R)e2, ext);
 }
 template <typename R> void np_flux_electric(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, cudaStream_t s) {
   count_launch();
-  k_np_flux_electric<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(gp), L_ze);
+  k_np_flux_electric<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(gp), (R)L_ze);
 }
 template <typename R> void np_impermeability(const Grid &g, R *const *flux, R *const *sn, cudaStream_t s) {
   count_launch();

@@ -12,9 +12,9 @@ constexpr int KW = 16;  // x pencils per block
 typedef cplx<float> cf;
 
 __device__ __forceinline__ void kvec3(const Grid &g, int i, int j, int kz, float *k) {
-  k[0] = (float)g.wave[0] * (float)kx_of(g, i);
-  k[1] = (float)g.wave[1] * (float)ky_of(g, j);
-  k[2] = (float)g.wave[2] * (float)kz;
+  k[0] = g.wavef[0] * (float)kx_of(g, i);
+  k[1] = g.wavef[1] * (float)ky_of(g, j);
+  k[2] = g.wavef[2] * (float)kz;
 }
 
 // m(k) i k_D exp(i dx k_D / 2) p, m = -1/(eps_ref |k|^2), m(0) = 0
@@ -31,8 +31,10 @@ __device__ __forceinline__ cf grad_mult(const Grid &g, int i, int j, int kz, cf 
   return cf{gr * cs - gi * sn, gr * sn + gi * cs};
 }
 
-// Block reduction of (s0, s1) into partials[2*blockIdx.x + c].
-__device__ void block_partials(double s0, double s1, double *partials) {
+// Block reduction of the threads' FP32 sums (s0, s1) times `scale` into
+// partials[2*blockIdx.x + c]: FP32 within a warp, FP64 across the warps (one
+// FP64 operation per warp instead of per thread: FP64 is scarce on GB300).
+__device__ void block_partials(float s0, float s1, double scale, double *partials) {
   __shared__ double red[2][32];
   const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
   const int lane = lin & 31, wid = lin >> 5;
@@ -41,14 +43,14 @@ __device__ void block_partials(double s0, double s1, double *partials) {
     s1 += __shfl_down_sync(0xffffffffu, s1, o);
   }
   if (lane == 0) {
-    red[0][wid] = s0;
-    red[1][wid] = s1;
+    red[0][wid] = (double)s0;
+    red[1][wid] = (double)s1;
   }
   __syncthreads();
   if (lin < 2) {
     double v = 0.0;
     for (int w = 0; w < nthr / 32; w++) v += red[lin][w];
-    partials[2 * blockIdx.x + lin] = v;
+    partials[2 * blockIdx.x + lin] = v * scale;
   }
 }
 
@@ -57,8 +59,9 @@ __device__ void block_partials(double s0, double s1, double *partials) {
 // lanes) into finals[0..1] and re-arms the counter: the next kernel reads two
 // numbers instead of all partials. Partials of other blocks are read through
 // L2 (__ldcg) after the ticket, which follows each block's fence.
-__device__ void block_partials_final(double s0, double s1, double *partials, double *finals, unsigned *counter) {
-  block_partials(s0, s1, partials);
+__device__ void block_partials_final(float s0, float s1, double scale, double *partials, double *finals,
+                                     unsigned *counter) {
+  block_partials(s0, s1, scale, partials);
   __shared__ int last;
   const int lin = threadIdx.y * blockDim.x + threadIdx.x;
   __threadfence();
@@ -142,8 +145,10 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
   load_table(tws, twx, N);
   pencil_coords(g, q0, pj, pkz);
   __syncthreads();
-  float alpha = 0.f;
-  if (mode == KOP_S) alpha = (float)(rho / fin[0]);
+  __shared__ float salpha;  // one FP64 division per block
+  if (mode == KOP_S && lin == 0) salpha = (float)(rho / fin[0]);
+  __syncthreads();
+  const float alpha = (mode == KOP_S) ? salpha : 0.f;
   // vector update at the read modes of this block's pencils
   for (int it = lin; it < N * KW; it += nthr) {
     const int w = it % KW, e = it / KW;
@@ -452,8 +457,7 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
       s1 += fw * (vr * o.x + vi * o.y);
     }
   }
-  const double inv = 1.0 / (double)g.nreal();
-  if (mode != KOP_NONE) block_partials_final((double)s0 * inv, (double)s1 * inv, partials, finals, counter);
+  if (mode != KOP_NONE) block_partials_final(s0, s1, 1.0 / (double)g.nreal(), partials, finals, counter);
 }
 
 // Update kernel: KOP_XR_MPT modes per thread (independent loads), the block's
@@ -466,9 +470,14 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float 
                                                      const double *fin1, const double *fin2, double *part3,
                                                      double *fin3, unsigned *counter3) {
   const int lin = threadIdx.x;
-  const double r0v = fin1[0], tt = fin2[0], ts = fin2[1];
-  const float alpha = (float)(rho / r0v);
-  const float w = (float)((tt > 0.0) ? ts / tt : 0.0);
+  __shared__ float sc[2];  // alpha, omega: two FP64 divisions per block, not per thread
+  if (lin == 0) {
+    const double r0v = fin1[0], tt = fin2[0], ts = fin2[1];
+    sc[0] = (float)(rho / r0v);
+    sc[1] = (float)((tt > 0.0) ? ts / tt : 0.0);
+  }
+  __syncthreads();
+  const float alpha = sc[0], w = sc[1];
   constexpr int RL = H + 1;  // modes per z row
   const long nm = g.nmodes();
   const long base = (long)blockIdx.x * (KOP_XR_TPB * KOP_XR_MPT);
@@ -494,8 +503,7 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float 
     s0 += fw * (a.x * nr.x + a.y * nr.y);
     s1 += fw * (nr.x * nr.x + nr.y * nr.y);
   }
-  const double inv = 1.0 / (double)g.nreal();
-  block_partials_final((double)s0 * inv, (double)s1 * inv, part3, fin3, counter3);
+  block_partials_final(s0, s1, 1.0 / (double)g.nreal(), part3, fin3, counter3);
 }
 
 __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2) {

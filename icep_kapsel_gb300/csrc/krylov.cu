@@ -71,12 +71,14 @@ __global__ void k_dots_final(const double *partials, int nblocks, int n, double 
 
 template <typename R>
 __global__ void k_sum(Grid g, const R *a, double *partials, int absval) {
-  double s0 = 0.0;
+  // the thread's terms in the field type, the block and grid sums in FP64
+  R t0 = R(0);
   const unsigned N = (unsigned)g.nreal();
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
-    const double v = (double)a[real_index(g, t)];
-    s0 += absval ? fabs(v) : v;
+    const R v = a[real_index(g, t)];
+    t0 += absval ? fabs(v) : v;
   }
+  double s0 = (double)t0;
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int o = 16; o > 0; o >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, o);

@@ -44,9 +44,9 @@ __device__ __forceinline__ void ldv(const float *a, const KMode &m, int wt, R2 &
 
 template <typename R>
 __device__ __forceinline__ void kvec(const Grid &g, const KMode &m, R *k) {
-  k[0] = (R)g.wave[0] * (R)kx_of(g, m.i);
-  k[1] = (R)g.wave[1] * (R)ky_of(g, m.j);
-  k[2] = (R)g.wave[2] * (R)m.kz;
+  k[0] = wave_of<R>(g, 0) * (R)kx_of(g, m.i);
+  k[1] = wave_of<R>(g, 1) * (R)ky_of(g, m.j);
+  k[2] = wave_of<R>(g, 2) * (R)m.kz;
 }
 
 
@@ -54,7 +54,9 @@ __device__ __forceinline__ void kvec(const Grid &g, const KMode &m, R *k) {
 
 template <typename R>
 __global__ void k_kdots(Grid g, const R *a0, const R *b0, const R *a1, const R *b1, int n, double *partials) {
-  double s0 = 0.0, s1 = 0.0;
+  // the thread's terms in the field type (FP32 in MIXED precision: FP64 is
+  // scarce on GB300), the block and grid sums in FP64
+  R s0 = R(0), s1 = R(0);
   const unsigned N = (unsigned)g.nmodes();
   for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < N; t += gridDim.x * blockDim.x) {
     KMode m;
@@ -64,25 +66,24 @@ __global__ void k_kdots(Grid g, const R *a0, const R *b0, const R *a1, const R *
     R ar, ai, br, bi;
     ld(a0, m, w, ar, ai);
     ld(b0, m, w, br, bi);
-    s0 += (double)w * ((double)ar * (double)br + (double)ai * (double)bi);
+    s0 += (R)w * (ar * br + ai * bi);
     if (n > 1) {
       ld(a1, m, w, ar, ai);
       ld(b1, m, w, br, bi);
-      s1 += (double)w * ((double)ar * (double)br + (double)ai * (double)bi);
+      s1 += (R)w * (ar * br + ai * bi);
     }
   }
   const double inv = 1.0 / (double)g.nreal();
-  s0 *= inv;
-  s1 *= inv;
+  double d0 = (double)s0 * inv, d1 = (double)s1 * inv;
   __shared__ double red[2][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int o = 16; o > 0; o >>= 1) {
-    s0 += __shfl_down_sync(0xffffffffu, s0, o);
-    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    d0 += __shfl_down_sync(0xffffffffu, d0, o);
+    d1 += __shfl_down_sync(0xffffffffu, d1, o);
   }
   if (lane == 0) {
-    red[0][wid] = s0;
-    red[1][wid] = s1;
+    red[0][wid] = d0;
+    red[1][wid] = d1;
   }
   __syncthreads();
   if (threadIdx.x < 2) {

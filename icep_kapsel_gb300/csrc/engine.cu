@@ -52,7 +52,7 @@ class Engine : public EngineBase {
   int npd = 0;
   PartParams pp;
   double *ukdc = nullptr;    // device double[3]
-  double *e_ext_n = nullptr; // device double[3]: E_ext * NX*NY*NZ
+  double e_ext_nh[3] = {0, 0, 0};  // E_ext * NX*NY*NZ (host)
   double *partials = nullptr;
   double *scal = nullptr;
   void *shift_tab = nullptr;  // staggered-shift tables referenced by g
@@ -116,7 +116,6 @@ class Engine : public EngineBase {
     cudaFreeHost(hp);
     cudaFree(dsek);
     cudaFree(ukdc);
-    cudaFree(e_ext_n);
     cudaFree(partials);
     cudaFree(scal);
     cudaFree(shift_tab);
@@ -306,13 +305,9 @@ class Engine : public EngineBase {
     for (int q = 0; q < ICEP_MAX_SPECIES; q++) pp.qe[q] = p.surface_charge[q] * p.elementary_charge;
     cudaMalloc(&ukdc, sizeof(double) * 3);
     cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
-    cudaMalloc(&e_ext_n, sizeof(double) * 3);
     {
-      double en[3];
       const double amp = (double)p.nx * p.ny * p.nz;
-      for (int d = 0; d < 3; d++) en[d] = p.e_ext[d] * amp;
-      cudaMemcpyAsync(e_ext_n, en, sizeof(en), cudaMemcpyHostToDevice, s);
-      cudaStreamSynchronize(s);
+      for (int d = 0; d < 3; d++) e_ext_nh[d] = p.e_ext[d] * amp;
     }
     cudaMalloc(&partials, sizeof(double) * 2 * DOT_BLOCKS);
     if (mixed && electrolyte && kop_supported(g)) {
@@ -1350,7 +1345,7 @@ class Engine : public EngineBase {
     // staggered grad of the potential minus E_ext, interpolated to nodes
     copy(F_WV1, F_POT);
     r2c(f[F_WV1]);
-    grad_k<R>(g, f[F_WV1], f[F_F0], f[F_F1], f[F_F2], R(1), true, P.external_field ? e_ext_n : nullptr, s);
+    grad_k<R>(g, f[F_WV1], f[F_F0], f[F_F1], f[F_F2], R(1), true, P.external_field ? e_ext_nh : nullptr, s);
     c2r(f[F_F0], f[F_F1], f[F_F2]);
     for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
     interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);

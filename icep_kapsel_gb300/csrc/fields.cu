@@ -107,12 +107,19 @@ __global__ void k_zeta_k2u_k(Grid g, const R *z0, const R *z1, const double *ukd
   R v0r = -(ky * wi2 - kz * wi1), v0i = (ky * wr2 - kz * wr1);
   R v1r = -(kz * wi0 - kx * wi2), v1i = (kz * wr0 - kx * wr2);
   R v2r = -(kx * wi1 - ky * wi0), v2i = (kx * wr1 - ky * wr0);
-  if (m.im == 0) {
-    v0r = (R)ukdc[0]; v1r = (R)ukdc[1]; v2r = (R)ukdc[2];
-  }
+  // the k = 0 mode takes uk_dc (k_set_k0), written after this kernel so that
+  // no warp issues the FP64 conversions under a predicate
   u0[m.im] = v0r; u0[m.im + 1] = v0i;
   u1[m.im] = v1r; u1[m.im + 1] = v1i;
   u2[m.im] = v2r; u2[m.im + 1] = v2i;
+}
+
+// u_d(k = 0) = uk_dc[d] (Zeta_k2u_k's mean flow, fft_wrapper.cxx:614-711)
+template <typename R>
+__global__ void k_set_k0(R *u0, R *u1, R *u2, const double *ukdc) {
+  u0[0] = (R)ukdc[0];
+  u1[0] = (R)ukdc[1];
+  u2[0] = (R)ukdc[2];
 }
 
 template <typename R>
@@ -207,7 +214,7 @@ __global__ void k_solenoidal(Grid g, R *u0, R *u1, R *u2) {
 }
 
 template <typename R>
-__global__ void k_grad(Grid g, const R *a, R *d0, R *d1, R *d2, R scale, int shift, const double *e_ext_n) {
+__global__ void k_grad(Grid g, const R *a, R *d0, R *d1, R *d2, R scale, int shift, int ext, R ex0, R ex1, R ex2) {
   Mode m;
   if (!mode_of(g, TID, m)) return;
   R k[3];
@@ -225,7 +232,7 @@ __global__ void k_grad(Grid g, const R *a, R *d0, R *d1, R *d2, R scale, int shi
       gr = tr;
       gi = ti;
     }
-    if (e_ext_n && m.im == 0) gr -= (R)e_ext_n[c];
+    if (ext && m.im == 0) gr -= (c == 0) ? ex0 : (c == 1) ? ex1 : ex2;
     d[c][m.im] = gr;
     d[c][m.im + 1] = gi;
   }
@@ -500,6 +507,8 @@ template <typename R> void truncate_23(const Grid &g, const FieldBatch<R> &fb, c
 template <typename R> void zeta_k2u_k(const Grid &g, const R *z0, const R *z1, const double *uk_dc, R *u0, R *u1, R *u2, cudaStream_t s) {
   count_launch();
   k_zeta_k2u_k<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, uk_dc, u0, u1, u2);
+  count_launch();
+  k_set_k0<R><<<1, 1, 0, s>>>(u0, u1, u2, uk_dc);
 }
 template <typename R> void u_k2zeta_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *uk_dc, cudaStream_t s) {
   count_launch();
@@ -518,8 +527,10 @@ template <typename R> void solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cud
   k_solenoidal<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2);
 }
 template <typename R> void grad_k(const Grid &g, const R *a, R *d0, R *d1, R *d2, R scale, bool shift, const double *e_ext_n, cudaStream_t s) {
+  const int ext = e_ext_n ? 1 : 0;
+  const R ex0 = ext ? (R)e_ext_n[0] : R(0), ex1 = ext ? (R)e_ext_n[1] : R(0), ex2 = ext ? (R)e_ext_n[2] : R(0);
   count_launch();
-  k_grad<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, d0, d1, d2, scale, shift ? 1 : 0, e_ext_n);
+  k_grad<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, d0, d1, d2, scale, shift ? 1 : 0, ext, ex0, ex1, ex2);
 }
 template <typename R> void div_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *div, bool shift, cudaStream_t s) {
   count_launch();

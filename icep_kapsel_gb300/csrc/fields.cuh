@@ -20,7 +20,8 @@ template <typename R> void ns_slaved_update(const Grid &g, R *z0, R *z1, const R
 template <typename R> void solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s);
 // A_k2da_k (fft_wrapper.cxx:214-237), optionally * Shift (Shift_vec_fw_imag,
 // fft_wrapper.h:841-858), optionally minus e_ext*N at k = 0
-// (Add_constant_field_k, fluid_solver.cxx:231-244); a may alias nothing.
+// (Add_constant_field_k, fluid_solver.cxx:231-244; e_ext_n: a HOST array of
+// the three values, or null); a may alias nothing.
 template <typename R> void grad_k(const Grid &g, const R *a, R *d0, R *d1, R *d2, R scale, bool shift, const double *e_ext_n, cudaStream_t s);
 // U_k2divergence_k (fft_wrapper.cxx:896-920) / U_k2divergence_k_shift (fft_wrapper.h:879-900)
 template <typename R> void div_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *div, bool shift, cudaStream_t s);

@@ -78,11 +78,10 @@ __global__ void k_sum(Grid g, const R *a, double *partials, int absval) {
     const R v = a[real_index(g, t)];
     t0 += absval ? fabs(v) : v;
   }
-  double s0 = (double)t0;
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int o = 16; o > 0; o >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, o);
-  if (lane == 0) red[wid] = s0;
+  for (int o = 16; o > 0; o >>= 1) t0 += __shfl_down_sync(0xffffffffu, t0, o);
+  if (lane == 0) red[wid] = (double)t0;
   __syncthreads();
   if (threadIdx.x == 0) {
     double v = 0.0;

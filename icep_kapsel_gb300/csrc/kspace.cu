@@ -73,23 +73,22 @@ __global__ void k_kdots(Grid g, const R *a0, const R *b0, const R *a1, const R *
       s1 += (R)w * (ar * br + ai * bi);
     }
   }
-  const double inv = 1.0 / (double)g.nreal();
-  double d0 = (double)s0 * inv, d1 = (double)s1 * inv;
+  // warp sums in the field type, one FP64 value per warp
   __shared__ double red[2][32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int o = 16; o > 0; o >>= 1) {
-    d0 += __shfl_down_sync(0xffffffffu, d0, o);
-    d1 += __shfl_down_sync(0xffffffffu, d1, o);
+    s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
   }
   if (lane == 0) {
-    red[0][wid] = d0;
-    red[1][wid] = d1;
+    red[0][wid] = (double)s0;
+    red[1][wid] = (double)s1;
   }
   __syncthreads();
   if (threadIdx.x < 2) {
     double v = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[threadIdx.x][w];
-    partials[blockIdx.x * 2 + threadIdx.x] = v;
+    partials[blockIdx.x * 2 + threadIdx.x] = v * (1.0 / (double)g.nreal());
   }
 }
 

@@ -78,6 +78,19 @@ __device__ __forceinline__ long stencil_pt(const PartParams &pp, const double *x
   }
 }
 
+// The scatter kernels run ceil(np_domain / TPB) blocks per particle: block b
+// serves particle b / chunks and stencil points (b % chunks) TPB + thread. One
+// thread computes the particle's cell (FP64) into shared memory.
+__device__ __forceinline__ const PCell &chunk_cell(const PartParams &pp, const icep_particle *p, int &n, int &m) {
+  __shared__ PCell spc;
+  const int chunks = (pp.np_domain + blockDim.x - 1) / blockDim.x;
+  n = (int)(blockIdx.x / chunks);
+  m = (int)((blockIdx.x - (unsigned)n * chunks) * blockDim.x + threadIdx.x);
+  if (threadIdx.x == 0) particle_cell(pp, p[n].x, spc);
+  __syncthreads();
+  return spc;
+}
+
 template <typename R>
 __device__ __forceinline__ R exp_t(R a);
 template <>
@@ -148,12 +161,10 @@ __device__ __forceinline__ R prof_dphi_sin(const PartParams &pp, R x) {
 template <typename R>
 __global__ void k_scatter_profile(PartParams pp, const icep_particle *__restrict__ p, const int *__restrict__ sek, R *out,
                                   R *aux, int kind) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long)pp.np * pp.np_domain) return;
-  const int n = (int)(t / pp.np_domain), m = (int)(t - (long)n * pp.np_domain);
+  int n, m;
+  const PCell &pc = chunk_cell(pp, p, n, m);
+  if (m >= pp.np_domain) return;
   R r[3], dist;
-  PCell pc;
-  if constexpr (!std::is_same<R, double>::value) particle_cell(pp, p[n].x, pc);
   const long im = stencil_pt<R>(pp, p[n].x, pc, sek, m, r, &dist);
   if (kind == PROF_PHI) {
     const R v = prof_phi<R>(pp, (R)dist);
@@ -186,12 +197,10 @@ __global__ void k_scatter_profile(PartParams pp, const icep_particle *__restrict
 template <typename R>
 __global__ void k_scatter_up(PartParams pp, const icep_particle *__restrict__ p, const int *__restrict__ sek,
                              const R *__restrict__ phs, R *u0, R *u1, R *u2) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long)pp.np * pp.np_domain) return;
-  const int n = (int)(t / pp.np_domain), m = (int)(t - (long)n * pp.np_domain);
+  int n, m;
+  const PCell &pc = chunk_cell(pp, p, n, m);
+  if (m >= pp.np_domain) return;
   R r[3], dist;
-  PCell pc;
-  if constexpr (!std::is_same<R, double>::value) particle_cell(pp, p[n].x, pc);
   const long im = stencil_pt<R>(pp, p[n].x, pc, sek, m, r, &dist);
   const R ps = phs[im];
   const R w = prof_phi<R>(pp, dist) / ((ps > R(1)) ? ps : R(1));
@@ -211,9 +220,11 @@ __global__ void k_scatter_up(PartParams pp, const icep_particle *__restrict__ p,
 template <typename R>
 __global__ void k_scatter_normal(PartParams pp, const icep_particle *__restrict__ p, const int *__restrict__ sek, R *s0,
                                  R *s1, R *s2) {
-  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long)pp.np * pp.np_domain) return;
-  const int n = (int)(t / pp.np_domain), m = (int)(t - (long)n * pp.np_domain);
+  // FP64 geometry in both precisions: the surface band |r - a| < xi/2 has a
+  // sharp edge, which FP32 distances would move
+  int n, m;
+  chunk_cell(pp, p, n, m);
+  if (m >= pp.np_domain) return;
   double r[3], dist;
   const long im = stencil_point(pp, p[n].x, sek, m, r, &dist);
   const double dr = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
@@ -270,9 +281,9 @@ __global__ void k_f_hydro(PartParams pp, icep_particle *p, const int *__restrict
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int c = 0; c < 6; c++) {
-    double v = acc[c];
+    R v = acc[c];  // warp sums in the field type, FP64 across warps
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) red[c][wid] = v;
+    if (lane == 0) red[c][wid] = (double)v;
   }
   __syncthreads();
   if (threadIdx.x < 6) {
@@ -502,7 +513,7 @@ __global__ void k_md_velocity(PartParams pp, icep_particle *p, int ab2) {
 }
 
 inline unsigned blocks_pts(const PartParams &pp) {
-  return div_up((long)pp.np * pp.np_domain, TPB);
+  return (unsigned)pp.np * div_up(pp.np_domain, TPB);
 }
 
 }  // namespace

@@ -194,16 +194,19 @@ __global__ void __launch_bounds__(DOT_TPB) k_rf_div_combine(Grid g, RfTab tab, c
       acc = fmaf((float)wt, fmaf(xr, xr, xi * xi), acc);
     }
   }
-  double v = (ACC64 ? acc64 : (double)acc) * post;
   __shared__ double red[32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  if (lane == 0) red[wid] = v;
+  if (ACC64) {
+    for (int o = 16; o > 0; o >>= 1) acc64 += __shfl_down_sync(0xffffffffu, acc64, o);
+  } else {  // warp sums in FP32, one FP64 value per warp
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  }
+  if (lane == 0) red[wid] = ACC64 ? acc64 : (double)acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double sum = 0.0;
     for (int q = 0; q < (int)(blockDim.x >> 5); q++) sum += red[q];
-    partials[2 * blockIdx.x] = sum;
+    partials[2 * blockIdx.x] = sum * post;
     partials[2 * blockIdx.x + 1] = 0.0;
   }
 }

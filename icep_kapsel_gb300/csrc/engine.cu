@@ -1186,9 +1186,11 @@ class Engine : public EngineBase {
    * FP32 rate. The potential's half spectrum x^ is float-float state kept
    * between steps. Each outer step forms the true residual r^ = b^ - A x^
    * (its norm by Parseval) and, while |r| > tol |b|, solves A d = r/|r| in
-   * FP32 with the k-space BiCGSTAB to a tolerance that leaves a factor-4
-   * margin, then x^ += |r| d^. The real FP32 potential is one FP32 inverse
-   * transform of x^ at the end.
+   * FP32 with the k-space BiCGSTAB to a tolerance that leaves a factor-2
+   * margin (the FP32 recursive residual tracks the true one closely at these
+   * levels; a cycle that still ends above tol is followed by another), then
+   * x^ += |r| d^. The real FP32 potential is one FP32 inverse transform of x^
+   * at the end.
    */
   int solve_potential_mixed(int rho_id, int pot_id) {
     const Grid &G = g;
@@ -1248,7 +1250,7 @@ class Engine : public EngineBase {
         // FP32 correction solve on the normalised residual
         const double rn = sqrt(rr / (double)G.nreal());
         rf_to_f32(nf, df(D_R), (float *)f[F_KR], 1.0 / rn, s);
-        double inner_tol = 0.25 * P.potential_tol * sqrt(bb / rr);
+        double inner_tol = 0.5 * P.potential_tol * sqrt(bb / rr);
         if (inner_tol < 2e-5) inner_tol = 2e-5;
         if (inner_tol > 0.5) inner_tol = 0.5;
         int it = 0;

@@ -1239,7 +1239,11 @@ class Engine : public EngineBase {
       const double tol2 = P.potential_tol * P.potential_tol * bb;
       // residual norms are summed in FP32 after scaling by a power of two
       // that brings sum_k |b^_k|^2 to order 1
-      const float prescale = (float)ldexp(1.0, -ilogb(sqrt((double)G.nreal() * bb)));
+      // (the exponent kept well inside FP32's range: a right-hand side at
+      // round-off level, e.g. uniform fields, must not overflow the scale)
+      int pe = -ilogb(sqrt((double)G.nreal() * bb));
+      pe = pe < -100 ? -100 : pe > 100 ? 100 : pe;
+      const float prescale = (float)ldexp(1.0, pe);
       for (int outer = 0; outer < 30; outer++) {
         residual_df(prescale);
         if ((st = read_scal())) return st;

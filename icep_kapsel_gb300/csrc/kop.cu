@@ -18,16 +18,20 @@ __device__ __forceinline__ void kvec3(const Grid &g, int i, int j, int kz, float
 }
 
 // m(k) i k_D exp(i dx k_D / 2) p, m = -1/(eps_ref |k|^2), m(0) = 0
-template <int D>
-__device__ __forceinline__ cf grad_mult(const Grid &g, int i, int j, int kz, cf p, float ieps) {
+// the spectral preconditioner m(k) = -1/(eps_ref |k|^2), m(0) = 0
+__device__ __forceinline__ float precond_m(const Grid &g, int i, int j, int kz, float ieps) {
   float k[3];
   kvec3(g, i, j, kz, k);
   const float k2 = k[0] * k[0] + k[1] * k[1] + k[2] * k[2];
-  const float mm = (k2 > 0.f) ? -ieps / k2 : 0.f;
-  const float re = p.x * mm, im = p.y * mm;
+  return (k2 > 0.f) ? -ieps / k2 : 0.f;
+}
+// i k_D exp(i dx k_D / 2) p (p already multiplied by m(k))
+template <int D>
+__device__ __forceinline__ cf grad_mult(const Grid &g, int i, int j, int kz, cf p) {
+  const float kd = g.wavef[D] * (float)((D == 0) ? kx_of(g, i) : (D == 1) ? ky_of(g, j) : kz);
   float cs, sn;
   shift_of(g, D, (D == 0) ? i : (D == 1) ? j : kz, cs, sn);
-  const float gr = -k[D] * im, gi = k[D] * re;
+  const float gr = -kd * p.y, gi = kd * p.x;
   return cf{gr * cs - gi * sn, gr * sn + gi * cs};
 }
 
@@ -97,7 +101,8 @@ __device__ __forceinline__ cf ldw(const float *a, long idx, int wt) {
 }
 
 // First-stage source of the inverse x transforms: the gradient multiplier of
-// component d applied to the updated vector held in shared memory (`raw`,
+// component d applied to the updated vector times m(k), held in shared
+// memory (`raw`,
 // element e of pencil w at raw[e*sw + w]), with the i-direction half of the
 // reference's Hermitian completion on the pencils (j, kz), j in {0, NY/2},
 // kz in {0, NZ/2} (as GPencilsXInv in the plain passes).
@@ -107,22 +112,21 @@ struct SrcGradXInv {
   const int *pj, *pkz;  // (j, kz) of the block's pencils
   int sw, nvalid;
   Grid g;
-  float ieps;
   __device__ __forceinline__ cf load(int w, int e) const {
     if (w >= nvalid) return cf{0.f, 0.f};
     const int j = pj[w], kz = pkz[w];
     if ((j == 0 || j == g.ny / 2) && (kz == 0 || kz == g.hnz - 1)) {
       if (e == 0 || e == g.nx / 2) {
-        const cf v = grad_mult<D>(g, e, j, kz, cf{raw[e * sw + w].x, 0.f}, ieps);
+        const cf v = grad_mult<D>(g, e, j, kz, cf{raw[e * sw + w].x, 0.f});
         return cf{v.x, 0.f};
       }
       const bool kept = (kz == 0) ? (e <= g.nx / 2) : (e > g.nx / 2);
       if (!kept) {
         const int m = g.nx - e;
-        return cconj(grad_mult<D>(g, m, j, kz, raw[m * sw + w], ieps));
+        return cconj(grad_mult<D>(g, m, j, kz, raw[m * sw + w]));
       }
     }
-    return grad_mult<D>(g, e, j, kz, raw[e * sw + w], ieps);
+    return grad_mult<D>(g, e, j, kz, raw[e * sw + w]);
   }
 };
 
@@ -160,8 +164,12 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
     const int j = pj[w], kz = pkz[w];
     const long idx = (long)e * nq + q;
     const int wt = read_weight(g, e, j, kz);
+    // raw holds the vector times the preconditioner m(k), once per mode for
+    // the three gradient components
+    const float mk = precond_m(g, e, j, kz, ieps);
     if (mode == KOP_NONE) {
-      raw[e * sw + w] = ldw(vec, idx, wt);
+      const cf a = ldw(vec, idx, wt);
+      raw[e * sw + w] = cf{a.x * mk, a.y * mk};
       continue;
     }
     const cf rr = ldw(r, idx, wt), vv = ldw(v, idx, wt);
@@ -172,17 +180,17 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
     } else {
       nv = cf{rr.x - alpha * vv.x, rr.y - alpha * vv.y};
     }
-    raw[e * sw + w] = nv;
+    raw[e * sw + w] = cf{nv.x * mk, nv.y * mk};
     if (wt > 0) reinterpret_cast<float2 *>(vec)[idx] = make_float2(nv.x, nv.y);
   }
   __syncthreads();
-  block_fft<float, N, KW>(SrcGradXInv<0>{raw, pj, pkz, sw, nvalid, g, ieps},
+  block_fft<float, N, KW>(SrcGradXInv<0>{raw, pj, pkz, sw, nvalid, g},
                           GPencils<float>{reinterpret_cast<cf *>(w0), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
-  block_fft<float, N, KW>(SrcGradXInv<1>{raw, pj, pkz, sw, nvalid, g, ieps},
+  block_fft<float, N, KW>(SrcGradXInv<1>{raw, pj, pkz, sw, nvalid, g},
                           GPencils<float>{reinterpret_cast<cf *>(w1), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
-  block_fft<float, N, KW>(SrcGradXInv<2>{raw, pj, pkz, sw, nvalid, g, ieps},
+  block_fft<float, N, KW>(SrcGradXInv<2>{raw, pj, pkz, sw, nvalid, g},
                           GPencils<float>{reinterpret_cast<cf *>(w2), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
 }
@@ -400,11 +408,10 @@ struct DivAcc {
   __device__ __forceinline__ void store(int w, int e, cf v) const {
     if (w >= nvalid) return;
     const int j = pj[w], kz = pkz[w];
-    float k[3];
-    kvec3(g, e, j, kz, k);
+    const float kd = g.wavef[D] * (float)((D == 0) ? kx_of(g, e) : (D == 1) ? ky_of(g, j) : kz);
     float cs, sn;
     shift_of(g, D, (D == 0) ? e : (D == 1) ? j : kz, cs, sn);
-    const float ksr = k[D] * cs, ksi = -k[D] * sn;
+    const float ksr = kd * cs, ksi = -kd * sn;
     cf a = (D == 0) ? cf{0.f, 0.f} : acc[e * sw + w];
     a.x += v.x * ksr - v.y * ksi;
     a.y += v.x * ksi + v.y * ksr;

@@ -231,8 +231,8 @@ int icep_batch_step(icep_batch *batch, int nsteps);
  * Charge_field2potential_dielectric with flexible GMRES whose preconditioner
  * is the spectral one applied to the residual plus a U-Net correction of it
  * (computed on the half-resolution grid, BF16 tensor cores); the spectral BiCGSTAB is the fallback when the
- * flexible iteration stagnates, and the FP64 true residual decides
- * convergence as for the plain solver. Before training (or with
+ * flexible iteration stagnates, and the true residual (float-float, 48-bit)
+ * decides convergence as for the plain solver. Before training (or with
  * icep_learned_enable(ctx, 0)) the network is not applied. */
 /* Train on the GPU: `configs` random particle configurations (the context's
  * particle count and radius, new positions, eps_p uniform in [1, 10] when

@@ -4,7 +4,7 @@ float-float arithmetic, 48-bit significands, with iterative refinement)
 against the FP64 path. Tolerances are per field, relative L2 after a few
 steps:
 
-  potential (mean removed)   2e-5   (FP32 permittivity/charge; FP64 solve)
+  potential (mean removed)   2e-5   (FP32 permittivity/charge; float-float refinement)
   zeta, u                    1e-3   (FP32 FFTs; small fields, relative error)
   concentrations             1e-6   (dominated by the uniform salt)
   particle positions         1e-9   (FP64 integration of FP32-sized forces)

@@ -153,35 +153,53 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
   if (mode == KOP_S && lin == 0) salpha = (float)(rho / fin[0]);
   __syncthreads();
   const float alpha = (mode == KOP_S) ? salpha : 0.f;
-  // vector update at the read modes of this block's pencils
-  for (int it = lin; it < N * KW; it += nthr) {
-    const int w = it % KW, e = it / KW;
-    if (w >= nvalid) {
-      raw[e * sw + w] = cf{0.f, 0.f};
-      continue;
+  // vector update at the read modes of this block's pencils: xblock gives
+  // KW * N/8 threads, so every thread has XPT = 8 items; the loads of a batch
+  // of XB items are issued together before any update is computed or stored
+  static_assert(N / 8 <= 512 / KW, "xblock(N) = KW x N/8 threads");
+  constexpr int XPT = 8, XB = 4;
+  for (int u0 = 0; u0 < XPT; u0 += XB) {
+    cf lr[XB], lv[XB], lp[XB];
+#pragma unroll
+    for (int u = 0; u < XB; u++) {
+      const int it = lin + (u0 + u) * nthr;
+      const int w = it % KW, e = it / KW;
+      lr[u] = lv[u] = lp[u] = cf{0.f, 0.f};
+      if (w >= nvalid) continue;
+      const long idx = (long)e * nq + q0 + w;
+      const int wt = read_weight(g, e, pj[w], pkz[w]);
+      if (mode == KOP_NONE) {
+        lp[u] = ldw(vec, idx, wt);
+        continue;
+      }
+      lr[u] = ldw(r, idx, wt);
+      lv[u] = ldw(v, idx, wt);
+      if (mode == KOP_P) lp[u] = ldw(vec, idx, wt);
     }
-    const int q = q0 + w;
-    const int j = pj[w], kz = pkz[w];
-    const long idx = (long)e * nq + q;
-    const int wt = read_weight(g, e, j, kz);
-    // raw holds the vector times the preconditioner m(k), once per mode for
-    // the three gradient components
-    const float mk = precond_m(g, e, j, kz, ieps);
-    if (mode == KOP_NONE) {
-      const cf a = ldw(vec, idx, wt);
-      raw[e * sw + w] = cf{a.x * mk, a.y * mk};
-      continue;
+#pragma unroll
+    for (int u = 0; u < XB; u++) {
+      const int it = lin + (u0 + u) * nthr;
+      const int w = it % KW, e = it / KW;
+      if (w >= nvalid) {
+        raw[e * sw + w] = cf{0.f, 0.f};
+        continue;
+      }
+      const int j = pj[w], kz = pkz[w];
+      // raw holds the vector times the preconditioner m(k), once per mode for
+      // the three gradient components
+      const float mk = precond_m(g, e, j, kz, ieps);
+      cf nv;
+      if (mode == KOP_NONE) {
+        nv = lp[u];
+      } else if (mode == KOP_P) {
+        nv = cf{lr[u].x + beta * (lp[u].x - omega * lv[u].x), lr[u].y + beta * (lp[u].y - omega * lv[u].y)};
+      } else {
+        nv = cf{lr[u].x - alpha * lv[u].x, lr[u].y - alpha * lv[u].y};
+      }
+      raw[e * sw + w] = cf{nv.x * mk, nv.y * mk};
+      if (mode != KOP_NONE && read_weight(g, e, j, kz) > 0)
+        reinterpret_cast<float2 *>(vec)[(long)e * nq + q0 + w] = make_float2(nv.x, nv.y);
     }
-    const cf rr = ldw(r, idx, wt), vv = ldw(v, idx, wt);
-    cf nv;
-    if (mode == KOP_P) {
-      const cf pp = ldw(vec, idx, wt);
-      nv = cf{rr.x + beta * (pp.x - omega * vv.x), rr.y + beta * (pp.y - omega * vv.y)};
-    } else {
-      nv = cf{rr.x - alpha * vv.x, rr.y - alpha * vv.y};
-    }
-    raw[e * sw + w] = cf{nv.x * mk, nv.y * mk};
-    if (wt > 0) reinterpret_cast<float2 *>(vec)[idx] = make_float2(nv.x, nv.y);
   }
   __syncthreads();
   block_fft<float, N, KW>(SrcGradXInv<0>{raw, pj, pkz, sw, nvalid, g},
@@ -444,11 +462,23 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
   block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w2)), (long)q0, 1, (long)nq, nvalid},
                           DivAcc<2>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
   float s0 = 0.f, s1 = 0.f;  // the thread's few terms in FP32; blocks and their sum in FP64
-  for (int it = lin; it < N * KW; it += nthr) {
+  static_assert(N / 8 <= 512 / KW, "xblock(N) = KW x N/8 threads");
+  constexpr int XPT = 8;
+  cf lo[XPT];  // the dot operands, all loads in flight before use
+#pragma unroll
+  for (int u = 0; u < XPT; u++) {
+    const int it = lin + u * nthr;
+    const int w = it % KW, e = it / KW;
+    lo[u] = cf{0.f, 0.f};
+    if (mode == KOP_NONE || w >= nvalid) continue;
+    lo[u] = ldw(other, (long)e * nq + q0 + w, read_weight(g, e, pj[w], pkz[w]));
+  }
+#pragma unroll
+  for (int u = 0; u < XPT; u++) {
+    const int it = lin + u * nthr;
     const int w = it % KW, e = it / KW;
     if (w >= nvalid) continue;
-    const int j = pj[w], kz = pkz[w];
-    const int wt = read_weight(g, e, j, kz);
+    const int wt = read_weight(g, e, pj[w], pkz[w]);
     if (wt == 0) continue;
     const long idx = (long)e * nq + q0 + w;
     const cf a = acc[e * sw + w];
@@ -456,7 +486,7 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
     reinterpret_cast<float2 *>(out)[idx] = make_float2(val.x, val.y);
     if (mode == KOP_NONE) continue;
     const float vr = val.x, vi = (wt == 1) ? 0.f : val.y, fw = (float)wt;
-    const cf o = ldw(other, idx, wt);
+    const cf o = lo[u];
     if (mode == KOP_P) {
       s0 += fw * (o.x * vr + o.y * vi);
     } else {

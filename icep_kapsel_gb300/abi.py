@@ -60,6 +60,8 @@ class Params(C.Structure):
         ("janus_axis", C.c_int * MAX_SPECIES),
         ("fix_cell", C.c_int),
         ("surface_charge", C.c_double * MAX_SPECIES),
+        ("ac", C.c_int),
+        ("frequency", C.c_double),
     ]
 
 

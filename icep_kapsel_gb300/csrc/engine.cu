@@ -52,7 +52,17 @@ class Engine : public EngineBase {
   int npd = 0;
   PartParams pp;
   double *ukdc = nullptr;    // device double[3]
-  double e_ext_nh[3] = {0, 0, 0};  // E_ext * NX*NY*NZ (host)
+  // E_ext at the current time (times sin(2 pi f t) for an AC field) and the
+  // same times NX*NY*NZ (the k = 0 term of Add_constant_field_k)
+  double ext_now[3] = {0, 0, 0}, e_ext_nh[3] = {0, 0, 0};
+  void refresh_ext() {
+    const double f = P.ac ? sin(2.0 * M_PI * P.frequency * time) : 1.0;
+    const double amp = (double)P.nx * P.ny * P.nz * f;
+    for (int d = 0; d < 3; d++) {
+      ext_now[d] = P.ac ? P.e_ext[d] * f : P.e_ext[d];
+      e_ext_nh[d] = P.e_ext[d] * amp;
+    }
+  }
   double *partials = nullptr;
   double *scal = nullptr;
   void *shift_tab = nullptr;  // staggered-shift tables referenced by g
@@ -305,10 +315,7 @@ class Engine : public EngineBase {
     for (int q = 0; q < ICEP_MAX_SPECIES; q++) pp.qe[q] = p.surface_charge[q] * p.elementary_charge;
     cudaMalloc(&ukdc, sizeof(double) * 3);
     cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
-    {
-      const double amp = (double)p.nx * p.ny * p.nz;
-      for (int d = 0; d < 3; d++) e_ext_nh[d] = p.e_ext[d] * amp;
-    }
+    refresh_ext();
     cudaMalloc(&partials, sizeof(double) * 2 * DOT_BLOCKS);
     if (mixed && electrolyte && kop_supported(g)) {
       kop_npb = kop_pencil_blocks(g);
@@ -499,10 +506,10 @@ class Engine : public EngineBase {
   }
   // Build_rhs (operate_dielectric.cxx:524-540)
   void build_rhs(int rhs_id, int rho_id) {
-    eps_face_E<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EPS], P.e_ext[0], P.e_ext[1], P.e_ext[2], s);
+    eps_face_E<R>(g, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EPS], ext_now[0], ext_now[1], ext_now[2], s);
     FieldBatch<R> nz{};  // zero components of E_ext: cleared (with their padding), not transformed
     for (int d = 0; d < 3; d++) {
-      if (P.e_ext[d] != 0.0) nz.p[nz.n++] = f[F_WV3_0 + d];
+      if (ext_now[d] != 0.0) nz.p[nz.n++] = f[F_WV3_0 + d];
       else zero(F_WV3_0 + d);
     }
     if (nz.n) fft_r2c(fft, nz, s);
@@ -1063,6 +1070,8 @@ class Engine : public EngineBase {
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
     memcpy(keep.data(), hp, sizeof(icep_particle) * np);
     const double e_keep[3] = {P.e_ext[0], P.e_ext[1], P.e_ext[2]};
+    const int ac_keep = P.ac;
+    P.ac = 0;  // training fields are DC fields of random direction
     double emag = sqrt(e_keep[0] * e_keep[0] + e_keep[1] * e_keep[1] + e_keep[2] * e_keep[2]);
     if (!(emag > 0)) emag = 0.1;
     std::mt19937_64 rng(seed);
@@ -1080,6 +1089,7 @@ class Engine : public EngineBase {
       double e[3] = {nd(rng), nd(rng), nd(rng)};
       const double en = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
       for (int d = 0; d < 3; d++) P.e_ext[d] = emag * e[d] / en;
+      refresh_ext();
       make_dielectric_field(F_WORK, F_WV1);
       const double eref = mean_eps();
       zero(F_KT);
@@ -1095,6 +1105,8 @@ class Engine : public EngineBase {
     if (loss_last) *loss_last = loss;
     // the context's own state back
     for (int d = 0; d < 3; d++) P.e_ext[d] = e_keep[d];
+    P.ac = ac_keep;
+    refresh_ext();
     memcpy(hp, keep.data(), sizeof(icep_particle) * np);
     cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
     make_dielectric_field(F_WORK, F_WV1);
@@ -1213,10 +1225,10 @@ class Engine : public EngineBase {
     }
     xp_valid = true;
     // b^: components of E_ext that are zero give zero fields and are skipped
-    const bool use[3] = {P.e_ext[0] != 0.0, P.e_ext[1] != 0.0, P.e_ext[2] != 0.0};
+    const bool use[3] = {ext_now[0] != 0.0, ext_now[1] != 0.0, ext_now[2] != 0.0};
     {
       dfl *w[3] = {df(D_W3_0), df(D_W3_1), df(D_W3_2)};
-      rf_eps_face_e(G, w[0], w[1], w[2], (const float *)f[F_EPS], P.e_ext, use, s);
+      rf_eps_face_e(G, w[0], w[1], w[2], (const float *)f[F_EPS], ext_now, use, s);
       FieldBatch<dfl> nz{};
       for (int d = 0; d < 3; d++)
         if (use[d]) nz.p[nz.n++] = w[d];
@@ -1282,6 +1294,10 @@ class Engine : public EngineBase {
         total_inner += it;
         rf_add_f32(nf, (const float *)f[F_KX], df(D_X), rn, s);
       }
+    } else {
+      // b = 0 (e.g. an AC field at a zero crossing with no free charge):
+      // x = 0, as the reference's BiCGSTAB returns for a zero right-hand side
+      cudaMemsetAsync(d64[D_X], 0, sizeof(double) * nf, s);
     }
     rf_to_f32(nf, df(D_X), (float *)f[pot_id], 1.0, s);
     c2r(f[pot_id]);
@@ -1337,8 +1353,8 @@ class Engine : public EngineBase {
   void maxwell_stress(int rho_id) {
     staggered_grad(F_EPS, F_GE0, F_WV1);
     staggered_grad(F_POT, F_F0, F_WV1);
-    maxwell_e2<R>(g, f[F_F0], f[F_F1], f[F_F2], f[F_WV1], P.e_ext[0], P.e_ext[1], P.e_ext[2], P.external_field, s);
-    maxwell_face<R>(g, vec(F_F0), f[rho_id], f[F_WV1], vec(F_GE0), P.e_ext[0], P.e_ext[1], P.e_ext[2],
+    maxwell_e2<R>(g, f[F_F0], f[F_F1], f[F_F2], f[F_WV1], ext_now[0], ext_now[1], ext_now[2], P.external_field, s);
+    maxwell_face<R>(g, vec(F_F0), f[rho_id], f[F_WV1], vec(F_GE0), ext_now[0], ext_now[1], ext_now[2],
                     P.external_field, s);
     for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
     interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);
@@ -1499,6 +1515,8 @@ class Engine : public EngineBase {
     u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
     cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
     if (electrolyte) {
+      time = 0.0;  // Init_potential_dielectric runs at jikan.time = 0
+      refresh_ext();
       for (int d = 0; d < 3; d++) zero(F_GE0 + d);
       init_ions();
       // Init_potential_dielectric (operate_dielectric.cxx:574-609)
@@ -1515,6 +1533,7 @@ class Engine : public EngineBase {
 
   int step(int n) override {
     for (int k = 0; k < n; k++) {
+      refresh_ext();  // E_ext sin(Angular_Frequency jikan.time) of an AC field
       int st = time_evolution_hydro();
       if (st) return st;
       time += P.dt;

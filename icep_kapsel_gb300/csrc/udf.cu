@@ -470,11 +470,14 @@ static bool fill(Bound &b, Result &r) {
     if (!b.str(ce + "Electric_field.type", v)) return bad(r, b);
     if (v == "ON") {
       if (!b.str(ce + "Electric_field.ON.type", v)) return bad(r, b);
-      if (v != "DC") return unsupported(r, "an AC external field");
-      const std::string ef = ce + "Electric_field.ON.DC.";
+      if (v != "DC" && v != "AC") return bad(r, b);
+      // DC: E_ext; AC: E_ext sin(2 pi Frequency t) (input.cxx:812-855)
+      const std::string ef = ce + "Electric_field.ON." + v + ".";
       p.external_field = 1;
+      p.ac = v == "AC" ? 1 : 0;
       if (!b.num(ef + "Ex", p.e_ext[0]) || !b.num(ef + "Ey", p.e_ext[1]) || !b.num(ef + "Ez", p.e_ext[2]))
         return bad(r, b);
+      if (p.ac && !b.num(ef + "Frequency", p.frequency)) return bad(r, b);
     }
   }
   // particles (object_type.spherical_particle, input.cxx:878-1100)
@@ -555,6 +558,11 @@ static bool fill(Bound &b, Result &r) {
       if (p.sw_eq == ICEP_ELECTROLYTE) {
         const double diffusion_time = 1. / (p.kbt * max_onsager * kmax2);
         tdump = tdump < diffusion_time ? tdump : diffusion_time;
+        if (p.external_field && p.ac) {  // a hundredth of the AC period (input.cxx:369-375)
+          const double frequency_time = 1. / p.frequency;
+          const double t_ac = 1.e-2 * frequency_time;
+          tdump = tdump < t_ac ? tdump : t_ac;
+        }
       }
       p.dt = factor * tdump;
     }

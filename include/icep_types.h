@@ -110,6 +110,12 @@ typedef struct icep_params {
    * particles' surface charge (Conc_k2charge_field, operate_electrolyte.cxx:
    * 45-74) and the ions start with their counterions */
   double surface_charge[ICEP_MAX_SPECIES];
+  /* Electric_field.ON.AC (input.cxx:826-845): ac = 1 multiplies E_ext by
+   * sin(2 pi frequency t) at the step's time t (Make_Maxwell_force_x_on_fluid,
+   * operate_dielectric.cxx:620-627; Add_constant_field_k, fluid_solver.cxx:
+   * 231-244; Init_potential_dielectric at t = 0) */
+  int ac;
+  double frequency;
 } icep_params;
 
 /*

@@ -1247,13 +1247,21 @@ static void apply_A(ko_ctx *c, const double *x, double *y) {
   c->matvecs++;
 }
 
+/* E_ext at the context's time: times sin(2 pi f t) for an AC field
+ * (operate_dielectric.cxx:620-627) */
+static void ext_now(const ko_ctx *c, double *E) {
+  const double s = c->P.ac ? sin(2.0 * M_PI * c->P.frequency * c->time) : 1.0;
+  for (int d = 0; d < DIM; d++) E[d] = c->P.ac ? c->P.e_ext[d] * s : c->P.e_ext[d];
+}
+
 /* Build_rhs (operate_dielectric.cxx:524-540) with
  * Interpolate_scalar_on_staggered_grid (operate_dielectric.cxx:57-76):
  * b = D^-.(eps_face E_ext) - rho */
 static void build_rhs(ko_ctx *c, double *rhs, const double *rho) {
   double *w3[3] = {c->f[F_WV3_0], c->f[F_WV3_1], c->f[F_WV3_2]};
   const double *eps = c->f[F_EPS];
-  const double *E = c->P.e_ext;
+  double E[3];
+  ext_now(c, E);
   zero_real(c, rhs);
   for (int d = 0; d < DIM; d++) zero_real(c, w3[d]);
 #pragma omp parallel for schedule(static)
@@ -1385,7 +1393,7 @@ static long bicgstab_spectral(ko_ctx *c, double *b, double *x, double tol, long 
       for (int k = 0; k < c->nz; k++) eref += c->f[F_EPS][IDX(c, i, j, k)];
   eref /= (double)n;
   double *r = (double *)malloc(sizeof(double) * n), *r0 = (double *)malloc(sizeof(double) * n);
-  const size_t nn = (size_t)c->nu;
+  const size_t nn = c->nu > 0 ? (size_t)c->nu : 1;
   double *v = (double *)calloc(nn, sizeof(double)), *p = (double *)calloc(nn, sizeof(double));
   double *s = (double *)malloc(sizeof(double) * n), *t = (double *)malloc(sizeof(double) * n);
   double *y = (double *)malloc(sizeof(double) * n), *z = (double *)malloc(sizeof(double) * n);
@@ -1513,7 +1521,8 @@ static void maxwell_force(ko_ctx *c, double **force, double *rho) {
   double *eps = c->f[F_EPS], *pot = c->f[F_POT];
   double *ge[3] = {c->f[F_GE0], c->f[F_GE1], c->f[F_GE2]};
   double *w1 = c->f[F_WV1];
-  const double *E = c->P.e_ext;
+  double E[3];
+  ext_now(c, E);
   const int ext = c->P.external_field;
   make_dielectric_field(c, eps, force[0]);
   conc_k2charge(c, rho, force[0], force[1]);
@@ -1582,8 +1591,9 @@ static void nssolute_solver_euler(ko_ctx *c) {
   a_k2da_k(c, pot, gp);
   shift_fw(c, gp);
   fft_c2r(c, pot);
-  if (c->P.external_field) {
+  if (c->P.external_field) {  /* Add_constant_field_k (fluid_solver.cxx:231-244) */
     double amp = (double)c->nx * c->ny * c->nz;
+    if (c->P.ac) amp *= sin(2.0 * M_PI * c->P.frequency * c->time);
     for (int d = 0; d < DIM; d++) gp[d][0] -= c->P.e_ext[d] * amp;
   }
   for (int d = 0; d < DIM; d++) fft_c2r(c, gp[d]);

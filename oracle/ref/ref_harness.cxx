@@ -230,7 +230,8 @@ static void set_globals(const icep_params *q) {
   Elementary_charge = q->elementary_charge;
   External_field = q->external_field;
   for (int d = 0; d < DIM; d++) E_ext[d] = q->e_ext[d];
-  AC = 0;
+  AC = q->ac ? 1 : 0;  // Electric_field.ON.AC (input.cxx:826-845, 370-374)
+  Angular_Frequency = 2.0 * M_PI * q->frequency;
   N_spec = 2;
   Poisson_Boltzmann = 0;
   Rigid_Number = 0;

@@ -73,6 +73,16 @@ def icep_case(n=32, npart=4, minsep=12.0, seed=2, a=4.0, eps_f=1.0, eps_p=10.0, 
     return p, abi.make_particles(x, eps_p=eps)
 
 
+def ac_case(frequency=8.0, tol=1e-7, solver=abi.SOLVER_REF, precision=abi.FP64):
+    """An AC external field E_ext sin(2 pi f t) (Electric_field.ON.AC): with
+    dt = 0.01 and f = 8 the phase advances 0.5 rad a step, so the field is
+    zero at t = 0 (the initial solve and the first step) and grows after."""
+    p, parts = icep_case(e_ext=(0.0, 0.05, 0.1), tol=tol, solver=solver, precision=precision)
+    p.ac = 1
+    p.frequency = frequency
+    return p, parts
+
+
 def unit_quaternions(n, seed):
     """n orientations uniform on the rotation group (normalised Gaussian 4-vectors)."""
     q = np.random.default_rng(seed).standard_normal((n, 4))

@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32", "janus32", "charged32"]
+CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32", "janus32", "charged32", "ac32"]
 
 
 def small_case():
@@ -231,6 +231,25 @@ def run_case(name, out):
         r.call("charge_field")
         data["rho"] = r.get("rho")[:, :, :32]
         data["phi_p"] = r.get("work")[:, :, :32]
+    elif name == "ac32":
+        # an AC field: zero at t = 0 (initial solve and first step), then
+        # E_ext sin(2 pi f t) in the Poisson right-hand side, the ions' flux
+        # and the Maxwell stress of the next two steps
+        p, parts = cases.ac_case()
+        r = pyoracle.RefKapsel(p, parts)
+        r.init_state()
+        meta["init_iterations"] = int(r.last_iterations())
+        r.step(1)
+        meta["step0_iterations"] = int(r.last_iterations())
+        data["pot_step0"] = r.get("pot")[:, :, :32]
+        r.step(2)
+        meta["step_iterations"] = int(r.last_iterations())
+        meta["step_error"] = float(r.last_error())
+        for k in ("zeta0", "zeta1", "c0", "c1"):
+            data[k] = r.get(k)
+        data["pot"] = r.get("pot")[:, :, :32]
+        for k, v in abi.particles_to_numpy(r.particles(), p.n_particles).items():
+            data["p_" + k] = v
     else:
         raise ValueError(name)
     meta["params"] = abi.params_dict(p)

@@ -79,8 +79,27 @@ def rewrite(tmp_path, old, new):
     return str(d / "input.udf")
 
 
+def test_ac_field(rt, tmp_path):
+    """Electric_field.ON.AC: E_ext and Frequency land in e_ext / frequency
+    with ac = 1, and the auto time step takes a hundredth of the period when
+    that is shorter than the viscous and diffusive times (input.cxx:369-375)."""
+    path = rewrite(tmp_path, '{"ON", {"DC", {0.0, 0.0, 0.1}{0.0, 0.0, 0.0, 0.0}}}',
+                   '{"ON", {"AC", {0.0, 0.0, 0.1}{0.0, 0.05, 0.1, 8.0}}}')
+    p, _, _, _ = rt.udf_read(path)
+    assert (p.external_field, p.ac, p.frequency) == (1, 1, 8.0)
+    assert list(p.e_ext) == [0.0, 0.05, 0.1]
+    assert p.dt == 0.01  # manual
+    d = tmp_path / "udf"
+    (d / "input.udf").write_text((d / "input.udf").read_text().replace(
+        'time_increment:{"manual",{1.0}{0.01}}', 'time_increment:{"auto",{1.0}{0.01}}'))
+    p, _, _, _ = rt.udf_read(str(d / "input.udf"))
+    assert p.dt == 1.0 * (1.e-2 * (1. / 8.0))
+    # the DC file keeps ac = 0
+    p, _, _, _ = rt.udf_read(FIX)
+    assert p.ac == 0
+
+
 @pytest.mark.parametrize("old,new", [
-    ('{"ON", {"DC", {0.0, 0.0, 0.1}', '{"ON", {"AC", {0.0, 0.0, 0.1}'),  # AC field
     ('"Uniform",', '"Poisson_Boltzmann",'),
     ('{"salt", {1.0, 7.24}', '{"saltfree", {1.0, 7.24}'),
     ('{"user_specify",\n', '{"uniform_random",\n'),  # fine: placement by rand()

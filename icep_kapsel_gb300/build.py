@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libicep_gb300.so")
 BIN = os.path.join(HERE, "icep_kapsel")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["fft_df.cu", "fft.cu", "fields.cu", "particles.cu", "krylov.cu", "kspace.cu", "kop.cu", "unet.cu", "engine.cu", "icep_abi.cu", "lj_noalloc.cu", "probe.cu", "refine.cu", "udf.cu"]
+SOURCES = ["fft_df.cu", "fft.cu", "fields.cu", "particles.cu", "krylov.cu", "kspace.cu", "kop.cu", "unet.cu", "engine.cu", "icep_abi.cu", "lj_noalloc.cu", "probe.cu", "refine.cu", "udf.cu", "avs.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -48,7 +48,7 @@ def build(force=False, verbose=False):
     nv = nvcc()
 
     def one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
+        obj = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         cmd = [nv] + ARCH + FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

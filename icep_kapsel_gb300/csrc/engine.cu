@@ -38,7 +38,7 @@ class Engine : public EngineBase {
   R *f[F_COUNT];
   double *stage = nullptr;  // FP64 staging for get/set of FP32 fields
   // per-field FP64 staging of the batched host I/O (MIXED), allocated on first use
-  static constexpr int NSTAGE = 6;
+  static constexpr int NSTAGE = 8;
   double *stage_n[NSTAGE] = {nullptr};
   // the FP64 potential last handed to the host (MIXED): a potential passed
   // back unchanged keeps the solver's float-float state
@@ -1069,6 +1069,10 @@ class Engine : public EngineBase {
     cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
     memcpy(keep.data(), hp, sizeof(icep_particle) * np);
+    // the parameters before training, restored if training does not help
+    float *snap = nullptr;
+    if (cudaMalloc(&snap, sizeof(float) * net.nparams) != cudaSuccess) return fail(ICEP_ERR_CUDA, "learned_train");
+    cudaMemcpyAsync(snap, net.params, sizeof(float) * net.nparams, cudaMemcpyDeviceToDevice, s);
     const double e_keep[3] = {P.e_ext[0], P.e_ext[1], P.e_ext[2]};
     const int ac_keep = P.ac;
     P.ac = 0;  // training fields are DC fields of random direction
@@ -1110,10 +1114,32 @@ class Engine : public EngineBase {
     memcpy(hp, keep.data(), sizeof(icep_particle) * np);
     cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
     make_dielectric_field(F_WORK, F_WV1);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
-    if (st == ICEP_OK) net_trained = true;
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+      cudaFree(snap);
+      return cuda_status("learned_train");
+    }
+    if (st == ICEP_OK) {
+      // keep the trained parameters only if they do not make the one-step
+      // residual of the context's own problem worse than the spectral
+      // preconditioner alone; else go back to the parameters before training
+      const bool was = net_trained;
+      net_trained = true;
+      double ls = 0, ll = 0;
+      st = learned_eval(2, &ls, &ll);
+      if (st == ICEP_OK && !(ll <= ls)) {
+        cudaMemcpyAsync(net.params, snap, sizeof(float) * net.nparams, cudaMemcpyDeviceToDevice, s);
+        net.pack(s);
+        net_trained = was;
+        last_train_kept = false;
+      } else {
+        last_train_kept = true;
+      }
+      if (cudaStreamSynchronize(s) != cudaSuccess) st = cuda_status("learned_train");
+    }
+    cudaFree(snap);
     return st;
   }
+  bool last_train_kept = false;  // whether the last learned_train kept its parameters
   int learned_enable(int on) override {
     if (!learned) return unsupported_learned();
     net_use = on != 0;
@@ -1633,6 +1659,45 @@ class Engine : public EngineBase {
     }
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_fields");
     return ICEP_OK;
+  }
+  // The fields of Output_dielectric_charge_field_data (output.cxx:262-320)
+  // with vel, phi and charge printed, into host FP64 arrays (NULL skips):
+  // u = Zeta_k2u(zeta, uk_dc); phi = the sum of Phi and the surface charge
+  // of Make_phi_qq_particle (operate_electrolyte.cxx:179-243) times 4 pi a^2;
+  // the solute charge e sum_n z_n c_n (1 - phi); the potential; eps. The
+  // step state is not touched: the work goes to the Krylov work vectors.
+  const icep_params &params() const override { return P; }
+  int n_particles() const override { return np; }
+  int charge_field_data(double *const *out) override {
+    if (!electrolyte) return fail(ICEP_ERR_UNSUPPORTED, "charge field output needs the electrolyte model");
+    const int U0 = F_KR, U1 = F_KR0, U2 = F_KP, PHI = F_KV, SURF = F_KS, C0 = F_KT, C1 = F_KY, SOL = F_KZ;
+    zeta_k2u_k<R>(g, f[F_ZETA0], f[F_ZETA1], ukdc, f[U0], f[U1], f[U2], s);
+    c2r(f[U0], f[U1], f[U2]);
+    zero(PHI);
+    zero(SURF);
+    scatter_profile<R>(pp, dp, dsek, f[PHI], f[SURF], PROF_QQ, s);
+    sum_abs_real<R>(g, f[SURF], partials, scal, S_AUX1, s);
+    int st = read_scal();
+    if (st) return st;
+    // 0/0 = NaN everywhere when no particle is charged, as the reference's
+    const double rescale = abs_total_qe / (hscal[S_AUX1] * P.dx * P.dx * P.dx);
+    scale_copy<R>(g, f[SURF], f[SURF], (R)rescale, s);
+    const double area = (4. * M_PI) * (radius * radius);
+    scale_copy<R>(g, f[SURF], f[SURF], (R)area, s);
+    copy(C0, F_C0);
+    copy(C1, F_C1);
+    c2r(f[C0], f[C1]);
+    solute_charge<R>(g, f[SOL], f[C0], f[C1], f[PHI], valency_e[0], valency_e[1], s);
+    const int ids[8] = {U0, U1, U2, PHI, SURF, SOL, F_POT, F_EPS};
+    int sel[8];
+    double *dst[8];
+    int n = 0;
+    for (int k = 0; k < 8; k++)
+      if (out[k]) {
+        sel[n] = ids[k];
+        dst[n++] = out[k];
+      }
+    return n ? get_fields(sel, dst, n) : sync();
   }
   int set_field(int id, const double *host) override {
     if (id < 0 || id >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");

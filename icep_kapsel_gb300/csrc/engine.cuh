@@ -38,6 +38,11 @@ struct EngineBase {
   // accumulated device time per step phase (ICEP_PHASE_PROFILE=1 at create)
   virtual int phase_times(double *ms, int n) = 0;
   // checkpoint / restart of the step state (fields, particles, time)
+  // Output_dielectric_charge_field_data's fields (u0 u1 u2 phi surface
+  // solute potential eps) into host FP64 arrays; NULL entries are skipped
+  virtual int charge_field_data(double *const *out) = 0;
+  virtual const icep_params &params() const = 0;
+  virtual int n_particles() const = 0;
   virtual int save_checkpoint(const char *path) = 0;
   virtual int load_checkpoint(const char *path) = 0;
   // learned preconditioner (MIXED precision with solver ICEP_SOLVER_LEARNED)

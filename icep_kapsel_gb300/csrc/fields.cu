@@ -381,6 +381,16 @@ __global__ void k_charge_add(Grid g, R *rho, const R *c, const R *phi, R ze, int
   rho[p.im] = first ? v : rho[p.im] + v;
 }
 
+// the solute charge of the field output (output.cxx:286-297):
+// (e z_0 c_0 + e z_1 c_1) (1 - phi)
+template <typename R>
+__global__ void k_solute_charge(Grid g, R *out, const R *c0, const R *c1, const R *phi, R ze0, R ze1) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R q = ze0 * c0[p.im] + ze1 * c1[p.im];
+  out[p.im] = q * (R(1) - phi[p.im]);
+}
+
 template <typename R>
 __global__ void k_eps_face_mul(Grid g, R *w0, R *w1, R *w2, const R *eps) {
   Pt p;
@@ -576,6 +586,11 @@ template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R
   count_launch();
   k_charge_add<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c, phi, (R)ze, first ? 1 : 0);
 }
+template <typename R>
+void solute_charge(const Grid &g, R *out, const R *c0, const R *c1, const R *phi, double ze0, double ze1, cudaStream_t s) {
+  count_launch();
+  k_solute_charge<R><<<nblk_real(g), TPB, 0, s>>>(g, out, c0, c1, phi, (R)ze0, (R)ze1);
+}
 template <typename R> void eps_face_mul(const Grid &g, R *w0, R *w1, R *w2, const R *eps, cudaStream_t s) {
   count_launch();
   k_eps_face_mul<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps);
@@ -637,6 +652,7 @@ template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s) {
   template void eps_from_profile<R>(const Grid &, R *, const R *, const R *, double, double, double, cudaStream_t);    \
   template void eps_janus<R>(const Grid &, R *, const R *, const R *, double, double, cudaStream_t);                   \
   template void charge_add<R>(const Grid &, R *, const R *, const R *, double, bool, cudaStream_t);                    \
+  template void solute_charge<R>(const Grid &, R *, const R *, const R *, const R *, double, double, cudaStream_t);     \
   template void eps_face_mul<R>(const Grid &, R *, R *, R *, const R *, cudaStream_t);                                 \
   template void eps_face_E<R>(const Grid &, R *, R *, R *, const R *, double, double, double, cudaStream_t);           \
   template void axpby_real<R>(const Grid &, const R *, R *, R, R, cudaStream_t);                                       \

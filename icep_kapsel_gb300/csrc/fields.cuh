@@ -51,6 +51,9 @@ template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_
 template <typename R> void eps_janus(const Grid &g, R *eps, const R *phi_sin, const R *eps_j, double ef, double dc, cudaStream_t s);
 // rho += ze c (1 - phi) (Conc_k2charge_field_no_surfase_charge, operate_dielectric.cxx:135-160)
 template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s);
+// out = (ze0 c0 + ze1 c1) (1 - phi) (real points): the solute charge of the field output
+template <typename R>
+void solute_charge(const Grid &g, R *out, const R *c0, const R *c1, const R *phi, double ze0, double ze1, cudaStream_t s);
 // w_d *= 0.5 (eps(i+e_d) + eps(i)) (Ax, operate_dielectric.cxx:494-510)
 template <typename R> void eps_face_mul(const Grid &g, R *w0, R *w1, R *w2, const R *eps, cudaStream_t s);
 // w_d = (0.5 eps(i+e_d) + 0.5 eps(i)) E_d (Interpolate_scalar_on_staggered_grid, operate_dielectric.cxx:57-76)

@@ -99,6 +99,40 @@ int icep_load_checkpoint(icep_ctx *c, const char *path) {
   return ok(c) && path ? wrap(c, c->e->load_checkpoint(path)) : ICEP_ERR_ARG;
 }
 
+int icep_charge_field_data(icep_ctx *c, double *u0, double *u1, double *u2, double *phi, double *surface_charge,
+                           double *solute_charge, double *potential, double *epsilon) {
+  if (!ok(c)) return ICEP_ERR_ARG;
+  double *out[8] = {u0, u1, u2, phi, surface_charge, solute_charge, potential, epsilon};
+  return wrap(c, c->e->charge_field_data(out));
+}
+
+int icep_output_avs(icep_ctx *c, const char *out_dir, const char *out_name, int ascii) {
+  if (!ok(c) || !out_dir || !out_name) return ICEP_ERR_ARG;
+  icep::EngineBase *e = c->e;
+  const icep_params &p = e->params();
+  const size_t nf = (size_t)p.nx * p.ny * (2 * (p.nz / 2 + 1));
+  std::vector<double> buf(7 * nf);
+  double *out[8];
+  for (int k = 0; k < 7; k++) out[k] = buf.data() + k * nf;
+  out[7] = nullptr;
+  int st = e->charge_field_data(out);
+  if (st) return wrap(c, st);
+  const double *fields[7] = {out[0], out[1], out[2], out[3], out[4], out[5], out[6]};
+  st = icep_avs_charge_frame(out_dir, out_name, ascii, p.nx, p.ny, p.nz, e->ts, e->time, fields);
+  if (st) {
+    c->err = "cannot write the AVS field frame";
+    return st;
+  }
+  const int np = e->n_particles();
+  if (np > 0) {
+    std::vector<icep_particle> parts((size_t)np);
+    if ((st = e->get_particles(parts.data()))) return wrap(c, st);
+    st = icep_avs_particles(out_dir, out_name, ascii, e->ts, e->time, parts.data(), np, p.a * p.dx);
+    if (st) c->err = "cannot write the AVS particle frame";
+  }
+  return st;
+}
+
 int icep_time_evolution(icep_ctx *c, double *zeta0, double *zeta1, double *uk_dc, double *conc0, double *conc1,
                         double *potential, icep_particle *particles, int nsteps) {
   if (!ok(c) || !zeta0 || !zeta1 || !uk_dc || !particles || nsteps < 0) return ICEP_ERR_ARG;

@@ -9,8 +9,12 @@
 // restart from an icep checkpoint), then GTS * Num_snap steps. Every GTS
 // steps one line per particle goes to out_dir/particles_<ts>.dat
 // (spec, x, v, omega, q) and a status line to stderr; at the end the state is
-// written to out_dir/restart.ckpt (icep_save_checkpoint). Exit status 0 on
-// success, else the library's status code.
+// written to out_dir/restart.ckpt (icep_save_checkpoint). With output.AVS
+// ON and FileType BINARY or ASCII the reference's AVS field and particle
+// frames are written too (Init_output and the main loop's frames,
+// output.cxx:15-31, sp_3d_ns.cxx:482-497) into output.ON.Out_dir; EXTENDED
+// (HDF5) output is refused, as by a reference built without it. Exit status
+// 0 on success, else the library's status code.
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -93,6 +97,33 @@ int main(int argc, char **argv) {
     fprintf(stderr, "icep_kapsel: %s: %s\n", input.c_str(), err);
     return st;
   }
+  // output.AVS (input.cxx:1782-1830)
+  std::string avs_dir, avs_name;
+  int avs_ascii = -1;
+  {
+    char v[512];
+    if (icep_udf_value(input.c_str(), "output.AVS", v, sizeof(v)) == ICEP_OK && std::string(v) == "ON") {
+      char d[512], n[512], t[64];
+      if (icep_udf_value(input.c_str(), "output.ON.Out_dir", d, sizeof(d)) ||
+          icep_udf_value(input.c_str(), "output.ON.Out_name", n, sizeof(n)) ||
+          icep_udf_value(input.c_str(), "output.ON.FileType", t, sizeof(t))) {
+        fprintf(stderr, "icep_kapsel: %s: output.ON is incomplete\n", input.c_str());
+        return ICEP_ERR_ARG;
+      }
+      const std::string type(t);
+      if (type == "EXTENDED") {
+        fprintf(stderr, "icep_kapsel: EXTENDED (HDF5) output is not built; use BINARY or ASCII\n");
+        return ICEP_ERR_UNSUPPORTED;
+      }
+      if (p.sw_eq != ICEP_ELECTROLYTE) {
+        fprintf(stderr, "icep_kapsel: AVS field output is built for the electrolyte model only\n");
+        return ICEP_ERR_UNSUPPORTED;
+      }
+      avs_dir = d;
+      avs_name = n;
+      avs_ascii = type == "ASCII" ? 1 : 0;
+    }
+  }
   if (precision >= 0) p.precision = precision;
   if (solver >= 0) p.solver = solver;
   mkdir(out.c_str(), 0755);
@@ -108,6 +139,13 @@ int main(int argc, char **argv) {
   fprintf(stderr, "# icep_kapsel: %dx%dx%d, %d particles, dt %.6g, %ld steps (GTS %d)\n", p.nx, p.ny, p.nz, np, p.dt,
           total, gts);
   std::vector<icep_particle> buf((size_t)(np > 0 ? np : 1));
+  if (!st && avs_ascii >= 0) {
+    st = icep_avs_init(avs_dir.c_str(), avs_name.c_str(), avs_ascii, p.nx, p.ny, p.nz, p.dx, nsnap + 1, np);
+    if (st) fprintf(stderr, "icep_kapsel: cannot write the AVS headers in %s\n", avs_dir.c_str());
+  }
+  // a frame at the start, unless resumed (the reference skips the resumed step's frame)
+  if (!st && avs_ascii >= 0 && restart.empty())
+    st = check(ctx, icep_output_avs(ctx, avs_dir.c_str(), avs_name.c_str(), avs_ascii), "output_avs");
   if (!st) st = dump(ctx, out, np, buf);
   for (long k = 0; k < total && !st; k++) {
     st = check(ctx, icep_step(ctx, 1), "step");
@@ -120,7 +158,9 @@ int main(int argc, char **argv) {
       double t = 0.0;
       icep_get_time(ctx, &ts, &t);
       fprintf(stderr, "# ts %d time %.6g poisson iterations %d residual %.3g\n", ts, t, it, e);
-      st = dump(ctx, out, np, buf);
+      if (avs_ascii >= 0)
+        st = check(ctx, icep_output_avs(ctx, avs_dir.c_str(), avs_name.c_str(), avs_ascii), "output_avs");
+      if (!st) st = dump(ctx, out, np, buf);
     }
   }
   if (!st) st = check(ctx, icep_save_checkpoint(ctx, (out + "/restart.ckpt").c_str()), "save_checkpoint");

@@ -228,6 +228,30 @@ class Simulation:
         """Restore the step state written by save_checkpoint."""
         self._check(self.lib.icep_load_checkpoint(self.ctx, os.fsencode(path)), "load_checkpoint")
 
+    OUTPUT_FIELDS = ("u0", "u1", "u2", "phi", "surface_charge", "solute_charge", "potential", "epsilon")
+
+    def charge_field_data(self):
+        """The fields of Output_dielectric_charge_field_data (icep_charge_field_data)
+        as a dict of [NX][NY][NZ_] arrays."""
+        out = {k: np.zeros(self._shape(), dtype=np.float64) for k in self.OUTPUT_FIELDS}
+        self._check(self.lib.icep_charge_field_data(self.ctx, *[_dp(out[k]) for k in self.OUTPUT_FIELDS]),
+                    "charge_field_data")
+        return out
+
+    def output_avs(self, out_dir, name, ascii=False):
+        """One AVS frame of the current state (icep_output_avs); call
+        avs_init(out_dir, name, ...) once before the first frame."""
+        self._check(self.lib.icep_output_avs(self.ctx, os.fsencode(out_dir), os.fsencode(name), int(ascii)),
+                    "output_avs")
+
+    def avs_init(self, out_dir, name, nstep, ascii=False):
+        """The AVS headers for this context's mesh (icep_avs_init)."""
+        p = self.params
+        st = self.lib.icep_avs_init(os.fsencode(out_dir), os.fsencode(name), int(ascii), p.nx, p.ny, p.nz,
+                                    C.c_double(p.dx), int(nstep), p.n_particles)
+        if st:
+            raise IcepError("avs_init failed (%d)" % st)
+
     # reference-named phases
     def fft_r2c(self, a):
         a = np.ascontiguousarray(a, dtype=np.float64).copy()

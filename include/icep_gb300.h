@@ -119,7 +119,7 @@ int icep_save_checkpoint(icep_ctx *ctx, const char *path);
  * needs max_particles >= n_particles. Returns ICEP_ERR_UNSUPPORTED (with the
  * reason in err) for settings outside this path: shear flows, chains and
  * rigid bodies, Dielectric_property OFF, salt-free
- * electrolytes, AC fields, pinned particles, lattice or random-walk
+ * electrolytes, pinned particles, lattice or random-walk
  * initial configurations, resumed runs (use icep_load_checkpoint). */
 int icep_udf_read(const char *path, icep_params *params, icep_particle *particles, int max_particles,
                   int *n_particles, int *gts, int *num_snap, char *err, int err_len);
@@ -129,6 +129,53 @@ int icep_udf_read(const char *path, icep_params *params, icep_particle *particle
  * gives a list's length). On an error, value holds the message. */
 int icep_udf_value(const char *path, const char *key, char *value, int len);
 int icep_load_checkpoint(icep_ctx *ctx, const char *path);
+
+/* Field output. The fields Output_dielectric_charge_field_data computes
+ * (output.cxx:262-320) with velocity, phi and charge printed (what AVS
+ * output prints, Init_output, output.cxx:18-22), as host FP64 arrays in the
+ * reference layout [NX][NY][NZ_]; any pointer may be NULL:
+ *   u0, u1, u2       Zeta_k2u(zeta, uk_dc)                            (u)
+ *   phi              the sum of Phi over the particles, unclipped
+ *                    (Make_phi_qq_particle, operate_electrolyte.cxx:179-243)
+ *   surface_charge   its rescaled surface charge times 4 pi a^2       (up[0])
+ *   solute_charge    e sum_n z_n c_n (1 - phi)                          (up[1])
+ *   potential        the potential                                     (Potential)
+ *   epsilon          the permittivity of the last step                 (up[2])
+ * With no charged particle the surface charge is 0/0 = NaN everywhere, as the
+ * reference's. The step state is left as it is (the reference transforms the
+ * concentrations to real space and back). Electrolyte contexts only
+ * (ICEP_ERR_UNSUPPORTED otherwise). */
+int icep_charge_field_data(icep_ctx *ctx, double *u0, double *u1, double *u2, double *phi, double *surface_charge,
+                           double *solute_charge, double *potential, double *epsilon);
+
+/* AVS/Express output of the reference's default writers (SW_OUTFORMAT
+ * OUT_AVS_BINARY, ascii = 0, or OUT_AVS_ASCII, ascii = 1), the same files,
+ * names and bytes:
+ *   icep_avs_init         Set_avs_parameters + Init_avs + Init_avs_p
+ *                         (avs_output.cxx:46-186, avs_output_p.cxx:13-27):
+ *                         out_dir/avs/, out_dir/<name>.fld (veclen 7, nstep),
+ *                         out_dir/<name>.cod (uniform field extents, dx) and,
+ *                         with particles, out_dir/<name>p.fld;
+ *   icep_avs_charge_frame Output_avs_charge (avs_output.cxx:332-380): appends
+ *                         the frame to <name>.fld and writes
+ *                         out_dir/avs/<name>_<ts>.dat with the 7 fields
+ *                         ux uy uz phi surface_charge rho e_potential as
+ *                         float32, x fastest (fields[0..6], [NX][NY][NZ_]);
+ *   icep_avs_particles    Output_avs_p (avs_output_p.cxx:73-157): appends to
+ *                         <name>p.fld, writes avs/<name>p_<ts>.cod (z, y, x)
+ *                         and .dat (radius, body axes from the quaternion);
+ *   icep_output_avs       one frame of a context's current state (the field
+ *                         frame, then the particle frame when there are
+ *                         particles) at its ts and time, as the reference's
+ *                         main loop writes every GTS steps (sp_3d_ns.cxx:482-497).
+ * ICEP_ERR_IO when a file cannot be written. */
+int icep_avs_init(const char *out_dir, const char *out_name, int ascii, int nx, int ny, int nz, double dx, int nstep,
+                  int n_particles);
+int icep_avs_charge_frame(const char *out_dir, const char *out_name, int ascii, int nx, int ny, int nz, int ts,
+                          double time, const double *const *fields);
+int icep_avs_particles(const char *out_dir, const char *out_name, int ascii, int ts, double time,
+                       const icep_particle *particles, int n_particles, double radius);
+int icep_output_avs(icep_ctx *ctx, const char *out_dir, const char *out_name, int ascii);
 
 /* ---- phase entry points (operate on the context's device state) -------- */
 
@@ -240,7 +287,10 @@ int icep_batch_step(icep_batch *batch, int nsteps);
  * `steps_per_config` Adam steps along the chain of residuals r -> r - A P(r)
  * starting from the right-hand side; loss |r - A P(r)|^2 / |r|^2 with
  * P(r) = M^-1 (r + rms(r) prolong(net(eps, r))). The
- * context's particles and field are restored afterwards. */
+ * context's particles and field are restored afterwards. The trained
+ * parameters are kept only if their mean one-step loss on the context's own
+ * residual chain (two links) is not above the spectral preconditioner's;
+ * else the parameters from before the call come back. */
 int icep_learned_train(icep_ctx *ctx, int configs, int steps_per_config, unsigned seed, double lr, double *loss_first,
                        double *loss_last);
 /* 1: apply the network in the preconditioner, 0: spectral part only. */

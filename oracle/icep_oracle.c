@@ -1926,8 +1926,40 @@ enum {
   C_ZETA_K2U_K = 1, C_U_K2ZETA_K, C_U2ADVECTION_K, C_SOLENOIDAL_U, C_NS_SLAVED_EULER,
   C_MAKE_PHI_SUM, C_MAKE_U_SUM, C_F_HYDRO, C_LJ, C_POS_EULER, C_POS_AB2, C_VEL_EULER,
   C_VEL_AB2, C_DIELECTRIC_FIELD, C_BUILD_RHS, C_SOLVE_POTENTIAL, C_MAXWELL, C_NSSOLUTE_EULER,
-  C_SURFACE_NORMAL, C_F_PARTICLE_SOLE, C_TRUNCATE, C_CHARGE_FIELD, C_INIT_ION, C_ZETA_K2U
+  C_SURFACE_NORMAL, C_F_PARTICLE_SOLE, C_TRUNCATE, C_CHARGE_FIELD, C_INIT_ION, C_ZETA_K2U,
+  C_CHARGE_OUTPUT
 };
+
+/* The fields of Output_dielectric_charge_field_data (output.cxx:262-320)
+ * with vel, phi and charge printed: u = Zeta_k2u(zeta, uk_dc); phi = the
+ * unclipped sum of Phi and up0 = the rescaled surface charge times 4 pi a^2
+ * (Make_phi_qq_particle; 0/0 = NaN without charged particles);
+ * up1 = (sum_n e z_n c_n) (1 - phi); up2 = eps. The concentrations are
+ * transformed into scratch, not in place. */
+static void charge_output(ko_ctx *c) {
+  double *zeta[2] = {c->f[F_ZETA0], c->f[F_ZETA1]};
+  double *u[3] = {c->f[F_U0], c->f[F_U1], c->f[F_U2]};
+  double *phi = c->f[F_PHI], *up0 = c->f[F_UP0], *up1 = c->f[F_UP1], *up2 = c->f[F_UP2];
+  double *c0 = c->f[F_F0], *c1 = c->f[F_F1];
+  zeta_k2u(c, zeta, c->uk_dc, u);
+  zero_real(c, phi);
+  zero_real(c, up0);
+  make_phi_qq(c, phi, up0);
+  memcpy(c0, c->f[F_C0], sizeof(double) * c->nf);
+  memcpy(c1, c->f[F_C1], sizeof(double) * c->nf);
+  fft_c2r(c, c0);
+  fft_c2r(c, c1);
+  const double area = (4. * M_PI) * (c->radius * c->radius);
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      for (int k = 0; k < c->nz; k++) {
+        const long im = IDX(c, i, j, k);
+        const double q = c->valency_e[0] * c0[im] + c->valency_e[1] * c1[im];
+        up0[im] *= area;
+        up1[im] = q * (1. - phi[im]);
+        up2[im] = c->f[F_EPS][im];
+      }
+}
 int ko_call(ko_ctx *c, int fn) {
   double *zeta[2] = {c->f[F_ZETA0], c->f[F_ZETA1]};
   double *u[3] = {c->f[F_U0], c->f[F_U1], c->f[F_U2]};
@@ -1969,6 +2001,7 @@ int ko_call(ko_ctx *c, int fn) {
     case C_TRUNCATE: truncate_23(c, zeta[0]); truncate_23(c, zeta[1]); break;
     case C_CHARGE_FIELD: conc_k2charge(c, c->f[F_RHO], c->f[F_WORK], c->f[F_UP0]); break;
     case C_INIT_ION: init_ions(c); break;
+    case C_CHARGE_OUTPUT: charge_output(c); break;
     default: return 1;
   }
   return 0;

@@ -30,7 +30,7 @@ CALLS = ["zeta_k2u_k", "u_k2zeta_k", "u2advection_k", "solenoidal_u", "ns_slaved
          "make_phi_sum", "make_u_sum", "f_hydro", "lj", "pos_euler", "pos_ab2", "vel_euler",
          "vel_ab2", "dielectric_field", "build_rhs", "solve_potential", "maxwell",
          "nssolute_euler", "surface_normal", "f_particle_sole", "truncate", "charge_field",
-         "init_ion", "zeta_k2u"]
+         "init_ion", "zeta_k2u", "charge_output"]
 CALL_ID = {n: i + 1 for i, n in enumerate(CALLS)}
 
 _DP = C.POINTER(C.c_double)
@@ -231,6 +231,8 @@ class RefKapsel(_Base):
         L.kref_last_error.restype = C.c_double
         L.kref_matvec_count.restype = C.c_long
         L.kref_sekibun.argtypes = [C.POINTER(C.c_int)]
+        if hasattr(L, "kref_avs"):
+            L.kref_avs.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_int, C.POINTER(_DP)]
         self.params = params
         self.np = params.n_particles
         rc = L.kref_setup(C.byref(params), particles, self.np)
@@ -297,6 +299,15 @@ class RefKapsel(_Base):
 
     def matvecs(self):
         return self.lib.kref_matvec_count()
+
+    def avs(self, out_dir, name, ascii, num_snap, fields):
+        """The reference's AVS writers: headers and one frame of `fields`
+        (7 arrays [NX][NY][NZ_]) and the particles, at the set ts and time."""
+        arrs = [np.ascontiguousarray(f, dtype=np.float64) for f in fields]
+        ptrs = (_DP * 7)(*[_dp(a) for a in arrs])
+        st = self.lib.kref_avs(os.fsencode(out_dir), os.fsencode(name), int(ascii), int(num_snap), ptrs)
+        if st:
+            raise RuntimeError("kref_avs failed")
 
     def sekibun(self):
         n = self.lib.kref_np_domain()

@@ -29,6 +29,8 @@
 #include "fft_wrapper.h"
 #include "operate_omega.h"
 #include "solute_rhs.h"
+#include "avs_output.h"
+#include "avs_output_p.h"
 
 #include "../../include/icep_types.h"
 
@@ -111,6 +113,10 @@ double degree_oblique;
 double eps_fluid, eps_particle_bottom, eps_particle_top;
 double kBT;
 int AC;
+/* the AVS writers' globals (input.cxx) */
+char Out_dir[256], Out_name[256];
+OUTFORMAT SW_OUTFORMAT = OUT_NONE;
+int Num_snap;
 double **GRvecs, **GRvecs_body;
 double **forceGrs, **forceGrs_previous, **forceGs, **forceGs_previous;
 double **omegaGs, **omegaGs_old, **torqueGrs, **torqueGrs_previous;
@@ -509,8 +515,34 @@ enum {
   C_ZETA_K2U_K = 1, C_U_K2ZETA_K, C_U2ADVECTION_K, C_SOLENOIDAL_U, C_NS_SLAVED_EULER,
   C_MAKE_PHI_SUM, C_MAKE_U_SUM, C_F_HYDRO, C_LJ, C_POS_EULER, C_POS_AB2, C_VEL_EULER,
   C_VEL_AB2, C_DIELECTRIC_FIELD, C_BUILD_RHS, C_SOLVE_POTENTIAL, C_MAXWELL, C_NSSOLUTE_EULER,
-  C_SURFACE_NORMAL, C_F_PARTICLE_SOLE, C_TRUNCATE, C_CHARGE_FIELD, C_INIT_ION, C_ZETA_K2U
+  C_SURFACE_NORMAL, C_F_PARTICLE_SOLE, C_TRUNCATE, C_CHARGE_FIELD, C_INIT_ION, C_ZETA_K2U,
+  C_CHARGE_OUTPUT
 };
+
+/* The fields Output_dielectric_charge_field_data computes (output.cxx:
+ * 262-320) with vel, phi and charge printed, restated around the reference's
+ * own Zeta_k2u, Make_phi_qq_particle and FFTs (output.cxx itself needs the
+ * writers): u -> u0..u2, phi, up0 surface charge, up1 solute charge, up2 eps.
+ * The concentrations go to real space and back, as there. */
+static void charge_output() {
+  Zeta_k2u(zeta, uk_dc, u);
+  Reset_phi(phi);
+  Reset_phi(up[0]);
+  Make_phi_qq_particle(phi, up[0], particles);
+  for (int n = 0; n < N_spec; n++) A_k2a(Concentration[n]);
+  const double area = PI4 * SQ(RADIUS);
+  for (int i = 0; i < NX; i++)
+    for (int j = 0; j < NY; j++)
+      for (int k = 0; k < NZ; k++) {
+        const int im = (i * NY * NZ_) + (j * NZ_) + k;
+        double q = 0.0;
+        for (int n = 0; n < N_spec; n++) q += Elementary_charge * Valency[n] * Concentration[n][im];
+        up[0][im] *= area;
+        up[1][im] = q * (1.0 - phi[im]);
+        up[2][im] = epsilon[im];
+      }
+  for (int n = 0; n < N_spec; n++) A2a_k(Concentration[n]);
+}
 int kref_call(int fn) {
   const Index_range *ijk_range = ijk_range_two_third_filter;
   const int n_ijk_range = n_ijk_range_two_third_filter;
@@ -557,8 +589,29 @@ int kref_call(int fn) {
       else Conc_k2charge_field_no_surfase_charge(particles, Concentration, rho_free_buf, work_buf, up[0]);
       break;
     case C_INIT_ION: Init_rho_ion_dielectric(Concentration, particles, jikan); break;
+    case C_CHARGE_OUTPUT: charge_output(); break;
     default: return 1;
   }
+  return 0;
+}
+
+/* The reference's AVS writers on caller fields: Set_avs_parameters, Init_avs
+ * and Init_avs_p (avs_output.cxx:46-186, avs_output_p.cxx:13-27), then one
+ * frame: Output_avs_charge with fields[0..6] = u0 u1 u2 phi surface_charge
+ * solute_charge potential ([NX][NY][NZ_]) and Output_avs_p of the harness
+ * particles, at the harness ts and time (sp_3d_ns.cxx:482-497). */
+int kref_avs(const char *dir, const char *name, int ascii, int num_snap, const double *const *fields) {
+  snprintf(Out_dir, sizeof(Out_dir), "%s", dir);
+  snprintf(Out_name, sizeof(Out_name), "%s", name);
+  SW_OUTFORMAT = ascii ? OUT_AVS_ASCII : OUT_AVS_BINARY;
+  Num_snap = num_snap;
+  Set_avs_parameters(Avs_parameters);
+  Init_avs(Avs_parameters);
+  if (Particle_Number > 0) Init_avs_p(Avs_parameters);
+  double *uf[DIM] = {(double *)fields[0], (double *)fields[1], (double *)fields[2]};
+  Output_avs_charge(Avs_parameters, uf, (double *)fields[3], (double *)fields[4], (double *)fields[5],
+                    (double *)fields[6], jikan);
+  if (Particle_Number > 0) Output_avs_p(Avs_parameters, particles, jikan);
   return 0;
 }
 

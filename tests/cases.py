@@ -83,6 +83,32 @@ def ac_case(frequency=8.0, tol=1e-7, solver=abi.SOLVER_REF, precision=abi.FP64):
     return p, parts
 
 
+def splitmix64(n, seed):
+    """n pseudo-random uint64 (splitmix64), reproducible on any numpy."""
+    with np.errstate(over="ignore"):
+        z = (np.uint64(seed) + np.arange(1, n + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        return z ^ (z >> np.uint64(31))
+
+
+def avs_inputs(nx, ny, nz, npart, seed=7):
+    """Inputs for the AVS writers: 7 fields in the [NX][NY][NZ_] layout with
+    values of ~40 significant bits (so the float32 cast rounds) and signs,
+    particle positions in the box and unit quaternions."""
+    nz_ = 2 * (nz // 2 + 1)
+    n = nx * ny * nz_
+    fields = []
+    for v in range(7):
+        r = splitmix64(n, seed + v).astype(np.float64) / 2.0 ** 64  # [0, 1)
+        fields.append(np.ascontiguousarray(((r - 0.5) * 10.0 ** (v - 3)).reshape(nx, ny, nz_)))
+    r = splitmix64(npart * 7, seed + 100).astype(np.float64) / 2.0 ** 64
+    x = r[:3 * npart].reshape(npart, 3) * np.array([nx, ny, nz], dtype=np.float64)
+    q = r[3 * npart:].reshape(npart, 4) - 0.5
+    q = q / np.sqrt((q * q).sum(axis=1, keepdims=True))
+    return fields, x, q
+
+
 def unit_quaternions(n, seed):
     """n orientations uniform on the rotation group (normalised Gaussian 4-vectors)."""
     q = np.random.default_rng(seed).standard_normal((n, 4))

@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32", "janus32", "charged32", "ac32"]
+CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32", "janus32", "charged32", "ac32", "out32", "avs16"]
 
 
 def small_case():
@@ -250,6 +250,59 @@ def run_case(name, out):
         data["pot"] = r.get("pot")[:, :, :32]
         for k, v in abi.particles_to_numpy(r.particles(), p.n_particles).items():
             data["p_" + k] = v
+    elif name == "out32":
+        # the field output (Output_dielectric_charge_field_data's fields) of
+        # the charged case after its initial solve, with a flow: zeta from
+        # the icep32 fixture and a mean velocity uk_dc
+        ic = np.load(os.path.join(HERE, "icep32.npz"))
+        p, parts = cases.charged_case()
+        r = pyoracle.RefKapsel(p, parts)
+        r.init_state()
+        r.set("zeta0", ic["zeta0"])
+        r.set("zeta1", ic["zeta1"])
+        r.set_uk_dc(np.array([30.0, -60.0, 15.0]))  # the k = 0 coefficient: N times the mean
+        r.call("charge_output")
+        for k in ("u0", "u1", "u2", "phi", "up0", "up1", "up2"):
+            data[k] = r.get(k)[:, :, :32]
+        data["pot"] = r.get("pot")[:, :, :32]
+        # uncharged particles: the surface charge's rescale is 0/0
+        q, qparts = cases.icep_case()
+        t = pyoracle.RefKapsel(q, qparts)
+        t.init_state()
+        t.call("charge_output")
+        meta["uncharged_surface_all_nan"] = bool(np.all(np.isnan(t.get("up0")[:, :, :32])))
+    elif name == "avs16":
+        # the reference's AVS writers (binary and ASCII) on seeded fields and
+        # particles: the SHA-256 of every file they write, and the text of
+        # the headers (the scratch directories are removed afterwards)
+        import hashlib
+        import shutil
+        p, _ = small_case()
+        fields, x, q = cases.avs_inputs(16, 16, 16, p.n_particles)
+        parts = abi.make_particles(x)
+        for i in range(p.n_particles):
+            for d in range(4):
+                parts[i].q[d] = q[i, d]
+                parts[i].q_old[d] = q[i, d]
+        r = pyoracle.RefKapsel(p, parts)
+        r.set_ts(20, 0.25)
+        files, text = {}, {}
+        for ascii in (0, 1):
+            d = os.path.join(HERE, "_avs16_scratch_%d" % ascii)
+            shutil.rmtree(d, ignore_errors=True)
+            os.makedirs(d)
+            r.avs(d, "data", ascii, 5, fields)
+            for root, _, names in os.walk(d):
+                for nm in names:
+                    path = os.path.join(root, nm)
+                    rel = "%d/%s" % (ascii, os.path.relpath(path, d))
+                    blob = open(path, "rb").read()
+                    files[rel] = [hashlib.sha256(blob).hexdigest(), len(blob)]
+                    if nm.endswith(".fld") or nm == "data.cod":
+                        text[rel] = blob.decode()
+            shutil.rmtree(d)
+        meta["files"] = files
+        meta["text"] = text
     else:
         raise ValueError(name)
     meta["params"] = abi.params_dict(p)

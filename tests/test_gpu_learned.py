@@ -86,8 +86,9 @@ def test_learned_solve_matches_plain():
     print("\none-step loss on the context's residuals: spectral %.4f, learned before %.4f after %.4f"
           % (ls1, ll0, ll1))
     # the trained correction never makes the preconditioner worse than the
-    # spectral one alone (on this problem it gains little: the measured
-    # numbers are printed above and reported by bench.py)
+    # spectral one alone: learned_train keeps its parameters only when they
+    # do not (on this problem it gains little: the measured numbers are
+    # printed above and reported by bench.py)
     assert ll1 <= ls1 * 1.001
     plain.step(3)
     lrn.step(3)

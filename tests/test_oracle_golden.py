@@ -250,3 +250,33 @@ def test_ac32(oracle_so):
     d.step(3)
     b = d.get("pot")[:, :, :32]
     assert rel(b - b.mean(), g["pot"] - g["pot"].mean()) > 0.05
+
+
+def test_out32(oracle_so):
+    """The fields of the field output (Output_dielectric_charge_field_data,
+    restated in the reference harness around its own Zeta_k2u and
+    Make_phi_qq_particle): u with a mean flow, the unclipped phi, the
+    surface charge times 4 pi a^2, the solute charge and eps; with uncharged
+    particles the surface charge is 0/0 = NaN in the reference and here."""
+    g, meta = load("out32")
+    ic, _ = load("icep32")
+    p, parts = cases.charged_case()
+    o = pyoracle.Oracle(p, parts, so=oracle_so)
+    o.init_state()
+    o.set("zeta0", ic["zeta0"])
+    o.set("zeta1", ic["zeta1"])
+    o.set_uk_dc(np.array([30.0, -60.0, 15.0]))
+    o.call("charge_output")
+    for k in ("u0", "u1", "u2"):
+        assert rel(o.get(k)[:, :, :32], g[k]) < 1e-13, k
+    assert abs(g["u0"].mean() - 30.0 / 32 ** 3) < 1e-15
+    assert rel(o.get("phi")[:, :, :32], g["phi"]) < 1e-14
+    assert rel(o.get("up0")[:, :, :32], g["up0"]) < 1e-13
+    assert rel(o.get("up1")[:, :, :32], g["up1"]) < 1e-12
+    assert rel(o.get("up2")[:, :, :32], g["up2"]) < 1e-13
+    assert meta["uncharged_surface_all_nan"]
+    q, qparts = cases.icep_case()
+    t = pyoracle.Oracle(q, qparts, so=oracle_so)
+    t.init_state()
+    t.call("charge_output")
+    assert np.all(np.isnan(t.get("up0")[:, :, :32]))

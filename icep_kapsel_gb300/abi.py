@@ -62,6 +62,9 @@ class Params(C.Structure):
         ("surface_charge", C.c_double * MAX_SPECIES),
         ("ac", C.c_int),
         ("frequency", C.c_double),
+        ("salt_free", C.c_int),
+        ("valency_counterion", C.c_double),
+        ("onsager_counterion", C.c_double),
     ]
 
 

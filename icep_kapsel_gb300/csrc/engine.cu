@@ -95,6 +95,7 @@ class Engine : public EngineBase {
   bool mixed = false;
   bool janus = false;  // Janus permittivity field (particle 0's species has an axis)
   bool have_sc = false;  // charged particles (Conc_k2charge_field with Make_phi_qq_particle)
+  bool salt_free = false;  // one ion species (N_spec = 1), the counterions
   // optional per-phase device timing of the step (CUDA events at phase
   // boundaries, accumulated in ms)
   static constexpr int NPH = 10;
@@ -186,6 +187,19 @@ class Engine : public EngineBase {
       if ((p.surface_charge[q] != 0.0) != have_sc)
         return fail(ICEP_ERR_ARG, "surface charges must be non-zero for every species or for none");
     if (have_sc && p.sw_eq != ICEP_ELECTROLYTE) return fail(ICEP_ERR_ARG, "surface charges need the Electrolyte model");
+    // salt-free: the counterions of charged particles of one sign, the
+    // counterions' valency opposite to it (Init_rho_ion_dielectric's
+    // no-charge branch needs two species; Init_rho_ion,
+    // operate_electrolyte.cxx:740-787, exits otherwise)
+    salt_free = p.sw_eq == ICEP_ELECTROLYTE && p.salt_free != 0;
+    if (salt_free) {
+      if (!have_sc) return fail(ICEP_ERR_ARG, "salt-free electrolyte needs charged particles");
+      for (int q = 0; q < p.n_species; q++)
+        if (p.surface_charge[q] * p.surface_charge[0] <= 0.)
+          return fail(ICEP_ERR_ARG, "salt-free electrolyte with particles of both signs");
+      if (p.valency_counterion * p.surface_charge[0] >= 0.)
+        return fail(ICEP_ERR_ARG, "counterion valency must be opposite to the surface charge");
+    }
     if (janus) {
       if (p.per_particle_eps) return fail(ICEP_ERR_ARG, "Janus particles with per-particle permittivity");
       for (int q = 0; q < n; q++)
@@ -217,6 +231,12 @@ class Engine : public EngineBase {
     valency_e[1] = p.valency_neg * p.elementary_charge;
     onsager[0] = p.onsager_pos;
     onsager[1] = p.onsager_neg;
+    if (salt_free) {  // N_spec = 1: the second species is absent (zero)
+      valency_e[0] = p.valency_counterion * p.elementary_charge;
+      valency_e[1] = 0.0;
+      onsager[0] = p.onsager_counterion;
+      onsager[1] = 0.0;
+    }
     const size_t fb = sizeof(R) * g.nf();
     for (int i = 0; i < F_COUNT; i++) {
       if (cudaMalloc(&f[i], fb) != cudaSuccess) return fail(ICEP_ERR_CUDA, "cudaMalloc of fields failed");
@@ -1401,7 +1421,7 @@ class Engine : public EngineBase {
     zeta_k2u();
     for (int d = 0; d < 3; d++) zero(F_SN0 + d);
     scatter_normal<R>(pp, dp, dsek, f[F_SN0], f[F_SN1], f[F_SN2], s);
-    for (int n = 0; n < 2; n++) {
+    for (int n = 0; n < (salt_free ? 1 : 2); n++) {  // F_CRHS1 stays zero without a second species
       truncate_23<R>(g, batch(f[F_C0 + n]), s);
       // Diffusion_flux_single: grad(kBT L c)
       grad_k<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], (R)(P.kbt * onsager[n]), false, nullptr, s);
@@ -1512,6 +1532,20 @@ class Engine : public EngineBase {
       rho_inf *= P.eps_fluid;
       cp = pos / (volume_phi * dx3) + rho_inf / (z0 * (z0 - z1));
       cm = neg / (volume_phi * dx3) + -rho_inf / (z1 * (z0 - z1));
+      if (salt_free) {
+        // Set_uniform_ion_charge_density_nosalt (operate_electrolyte.cxx:459-493):
+        // Counterion_number = -sum_i Surface_charge_i N_i / Valency_counterion
+        // over the fluid volume, the same density everywhere
+        double surface_ion_number = 0.;
+        for (int sp = 0; sp < P.n_species; sp++) {
+          int cnt = 0;
+          for (int q = 0; q < np; q++) cnt += (hp[q].spec == sp);
+          surface_ion_number -= P.surface_charge[sp] * cnt;
+        }
+        const double counterion_number = surface_ion_number / P.valency_counterion;
+        cp = counterion_number / (volume_phi * dx3);
+        cm = 0.0;
+      }
     }
     for (int n = 0; n < 2; n++) {
       zero(F_C0 + n);

@@ -460,13 +460,23 @@ static bool fill(Bound &b, Result &r) {
         !b.num(dp + "particle_bottom", p.eps_particle_bottom))
       return bad(r, b);
     if (!b.str(ce + "Add_salt.type", v)) return bad(r, b);
-    if (v != "salt") return unsupported(r, "Add_salt " + v + " (this path is the salt solution)");
-    const std::string sa = ce + "Add_salt.salt.";
-    if (!b.num(sa + "Valency_positive_ion", p.valency_pos) || !b.num(sa + "Valency_negative_ion", p.valency_neg) ||
-        !b.num(sa + "Onsager_coeff_positive_ion", p.onsager_pos) ||
-        !b.num(sa + "Onsager_coeff_negative_ion", p.onsager_neg) || !b.num(sa + "Debye_length", p.debye_length))
+    if (v == "saltfree") {  // N_spec = 1: the counterions only (input.cxx:756-766)
+      const std::string sf = ce + "Add_salt.saltfree.";
+      p.salt_free = 1;
+      if (!b.num(sf + "Valency_counterion", p.valency_counterion) ||
+          !b.num(sf + "Onsager_coeff_counterion", p.onsager_counterion))
+        return bad(r, b);
+      max_onsager = p.onsager_counterion;
+    } else if (v == "salt") {
+      const std::string sa = ce + "Add_salt.salt.";
+      if (!b.num(sa + "Valency_positive_ion", p.valency_pos) || !b.num(sa + "Valency_negative_ion", p.valency_neg) ||
+          !b.num(sa + "Onsager_coeff_positive_ion", p.onsager_pos) ||
+          !b.num(sa + "Onsager_coeff_negative_ion", p.onsager_neg) || !b.num(sa + "Debye_length", p.debye_length))
+        return bad(r, b);
+      max_onsager = p.onsager_pos > p.onsager_neg ? p.onsager_pos : p.onsager_neg;
+    } else {
       return bad(r, b);
-    max_onsager = p.onsager_pos > p.onsager_neg ? p.onsager_pos : p.onsager_neg;
+    }
     if (!b.str(ce + "Electric_field.type", v)) return bad(r, b);
     if (v == "ON") {
       if (!b.str(ce + "Electric_field.ON.type", v)) return bad(r, b);

@@ -78,7 +78,8 @@ int icep_step(icep_ctx *ctx, int nsteps);
 /*
  * Drop-in form of one call of Time_evolution (sp_3d_ns.cxx:10) on host
  * arrays: zeta (2 fields), uk_dc[3], conc (2 k-space fields, Electrolyte
- * only, may be NULL), potential (1 real field, Dielectric only, may be NULL)
+ * only, may be NULL; a salt-free run has one, conc1 NULL), potential (1 real
+ * field, Dielectric only, may be NULL)
  * and the particle array are uploaded, nsteps steps run on the GPU, and the
  * same arrays are written back.
  */
@@ -118,8 +119,7 @@ int icep_save_checkpoint(icep_ctx *ctx, const char *path);
  * GTS * Num_snap steps). particles may be NULL to query n_particles; else it
  * needs max_particles >= n_particles. Returns ICEP_ERR_UNSUPPORTED (with the
  * reason in err) for settings outside this path: shear flows, chains and
- * rigid bodies, Dielectric_property OFF, salt-free
- * electrolytes, pinned particles, lattice or random-walk
+ * rigid bodies, Dielectric_property OFF, pinned particles, lattice or random-walk
  * initial configurations, resumed runs (use icep_load_checkpoint). */
 int icep_udf_read(const char *path, icep_params *params, icep_particle *particles, int max_particles,
                   int *n_particles, int *gts, int *num_snap, char *err, int err_len);

@@ -116,6 +116,15 @@ typedef struct icep_params {
    * 231-244; Init_potential_dielectric at t = 0) */
   int ac;
   double frequency;
+  /* Add_salt saltfree (input.cxx:751-766): salt_free = 1 runs one ion
+   * species, the counterions of the charged particles (N_spec = 1,
+   * Valency_counterion, Onsager_coeff_counterion; Init_rho_ion,
+   * operate_electrolyte.cxx:738-862); every species needs a surface charge
+   * of one sign, opposite to the counterions'. 0: the salt solution. The
+   * second concentration field stays zero. */
+  int salt_free;
+  double valency_counterion;
+  double onsager_counterion;
 } icep_params;
 
 /*

@@ -1729,12 +1729,25 @@ static void time_evolution_hydro(ko_ctx *c) {
 /* Init_rho_ion_dielectric without surface charge (operate_electrolyte.cxx:912-979)
  * with Set_uniform_ion_charge_density_salt_dielectric (:864-910): uniform
  * salt concentrations rho_inf/(z_n (z_+ - z_-)), transformed to k-space. */
+/* Salt-free (N_spec = 1): species 0 are the counterions (Valency_counterion,
+ * Onsager_coeff_counterion, Init_rho_ion, operate_electrolyte.cxx:755-758);
+ * species 1 is absent: zero valency, mobility and concentration, so every
+ * sum over species adds exact zeros. */
+static void set_salt_free_species(ko_ctx *c) {
+  if (!c->P.salt_free) return;
+  c->valency_e[0] = c->P.valency_counterion * c->P.elementary_charge;
+  c->valency_e[1] = 0.0;
+  c->onsager[0] = c->P.onsager_counterion;
+  c->onsager[1] = 0.0;
+}
+
 static void init_ions(ko_ctx *c) {
   const double z0 = c->P.valency_pos, z1 = c->P.valency_neg;
   c->valency_e[0] = z0 * c->P.elementary_charge;
   c->valency_e[1] = z1 * c->P.elementary_charge;
   c->onsager[0] = c->P.onsager_pos;
   c->onsager[1] = c->P.onsager_neg;
+  set_salt_free_species(c);
   make_phi_particle(c, c->f[F_PHI]);
   double rho_inf = c->P.kbt * c->P.dielectric_cst * c->P.eps_fluid /
                    SQ(c->P.elementary_charge * c->P.debye_length * c->radius);
@@ -1761,6 +1774,22 @@ static void init_ions(ko_ctx *c) {
     rho_inf *= c->P.eps_fluid;
     cp = pos / (volume_phi * c->dx3) + rho_inf / (z0 * (z0 - z1));
     cm = neg / (volume_phi * c->dx3) + -rho_inf / (z1 * (z0 - z1));
+    if (c->P.salt_free) {
+      /* N_spec = 1 (Init_rho_ion, operate_electrolyte.cxx:740-787, and
+       * Set_uniform_ion_charge_density_nosalt, :459-493): the counterions
+       * -sum_i Q_i N_i / z_c spread evenly at Counterion_number over the
+       * fluid volume (the reference's OpenMP loop there marks the density
+       * private, uninitialised in each thread; this is the serial meaning) */
+      double surface_ion_number = 0.;
+      for (int sp = 0; sp < c->P.n_species; sp++) {
+        int cnt = 0;
+        for (int n = 0; n < c->np; n++) cnt += (c->p[n].spec == sp);
+        surface_ion_number -= c->P.surface_charge[sp] * cnt;
+      }
+      const double counterion_number = surface_ion_number / c->P.valency_counterion;
+      cp = counterion_number / (volume_phi * c->dx3);
+      cm = 0.0;
+    }
   }
   for (int n = 0; n < 2; n++) {
     double *cf = c->f[F_C0 + n];
@@ -1844,6 +1873,7 @@ ko_ctx *ko_create(const icep_params *P, const icep_particle *p, int np) {
   c->valency_e[1] = P->valency_neg * P->elementary_charge;
   c->onsager[0] = P->onsager_pos;
   c->onsager[1] = P->onsager_neg;
+  set_salt_free_species(c);
   build_sekibun(c);
   c->np = np;
   c->p = (icep_particle *)calloc(np > 0 ? np : 1, sizeof(icep_particle));

@@ -128,6 +128,7 @@ extern void (*Charge_field2potential_dielectric)(double *, double *, double *, d
 
 /* ---- harness state (main()'s locals, sp_3d_ns.cxx:404-420) ---------------- */
 static double *zeta[DIM - 1];
+static double *c1_absent = nullptr;  // c1 of a salt-free run (N_spec = 1)
 static double uk_dc[DIM];
 static CTime jikan;
 static Particle *particles = nullptr;
@@ -238,7 +239,9 @@ static void set_globals(const icep_params *q) {
   for (int d = 0; d < DIM; d++) E_ext[d] = q->e_ext[d];
   AC = q->ac ? 1 : 0;  // Electric_field.ON.AC (input.cxx:826-845, 370-374)
   Angular_Frequency = 2.0 * M_PI * q->frequency;
-  N_spec = 2;
+  N_spec = q->salt_free ? 1 : 2;  // Add_salt saltfree / salt (input.cxx:751-770)
+  Valency_counterion = q->valency_counterion;
+  Onsager_coeff_counterion = q->onsager_counterion;
   Poisson_Boltzmann = 0;
   Rigid_Number = 0;
   degree_oblique = 0.0;
@@ -284,6 +287,10 @@ static void mem_alloc() {
       memset(Concentration_rhs1[n], 0, bytes);
     }
     for (int d = 0; d < DIM; d++) memset(Surface_normal[d], 0, bytes);
+    if (N_spec == 1) {  // the registry's c1 of a salt-free run: zeros
+      c1_absent = dalloc(NX * NY * NZ_);
+      memset(c1_absent, 0, bytes);
+    }
     if (Dielectric) {
       memset(Potential, 0, bytes);
       memset(epsilon, 0, bytes);
@@ -480,7 +487,7 @@ static double *field_ptr(int id) {
     case F_EPS: return epsilon;
     case F_GE0: case F_GE1: case F_GE2: return grad_epsilon ? grad_epsilon[id - F_GE0] : nullptr;
     case F_C0: return Concentration ? Concentration[0] : nullptr;
-    case F_C1: return Concentration ? Concentration[1] : nullptr;
+    case F_C1: return Concentration ? (N_spec > 1 ? Concentration[1] : c1_absent) : nullptr;
     case F_RHO: return rho_free_buf;
     case F_WORK: return work_buf;
     case F_SN0: case F_SN1: case F_SN2: return Surface_normal ? Surface_normal[id - F_SN0] : nullptr;

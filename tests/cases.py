@@ -148,6 +148,22 @@ def charged_case(n=32, npart=4, seed=2, charges=(-5.0,), tol=1e-7, solver=abi.SO
     return p, abi.make_particles(x, spec=[i % len(charges) for i in range(npart)])
 
 
+def saltfree_case(n=32, npart=4, seed=2, charges=(-5.0, -3.0), tol=1e-7, solver=abi.SOLVER_REF,
+                  precision=abi.FP64, valency=1.0, onsager=7.24):
+    """Charged particles with their counterions only (Add_salt saltfree,
+    N_spec = 1): two negatively charged species, monovalent counterions;
+    the salt keys are zeroed to show they are not used."""
+    p, parts = charged_case(n=n, npart=npart, seed=seed, charges=charges, tol=tol, solver=solver,
+                            precision=precision)
+    p.salt_free = 1
+    p.valency_counterion = valency
+    p.onsager_counterion = onsager
+    p.valency_pos = p.valency_neg = 0.0
+    p.onsager_pos = p.onsager_neg = 0.0
+    p.debye_length = 0.0
+    return p, parts
+
+
 def lj_dense_case(n=32, npart=24, seed=7, minsep=7.2):
     """Particles closer than the WCA cutoff (2^(1/6) * 8 = 8.98) so that the
     cell-list scan and its multiplicity at 32^3 (2 cells per side) matter."""

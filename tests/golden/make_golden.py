@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32", "janus32", "charged32", "ac32", "out32", "avs16"]
+CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32", "janus32", "charged32", "ac32", "out32", "avs16", "saltfree32"]
 
 
 def small_case():
@@ -303,6 +303,18 @@ def run_case(name, out):
             shutil.rmtree(d)
         meta["files"] = files
         meta["text"] = text
+    elif name == "saltfree32":
+        # counterions only (N_spec = 1): the uniform counterion density over
+        # the fluid volume, the charge field and the initial potential
+        p, parts = cases.saltfree_case()
+        r = pyoracle.RefKapsel(p, parts)
+        r.init_state()
+        meta["init_iterations"] = int(r.last_iterations())
+        meta["init_error"] = float(r.last_error())
+        data["c0"] = r.get("c0")
+        data["pot"] = r.get("pot")[:, :, :32]
+        r.call("charge_field")
+        data["rho"] = r.get("rho")[:, :, :32]
     else:
         raise ValueError(name)
     meta["params"] = abi.params_dict(p)

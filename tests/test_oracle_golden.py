@@ -280,3 +280,22 @@ def test_out32(oracle_so):
     t.init_state()
     t.call("charge_output")
     assert np.all(np.isnan(t.get("up0")[:, :, :32]))
+
+
+def test_saltfree32(oracle_so):
+    """Salt-free electrolyte (Add_salt saltfree, N_spec = 1): the counterions
+    of two negatively charged species spread evenly over the fluid volume
+    (Init_rho_ion with Set_uniform_ion_charge_density_nosalt), the charge
+    field and the initial potential; the absent second species stays zero."""
+    g, meta = load("saltfree32")
+    p, parts = cases.saltfree_case()
+    o = pyoracle.Oracle(p, parts, so=oracle_so)
+    o.init_state()
+    assert rel(o.get("c0"), g["c0"]) < 1e-14
+    assert np.abs(o.get("c1")).max() == 0.0
+    # 16 counterions (charges -5, -3 on two particles each) over the fluid volume
+    assert abs(g["c0"][0, 0, 0] / 32 ** 3 * (32 ** 3 - 4 * 268.0) - 16.0) < 0.5
+    a = o.get("pot")[:, :, :32]
+    assert rel(a - a.mean(), g["pot"] - g["pot"].mean()) < 2e-5
+    o.call("charge_field")
+    assert rel(o.get("rho")[:, :, :32], g["rho"]) < 1e-12

@@ -99,9 +99,26 @@ def test_ac_field(rt, tmp_path):
     assert p.ac == 0
 
 
+def test_saltfree(rt, tmp_path):
+    """Add_salt saltfree: one ion species with the counterion valency and
+    Onsager coefficient, which also sets the diffusive time of the auto time
+    step (input.cxx:355-360)."""
+    path = rewrite(tmp_path, '{"salt", {1.0, 7.24}{1.0, -1.0, 7.24, 7.24, 10.0}}',
+                   '{"saltfree", {2.0, 3.5}{1.0, -1.0, 7.24, 7.24, 10.0}}')
+    p, _, _, _ = rt.udf_read(path)
+    assert (p.salt_free, p.valency_counterion, p.onsager_counterion) == (1, 2.0, 3.5)
+    d = tmp_path / "udf"
+    (d / "input.udf").write_text((d / "input.udf").read_text().replace(
+        'time_increment:{"manual",{1.0}{0.01}}', 'time_increment:{"auto",{1.0}{0.01}}'))
+    p, _, _, _ = rt.udf_read(str(d / "input.udf"))
+    kmax2 = 3 * (2 * np.pi / 32 * 11) ** 2
+    assert abs(p.dt - 1.0 / (1.0 * 3.5 * kmax2)) < 1e-15
+    p, _, _, _ = rt.udf_read(FIX)
+    assert p.salt_free == 0
+
+
 @pytest.mark.parametrize("old,new", [
     ('"Uniform",', '"Poisson_Boltzmann",'),
-    ('{"salt", {1.0, 7.24}', '{"saltfree", {1.0, 7.24}'),
     ('{"user_specify",\n', '{"uniform_random",\n'),  # fine: placement by rand()
 ])
 def test_unsupported_or_changed(rt, tmp_path, old, new):

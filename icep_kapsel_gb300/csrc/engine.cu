@@ -1645,8 +1645,8 @@ class Engine : public EngineBase {
     }
     if (same) return ICEP_OK;
     x64_valid = xp_valid = pot_export_valid = false;
-    if (sizeof(R) == sizeof(double)) cudaMemcpyAsync(f[F_POT], dev, sizeof(double) * g.nf(), cudaMemcpyDeviceToDevice, s);
-    else convert_d2f(g.nf(), dev, (float *)f[F_POT], s);
+    if (sizeof(R) == sizeof(double)) cudaMemcpyAsync(f[F_POT], dev, sizeof(double) * g.nf(), cudaMemcpyDefault, s);
+    else link_d2f(g.nf(), dev, (float *)f[F_POT], s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_field");
     return ICEP_OK;
   }
@@ -1655,22 +1655,29 @@ class Engine : public EngineBase {
     if (!stage_n[k] && cudaMalloc(&stage_n[k], sizeof(double) * g.nf()) != cudaSuccess) return nullptr;
     return stage_n[k];
   }
+  // Host arrays pinned through icep_pin_host are read and written by the
+  // conversion kernels themselves over the CPU-GPU link (no staging copy);
+  // others go through device staging buffers and the copy engines.
   int set_fields(const int *ids, const double *const *host, int n) override {
     const long nf = g.nf();
-    int pot_k = -1;
+    const double *pot_src = nullptr;
     for (int k = 0; k < n; k++) {
       if (ids[k] < 0 || ids[k] >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
       if (sizeof(R) == sizeof(double) && !(ids[k] == F_POT && mixed)) {
         cudaMemcpyAsync(f[ids[k]], host[k], sizeof(double) * nf, cudaMemcpyHostToDevice, s);
         continue;
       }
-      double *st = stage_buf(k);
-      if (!st) return fail(ICEP_ERR_CUDA, "staging buffers");
-      cudaMemcpyAsync(st, host[k], sizeof(double) * nf, cudaMemcpyHostToDevice, s);
-      if (ids[k] == F_POT && mixed) pot_k = k;
-      else convert_d2f(nf, st, (float *)f[ids[k]], s);
+      const double *src = static_cast<const double *>(host_mapped(host[k], sizeof(double) * nf));
+      if (!src) {
+        double *st = stage_buf(k);
+        if (!st) return fail(ICEP_ERR_CUDA, "staging buffers");
+        cudaMemcpyAsync(st, host[k], sizeof(double) * nf, cudaMemcpyHostToDevice, s);
+        src = st;
+      }
+      if (ids[k] == F_POT && mixed) pot_src = src;
+      else link_d2f(nf, src, (float *)f[ids[k]], s);
     }
-    if (pot_k >= 0) return import_potential(stage_n[pot_k]);  // synchronises
+    if (pot_src) return import_potential(pot_src);  // synchronises
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_fields");
     return ICEP_OK;
   }
@@ -1682,14 +1689,21 @@ class Engine : public EngineBase {
         cudaMemcpyAsync(host[k], f[ids[k]], sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
         continue;
       }
-      double *st = stage_buf(k);
-      if (!st) return fail(ICEP_ERR_CUDA, "staging buffers");
+      double *dst = static_cast<double *>(host_mapped(host[k], sizeof(double) * nf));
       if (ids[k] == F_POT && mixed && x64_valid) {
+        double *st = stage_buf(k);
+        if (!st) return fail(ICEP_ERR_CUDA, "staging buffers");
         if (export_potential(st)) return fail(ICEP_ERR_CUDA, "potential export");
+        if (dst) link_copy(nf, st, dst, s);
+        else cudaMemcpyAsync(host[k], st, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
+      } else if (dst) {
+        link_f2d(nf, (const float *)f[ids[k]], dst, s);
       } else {
+        double *st = stage_buf(k);
+        if (!st) return fail(ICEP_ERR_CUDA, "staging buffers");
         convert_f2d(nf, (const float *)f[ids[k]], st, s);
+        cudaMemcpyAsync(host[k], st, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
       }
-      cudaMemcpyAsync(host[k], st, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
     }
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_fields");
     return ICEP_OK;

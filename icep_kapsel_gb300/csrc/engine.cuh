@@ -71,6 +71,9 @@ struct EngineBase {
 };
 
 EngineBase *make_engine(const icep_params &p, const icep_particle *parts, int np, int *status, std::string &err);
+// The device address of host memory [p, p + bytes) when it lies inside one
+// range pinned (mapped) through icep_pin_host, else nullptr.
+void *host_mapped(const void *p, size_t bytes);
 
 // ids of Engine::call (same numbering as the oracle's ko_call)
 enum CallId {

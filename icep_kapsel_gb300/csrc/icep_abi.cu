@@ -1,7 +1,10 @@
 // icep_abi.cu -- the extern "C" entry points declared in include/icep_gb300.h.
 #include <string.h>
 
+#include <stdint.h>
+
 #include <algorithm>
+#include <mutex>
 #include <atomic>
 #include <string>
 #include <thread>
@@ -12,7 +15,26 @@
 
 namespace icep {
 unsigned long long g_kernel_launches = 0;
+
+// Host ranges pinned through icep_pin_host, registered as mapped: the
+// drop-in calls read and write them from kernels over the CPU-GPU link.
+namespace {
+struct PinRange {
+  uintptr_t lo;
+  size_t n;
+  char *dev;
+};
+std::mutex g_pin_mu;
+std::vector<PinRange> g_pins;
+}  // namespace
+void *host_mapped(const void *p, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_pin_mu);
+  const uintptr_t a = (uintptr_t)p;
+  for (const PinRange &r : g_pins)
+    if (a >= r.lo && bytes <= r.n && a - r.lo <= r.n - bytes) return r.dev + (a - r.lo);
+  return nullptr;
 }
+}  // namespace icep
 
 struct icep_ctx {
   icep::EngineBase *e = nullptr;
@@ -225,9 +247,27 @@ int icep_phase_times(icep_ctx *c, double *ms, int n) {
 }
 unsigned long long icep_kernel_launches(void) { return __atomic_load_n(&icep::g_kernel_launches, __ATOMIC_RELAXED); }
 int icep_pin_host(void *p, size_t bytes) {
-  return (p && cudaHostRegister(p, bytes, cudaHostRegisterDefault) == cudaSuccess) ? ICEP_OK : ICEP_ERR_CUDA;
+  if (!p || !bytes) return ICEP_ERR_ARG;
+  if (cudaHostRegister(p, bytes, cudaHostRegisterMapped) != cudaSuccess) return ICEP_ERR_CUDA;
+  void *dev = nullptr;
+  if (cudaHostGetDevicePointer(&dev, p, 0) == cudaSuccess && dev) {
+    std::lock_guard<std::mutex> lk(icep::g_pin_mu);
+    icep::g_pins.push_back(icep::PinRange{(uintptr_t)p, bytes, (char *)dev});
+  } else {
+    cudaGetLastError();  // pinned, not mapped: the calls stage through device buffers
+  }
+  return ICEP_OK;
 }
-int icep_unpin_host(void *p) { return (p && cudaHostUnregister(p) == cudaSuccess) ? ICEP_OK : ICEP_ERR_CUDA; }
+int icep_unpin_host(void *p) {
+  if (!p) return ICEP_ERR_ARG;
+  {
+    std::lock_guard<std::mutex> lk(icep::g_pin_mu);
+    for (size_t k = 0; k < icep::g_pins.size();)
+      if (icep::g_pins[k].lo == (uintptr_t)p) icep::g_pins.erase(icep::g_pins.begin() + (long)k);
+      else k++;
+  }
+  return cudaHostUnregister(p) == cudaSuccess ? ICEP_OK : ICEP_ERR_CUDA;
+}
 
 /* generic dispatch used by the Python layer (same numbering as the oracle) */
 int icep_call(icep_ctx *c, int fn) { return ok(c) ? wrap(c, c->e->call(fn)) : ICEP_ERR_ARG; }

@@ -1,4 +1,6 @@
 // krylov.cu -- see krylov.cuh.
+#include <stdint.h>
+
 #include "krylov.cuh"
 
 namespace icep {
@@ -156,6 +158,25 @@ __global__ void k_d2f(long n, const double *x, float *y) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) y[t] = (float)x[t];
 }
+// Conversions that read or write host memory mapped into the device's
+// address space: 16-byte accesses (two values per thread and iteration) and
+// a grid of a few blocks per SM striding over the array, so that many
+// requests cross the CPU-GPU link at once.
+__global__ void k_d2f_link(long n2, const double2 *__restrict__ x, float2 *__restrict__ y) {
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n2; t += (long)gridDim.x * blockDim.x) {
+    const double2 v = x[t];
+    y[t] = make_float2((float)v.x, (float)v.y);
+  }
+}
+__global__ void k_f2d_link(long n2, const float2 *__restrict__ x, double2 *__restrict__ y) {
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n2; t += (long)gridDim.x * blockDim.x) {
+    const float2 v = x[t];
+    y[t] = make_double2((double)v.x, (double)v.y);
+  }
+}
+__global__ void k_copy_link(long n2, const double2 *__restrict__ x, double2 *__restrict__ y) {
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n2; t += (long)gridDim.x * blockDim.x) y[t] = x[t];
+}
 // element-wise over all n values (k-space arrays included)
 __global__ void k_scale_d2f_all(long n, const double *x, float *y, double a) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -245,6 +266,36 @@ void convert_f2d(long n, const float *x, double *y, cudaStream_t s) {
 void convert_d2f(long n, const double *x, float *y, cudaStream_t s) {
   count_launch();
   k_d2f<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y);
+}
+namespace {
+bool link_ok(long n, const void *a, const void *b) {
+  return (n % 2) == 0 && ((uintptr_t)a % 16) == 0 && ((uintptr_t)b % 16) == 0;
+}
+unsigned link_blocks(long n2) {
+  const long want = (n2 + TPB - 1) / TPB, cap = 152L * 8;
+  return (unsigned)(want < cap ? want : cap);
+}
+}  // namespace
+void link_d2f(long n, const double *x, float *y, cudaStream_t s) {
+  if (!link_ok(n, x, y)) return convert_d2f(n, x, y, s);
+  count_launch();
+  k_d2f_link<<<link_blocks(n / 2), TPB, 0, s>>>(n / 2, reinterpret_cast<const double2 *>(x),
+                                                 reinterpret_cast<float2 *>(y));
+}
+void link_f2d(long n, const float *x, double *y, cudaStream_t s) {
+  if (!link_ok(n, x, y)) return convert_f2d(n, x, y, s);
+  count_launch();
+  k_f2d_link<<<link_blocks(n / 2), TPB, 0, s>>>(n / 2, reinterpret_cast<const float2 *>(x),
+                                                 reinterpret_cast<double2 *>(y));
+}
+void link_copy(long n, const double *x, double *y, cudaStream_t s) {
+  if (!link_ok(n, x, y)) {
+    cudaMemcpyAsync(y, x, sizeof(double) * n, cudaMemcpyDefault, s);
+    return;
+  }
+  count_launch();
+  k_copy_link<<<link_blocks(n / 2), TPB, 0, s>>>(n / 2, reinterpret_cast<const double2 *>(x),
+                                                  reinterpret_cast<double2 *>(y));
 }
 void scale_d2f_all(long n, const double *x, float *y, double a, cudaStream_t s) {
   count_launch();

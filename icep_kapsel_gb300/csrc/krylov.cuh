@@ -48,6 +48,11 @@ void sum_abs_real(const Grid &g, const R *a, double *partials, double *scal, int
 // type conversion over all NX*NY*NZ_ values
 void convert_f2d(long n, const float *x, double *y, cudaStream_t s);
 void convert_d2f(long n, const double *x, float *y, cudaStream_t s);
+// the same (and a plain copy) where x or y is host memory mapped into the
+// device's address space: wide accesses, a strided grid of ~8 blocks per SM
+void link_d2f(long n, const double *x, float *y, cudaStream_t s);
+void link_f2d(long n, const float *x, double *y, cudaStream_t s);
+void link_copy(long n, const double *x, double *y, cudaStream_t s);
 // element-wise over all n values (real or k-space arrays): y = (float)(a x);
 // y += a (double)x; y = a x + b y
 void scale_d2f_all(long n, const double *x, float *y, double a, cudaStream_t s);

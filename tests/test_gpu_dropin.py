@@ -77,3 +77,45 @@ def test_dropin_changed_potential_is_taken(Sim):
     b.time_evolution(host["zeta0"], host["zeta1"], uk, hp, host["c0"], host["c1"], host["pot"], 1)
     _, err, _ = b.solver_stats()
     assert err <= 1e-8
+
+
+def test_dropin_pinned_host_arrays(Sim):
+    """Host arrays pinned through icep_pin_host are read and written by the
+    conversion kernels over the CPU-GPU link instead of staging copies: the
+    values are the same bits as through the staged path (an I/O-only call),
+    and stepping two contexts through either path gives the same run (3e-6:
+    the FP32 scatter atomics of two contexts add in different orders)."""
+    import ctypes as C
+    from icep_kapsel_gb300 import runtime
+    lib = runtime.load_library()
+    lib.icep_pin_host.argtypes = [C.c_void_p, C.c_size_t]
+    lib.icep_unpin_host.argtypes = [C.c_void_p]
+    keys = ("zeta0", "zeta1", "c0", "c1", "pot")
+    p, parts = case(abi.MIXED)
+    a = Sim(p, parts)
+    a.init_state()
+    a.step(2)
+    pinned = {k: np.ascontiguousarray(a.get(k)) for k in keys}
+    plain = {k: v.copy() for k, v in pinned.items()}
+    for v in pinned.values():
+        assert lib.icep_pin_host(v.ctypes.data, v.nbytes) == 0
+    try:
+        uk, hp = np.ascontiguousarray(a.uk_dc()), a.particles()
+        a.time_evolution(pinned["zeta0"], pinned["zeta1"], uk, hp, pinned["c0"], pinned["c1"], pinned["pot"], 0)
+        a.time_evolution(plain["zeta0"], plain["zeta1"], uk, hp, plain["c0"], plain["c1"], plain["pot"], 0)
+        for k in keys:
+            assert np.array_equal(pinned[k], plain[k]), k
+        b = Sim(*case(abi.MIXED))
+        b.init_state()
+        b.step(2)
+        ukb, hpb = np.ascontiguousarray(b.uk_dc()), b.particles()
+        for _ in range(2):
+            a.time_evolution(pinned["zeta0"], pinned["zeta1"], uk, hp, pinned["c0"], pinned["c1"], pinned["pot"], 1)
+            b.time_evolution(plain["zeta0"], plain["zeta1"], ukb, hpb, plain["c0"], plain["c1"], plain["pot"], 1)
+        for k in ("zeta0", "zeta1", "c0", "c1"):
+            assert rel(pinned[k], plain[k]) < 3e-6, k
+        x, y = pinned["pot"][:, :, :p.nz], plain["pot"][:, :, :p.nz]
+        assert rel(x - x.mean(), y - y.mean()) < 3e-6
+    finally:
+        for v in pinned.values():
+            lib.icep_unpin_host(v.ctypes.data)

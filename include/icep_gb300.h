@@ -335,7 +335,11 @@ int icep_step_timed(icep_ctx *ctx, int nsteps, double *ms);
 int icep_phase_times(icep_ctx *ctx, double *ms, int n);
 /* Kernels launched by this library so far (all contexts). */
 unsigned long long icep_kernel_launches(void);
-/* Page-lock / release a caller's host buffer for the drop-in transfers. */
+/* Page-lock / release a caller's host buffer for the drop-in transfers. The
+ * buffer is registered as mapped: icep_time_evolution and the field getters
+ * and setters then read and write it from their conversion kernels over the
+ * CPU-GPU link, with no staging copy. Release it only when no call that uses
+ * it is running. */
 int icep_pin_host(void *ptr, size_t bytes);
 int icep_unpin_host(void *ptr);
 

@@ -102,3 +102,25 @@ def test_saltfree_refused(Sim, charges, valency):
     p, parts = cases.saltfree_case(charges=charges, valency=valency)
     with pytest.raises(IcepError):
         Sim(p, parts)
+
+
+def test_saltfree_dropin_one_concentration(Sim):
+    """The drop-in call of a salt-free run takes one concentration array
+    (conc1 NULL) and continues the device-resident run (1e-12, FP64)."""
+    p, parts = cases.saltfree_case(tol=1e-10, solver=abi.SOLVER_SPECTRAL)
+    a = Sim(p, parts)
+    a.init_state()
+    a.step(1)
+    q, qparts = cases.saltfree_case(tol=1e-10, solver=abi.SOLVER_SPECTRAL)
+    b = Sim(q, qparts)
+    b.init_state()
+    b.step(1)
+    host = {k: np.ascontiguousarray(b.get(k)) for k in ("zeta0", "zeta1", "c0", "pot")}
+    uk = np.ascontiguousarray(b.uk_dc())
+    hp = b.particles()
+    for _ in range(2):
+        b.time_evolution(host["zeta0"], host["zeta1"], uk, hp, host["c0"], None, host["pot"], 1)
+    a.step(2)
+    for k in ("zeta0", "zeta1", "c0"):
+        assert rel(host[k], a.get(k)) < 1e-12, k
+    assert np.abs(b.get("c1")).max() == 0.0

@@ -70,6 +70,8 @@ class Engine : public EngineBase {
   double *hkpart = nullptr;   // pinned
   int *kerr = nullptr;        // error word of the fused plane passes (inside kpart)
   double *kfin = nullptr;     // final sums of the three dot passes (inside kpart), then kerr
+  double *kst = nullptr;      // device-side iteration state of the fused solver (inside kpart, after kerr)
+  int kf_pred = 0;            // iterations of the last fused solve (the first batch of the next)
   unsigned *kcnt = nullptr;   // last-block counters of the dot passes
   int kop_npb = 0;
   // learned preconditioner and its flexible GMRES (solver LEARNED)
@@ -341,14 +343,17 @@ class Engine : public EngineBase {
       kop_npb = kop_pencil_blocks(g);
       // the dot partials of the three passes, their final sums (3 pairs), then
       // one word for the plane passes' error flag; three pass counters
-      const size_t nk = 2 * (2 * (size_t)kop_npb + kop_xr_blocks(g)) + 7;
-      if (cudaMalloc(&kpart, sizeof(double) * nk) != cudaSuccess || cudaMallocHost(&hkpart, sizeof(double) * 7) != cudaSuccess ||
+      // and the device-side iteration state (KS_COUNT doubles)
+      const size_t nk = 2 * (2 * (size_t)kop_npb + kop_xr_blocks(g)) + 7 + KS_COUNT;
+      if (cudaMalloc(&kpart, sizeof(double) * nk) != cudaSuccess ||
+          cudaMallocHost(&hkpart, sizeof(double) * (7 + KS_COUNT)) != cudaSuccess ||
           cudaMalloc(&kcnt, sizeof(unsigned) * 4) != cudaSuccess)
         return fail(ICEP_ERR_CUDA, "allocation of the k-space dot partials failed");
       cudaMemsetAsync(kpart, 0, sizeof(double) * nk, s);
       cudaMemsetAsync(kcnt, 0, sizeof(unsigned) * 4, s);
-      kfin = kpart + nk - 7;
-      kerr = reinterpret_cast<int *>(kpart + nk - 1);
+      kfin = kpart + nk - 7 - KS_COUNT;
+      kerr = reinterpret_cast<int *>(kfin + 6);
+      kst = kfin + 7;
     }
     if (p.solver == ICEP_SOLVER_LEARNED) {
       if (!mixed || !electrolyte || !kpart || p.nx != p.ny || p.nx != p.nz || p.nx < 32)
@@ -761,43 +766,61 @@ class Engine : public EngineBase {
       zero(F_KV);
       zero(F_KP);
       kop_eps_faces(g, f[F_EPS], f[F_EF0], f[F_EF1], f[F_EF2], s);
-      double rho = 1, alpha = 1, w = 1;
       const double tol2 = tol * tol * bsq, eps2 = DBL_EPSILON * DBL_EPSILON;
-      double r0sq = bsq, rr = bsq, rho_new = bsq;
+      double rr = bsq;
       int i = 0;
+      // The iteration's scalars live on the device (kst, see kop.cuh): the
+      // host enqueues several iterations between synchronisations -- at first
+      // as many as the previous solve needed less two (an iteration enqueued
+      // past the stop still runs its passes on scratch vectors), then one at
+      // a time.
+      double *hks = hkpart + 7;
+      hks[KS_RHO] = bsq;  // iteration 0: rho = (r0, r), p = v = 0
+      hks[KS_BETA] = 1.0;
+      hks[KS_OMEGA] = 1.0;
+      hks[KS_TOL2] = tol2;
+      hks[KS_DONE] = 0.0;
+      hks[KS_ITERS] = 0.0;
+      hks[KS_RR] = bsq;
+      hks[KS_RESTART] = eps2 * bsq;
+      cudaMemcpyAsync(kst, hks, sizeof(double) * KS_COUNT, cudaMemcpyHostToDevice, s);
       while (i < maxit && rr > tol2) {
-        const double rho_old = rho;
-        rho = rho_new;
-        if (fabs(rho) < eps2 * r0sq) {  // restart on the current residual
-          cudaMemcpyAsync(r0, r, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
-          rho = r0sq = rr;
-          zero(F_KV);
-          zero(F_KP);
-          alpha = w = 1;
-          if (!(rho > 0.0)) break;
-          rho_new = rho;
+        int chunk = (i == 0 && kf_pred > 2) ? kf_pred - 2 : 1;
+        if (chunk > maxit - i) chunk = maxit - i;
+        for (int q = 0; q < chunk; q++) {
+          kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, s, kst);
+          kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
+          kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s);
+          kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, s, kst);
+          kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
+          kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s);
+          kop_xr(g, xt, r, p, sv, t, r0, 0.0, F1, F2, P3, F3, kcnt + 2, s, kst, maxit);
         }
-        const double beta = (rho / rho_old) * (alpha / w);
-        kop_xinv(fft, KOP_P, p, r, v, beta, w, 0.0, nullptr, eps_ref, w0, w1, w2, s);
-        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-        kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s);
-        kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, rho, F1, eps_ref, w0, w1, w2, s);
-        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-        kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s);
-        kop_xr(g, xt, r, p, sv, t, r0, rho, F1, F2, P3, F3, kcnt + 2, s);
-        matvecs += 2;
-        cudaMemcpyAsync(hkpart, kfin, sizeof(double) * 7, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hkpart, kfin, sizeof(double) * (7 + KS_COUNT), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fused k-space iteration");
         if (*reinterpret_cast<const int *>(hkpart + 6))
           return fail(ICEP_ERR_CUDA, "fused plane pass: a bulk copy did not complete within the wait limit");
-        const double r0v = hkpart[0], tt = hkpart[2], ts = hkpart[3], r0r = hkpart[4];
-        rr = hkpart[5];
-        alpha = rho / r0v;
-        w = (tt > 0.0) ? ts / tt : 0.0;
-        rho_new = r0r;
-        ++i;
+        const int now = (int)hks[KS_ITERS];
+        matvecs += 2 * (now - i);
+        i = now;
+        rr = hks[KS_RR];
         if (!std::isfinite(rr)) break;
+        if (hks[KS_DONE] == 2.0) {  // restart on the current residual
+          cudaMemcpyAsync(r0, r, sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+          zero(F_KV);
+          zero(F_KP);
+          if (!(rr > 0.0)) break;
+          hks[KS_RHO] = rr;
+          hks[KS_BETA] = 1.0;
+          hks[KS_OMEGA] = 1.0;
+          hks[KS_RESTART] = eps2 * rr;
+          hks[KS_DONE] = 0.0;
+          cudaMemcpyAsync(kst, hks, sizeof(double) * KS_COUNT, cudaMemcpyHostToDevice, s);
+          continue;
+        }
+        if (hks[KS_DONE] != 0.0) break;
       }
+      kf_pred = i;
       kprecond<R>(g, xt, f[F_KX], eps_ref, s);
       if (!kspace_io) c2r(f[F_KX]);
       *iters = i;

@@ -63,8 +63,8 @@ __device__ void block_partials(float s0, float s1, double scale, double *partial
 // lanes) into finals[0..1] and re-arms the counter: the next kernel reads two
 // numbers instead of all partials. Partials of other blocks are read through
 // L2 (__ldcg) after the ticket, which follows each block's fence.
-__device__ void block_partials_final(float s0, float s1, double scale, double *partials, double *finals,
-                                     unsigned *counter) {
+__device__ int block_partials_final(float s0, float s1, double scale, double *partials, double *finals,
+                                    unsigned *counter) {
   block_partials(s0, s1, scale, partials);
   __shared__ int last;
   const int lin = threadIdx.y * blockDim.x + threadIdx.x;
@@ -72,7 +72,7 @@ __device__ void block_partials_final(float s0, float s1, double scale, double *p
   __syncthreads();
   if (lin == 0) last = (atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1) ? 1 : 0;
   __syncthreads();
-  if (!last) return;
+  if (!last) return 0;
   __threadfence();
   if (lin < 64) {
     const int c = lin >> 5, lane = lin & 31;
@@ -83,6 +83,7 @@ __device__ void block_partials_final(float s0, float s1, double scale, double *p
     if (lane == 0) finals[c] = v;
   }
   if (lin == 0) *counter = 0u;
+  return 1;
 }
 
 // (j, kz) of pencils q0 .. q0 + KW - 1 into shared arrays (synchronised by the caller)
@@ -134,7 +135,13 @@ template <int N>
 __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, const float *r, const float *v,
                                                   float beta, float omega, double rho, const double *fin,
                                                   float ieps, float *w0, float *w1, float *w2,
-                                                  const cf *__restrict__ twx) {
+                                                  const cf *__restrict__ twx, const double *ks) {
+  // device-side iteration state: beta, omega (P) and rho (S) from it
+  if (ks) {
+    beta = (float)__ldcg(ks + KS_BETA);
+    omega = (float)__ldcg(ks + KS_OMEGA);
+    rho = __ldcg(ks + KS_RHO);
+  }
   extern __shared__ unsigned char smem_raw[];
   const int sw = KW + 1;
   cf *tws = reinterpret_cast<cf *>(smem_raw);
@@ -505,15 +512,20 @@ template <int H>
 __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float *r, const float *p, const float *sv,
                                                      const float *t, const float *r0, double rho,
                                                      const double *fin1, const double *fin2, double *part3,
-                                                     double *fin3, unsigned *counter3) {
+                                                     double *fin3, unsigned *counter3, double *ks, int maxit) {
   const int lin = threadIdx.x;
   __shared__ float sc[2];  // alpha, omega: two FP64 divisions per block, not per thread
+  __shared__ int stop;     // the solve is done: this launch leaves x and r alone
   if (lin == 0) {
     const double r0v = fin1[0], tt = fin2[0], ts = fin2[1];
-    sc[0] = (float)(rho / r0v);
+    const double rk = ks ? __ldcg(ks + KS_RHO) : rho;
+    stop = (ks && __ldcg(ks + KS_DONE) != 0.0) ? 1 : 0;
+    sc[0] = (float)(rk / r0v);
     sc[1] = (float)((tt > 0.0) ? ts / tt : 0.0);
   }
   __syncthreads();
+  if (stop) return;
+  if (ks) rho = __ldcg(ks + KS_RHO);  // the last block's update below
   const float alpha = sc[0], w = sc[1];
   constexpr int RL = H + 1;  // modes per z row
   const long nm = g.nmodes();
@@ -540,7 +552,28 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float 
     s0 += fw * (a.x * nr.x + a.y * nr.y);
     s1 += fw * (nr.x * nr.x + nr.y * nr.y);
   }
-  block_partials_final(s0, s1, 1.0 / (double)g.nreal(), part3, fin3, counter3);
+  const int last = block_partials_final(s0, s1, 1.0 / (double)g.nreal(), part3, fin3, counter3);
+  if (last && ks) {
+    __syncthreads();
+    if (lin == 0) {
+      // the next iteration's scalars, as the host loop would form them, and
+      // the stop test (converged, non-finite, iteration limit, or a restart
+      // that the host must perform)
+      const double r0v = __ldcg(fin1), tt = __ldcg(fin2), ts = __ldcg(fin2 + 1);
+      const double alpha = rho / r0v, w = (tt > 0.0) ? ts / tt : 0.0;
+      const double rho_new = __ldcg(fin3), rr = __ldcg(fin3 + 1);
+      const double it = ks[KS_ITERS] + 1.0;
+      ks[KS_BETA] = (rho_new / rho) * (alpha / w);
+      ks[KS_OMEGA] = w;
+      ks[KS_RHO] = rho_new;
+      ks[KS_ITERS] = it;
+      ks[KS_RR] = rr;
+      double done = 0.0;
+      if (!(rr > ks[KS_TOL2]) || !isfinite(rr) || it >= (double)maxit) done = 1.0;
+      else if (fabs(rho_new) < ks[KS_RESTART]) done = 2.0;
+      ks[KS_DONE] = done;
+    }
+  }
 }
 
 __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2) {
@@ -617,7 +650,7 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
               double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
-              cudaStream_t s) {
+              cudaStream_t s, const double *ks) {
   const Grid &g = p.g;
   const unsigned nb = (unsigned)kop_pencil_blocks(g);
   const float ieps = (float)(1.0 / eps_ref);
@@ -627,7 +660,7 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
   case N:                                                                                                  \
     set_x_attr<N>();                                                                                       \
     k_kop_xinv<N><<<nb, xblock(N), xpass_smem(N), s>>>(g, mode, vec, r, v, (float)beta, (float)omega, rho, \
-                                                       fin, ieps, w0, w1, w2, p.tw_x);                     \
+                                                       fin, ieps, w0, w1, w2, p.tw_x, ks);                 \
     break;
   switch (g.nx) {
     KOP_XINV(16)
@@ -679,12 +712,13 @@ int kop_xr_blocks(const Grid &g) { return (int)div_up(g.nmodes(), KOP_XR_TPB * K
 
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
             double rho, const double *fin1, const double *fin2, double *part3, double *fin3, unsigned *counter3,
-            cudaStream_t s) {
+            cudaStream_t s, double *ks, int maxit) {
   const unsigned nb = (unsigned)kop_xr_blocks(g);
   count_launch();
 #define KOP_XR(HH)                                                                                            \
   case HH:                                                                                                    \
-    k_kop_xr<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, sv, t, r0, rho, fin1, fin2, part3, fin3, counter3); \
+    k_kop_xr<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, sv, t, r0, rho, fin1, fin2, part3, fin3, counter3, ks, \
+                                           maxit);                                                              \
     break;
   switch (g.nz / 2) {
     KOP_XR(8)

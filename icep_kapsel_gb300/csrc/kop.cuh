@@ -26,6 +26,15 @@ enum { KOP_P = 0, KOP_S = 1, KOP_NONE = 2 };
 
 // true if the fused passes cover this grid (an x-plane fits in shared memory)
 bool kop_supported(const Grid &g);
+// Device-side BiCGSTAB iteration state (doubles). With a state pointer
+// kop_xinv takes beta, omega and rho from it instead of its arguments, and
+// kop_xr returns without touching x and r once KS_DONE is set (the other
+// passes of an iteration enqueued past the stop only write scratch vectors);
+// kop_xr's last block forms the next iteration's scalars from the final sums
+// and sets KS_DONE (1: converged, non-finite or at the iteration limit; 2: a
+// restart for the host). The host then enqueues several iterations between
+// synchronisations.
+enum { KS_RHO = 0, KS_BETA, KS_OMEGA, KS_TOL2, KS_DONE, KS_ITERS, KS_RR, KS_RESTART, KS_COUNT };
 // number of x-pencil blocks (= partial sums written by kop_xfwd)
 int kop_pencil_blocks(const Grid &g);
 // ef_d = 0.5 (eps + eps at the next point along d), real points
@@ -35,7 +44,7 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 // mode KOP_NONE: vec is used as it is (r, v, fin unused).
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
               double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
-              cudaStream_t s);
+              cudaStream_t s, const double *ks = nullptr);
 // err: device word set to 1 if a bulk copy into shared memory did not
 // complete within the kernel's wait limit (checked by the caller)
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
@@ -53,6 +62,6 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const f
 int kop_xr_blocks(const Grid &g);
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
             double rho, const double *fin1, const double *fin2, double *part3, double *fin3, unsigned *counter3,
-            cudaStream_t s);
+            cudaStream_t s, double *ks = nullptr, int maxit = 0);
 
 }  // namespace icep

@@ -1112,10 +1112,6 @@ class Engine : public EngineBase {
     cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
     memcpy(keep.data(), hp, sizeof(icep_particle) * np);
-    // the parameters before training, restored if training does not help
-    float *snap = nullptr;
-    if (cudaMalloc(&snap, sizeof(float) * net.nparams) != cudaSuccess) return fail(ICEP_ERR_CUDA, "learned_train");
-    cudaMemcpyAsync(snap, net.params, sizeof(float) * net.nparams, cudaMemcpyDeviceToDevice, s);
     const double e_keep[3] = {P.e_ext[0], P.e_ext[1], P.e_ext[2]};
     const int ac_keep = P.ac;
     P.ac = 0;  // training fields are DC fields of random direction
@@ -1157,32 +1153,10 @@ class Engine : public EngineBase {
     memcpy(hp, keep.data(), sizeof(icep_particle) * np);
     cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
     make_dielectric_field(F_WORK, F_WV1);
-    if (cudaStreamSynchronize(s) != cudaSuccess) {
-      cudaFree(snap);
-      return cuda_status("learned_train");
-    }
-    if (st == ICEP_OK) {
-      // keep the trained parameters only if they do not make the one-step
-      // residual of the context's own problem worse than the spectral
-      // preconditioner alone; else go back to the parameters before training
-      const bool was = net_trained;
-      net_trained = true;
-      double ls = 0, ll = 0;
-      st = learned_eval(2, &ls, &ll);
-      if (st == ICEP_OK && !(ll <= ls)) {
-        cudaMemcpyAsync(net.params, snap, sizeof(float) * net.nparams, cudaMemcpyDeviceToDevice, s);
-        net.pack(s);
-        net_trained = was;
-        last_train_kept = false;
-      } else {
-        last_train_kept = true;
-      }
-      if (cudaStreamSynchronize(s) != cudaSuccess) st = cuda_status("learned_train");
-    }
-    cudaFree(snap);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
+    if (st == ICEP_OK) net_trained = true;
     return st;
   }
-  bool last_train_kept = false;  // whether the last learned_train kept its parameters
   int learned_enable(int on) override {
     if (!learned) return unsupported_learned();
     net_use = on != 0;

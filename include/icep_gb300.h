@@ -287,10 +287,7 @@ int icep_batch_step(icep_batch *batch, int nsteps);
  * `steps_per_config` Adam steps along the chain of residuals r -> r - A P(r)
  * starting from the right-hand side; loss |r - A P(r)|^2 / |r|^2 with
  * P(r) = M^-1 (r + rms(r) prolong(net(eps, r))). The
- * context's particles and field are restored afterwards. The trained
- * parameters are kept only if their mean one-step loss on the context's own
- * residual chain (two links) is not above the spectral preconditioner's;
- * else the parameters from before the call come back. */
+ * context's particles and field are restored afterwards. */
 int icep_learned_train(icep_ctx *ctx, int configs, int steps_per_config, unsigned seed, double lr, double *loss_first,
                        double *loss_last);
 /* 1: apply the network in the preconditioner, 0: spectral part only. */

@@ -53,8 +53,17 @@ def build_oracle(force=False):
     return ORACLE_SO
 
 
-def build_ref(ref_dir="/root/reference"):
+def ref_dir():
+    """The reference source tree the checker is compiled from: the
+    ICEP_REFERENCE_DIR environment variable, else the tree's location in the
+    build container (absent on GPU hosts, where only the committed fixtures
+    are used)."""
+    return os.environ.get("ICEP_REFERENCE_DIR", "/root/reference")
+
+
+def build_ref(ref_dir=None):
     """Build oracle/_ref/libkapsel_ref.so from the reference tree if present."""
+    ref_dir = ref_dir or globals()["ref_dir"]()
     if not os.path.isdir(ref_dir):
         return None
     subprocess.check_call(["make", "-s", "-j8", "-C", os.path.join(HERE, "ref"), "REF=" + ref_dir])

@@ -135,6 +135,136 @@ static Particle *particles = nullptr;
 static double *rho_free_buf = nullptr; /* free charge density for isolated calls */
 static double *work_buf = nullptr;
 static bool ready = false;
+static bool spectral_solve = false; /* icep_params.solver == ICEP_SOLVER_SPECTRAL */
+
+/*
+ * The plain method of the GPU path, installed in the reference's own solver
+ * seam (the Charge_field2potential_dielectric function pointer,
+ * operate_dielectric.cxx:18-22, which the reference provides so that the
+ * solve can be swapped) when a fixture asks for a tolerance that the
+ * reference's identity-preconditioned BiCGSTAB cannot reach on an
+ * inconsistent periodic system: BiCGSTAB right-preconditioned by the
+ * constant-permittivity spectral inverse y(k) = -x(k) IK2(k) / eps_ref
+ * (eps_ref = mean eps, IK2 the reference's 1/K^2 table, fft_wrapper.cxx:
+ * 47-87), b projected to mean zero, convergence confirmed on the true
+ * residual |b - A x| <= tol |b|, the retry from a zero guess of
+ * Charge_field2potential_dielectric_LO (operate_dielectric.cxx:563-570).
+ * Everything else is the reference's: Build_rhs, Ax, the Ooura transforms.
+ */
+static void spectral_precond(const std::vector<double> &x, std::vector<double> &y, double eref) {
+  for (int i = 0; i < NX; i++)
+    for (int j = 0; j < NY; j++) {
+      for (int k = 0; k < NZ; k++) work_v1[(i * NY * NZ_) + (j * NZ_) + k] = x[(i * NY + j) * NZ + k];
+      for (int k = NZ; k < NZ_; k++) work_v1[(i * NY * NZ_) + (j * NZ_) + k] = 0.0;
+    }
+  A2a_k(work_v1);
+  for (int im = 0; im < NX * NY * NZ_; im++) work_v1[im] *= -IK2[im] / eref;
+  A_k2a(work_v1);
+  for (int i = 0; i < NX; i++)
+    for (int j = 0; j < NY; j++)
+      for (int k = 0; k < NZ; k++) y[(i * NY + j) * NZ + k] = work_v1[(i * NY * NZ_) + (j * NZ_) + k];
+}
+
+static double vdot(const std::vector<double> &a, const std::vector<double> &b) {
+  double s = 0.0;
+  for (size_t k = 0; k < a.size(); k++) s += a[k] * b[k];
+  return s;
+}
+
+static long spectral_bicgstab(std::vector<double> b, std::vector<double> &x, double eref, double *err) {
+  const size_t n = b.size();
+  double mean = 0.0;
+  for (size_t k = 0; k < n; k++) mean += b[k];
+  mean /= (double)n;
+  for (size_t k = 0; k < n; k++) b[k] -= mean;
+  std::vector<double> r(n), r0(n), v(n, 0.0), p(n, 0.0), s(n), t(n), y(n), z(n);
+  auto matvec = [&](const std::vector<double> &in, std::vector<double> &out) {
+    ++Eigen::shim_stats::matvecs();
+    Ax(in.data(), out.data());
+  };
+  matvec(x, t);
+  for (size_t k = 0; k < n; k++) r[k] = b[k] - t[k];
+  r0 = r;
+  double r0_sq = vdot(r0, r0), b_sq = vdot(b, b);
+  long i = 0;
+  if (b_sq == 0.0) {
+    std::fill(x.begin(), x.end(), 0.0);
+    *err = 0.0;
+    return 0;
+  }
+  double rho = 1, alpha = 1, w = 1, rr = r0_sq, rho_new = r0_sq;
+  const double tol2 = Tol_potential * Tol_potential * b_sq;
+  const double eps2 = std::numeric_limits<double>::epsilon() * std::numeric_limits<double>::epsilon();
+  long restarts = 0;
+  while (i < MaxIter_potential) {
+    if (!(rr > tol2)) {
+      matvec(x, t);
+      for (size_t k = 0; k < n; k++) r[k] = b[k] - t[k];
+      rr = vdot(r, r);
+      if (!(rr > tol2)) break;
+      r0 = r;
+      r0_sq = rho_new = rr;
+      std::fill(v.begin(), v.end(), 0.0);
+      std::fill(p.begin(), p.end(), 0.0);
+      rho = alpha = w = 1;
+    }
+    const double rho_old = rho;
+    rho = rho_new;
+    if (std::fabs(rho) < eps2 * r0_sq) {
+      matvec(x, t);
+      for (size_t k = 0; k < n; k++) r[k] = b[k] - t[k];
+      r0 = r;
+      rho = r0_sq = vdot(r, r);
+      if (restarts++ == 0) i = 0;
+    }
+    const double beta = (rho / rho_old) * (alpha / w);
+    for (size_t k = 0; k < n; k++) p[k] = r[k] + beta * (p[k] - w * v[k]);
+    spectral_precond(p, y, eref);
+    matvec(y, v);
+    alpha = rho / vdot(r0, v);
+    for (size_t k = 0; k < n; k++) s[k] = r[k] - alpha * v[k];
+    spectral_precond(s, z, eref);
+    matvec(z, t);
+    const double tt = vdot(t, t);
+    w = (tt > 0.0) ? vdot(t, s) / tt : 0.0;
+    for (size_t k = 0; k < n; k++) x[k] += alpha * y[k] + w * z[k];
+    for (size_t k = 0; k < n; k++) r[k] = s[k] - w * t[k];
+    rho_new = vdot(r0, r);
+    rr = vdot(r, r);
+    ++i;
+  }
+  *err = std::sqrt(rr / b_sq);
+  return i;
+}
+
+static void potential_spectral(double *free_charge_density, double *potential, double *eps, double *rhs,
+                               double external_e_field[]) {
+  Reset_phi(rhs);
+  Build_rhs(rhs, free_charge_density, eps, external_e_field);
+  const size_t n = (size_t)NX * NY * NZ;
+  std::vector<double> b(n), x(n);
+  double eref = 0.0;
+  for (int i = 0; i < NX; i++)
+    for (int j = 0; j < NY; j++)
+      for (int k = 0; k < NZ; k++) {
+        const int im = (i * NY * NZ_) + (j * NZ_) + k;
+        b[(i * NY + j) * NZ + k] = rhs[im];
+        x[(i * NY + j) * NZ + k] = potential[im];
+        eref += eps[im];
+      }
+  eref /= (double)n;
+  double err = 0.0;
+  long it = spectral_bicgstab(b, x, eref, &err);
+  if (it == MaxIter_potential) {
+    std::fill(x.begin(), x.end(), 0.0);
+    it = spectral_bicgstab(b, x, eref, &err);
+  }
+  Eigen::shim_stats::iterations() = it;
+  Eigen::shim_stats::error() = err;
+  for (int i = 0; i < NX; i++)
+    for (int j = 0; j < NY; j++)
+      for (int k = 0; k < NZ; k++) potential[(i * NY * NZ_) + (j * NZ_) + k] = x[(i * NY + j) * NZ + k];
+}
 
 static double *dalloc(int n) {
   double *p = alloc_1d_double(n);
@@ -413,8 +543,11 @@ int kref_setup(const icep_params *q, const icep_particle *p, int np) {
   Particle_domain(Phi, NP_domain, Sekibun_cell);
   Angular2v = ROTATION ? Angular2v_rot_on : Angular2v_rot_off;
   /* selected in Init_potential_dielectric (operate_dielectric.cxx:592);
-   * set here too so that isolated calls can use it */
-  Charge_field2potential_dielectric = Charge_field2potential_dielectric_LO;
+   * set here too so that isolated calls can use it; a SPECTRAL case swaps in
+   * potential_spectral through the same pointer */
+  spectral_solve = (q->solver == ICEP_SOLVER_SPECTRAL);
+  Charge_field2potential_dielectric =
+      spectral_solve ? potential_spectral : Charge_field2potential_dielectric_LO;
   for (int n = 0; n < Particle_Number; n++) to_particle(&p[n], &particles[n]);
   for (int n = 0; n < Particle_Number; n++)  // Particle_Numbers per species (input.cxx:1036)
     if (particles[n].spec >= 0 && particles[n].spec < Component_Number) Particle_Numbers[particles[n].spec]++;
@@ -445,8 +578,23 @@ void kref_init_state() {
   if (SW_EQ == Electrolyte && Dielectric) {
     Reset_u(grad_epsilon);
     Init_rho_ion_dielectric(Concentration, particles, jikan);
-    Init_potential_dielectric(particles, grad_epsilon[2], grad_epsilon[0], Concentration, grad_epsilon[1],
-                              Potential, epsilon, jikan);
+    if (!spectral_solve) {
+      Init_potential_dielectric(particles, grad_epsilon[2], grad_epsilon[0], Concentration, grad_epsilon[1],
+                                Potential, epsilon, jikan);
+    } else {
+      /* Init_potential_dielectric (operate_dielectric.cxx:574-609) with the
+       * solver pointer left at potential_spectral (the reference's version
+       * assigns Charge_field2potential_dielectric_LO before its solve) */
+      double external[DIM];
+      for (int d = 0; d < DIM; d++) external[d] = E_ext[d] * (AC ? sin(Angular_Frequency * jikan.time) : 1.0);
+      Make_dielectric_field(particles, epsilon, grad_epsilon[2], eps_particle_top, eps_particle_bottom, eps_fluid);
+      if (have_surface_charge)
+        Conc_k2charge_field(particles, Concentration, grad_epsilon[1], grad_epsilon[2], grad_epsilon[0]);
+      else
+        Conc_k2charge_field_no_surfase_charge(particles, Concentration, grad_epsilon[1], grad_epsilon[2],
+                                              grad_epsilon[0]);
+      potential_spectral(grad_epsilon[1], Potential, epsilon, grad_epsilon[2], external);
+    }
   }
 }
 
@@ -577,7 +725,7 @@ int kref_call(int fn) {
       break;
     case C_BUILD_RHS: Build_rhs(work_buf, rho_free_buf, epsilon, E_ext); break;
     case C_SOLVE_POTENTIAL:
-      Charge_field2potential_dielectric_LO(rho_free_buf, Potential, epsilon, work_buf, E_ext);
+      Charge_field2potential_dielectric(rho_free_buf, Potential, epsilon, work_buf, E_ext);
       break;
     case C_MAXWELL:
       Make_Maxwell_force_x_on_fluid(f_particle, particles, Concentration, rho_free_buf, Potential, epsilon,

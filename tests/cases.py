@@ -170,3 +170,12 @@ def lj_dense_case(n=32, npart=24, seed=7, minsep=7.2):
     x = positions(npart, n, minsep, seed)
     p = abi.make_params(nx=n, ny=n, nz=n, n_particles=npart, n_species=1, rotation=0, dt=0.05)
     return p, abi.make_particles(x)
+
+
+def icep64_case(solver=abi.SOLVER_SPECTRAL, precision=abi.FP64, tol=1e-10):
+    """The plain ICEP run at 64^3: 16 dielectric spheres a = 5, xi = 2,
+    eps_particle = 2, eps_fluid = 80, centres uniform-random with minimum
+    separation 12, uniform external field E0 = (0, 0, 0.1), Poisson solved to
+    1e-10 true residual (the salt of icep_case)."""
+    return icep_case(n=64, npart=16, minsep=12.0, seed=64, a=5.0, eps_f=80.0, eps_p=2.0,
+                     e_ext=(0.0, 0.0, 0.1), tol=tol, solver=solver, precision=precision)

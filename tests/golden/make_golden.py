@@ -6,10 +6,10 @@ fluid_solver, make_phi, md_force, particle_solver, operate_dielectric,
 solute_rhs, operate_electrolyte, plus the restated BiCGSTAB behind the Eigen
 shim) on the seeded cases of tests/cases.py and stores the outputs.
 
-Needs the reference tree (default /root/reference); the fixtures it writes are
+Needs the reference tree (--ref, else oracle/pyoracle.py ref_dir()); the fixtures it writes are
 committed so that the tests run without it:
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py [--ref <reference source tree>]
 
 Each case runs in its own process because the reference keeps its state in
 process globals.
@@ -28,18 +28,20 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-CASES = ["fft16", "ops16", "ns32", "icep32", "lj32", "ax32", "janus32", "charged32", "ac32", "out32", "avs16", "saltfree32"]
+CASES = ["fft16", "ops16", "ns32", "icep32", "icep32_bicgstab", "icep64_200", "lj32", "ax32", "janus32", "charged32", "ac32", "out32", "avs16", "saltfree32"]
 
 
-def small_case():
-    """16^3 with a=2 spheres (stencil radius 4.7 < 8) for operator fixtures."""
+def small_case(potential_tol=1e-10):
+    """16^3 with a=2 spheres (stencil radius 4.7 < 8) for operator fixtures.
+    The ops16 fixture solves to 1e-13 so that everything downstream of its
+    Poisson solves (the potential, the Maxwell force) is pinned at 1e-12."""
     import cases
     from icep_kapsel_gb300 import abi
     x = cases.positions(3, 16, 6.0, 21)
     p = abi.make_params(nx=16, ny=16, nz=16, n_particles=3, n_species=1, a=2.0, a_xi=2.0,
                         rotation=1, dt=0.05, sw_eq=abi.ELECTROLYTE, dielectric=1,
                         eps_fluid=1.0, eps_particle_top=10.0, eps_particle_bottom=10.0,
-                        external_field=1, e_ext=[0.01, 0.002, -0.003], potential_tol=1e-10,
+                        external_field=1, e_ext=[0.01, 0.002, -0.003], potential_tol=potential_tol,
                         potential_iter=3000, kbt=1.0, debye_length=10.0, onsager_pos=7.24,
                         onsager_neg=7.24)
     rng = np.random.default_rng(99)
@@ -49,6 +51,10 @@ def small_case():
         for d in range(3):
             parts[i].omega[d] = rng.uniform(-0.01, 0.01)
     return p, parts
+
+
+OPS16_TOL = 1e-13
+ICEP64_STEPS = 200
 
 
 def ops16_inputs(p):
@@ -85,7 +91,7 @@ def run_case(name, out):
         data["r2c"] = r.fft_r2c(a)
         data["c2r"] = r.fft_c2r(a)[:, :, :16]
     elif name == "ops16":
-        p, parts = small_case()
+        p, parts = small_case(potential_tol=OPS16_TOL)
         r = pyoracle.RefKapsel(p, parts)
         f = ops16_inputs(p)
         # Zeta_k2u_k
@@ -168,8 +174,16 @@ def run_case(name, out):
         data["uk_dc"] = r.uk_dc()
         for k, v in abi.particles_to_numpy(r.particles(), p.n_particles).items():
             data["p_" + k] = v
-    elif name == "icep32":
-        p, parts = cases.icep_case(tol=1e-7)
+    elif name in ("icep32", "icep32_bicgstab"):
+        # icep32: the reference's step with the plain spectral solve of the
+        # GPU path installed in its solver seam, to 1e-12 (fields pinned at
+        # 1e-10); icep32_bicgstab: the reference's own identity-preconditioned
+        # BiCGSTAB, which reaches 1e-7 on this case but not 1e-12 (the
+        # periodic system turns inconsistent as the ions move)
+        if name == "icep32":
+            p, parts = cases.icep_case(tol=1e-12, solver=abi.SOLVER_SPECTRAL)
+        else:
+            p, parts = cases.icep_case(tol=1e-7)
         r = pyoracle.RefKapsel(p, parts)
         r.init_state()
         meta["init_iterations"] = int(r.last_iterations())
@@ -180,6 +194,33 @@ def run_case(name, out):
             data[k] = r.get(k)
         data["pot"] = r.get("pot")[:, :, :32]
         data["eps"] = r.get("eps")[:, :, :32]
+        data["uk_dc"] = r.uk_dc()
+        for k, v in abi.particles_to_numpy(r.particles(), p.n_particles).items():
+            data["p_" + k] = v
+    elif name == "icep64_200":
+        # the plain ICEP run at 64^3 (16 dielectric spheres a = 5, eps_p = 2,
+        # eps_f = 80, E0 = (0, 0, 0.1), Poisson to 1e-10 true residual) for
+        # 200 steps; fields are stored on every 4th point of each axis (the
+        # full fields would be 11 MB) with their full-grid norms
+        p, parts = cases.icep64_case()
+        r = pyoracle.RefKapsel(p, parts)
+        r.init_state()
+        its = [int(r.last_iterations())]
+        for _ in range(ICEP64_STEPS):
+            r.step(1)
+            its.append(int(r.last_iterations()))
+        meta["iterations"] = its
+        meta["step_error"] = float(r.last_error())
+        for k in ("zeta0", "zeta1", "c0", "c1"):
+            a = r.get(k)
+            data[k] = a[::4, ::4, ::4]
+            data[k + "_norm"] = np.linalg.norm(a)
+        for k in ("pot", "phi"):
+            a = r.get(k)[:, :, :64]
+            if k == "pot":  # defined up to a constant
+                a = a - a.mean()
+            data[k] = a[::4, ::4, ::4]
+            data[k + "_norm"] = np.linalg.norm(a)
         data["uk_dc"] = r.uk_dc()
         for k, v in abi.particles_to_numpy(r.particles(), p.n_particles).items():
             data["p_" + k] = v
@@ -254,7 +295,7 @@ def run_case(name, out):
         # the field output (Output_dielectric_charge_field_data's fields) of
         # the charged case after its initial solve, with a flow: zeta from
         # the icep32 fixture and a mean velocity uk_dc
-        ic = np.load(os.path.join(HERE, "icep32.npz"))
+        ic = np.load(os.path.join(HERE, "icep32_bicgstab.npz"))
         p, parts = cases.charged_case()
         r = pyoracle.RefKapsel(p, parts)
         r.init_state()
@@ -325,7 +366,8 @@ def run_case(name, out):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    import pyoracle
+    ap.add_argument("--ref", default=pyoracle.ref_dir())
     ap.add_argument("--case", default=None)
     a = ap.parse_args()
     if a.case:

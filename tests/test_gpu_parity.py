@@ -78,7 +78,7 @@ def test_fft_sizes_against_oracle(Sim, n):
 def test_ops16_golden(Sim):
     g = load("ops16")
     mg = golden_module()
-    p, parts = mg.small_case()
+    p, parts = mg.small_case(potential_tol=mg.OPS16_TOL)
     o = Sim(p, parts)
     f = mg.ops16_inputs(p)
     tol = 1e-12
@@ -131,13 +131,13 @@ def test_ops16_golden(Sim):
     it, err = o.solve_potential()
     a = o.get("pot")[:, :, :16]
     b = g["pot_solved"]
-    assert rel(a - a.mean(), b - b.mean()) < 1e-8
-    assert err < 1e-10
+    assert rel(a - a.mean(), b - b.mean()) < 1e-11
+    assert err < mg.OPS16_TOL
     o.set("rho", f["rho"]); o.set("pot", f["pot"])
     o.set("c0", f["c0"]); o.set("c1", f["c0"])
     o.call("maxwell")
     for d in range(3):
-        assert rel(o.get("f%d" % d)[:, :, :16], g["maxwell_f%d" % d]) < 1e-7
+        assert rel(o.get("f%d" % d)[:, :, :16], g["maxwell_f%d" % d]) < tol
     o.set("zeta0", f["zeta0"]); o.set("zeta1", f["zeta1"]); o.set_uk_dc(f["uk_dc"])
     o.set("c0", f["c0"]); o.set("c1", f["c1"]); o.set("pot", f["pot"])
     o.call("nssolute_euler")
@@ -208,7 +208,32 @@ def test_ns32_fix_cell_against_oracle(Sim):
 
 
 def test_icep32_two_steps_golden(Sim):
+    """The full ICEP step (init + 2 steps) in FP64 against the reference's
+    own step with the spectral solve in its solver seam, both to a 1e-12 true
+    residual: every field and the particle state within 1e-10 relative L2."""
     g = load("icep32")
+    p, parts = cases.icep_case(tol=1e-12, solver=abi.SOLVER_SPECTRAL)
+    o = Sim(p, parts)
+    o.init_state()
+    o.step(2)
+    _, err, _ = o.solver_stats()
+    assert err <= 1e-12
+    for k in ("zeta0", "zeta1", "c0", "c1"):
+        assert rel(o.get(k), g[k]) < 1e-10, k
+    a = o.get("pot")[:, :, :32]
+    assert rel(a - a.mean(), g["pot"] - g["pot"].mean()) < 1e-10
+    assert rel(o.get("eps")[:, :, :32], g["eps"]) < 1e-12
+    assert rel(o.uk_dc(), g["uk_dc"]) < 1e-10
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    for k in ("x", "v", "f_hydro_previous", "fr_previous"):
+        assert rel(pa[k], g["p_" + k]) < 1e-10, k
+
+
+def test_icep32_bicgstab_two_steps_golden(Sim):
+    """The same step with the reference's own identity-preconditioned
+    BiCGSTAB (the REF solver) to 1e-7, the tightest tolerance it reaches on
+    this case: fields agree to a small multiple of the solver tolerance."""
+    g = load("icep32_bicgstab")
     p, parts = cases.icep_case(tol=1e-7)
     o = Sim(p, parts)
     o.init_state()
@@ -223,6 +248,36 @@ def test_icep32_two_steps_golden(Sim):
     pa = abi.particles_to_numpy(o.particles(), p.n_particles)
     assert rel(pa["x"], g["p_x"]) < 1e-12
     assert rel(pa["v"], g["p_v"]) < 2e-5
+
+
+def test_icep64_200_steps_golden(Sim):
+    """The plain ICEP run at 64^3 (16 spheres a = 5, eps_p = 2, eps_f = 80,
+    E0 = (0, 0, 0.1), Poisson to a 1e-10 true residual) for 200 steps in FP64,
+    against the reference's own step run for the same 200 steps with the
+    spectral solve in its solver seam. The fixture keeps every 4th point of
+    each axis; the bound is 1e-10 relative L2 on the velocity (vorticity),
+    phi, the ion densities, the potential and the particle state (the
+    velocity field is the linear image of the vorticity and uk_dc)."""
+    g = load("icep64_200")
+    p, parts = cases.icep64_case()
+    o = Sim(p, parts)
+    o.init_state()
+    o.step(200)
+    _, err, _ = o.solver_stats()
+    assert err <= 1e-10
+    for k in ("zeta0", "zeta1", "c0", "c1"):
+        a = o.get(k)
+        assert rel(a[::4, ::4, ::4], g[k]) < 1e-10, k
+        assert abs(np.linalg.norm(a) / g[k + "_norm"] - 1.0) < 1e-10, k
+    pot = o.get("pot")[:, :, :64]
+    pot = pot - pot.mean()
+    assert rel(pot[::4, ::4, ::4], g["pot"]) < 1e-10
+    phi = o.get("phi")[:, :, :64]
+    assert rel(phi[::4, ::4, ::4], g["phi"]) < 1e-10
+    assert rel(o.uk_dc(), g["uk_dc"]) < 1e-10
+    pa = abi.particles_to_numpy(o.particles(), p.n_particles)
+    for k in ("x", "v", "f_hydro_previous", "fr_previous"):
+        assert rel(pa[k], g["p_" + k]) < 1e-10, k
 
 
 def test_lj32_golden_and_neighbour_set(Sim):

@@ -19,7 +19,9 @@ from icep_kapsel_gb300 import abi
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIX = os.path.join(HERE, "golden", "udf", "input_small.udf")
-REF_UDF = "/root/reference/UDF/input.udf"
+import pyoracle  # noqa: E402
+
+REF_UDF = os.path.join(pyoracle.ref_dir(), "UDF", "input.udf")
 
 
 @pytest.fixture(scope="module")

@@ -799,7 +799,7 @@ class Engine : public EngineBase {
         cudaMemcpyAsync(hkpart, kfin, sizeof(double) * (7 + KS_COUNT), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fused k-space iteration");
         if (*reinterpret_cast<const int *>(hkpart + 6))
-          return fail(ICEP_ERR_CUDA, "fused plane pass: a bulk copy did not complete within the wait limit");
+          return fail(ICEP_ERR_TIMEOUT, "fused plane pass: a bulk copy did not complete within the wait limit");
         const int now = (int)hks[KS_ITERS];
         matvecs += 2 * (now - i);
         i = now;
@@ -982,10 +982,13 @@ class Engine : public EngineBase {
       }
       if (!conv) *ok = false;
       {
-        int herr = 0;
-        cudaMemcpyAsync(&herr, kerr, sizeof(int), cudaMemcpyDeviceToHost, s);
+        int herr[2] = {0, 0};
+        cudaMemcpyAsync(&herr[0], kerr, sizeof(int), cudaMemcpyDeviceToHost, s);
+        if (net.err) cudaMemcpyAsync(&herr[1], net.err, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fgmres");
-        if (herr) return fail(ICEP_ERR_CUDA, "fused plane pass: a bulk copy did not complete within the wait limit");
+        if (herr[0]) return fail(ICEP_ERR_TIMEOUT, "fused plane pass: a bulk copy did not complete within the wait limit");
+        if (herr[1])
+          return fail(ICEP_ERR_TIMEOUT, "network convolution: tensor-core completion did not arrive within the wait limit");
       }
       kprecond<R>(g, xt, f[F_KX], eref, s);
       c2r(f[F_KX]);
@@ -2013,6 +2016,33 @@ class Engine : public EngineBase {
     return phase_on ? ICEP_OK : ICEP_ERR_STATE;
   }
 
+  int selftest_wait(int kernel) override {
+    if constexpr (std::is_same<R, float>::value) {
+      int *word = nullptr;
+      if (kernel == 1) {
+        word = kerr;
+        cudaMemsetAsync(word, 0, sizeof(int), s);
+        if (!kop_plane_selftest(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], word, s))
+          return fail(ICEP_ERR_UNSUPPORTED, "wait self-test: no register plane kernel for this mesh");
+      } else if (kernel == 2 && learned) {
+        word = net.err;
+        cudaMemsetAsync(word, 0, sizeof(int), s);
+        net.selftest_wait(s);
+      } else {
+        return EngineBase::selftest_wait(kernel);
+      }
+      int h = 0;
+      cudaMemcpyAsync(&h, word, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("wait self-test");
+      cudaMemsetAsync(word, 0, sizeof(int), s);  // re-armed for the next solve
+      if (h) return fail(ICEP_ERR_TIMEOUT, kernel == 1 ? "fused plane pass: bounded wait ran out (self-test)"
+                                                        : "network convolution: bounded wait ran out (self-test)");
+      return ICEP_OK;
+    } else {
+      return EngineBase::selftest_wait(kernel);
+    }
+  }
+
   int sync() override {
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("sync");
     return ICEP_OK;
@@ -2062,6 +2092,16 @@ class Engine : public EngineBase {
       case C_TRUNCATE: truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s); break;
       case C_CHARGE_FIELD: st = conc_k2charge(F_RHO, F_WORK, F_UP0); break;
       case C_INIT_ION: init_ions(); break;
+      case C_APPLY_BK:
+        if constexpr (std::is_same<R, float>::value) {
+          if (!kop_supported(g)) return fail(ICEP_ERR_UNSUPPORTED, "apply_bk: no fused passes for this mesh");
+          mean_eps_cached = mean_eps();
+          kop_eps_faces(g, f[F_EPS], f[F_EF0], f[F_EF1], f[F_EF2], s);
+          apply_Bk(f[F_WV1], f[F_WORK]);
+          break;
+        } else {
+          return fail(ICEP_ERR_UNSUPPORTED, "apply_bk needs precision MIXED");
+        }
       default: return fail(ICEP_ERR_ARG, "unknown call id");
     }
     if (st) return st;

@@ -57,6 +57,12 @@ struct EngineBase {
     return unsupported_learned();
   }
   virtual int learned_backward(const double *gy, double *grad) { return unsupported_learned(); }
+  // launch one kernel whose bounded wait must run out (1: fused plane pass,
+  // 2: tcgen05 convolution) and return the status a solve would return
+  virtual int selftest_wait(int kernel) {
+    err = "the wait self-test needs a MIXED context (kernel 1) or solver LEARNED (kernel 2)";
+    return ICEP_ERR_UNSUPPORTED;
+  }
   int unsupported_learned() {
     err = "the learned preconditioner needs precision MIXED and solver LEARNED";
     return ICEP_ERR_UNSUPPORTED;
@@ -80,7 +86,11 @@ enum CallId {
   C_ZETA_K2U_K = 1, C_U_K2ZETA_K, C_U2ADVECTION_K, C_SOLENOIDAL_U, C_NS_SLAVED_EULER,
   C_MAKE_PHI_SUM, C_MAKE_U_SUM, C_F_HYDRO, C_LJ, C_POS_EULER, C_POS_AB2, C_VEL_EULER,
   C_VEL_AB2, C_DIELECTRIC_FIELD, C_BUILD_RHS, C_SOLVE_POTENTIAL, C_MAXWELL, C_NSSOLUTE_EULER,
-  C_SURFACE_NORMAL, C_F_PARTICLE_SOLE, C_TRUNCATE, C_CHARGE_FIELD, C_INIT_ION, C_ZETA_K2U
+  C_SURFACE_NORMAL, C_F_PARTICLE_SOLE, C_TRUNCATE, C_CHARGE_FIELD, C_INIT_ION, C_ZETA_K2U,
+  // 25 is the checkers' field-output call; MIXED only (a check of the fused
+  // operator): WORK = B WV1 = A M^-1 WV1 on the half spectrum in WV1, through
+  // the three fused passes
+  C_APPLY_BK = 26
 };
 
 }  // namespace icep

@@ -269,6 +269,8 @@ int icep_unpin_host(void *p) {
   return cudaHostUnregister(p) == cudaSuccess ? ICEP_OK : ICEP_ERR_CUDA;
 }
 
+int icep_selftest_wait(icep_ctx *c, int kernel) { return ok(c) ? wrap(c, c->e->selftest_wait(kernel)) : ICEP_ERR_ARG; }
+
 /* generic dispatch used by the Python layer (same numbering as the oracle) */
 int icep_call(icep_ctx *c, int fn) { return ok(c) ? wrap(c, c->e->call(fn)) : ICEP_ERR_ARG; }
 

@@ -265,20 +265,31 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
                "l"(src), "r"(bytes), "r"(mbar)
                : "memory");
 }
-// Wait for phase `parity` of the mbarrier, at most `limit` polls; on timeout
-// the error word is set (the host reports it) and the caller goes on.
-__device__ __forceinline__ void mbar_wait(uint32_t mbar, uint32_t parity, int *err) {
-  for (int it = 0; it < (1 << 16); it++) {
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for phase `parity` of the mbarrier for at most `limit_ns` of
+// %globaltimer time (a preempted kernel sees the copy complete when it
+// resumes, so a time limit does not fire under load); false on timeout.
+__device__ __forceinline__ bool mbar_wait_for(uint32_t mbar, uint32_t parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = globaltimer();
+  while (true) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
         : "r"(mbar), "r"(parity)
         : "memory");
-    if (done) return;
+    if (done) return true;
+    if (globaltimer() - t0 > limit_ns) return false;
   }
-  atomicExch(err, 1);
 }
+// Copy-arrival limit of the plane passes (a 66 KB copy lands in
+// microseconds) and the short limit of the bounded-wait self-test.
+constexpr unsigned long long KOP_WAIT_NS = 200ull * 1000 * 1000;
+constexpr unsigned long long KOP_TEST_WAIT_NS = 50ull * 1000;
 
 // First-stage source of the y transforms with the kz = 0 and kz = NZ/2
 // columns packed into pencil 0 (p holds that pencil's elements).
@@ -338,7 +349,14 @@ __global__ void __launch_bounds__(1024) k_kop_plane(Grid g, float *w0, float *w1
   load_table(sty, twy, NY);
   load_table(stz, twz, H);
   load_table(spost, post, H + 1);
-  mbar_wait(mb0, 0, err);
+  if (__syncthreads_or(!mbar_wait_for(mb0, 0, KOP_WAIT_NS))) {
+    // a copy did not land: report it, let both copies finish before the
+    // block's shared memory is released, and leave
+    if (lin == 0) atomicExch(err, 1);
+    mbar_wait_for(mb0, 0, KOP_WAIT_NS);
+    mbar_wait_for(mb1, 0, KOP_WAIT_NS);
+    return;
+  }
   // raw plane [j][k] (in B) -> swizzled y layout (columns 0..H-1) + column H
   for (int q = lin; q < NY * (H + 1); q += nthr) {
     const int j = q / (H + 1), k = q - j * (H + 1);
@@ -378,8 +396,11 @@ __global__ void __launch_bounds__(1024) k_kop_plane(Grid g, float *w0, float *w1
     }
     zbuf[swz(k, j, rsw)] = merge_inv(x, cconj(c), spost[k]);
   }
-  __syncthreads();
-  mbar_wait(mb1, 0, err);
+  if (__syncthreads_or(!mbar_wait_for(mb1, 0, KOP_WAIT_NS))) {
+    if (lin == 0) atomicExch(err, 1);
+    mbar_wait_for(mb1, 0, KOP_WAIT_NS);
+    return;
+  }
   // z inverse, times the scaled face permittivity, z forward: row j stays on
   // the same lane group throughout, so no block synchronisation in between
   constexpr int zst = Plan<H>::nstages;
@@ -421,6 +442,301 @@ __global__ void __launch_bounds__(1024) k_kop_plane(Grid g, float *w0, float *w1
       cplane[q] = yout[swz(j, k, ysw)];
     }
   }
+}
+
+// ---- register-resident plane pass -------------------------------------------
+//
+// The same transform as k_kop_plane with the 1D transforms held in registers:
+// a length-N DFT (N = T P) runs on T threads, thread t holding x[t + T m] for
+// m < P. Step 1 is a P-point DFT over m in registers and the twiddle
+// w_N^(t q1); one exchange through a shared region hands thread t' the T
+// values b[tau][q1] for q1 = t' + T s (s < P/T); step 2 is a T-point DFT over
+// tau, which leaves X[q1 + P q2] in register r = s + (P/T) q2, i.e. thread t'
+// holds X[t' + T r]: the output has the input's distribution, so an inverse
+// transform, the permittivity product and a forward transform chain with no
+// re-layout in between. A plane costs one shared-memory exchange per 1D
+// transform instead of one per radix stage.
+
+constexpr float KC1 = 0.92387953251128675613f;  // cos(pi/8)
+constexpr float KS1 = 0.38268343236508977173f;  // sin(pi/8)
+constexpr float KH = 0.70710678118654752440f;   // sqrt(1/2)
+
+// 16-point forward DFT in registers, natural order: 4 x 4 with the twiddles
+// w_16^(n1 k1) between the two radix-4 layers.
+__device__ __forceinline__ void dft16(cf *x) {
+  cf u[4][4];
+#pragma unroll
+  for (int n1 = 0; n1 < 4; n1++) {
+    cf v[4] = {x[n1], x[n1 + 4], x[n1 + 8], x[n1 + 12]};
+    dft4(v);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; k1++) u[n1][k1] = v[k1];
+  }
+  const cf w1{KC1, -KS1}, w2{KH, -KH}, w3{KS1, -KC1}, w6{-KH, -KH}, w9{-KC1, KS1};
+  u[1][1] = cmul(u[1][1], w1);
+  u[1][2] = cmul(u[1][2], w2);
+  u[1][3] = cmul(u[1][3], w3);
+  u[2][1] = cmul(u[2][1], w2);
+  u[2][2] = mul_mi(u[2][2]);
+  u[2][3] = cmul(u[2][3], w6);
+  u[3][1] = cmul(u[3][1], w3);
+  u[3][2] = cmul(u[3][2], w6);
+  u[3][3] = cmul(u[3][3], w9);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; k1++) {
+    cf v[4] = {u[0][k1], u[1][k1], u[2][k1], u[3][k1]};
+    dft4(v);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; k2++) x[k1 + 4 * k2] = v[k2];
+  }
+}
+template <int P>
+__device__ __forceinline__ void dftp(cf *x) {
+  static_assert(P == 4 || P == 8 || P == 16, "register DFT length");
+  if constexpr (P == 16) dft16(x);
+  else if constexpr (P == 8) dft8(x);
+  else dft4(x);
+}
+
+// Position of b[tau][q1] in an exchange region of T*P values: T per q1, the
+// thread index XOR-swizzled so that both the writes (fixed q1) and the reads
+// (fixed tau, q1 = t' + T s) of a half-warp hit distinct banks; `par` is bit
+// 3 of the region index (regions 8 apart share a half-warp for T = 8).
+template <int T>
+__device__ __forceinline__ int xpos(int q1, int tau, int par) {
+  if constexpr (T == 8) return 8 * q1 + (tau ^ ((q1 >> 1) & 3) ^ (par << 2));
+  else return 4 * q1 + (tau ^ (q1 & 3));
+}
+
+// Length-(T P) DFT of the thread's P registers (see above): forward, or the
+// inverse as conj(DFT(conj x)). `reg` is the transform's exchange region,
+// `tw` the table w_N^m, m < N. The caller orders reuse of `reg` around it.
+template <int T, int P>
+__device__ __forceinline__ void reg_dft(cf *x, int t, cf *reg, int par, const cf *tw, bool inverse) {
+  static_assert(P >= T, "each thread takes P/T of the T-point DFTs");
+  if (inverse) {
+#pragma unroll
+    for (int m = 0; m < P; m++) x[m] = cconj(x[m]);
+  }
+  dftp<P>(x);
+#pragma unroll
+  for (int q1 = 1; q1 < P; q1++) x[q1] = cmul(x[q1], tw[t * q1]);
+#pragma unroll
+  for (int q1 = 0; q1 < P; q1++) reg[xpos<T>(q1, t, par)] = x[q1];
+  __syncwarp();
+  constexpr int S = P / T;
+#pragma unroll
+  for (int s = 0; s < S; s++) {
+    cf c[T];
+    const int q1 = t + T * s;
+#pragma unroll
+    for (int tau = 0; tau < T; tau++) c[tau] = reg[xpos<T>(q1, tau, par)];
+    dftp<T>(c);
+#pragma unroll
+    for (int q2 = 0; q2 < T; q2++) x[s + S * q2] = inverse ? cconj(c[q2]) : c[q2];
+  }
+}
+
+// shared -> global bulk copy of `bytes` from this CTA (16-byte aligned
+// addresses, size a multiple of 16), waited for before the CTA goes on
+__device__ __forceinline__ void bulk_s2g_wait(void *dst, uint32_t src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
+               : "memory");
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+// Thread shapes of the register plane pass: y transforms on TY = 8 threads
+// (PY = NY/8 values each) for the H columns; z transforms on TZ threads for
+// the NY rows, RZ rows per thread in turn.
+template <int NY, int H>
+struct RPlane {
+  static constexpr int TY = 8, PY = NY / 8;
+  static constexpr int TZ = (H >= 64) ? 8 : 4, PZ = H / TZ;
+  static constexpr int NT = H * TY;
+  static constexpr int RZ = NY * TZ / NT;
+  static constexpr int BUF = NY * (H + 1);  // complex values: the plane, [j][kz]
+  static_assert(PY >= TY && PZ >= TZ && RZ >= 1 && NY * TZ == RZ * NT, "register plane shape");
+  static_assert(H <= NY, "the y exchange regions fit in the plane buffer");
+};
+template <int NY, int H>
+__host__ __device__ constexpr size_t rplane_smem() {
+  return ((size_t)RPlane<NY, H>::BUF + NY + H + (H + 1)) * sizeof(cf) + 2 * sizeof(unsigned long long);
+}
+
+// Row j of the z phase for warp w, lane group jr, round p: rows of a
+// half-warp 8 (TZ = 8) or 4 (TZ = 4) apart, which keeps the row-major tile
+// accesses conflict-free.
+template <int TZ>
+__device__ __forceinline__ int rplane_row(int w, int jr, int p) {
+  if constexpr (TZ == 8) return (w & 7) + 8 * jr + 32 * (w >> 3) + 64 * p;
+  else return (w & 3) + 4 * jr + 32 * (w >> 2) + 64 * p;
+}
+
+// One block per (x-plane, component), H*8 threads. The plane arrives by one
+// bulk copy into `buf` ([j][kz], row stride H+1) and leaves by one. y phase:
+// thread (column k, t) holds rows t + 8m of its column (column 0 carries
+// the packed kz = 0 and kz = NZ/2 columns after their Hermitian completion
+// in j); z phase: thread (row j, tz) holds elements tz + TZ m of the merged
+// H-point complex row, which after the inverse are the real row's values,
+// multiplied by the scaled face permittivity (read from global memory
+// straight into registers) and transformed forward in place; the y forward
+// transform reads the split half spectrum. `test_wait` (the bounded-wait
+// self-test): no copy is issued and the wait runs out, which must reach the
+// host through `err`.
+template <int NY, int H>
+__global__ void __launch_bounds__(H * 8, (H >= 64) ? 2 : 4)
+    k_kop_plane_r(Grid g, float *w0, float *w1, float *w2, const float *ef0, const float *ef1, const float *ef2,
+                  const cf *__restrict__ twy, const cf *__restrict__ twz, const cf *__restrict__ post, float scale,
+                  int *err, int test_wait) {
+  using S = RPlane<NY, H>;
+  constexpr int TY = S::TY, PY = S::PY, TZ = S::TZ, PZ = S::PZ, RS = H + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cf *buf = reinterpret_cast<cf *>(smem_raw);
+  cf *sty = buf + S::BUF;
+  cf *stz = sty + NY;
+  cf *spost = stz + H;
+  unsigned long long *mb = reinterpret_cast<unsigned long long *>(spost + H + 1);
+  const int i = blockIdx.x, d = blockIdx.y;
+  float *data = (d == 0) ? w0 : (d == 1) ? w1 : w2;
+  const float *ef = (d == 0) ? ef0 : (d == 1) ? ef1 : ef2;
+  cf *cplane = reinterpret_cast<cf *>(data) + (long)i * S::BUF;
+  const float2 *efp = reinterpret_cast<const float2 *>(ef) + (long)i * S::BUF;  // [j][NZ_] floats as float2
+  const int lin = threadIdx.x, lane = lin & 31, w = lin >> 5;
+  constexpr uint32_t BYTES = S::BUF * sizeof(cf);
+  const uint32_t mb0 = smem_addr(&mb[0]);
+  if (lin == 0) {
+    mbar_init(mb0, 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (lin == 0) {
+    if (test_wait) {
+      mbar_expect_tx(mb0, 16);  // a transaction that nothing will complete
+    } else {
+      mbar_expect_tx(mb0, BYTES);
+      bulk_g2s(smem_addr(buf), cplane, BYTES, mb0);
+    }
+  }
+  for (int q = lin; q < NY; q += S::NT) sty[q] = twy[q];
+  for (int q = lin; q < H; q += S::NT) stz[q] = twz[q];
+  for (int q = lin; q <= H; q += S::NT) spost[q] = post[q];
+  const bool ok = mbar_wait_for(mb0, 0, test_wait ? KOP_TEST_WAIT_NS : KOP_WAIT_NS);
+  if (__syncthreads_or(!ok)) {
+    // the copy did not land: report it, let a copy still in flight finish
+    // before the block's shared memory is released, and leave
+    if (lin == 0) atomicExch(err, 1);
+    if (!test_wait) mbar_wait_for(mb0, 0, KOP_WAIT_NS);
+    return;
+  }
+  // ---- y inverse: thread (column k, t), rows t + 8m
+  const int t = lane & 7, kc = lane >> 3;
+  const int k = (w & 7) + 8 * kc + 32 * (w >> 3);
+  const int par = (k >> 3) & 1;
+  cf a[PY];
+  if (k == 0) {
+    // the j-direction half of the Hermitian completion of the kz = 0 and
+    // kz = NZ/2 columns (kz = 0 keeps rows 1..NY/2-1, kz = NZ/2 keeps rows
+    // NY/2+1..NY-1; rows 0 and NY/2 are used as they are), packed as
+    // Z = X0 + i XH
+#pragma unroll
+    for (int m = 0; m < PY; m++) {
+      const int j = t + 8 * m, jm = (NY - j) & (NY - 1);
+      const bool low = (j >= 1 && j < NY / 2), high = (j > NY / 2);
+      const cf x0 = high ? cconj(buf[jm * RS]) : buf[j * RS];
+      const cf xh = low ? cconj(buf[jm * RS + H]) : buf[j * RS + H];
+      a[m] = cf{x0.x - xh.y, x0.y + xh.x};
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < PY; m++) a[m] = buf[(t + 8 * m) * RS + k];
+  }
+  __syncthreads();  // the plane is in registers: buf becomes exchange space
+  reg_dft<TY, PY>(a, t, buf + k * (NY + 1), par, sty, true);
+  __syncthreads();  // every column's exchange is read
+#pragma unroll
+  for (int r = 0; r < PY; r++) buf[(t + 8 * r) * RS + k] = a[r];
+  __syncthreads();
+  // ---- z: merge, inverse, times the scaled face permittivity, forward
+  {
+    const int tz = lane & (TZ - 1), jr = lane / TZ;
+#pragma unroll 1
+    for (int p = 0; p < S::RZ; p++) {
+      const int j = rplane_row<TZ>(w, jr, p);
+      cf *row = buf + j * RS;
+      float2 e2[PZ];
+#pragma unroll
+      for (int m = 0; m < PZ; m++) e2[m] = __ldg(efp + j * RS + tz + TZ * m);
+      cf z[PZ];
+#pragma unroll
+      for (int m = 0; m < PZ; m++) {
+        const int n = tz + TZ * m;
+        cf x, c;
+        if (n == 0) {  // column 0 holds x0 + i xh, both real
+          const cf zz = row[0];
+          x = cf{zz.x, 0.f};
+          c = cf{zz.y, 0.f};
+        } else {
+          x = row[n];
+          c = row[H - n];
+        }
+        z[m] = merge_inv(x, cconj(c), spost[n]);
+      }
+      __syncwarp();  // the row's values are in registers: its storage becomes exchange space
+      const int rpar = (j >> 3) & 1;
+      reg_dft<TZ, PZ>(z, tz, row, rpar, stz, true);
+#pragma unroll
+      for (int m = 0; m < PZ; m++) z[m] = cf{(z[m].x * scale) * e2[m].x, (z[m].y * scale) * e2[m].y};
+      __syncwarp();
+      reg_dft<TZ, PZ>(z, tz, row, rpar, stz, false);
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < PZ; m++) row[tz + TZ * m] = z[m];
+    }
+  }
+  __syncthreads();
+  // ---- y forward of the split half spectrum (column 0: the real kz = 0 and
+  // kz = NZ/2 values packed)
+  if (k == 0) {
+#pragma unroll
+    for (int m = 0; m < PY; m++) {
+      const cf z0 = buf[(t + 8 * m) * RS], c0 = cconj(z0);
+      a[m] = cf{split_fwd(z0, c0, spost[0]).x, split_fwd(z0, c0, spost[H]).x};
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < PY; m++) {
+      const int j = t + 8 * m;
+      a[m] = split_fwd(buf[j * RS + k], cconj(buf[j * RS + H - k]), spost[k]);
+    }
+  }
+  __syncthreads();
+  reg_dft<TY, PY>(a, t, buf + k * (NY + 1), par, sty, false);
+  __syncthreads();
+  // unpacking of column 0 (partner row NY - j: lane (8 - t) & 7 of the same
+  // group, register PY-1-r; row 8r of lane 0 pairs with its own register
+  // (PY - r) mod PY), then the plane to buf in its global layout
+  if (w == 0) {
+#pragma unroll
+    for (int r = 0; r < PY; r++) {
+      const int src = (lane & ~7) | ((8 - t) & 7);
+      cf zm{__shfl_sync(0xffffffffu, a[PY - 1 - r].x, src), __shfl_sync(0xffffffffu, a[PY - 1 - r].y, src)};
+      if (t == 0) zm = a[(PY - r) & (PY - 1)];
+      if (k == 0) {
+        const cf z = a[r], zc = cconj(zm);
+        const int j = t + 8 * r;
+        buf[j * RS] = cf{0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y)};
+        buf[j * RS + H] = cf{0.5f * (z.y - zc.y), -0.5f * (z.x - zc.x)};
+      }
+    }
+  }
+  if (k != 0) {
+#pragma unroll
+    for (int r = 0; r < PY; r++) buf[(t + 8 * r) * RS + k] = a[r];
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  if (lin == 0) bulk_s2g_wait(cplane, smem_addr(buf), BYTES);
 }
 
 // Last-stage sink of the forward x transforms: acc += k_D exp(-i dx k_D/2) X_D
@@ -606,22 +922,42 @@ void set_x_attr() {
   attr = true;
 }
 
+// the register plane pass covers NY in {64, 128} and NZ/2 in {32, 64}
+template <int NY, int H>
+constexpr bool rplane_ok() {
+  return (NY == 64 || NY == 128) && (H == 32 || H == 64) && H <= NY;
+}
+
 template <int NY, int H>
 void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-                     const float *ef2, int *err, cudaStream_t s) {
-  const size_t sm = plane_smem_f(NY, H);
-  static bool attr = false;  // one attribute call per instantiation
-  if (!attr) {
-    cudaFuncSetAttribute(k_kop_plane<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    attr = true;
-  }
+                     const float *ef2, int *err, cudaStream_t s, int test_wait = 0) {
   const float scale = (float)(1.0 / ((double)p.g.nx * p.g.ny * p.g.nz));
-  count_launch();
-  probe_begin(PROBE_KOP_PLANE, s);
-  k_kop_plane<NY, H><<<dim3(p.g.nx, 3), 1024, sm, s>>>(p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z,
-                                                             p.tw_post, scale, err);
-  // algorithmic bytes: per field the half spectrum in and out and eps_face_d in
-  probe_end(PROBE_KOP_PLANE, 3.0 * 3.0 * sizeof(float) * (double)p.g.nreal(), s);
+  if constexpr (rplane_ok<NY, H>()) {
+    constexpr size_t sm = rplane_smem<NY, H>();
+    static bool attr = false;  // one attribute call per instantiation
+    if (!attr) {
+      cudaFuncSetAttribute(k_kop_plane_r<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      attr = true;
+    }
+    count_launch();
+    probe_begin(PROBE_KOP_PLANE, s);
+    k_kop_plane_r<NY, H><<<dim3(p.g.nx, 3), RPlane<NY, H>::NT, sm, s>>>(
+        p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z, p.tw_post, scale, err, test_wait);
+    // algorithmic bytes: per field the half spectrum in and out and eps_face_d in
+    probe_end(PROBE_KOP_PLANE, 3.0 * 3.0 * sizeof(float) * (double)p.g.nreal(), s);
+  } else {
+    const size_t sm = plane_smem_f(NY, H);
+    static bool attr = false;  // one attribute call per instantiation
+    if (!attr) {
+      cudaFuncSetAttribute(k_kop_plane<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      attr = true;
+    }
+    count_launch();
+    probe_begin(PROBE_KOP_PLANE, s);
+    k_kop_plane<NY, H><<<dim3(p.g.nx, 3), 1024, sm, s>>>(p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z,
+                                                               p.tw_post, scale, err);
+    probe_end(PROBE_KOP_PLANE, 3.0 * 3.0 * sizeof(float) * (double)p.g.nreal(), s);
+  }
 }
 
 template <int NY>
@@ -682,6 +1018,17 @@ void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const f
     case 64: launch_plane_n<64>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
     default: launch_plane_n<128>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
   }
+}
+
+bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0,
+                        const float *ef1, const float *ef2, int *err, cudaStream_t s) {
+  const int ny = p.g.ny, h = p.g.nz / 2;
+  if (ny == 128 && h == 64) launch_plane_nh<128, 64>(p, w0, w1, w2, ef0, ef1, ef2, err, s, 1);
+  else if (ny == 128 && h == 32) launch_plane_nh<128, 32>(p, w0, w1, w2, ef0, ef1, ef2, err, s, 1);
+  else if (ny == 64 && h == 64) launch_plane_nh<64, 64>(p, w0, w1, w2, ef0, ef1, ef2, err, s, 1);
+  else if (ny == 64 && h == 32) launch_plane_nh<64, 32>(p, w0, w1, w2, ef0, ef1, ef2, err, s, 1);
+  else return false;
+  return true;
 }
 
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,

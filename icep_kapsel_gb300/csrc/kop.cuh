@@ -49,6 +49,11 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
 // complete within the kernel's wait limit (checked by the caller)
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
                const float *ef2, int *err, cudaStream_t s);
+// Bounded-wait self-test of the plane pass: the register plane kernel
+// launched so that its copy-arrival wait runs out (no copy is issued), which
+// sets *err; false when the grid has no register plane kernel.
+bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0,
+                        const float *ef1, const float *ef2, int *err, cudaStream_t s);
 // mode KOP_P: partials[2b] = (other, out) with other = r0;
 // mode KOP_S: partials[2b] = (out, out), partials[2b+1] = (out, other) with other = s;
 // finals[c] = sum over blocks of partials[2b + c], summed by the last block

@@ -150,22 +150,34 @@ template <int M, int N>
 __host__ __device__ constexpr uint32_t tc_idesc() {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
-__device__ __forceinline__ void tc_wait(uint32_t mbar, uint32_t parity, int *err) {
-  for (int it = 0; it < (1 << 16); it++) {
+__device__ __forceinline__ unsigned long long tc_clock() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Wait for phase `parity` of the mbarrier for at most `limit_ns` of
+// %globaltimer time; false on timeout.
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity, unsigned long long limit_ns) {
+  const unsigned long long t0 = tc_clock();
+  while (true) {
     uint32_t done;
     asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
                  : "=r"(done)
                  : "r"(mbar), "r"(parity)
                  : "memory");
-    if (done) return;
+    if (done) return true;
+    if (tc_clock() - t0 > limit_ns) return false;
   }
-  atomicExch(err, 1);
 }
+// MMA-completion limit (a tap's MMAs take microseconds) and the short limit
+// of the bounded-wait self-test
+constexpr unsigned long long TC_WAIT_NS = 200ull * 1000 * 1000;
+constexpr unsigned long long TC_TEST_WAIT_NS = 50ull * 1000;
 
 template <int CINA, int CINB, int COUT, bool RELU>
 __global__ void __launch_bounds__(128) k_conv_tc(int lg, const bf16 *__restrict__ a, const bf16 *__restrict__ b,
                                                  const bf16 *__restrict__ W, const float *__restrict__ bias, bf16 *out,
-                                                 int *err) {
+                                                 int *err, int test_wait) {
   constexpr int CIN = CINA + CINB, KG = CIN / 8, KSTEPS = CIN / 16;
   constexpr int NCOL = COUT <= 32 ? 32 : (COUT <= 64 ? 64 : 128);
   constexpr int ABYTES = TC_M * CIN * 2, BBYTES = COUT * CIN * 2;
@@ -195,9 +207,14 @@ __global__ void __launch_bounds__(128) k_conv_tc(int lg, const bf16 *__restrict_
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
+  // test_wait (the bounded-wait self-test): no MMA is issued, so the first
+  // completion wait runs out and the timeout path below must reach the host
+  const unsigned long long lim = test_wait ? TC_TEST_WAIT_NS : TC_WAIT_NS;
+  bool failed = false;
   for (int t = 0; t < 27; t++) {
     const int buf = t & 1;
-    if (t >= 2) tc_wait(sh_addr(&mbar[buf]), ((t - 2) >> 1) & 1, err);  // the MMAs of tap t-2 read this buffer
+    // the MMAs of tap t-2 read this buffer
+    const bool late = (t >= 2) && !tc_wait(sh_addr(&mbar[buf]), ((t - 2) >> 1) & 1, lim);
     // operand rows: this thread's voxel neighbour at tap t, CIN channels in 16-byte chunks
     int dx, dy, dz;
     tap(t, dx, dy, dz);
@@ -221,8 +238,16 @@ __global__ void __launch_bounds__(128) k_conv_tc(int lg, const bf16 *__restrict_
           *reinterpret_cast<const uint4 *>(W + ((long)t * COUT + co) * CIN + c * 8);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == 0) {
+    if (__syncthreads_or(late)) {
+      // a completion did not arrive: report it, let the MMAs of taps t-2
+      // and t-1 finish before the accumulator is released, and leave
+      if (tid == 0) atomicExch(err, 1);
+      tc_wait(sh_addr(&mbar[buf ^ 1]), ((t - 1) >> 1) & 1, lim);
+      tc_wait(sh_addr(&mbar[buf]), ((t - 2) >> 1) & 1, lim);
+      failed = true;
+      break;
+    }
+    if (tid == 0 && !test_wait) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
       for (int kk = 0; kk < KSTEPS; kk++) {
@@ -241,11 +266,15 @@ __global__ void __launch_bounds__(128) k_conv_tc(int lg, const bf16 *__restrict_
     }
   }
   // the last commit (tap 26, buffer 0, its 14th) follows every MMA
-  tc_wait(sh_addr(&mbar[0]), 13 & 1, err);
+  if (!failed && __syncthreads_or(!tc_wait(sh_addr(&mbar[0]), 13 & 1, lim))) {
+    if (tid == 0) atomicExch(err, 1);
+    tc_wait(sh_addr(&mbar[0]), 13 & 1, lim);
+    failed = true;
+  }
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   // epilogue: warp w holds rows 32w..32w+31 of the accumulator
 #pragma unroll
-  for (int c0 = 0; c0 < COUT; c0 += 16) {
+  for (int c0 = 0; c0 < (failed ? 0 : COUT); c0 += 16) {
     uint32_t r[16];
     const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
     asm volatile(
@@ -568,7 +597,7 @@ void conv_mma(int lg, const bf16 *a, const bf16 *b, const bf16 *W, const float *
 
 template <int CINA, int CINB, int COUT, bool RELU>
 void conv_tc(int lg, const bf16 *a, const bf16 *b, const bf16 *W, const float *bias, bf16 *out, int *err,
-             cudaStream_t s) {
+             cudaStream_t s, int test_wait = 0) {
   const long V = 1L << (3 * lg);
   constexpr int CIN = CINA + CINB;
   const size_t sm = 2 * (size_t)(TC_M * CIN + COUT * CIN) * sizeof(bf16);
@@ -578,7 +607,8 @@ void conv_tc(int lg, const bf16 *a, const bf16 *b, const bf16 *W, const float *b
     attr = true;
   }
   count_launch();
-  k_conv_tc<CINA, CINB, COUT, RELU><<<(unsigned)((V + TC_M - 1) / TC_M), 128, sm, s>>>(lg, a, b, W, bias, out, err);
+  k_conv_tc<CINA, CINB, COUT, RELU><<<(unsigned)((V + TC_M - 1) / TC_M), 128, sm, s>>>(lg, a, b, W, bias, out, err,
+                                                                                    test_wait);
 }
 
 template <typename TA, typename TZ, int CINA, int CINB, int COUT>
@@ -676,6 +706,10 @@ void UNet::pack(cudaStream_t s) {
     count_launch();
     k_pack_layer<<<nb256(cnt), 256, 0, s>>>(cin[l], cout[l], params + woff[l], wf + wbf_off[l], wb + wbf_off[l]);
   }
+}
+
+void UNet::selftest_wait(cudaStream_t s) {
+  conv_tc<16, 0, 16, true>(ilog2(n), e0a, nullptr, wf + wbf_off[L_C0B], params + boff[L_C0B], e0, err, s, 1);
 }
 
 void UNet::forward(cudaStream_t s) {

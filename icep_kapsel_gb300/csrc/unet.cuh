@@ -53,6 +53,9 @@ struct UNet {
   // grads = dL/dparams given gy = dL/dy (forward() must have run on the same x)
   void backward(cudaStream_t s);
   void adam_step(float lr, cudaStream_t s);
+  // one tcgen05 convolution launched so that its completion wait runs out
+  // (no MMA is issued), which sets *err
+  void selftest_wait(cudaStream_t s);
 };
 
 // x (coarse, 2 ch) from the fine permittivity and a fine real residual

@@ -29,6 +29,7 @@ CALLS = ["zeta_k2u_k", "u_k2zeta_k", "u2advection_k", "solenoidal_u", "ns_slaved
          "nssolute_euler", "surface_normal", "f_particle_sole", "truncate", "charge_field",
          "init_ion", "zeta_k2u"]
 CALL_ID = {n: i + 1 for i, n in enumerate(CALLS)}
+CALL_ID["apply_bk"] = 26  # MIXED: WORK = B WV1 through the fused k-space passes (25: the checkers' field output)
 
 _DP = C.POINTER(C.c_double)
 _lib = None
@@ -109,6 +110,7 @@ def load_library(path=None):
     L.icep_learned_forward.argtypes = [V, _DP, _DP, C.c_double, _DP]
     L.icep_learned_backward.argtypes = [V, _DP, _DP]
     L.icep_learned_stats.argtypes = [V, C.POINTER(I), C.POINTER(I)]
+    L.icep_selftest_wait.argtypes = [V, I]
     _lib = L
     return L
 
@@ -194,6 +196,13 @@ class Simulation:
 
     def call(self, name):
         self._check(self.lib.icep_call(self.ctx, CALL_ID[name]), name)
+
+    def selftest_wait(self, kernel):
+        """icep_selftest_wait: the status (ICEP_ERR_TIMEOUT expected) and the
+        error text of a kernel launched so that its bounded wait runs out."""
+        st = self.lib.icep_selftest_wait(self.ctx, int(kernel))
+        msg = self.lib.icep_last_error(self.ctx)
+        return st, (msg.decode() if msg else "")
 
     def particles(self):
         arr = (abi.Particle * max(self.np, 1))()

@@ -31,6 +31,10 @@ extern "C" {
 #define ICEP_ERR_NOT_CONVERGED 4
 #define ICEP_ERR_STATE 5
 #define ICEP_ERR_IO 6
+/* A bounded wait inside a kernel ran out (an asynchronous copy or tensor-core
+ * operation did not complete in time): the kernel skipped its work and
+ * returned, the context stays usable, the step's results are not valid. */
+#define ICEP_ERR_TIMEOUT 7
 
 typedef struct icep_ctx icep_ctx;
 
@@ -330,6 +334,15 @@ int icep_step_timed(icep_ctx *ctx, int nsteps, double *ms);
  * 6 particle forces and velocities, 7 rigidity force, 8 back to vorticity,
  * 9 unused. Returns ICEP_ERR_STATE when profiling is off. */
 int icep_phase_times(icep_ctx *ctx, double *ms, int n);
+/* Check of the bounded device waits (no counterpart in the reference):
+ * launches one kernel in a mode that issues no asynchronous copy or MMA, so
+ * that its mbarrier wait runs out after ~50 us -- kernel 1: the fused plane
+ * pass of the k-space Poisson operator (MIXED context, 64^3 or 128^3 class
+ * meshes), 2: the network's tcgen05 convolution (solver LEARNED) -- and
+ * returns the status a solve would return when that happens:
+ * ICEP_ERR_TIMEOUT, with the context left usable (ICEP_ERR_UNSUPPORTED for
+ * other contexts, ICEP_OK if the wait did not run out). */
+int icep_selftest_wait(icep_ctx *ctx, int kernel);
 /* Kernels launched by this library so far (all contexts). */
 unsigned long long icep_kernel_launches(void);
 /* Page-lock / release a caller's host buffer for the drop-in transfers. The

@@ -1,0 +1,121 @@
+"""The fused k-space Poisson operator of the MIXED solve and the bounded waits
+of its kernels.
+
+test_fused_operator_against_fp64: WORK = B WV1 = A M^-1 WV1 through the three
+fused passes (inverse x pass with the gradient multipliers, the plane pass,
+forward x pass with the staggered divergence) against an FP64 numpy
+restatement of the same operator: the reference's Ax (operate_dielectric.cxx:
+485-522: spectral staggered gradient i k exp(i dx k/2), face permittivity
+0.5 (eps + eps at the next point), staggered divergence) applied to
+M^-1 x, M^-1 = -1/(eps_ref |k|^2), on a random Hermitian-consistent half
+spectrum. The 64^3 and 128^3 meshes run the register-resident plane kernel,
+32^3 the shared-memory one. Tolerance: 2e-5 relative L2 (FP32 transforms).
+
+test_bounded_wait_*: a kernel launched so that its mbarrier wait runs out
+(nothing issued that could complete it) reports ICEP_ERR_TIMEOUT to the host
+through its error word, skips its work, and the context then steps normally.
+"""
+import numpy as np
+import pytest
+
+import cases
+from icep_kapsel_gb300 import abi
+
+pytestmark = pytest.mark.gpu
+
+ICEP_ERR_TIMEOUT = 7
+
+
+@pytest.fixture(scope="module")
+def Sim():
+    from icep_kapsel_gb300.build import build
+    build()
+    from icep_kapsel_gb300.runtime import Simulation
+    return Simulation
+
+
+def read_weight(n, h):
+    """Weights of the half-spectrum modes in a Parseval inner product (2, 1 at
+    self-conjugate points, 0 where the inverse transform does not read)."""
+    i = np.arange(n)[:, None, None]
+    j = np.arange(n)[None, :, None]
+    kz = np.arange(h + 1)[None, None, :]
+    w = np.full((n, n, h + 1), 2, dtype=np.int8)
+    edge = (kz == 0) | (kz == h)
+    selfc = (((n - i) % n) == i) & (((n - j) % n) == j)
+    kept = np.where((j >= 1) & (j <= n // 2 - 1), True, np.where((j == 0) | (j == n // 2), i <= n // 2, False))
+    kept = np.where(kz == h, ~kept, kept)
+    w = np.where(edge & selfc, 1, np.where(edge & ~kept, 0, w))
+    return np.broadcast_to(w, (n, n, h + 1))
+
+
+def apply_b_fp64(ph, eps, n):
+    h = n // 2
+    wave = 2 * np.pi / n
+    kint = np.where(np.arange(n) > n // 2, np.arange(n) - n, np.arange(n))
+    ks = [kint[:, None, None] * wave, kint[None, :, None] * wave, np.arange(h + 1)[None, None, :] * wave]
+    k2 = ks[0] ** 2 + ks[1] ** 2 + ks[2] ** 2
+    eref = eps.mean()
+    m = np.where(k2 > 0, -1.0 / (eref * np.where(k2 > 0, k2, 1.0)), 0.0)
+    out = np.zeros((n, n, h + 1), complex)
+    for d in range(3):
+        sh = np.exp(0.5j * ks[d])
+        w = np.fft.irfftn(m * 1j * ks[d] * sh * ph, s=(n, n, n), axes=(0, 1, 2))
+        ef = 0.5 * (eps + np.roll(eps, -1, axis=d))
+        out += 1j * ks[d] * np.conj(sh) * np.fft.rfftn(ef * w)
+    return out
+
+
+@pytest.mark.parametrize("n", [32, 64, 128])
+def test_fused_operator_against_fp64(Sim, n):
+    p, parts = cases.icep_case(n=n, npart=max(4, n // 8), minsep=10.0, seed=7, eps_f=80.0, eps_p=2.0,
+                               e_ext=(0.0, 0.0, 0.1), tol=1e-8, solver=abi.SOLVER_SPECTRAL,
+                               precision=abi.MIXED)
+    s = Sim(p, parts)
+    s.call("dielectric_field")
+    eps = s.get("eps")[:, :, :n]
+    assert eps.min() < 10 and eps.max() > 70
+    rng = np.random.default_rng(n)
+    ph = np.fft.rfftn(rng.standard_normal((n, n, n)))
+    buf = np.zeros((n, n, n + 2))
+    buf[:, :, 0::2] = ph.real
+    buf[:, :, 1::2] = ph.imag
+    s.set("wv1", buf)
+    s.call("apply_bk")
+    got = s.get("work")
+    gh = got[:, :, 0::2] + 1j * got[:, :, 1::2]
+    ref = apply_b_fp64(ph, eps, n)
+    wt = read_weight(n, n // 2)
+    d2 = np.where(wt == 2, np.abs(gh - ref) ** 2, 0.0) + np.where(wt == 1, (gh.real - ref.real) ** 2, 0.0)
+    r2 = np.where(wt == 2, np.abs(ref) ** 2, 0.0) + np.where(wt == 1, ref.real ** 2, 0.0)
+    err = float(np.sqrt(d2.sum() / r2.sum()))
+    assert err < 2e-5, err
+    s.close()
+
+
+def test_bounded_wait_plane_pass(Sim):
+    p, parts = cases.icep_case(n=64, npart=8, minsep=10.0, seed=5, eps_f=80.0, eps_p=2.0, e_ext=(0.0, 0.0, 0.1),
+                               tol=1e-8, solver=abi.SOLVER_SPECTRAL, precision=abi.MIXED)
+    s = Sim(p, parts)
+    s.init_state()
+    st, msg = s.selftest_wait(1)
+    assert st == ICEP_ERR_TIMEOUT, (st, msg)
+    assert "bounded wait" in msg
+    s.step(2)  # the context stays usable: the next solve converges
+    _, err, _ = s.solver_stats()
+    assert err <= 1e-8
+    assert np.isfinite(s.get("zeta0")).all()
+    s.close()
+
+
+def test_bounded_wait_convolution(Sim):
+    p, parts = cases.icep_case(n=32, npart=4, minsep=10.0, seed=6, eps_f=80.0, eps_p=2.0, e_ext=(0.0, 0.0, 0.1),
+                               tol=1e-8, solver=abi.SOLVER_LEARNED, precision=abi.MIXED)
+    s = Sim(p, parts)
+    s.init_state()
+    st, msg = s.selftest_wait(2)
+    assert st == ICEP_ERR_TIMEOUT, (st, msg)
+    s.step(1)
+    _, err, _ = s.solver_stats()
+    assert err <= 1e-8
+    s.close()

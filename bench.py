@@ -151,6 +151,27 @@ def reduce_max(dist, x):
     return float(t.item())
 
 
+base_oracle = [None]
+
+
+def mixed_error(args, o, nsteps):
+    """Per-field relative L2 error of the MIXED GPU path against the FP64
+    oracle after the same `nsteps` steps of the workload (same algorithm:
+    spectral-preconditioned solve to the same true residual)."""
+    import cases
+    from icep_kapsel_gb300 import abi
+    from icep_kapsel_gb300.runtime import Simulation
+    p, parts = workload(args, abi.MIXED, abi.SOLVER_SPECTRAL)
+    m = Simulation(p, parts)
+    m.init_state()
+    m.step(nsteps)
+    e = cases.mixed_vs_oracle_errors(m, o, args.n, args.np)
+    m.close()
+    return {"steps": nsteps, "relative_l2": e,
+            "fields": "zeta0/zeta1 vorticity, u velocity, phi profile, pot potential (mean removed), "
+                      "c0/c1 ion densities, particle_x/particle_v positions/velocities"}
+
+
 def cpu_baseline(args, sample_steps=8):
     """The oracle (FP64 C restatement, all host threads) on a bounded sample of
     the same workload, with the GPU path's algorithm (spectral-preconditioned
@@ -168,6 +189,7 @@ def cpu_baseline(args, sample_steps=8):
         it.append(o.last_iterations())
     dt = time.perf_counter() - t0
     cores = o.lib.ko_max_threads()
+    base_oracle[0] = o  # its state after 1 + sample_steps steps, for the MIXED error
     return {"value": sample_steps / dt, "unit": UNIT, "cores": int(cores), "kind": "port",
             "sample": "%d full steps (after 1 warm-up step) of the %d^3 / %d-sphere workload: FP64 C restatement, "
                       "OpenMP, spectral-preconditioned Poisson solve to %g (%s iterations per step), %.1f s"
@@ -230,6 +252,7 @@ def run_gpu(args, world, rank, local, dist):
     lib = load_library()
     lib.icep_step_timed.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
     lib.icep_kernel_launches.restype = C.c_ulonglong
+    lib.icep_algorithmic_bytes.restype = C.c_ulonglong
     lib.icep_probe_start.argtypes = [C.c_int, C.c_int]
     lib.icep_probe_stop.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_longlong), C.POINTER(C.c_double)]
     lib.icep_pin_host.argtypes = [C.c_void_p, C.c_size_t]
@@ -245,6 +268,7 @@ def run_gpu(args, world, rank, local, dist):
         dist.barrier()
     ms = C.c_double(0)
     launches0 = lib.icep_kernel_launches()
+    abytes0 = lib.icep_algorithmic_bytes()
     # the dominant kernel's launches are timed with CUDA events on their
     # stream while the timed steps run
     lib.icep_probe_start(PROBE_KIND, 1 << 16)
@@ -255,12 +279,14 @@ def run_gpu(args, world, rank, local, dist):
     pms, pn, pbytes = C.c_double(0), C.c_longlong(0), C.c_double(0)
     lib.icep_probe_stop(C.byref(pms), C.byref(pn), C.byref(pbytes))
     launches = int(lib.icep_kernel_launches() - launches0)
+    step_bytes = float(lib.icep_algorithmic_bytes() - abytes0) / args.steps
     iters, err, _ = sim.solver_stats()
     t_ms = reduce_max(dist, ms.value)
     if dist is not None:
         dist.barrier()
     value = world * args.steps / (t_ms / 1000.0)
     peak, peak_kind = measured_peaks()
+    step_gbs = step_bytes / (t_ms / args.steps * 1e-3) / 1e9
     achieved = pbytes.value / (pms.value * 1e-3) / 1e9 if pms.value > 0 else None
     per_launch_bytes = pbytes.value / pn.value if pn.value else None
     traffic = TRAFFIC.get((args.n, args.precision, PROBE_KERNEL))
@@ -292,8 +318,11 @@ def run_gpu(args, world, rank, local, dist):
     if rank != 0:
         return
     base = None
+    fp64_error = None
     if not args.no_cpu_baseline:
         base = cpu_baseline(args)
+        if args.precision == "mixed":
+            fp64_error = mixed_error(args, base_oracle[0], 9)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
@@ -305,12 +334,20 @@ def run_gpu(args, world, rank, local, dist):
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes},
             "gpu_launches": launches,
+            "grid_point_steps_per_s": value * args.n ** 3,
             "roofline": {"bound": "hbm", "kernel": PROBE_KERNEL, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind + " (hbm_gbs, copy)", "unit": "GB/s",
                          "frac": achieved / peak if achieved else None, "traffic": traffic,
                          "launches_timed": pn.value, "ms_per_launch": pms.value / pn.value if pn.value else None,
-                         "bytes_per_launch": per_launch_bytes},
+                         "bytes_per_launch": per_launch_bytes,
+                         "step": {"algorithmic_bytes_per_step": step_bytes, "achieved": step_gbs, "peak": peak,
+                                  "unit": "GB/s", "frac": step_gbs / peak,
+                                  "definition": "every kernel of the step adds its external inputs and outputs "
+                                                "(icep_algorithmic_bytes), summed over the timed steps, divided "
+                                                "by the steps' device time"}},
             "cpu_baseline": base}
+    if fp64_error is not None:
+        line["fp64_oracle_error"] = fp64_error
     if learned is not None:
         line["learned"] = learned
     if batched is not None:

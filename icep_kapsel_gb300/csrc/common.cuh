@@ -102,6 +102,34 @@ inline unsigned div_up(long a, long b) { return (unsigned)((a + b - 1) / b); }
 // icep_kernel_launches() so that a benchmark can report its launch count.
 extern unsigned long long g_kernel_launches;
 inline void count_launch() { __atomic_fetch_add(&g_kernel_launches, 1ULL, __ATOMIC_RELAXED); }
+// Algorithmic bytes of the kernels launched (all contexts; read by
+// icep_algorithmic_bytes()): each launch adds its external inputs and
+// outputs -- one grid field of NX NY NZ values of its type per field read or
+// written (a half spectrum counts as one field, an in-place update as one
+// read and one write), one field per field and pass of a 3D transform (the
+// 2 N s of a transform over its two passes), Np n_dom s per component of a
+// scatter (read and write: 2) or gather -- so that a step's total over its
+// time is its roofline figure.
+extern unsigned long long g_alg_bytes;
+inline void count_launch(double bytes) {
+  count_launch();
+  if (bytes > 0) __atomic_fetch_add(&g_alg_bytes, (unsigned long long)(bytes + 0.5), __ATOMIC_RELAXED);
+}
+// bytes of `nfields` grid fields of element type R
+template <typename R>
+inline double fld(const Grid &g, double nfields) { return nfields * (double)g.nreal() * sizeof(R); }
+// number of distinct non-null operands (a dot product reads each field once)
+inline double ndistinct(const void *a, const void *b, const void *c = nullptr, const void *d = nullptr) {
+  const void *v[4] = {a, b, c, d};
+  int n = 0;
+  for (int i = 0; i < 4; i++) {
+    if (!v[i]) continue;
+    bool seen = false;
+    for (int j = 0; j < i; j++) seen = seen || (v[j] == v[i]);
+    if (!seen) n++;
+  }
+  return (double)n;
+}
 
 // Field slots of a context (ids shared with the oracle and the C-ABI).
 enum FieldId {

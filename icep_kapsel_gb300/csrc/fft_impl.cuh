@@ -296,7 +296,7 @@ bool use_plane(const Grid &g) {
 template <typename R, int NY, int H>
 void launch_plane_nh(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, cudaStream_t s) {
   const size_t sm = plane_smem<R>(NY, H);
-  count_launch();
+  count_launch(fld<R>(p.g, 1.0 * fb.n));
   if (!inverse) {
     k_plane_fwd<R, NY, H><<<dim3(p.g.nx, fb.n), 1024, sm, s>>>(fb, p.g, p.tw_y, p.tw_z, p.tw_post);
   } else {
@@ -332,7 +332,7 @@ void launch_pencils_n(const FFTPlan<R> &p, const FieldBatch<R> &fb, int axis, bo
   const int tiles_per_row = (g.hnz + W - 1) / W;
   const unsigned nblk = axis == 1 ? (unsigned)(g.nx * tiles_per_row) : div_up((long)g.ny * g.hnz, W);
   const dim3 block(W, N / 8 < 512 / W ? N / 8 : 512 / W);
-  count_launch();
+  count_launch(fld<R>(g, (axis == 0 ? 1.0 : 0.5) * fb.n));
   const cplx<R> *tw = axis == 0 ? p.tw_x : p.tw_y;
   if (inverse)
     k_pencils<R, N, true, W><<<dim3(nblk, fb.n), block, pencil_smem<R>(N), s>>>(fb, g, axis, tiles_per_row, tw);
@@ -358,7 +358,7 @@ void launch_rows_n(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, c
   const dim3 grid(div_up((long)g.nx * g.ny, W), fb.n);
   const dim3 block(W, H / 8 < 512 / W ? H / 8 : 512 / W);
   const R scale = from_double<R>(1.0 / ((double)g.nx * g.ny * g.nz));
-  count_launch();
+  count_launch(fld<R>(g, 0.5 * fb.n));
   if (inverse) k_rows<R, H, true, W><<<grid, block, row_smem<R>(H), s>>>(fb, g, p.tw_z, p.tw_post, scale);
   else k_rows<R, H, false, W><<<grid, block, row_smem<R>(H), s>>>(fb, g, p.tw_z, p.tw_post, scale);
 }

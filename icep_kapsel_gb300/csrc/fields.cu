@@ -511,124 +511,124 @@ inline unsigned nblk_real(const Grid &g) { return div_up(g.nreal(), TPB); }
 }  // namespace
 
 template <typename R> void truncate_23(const Grid &g, const FieldBatch<R> &fb, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 2.0 * fb.n));
   k_truncate<R><<<dim3(nblk_modes(g), fb.n), TPB, 0, s>>>(fb, g);
 }
 template <typename R> void zeta_k2u_k(const Grid &g, const R *z0, const R *z1, const double *uk_dc, R *u0, R *u1, R *u2, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 5));
   k_zeta_k2u_k<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, uk_dc, u0, u1, u2);
   count_launch();
   k_set_k0<R><<<1, 1, 0, s>>>(u0, u1, u2, uk_dc);
 }
 template <typename R> void u_k2zeta_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *uk_dc, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 5));
   k_u_k2zeta_k<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, z0, z1, uk_dc);
 }
 template <typename R> void advection_combine(const Grid &g, R *u0, R *u1, R *u2, R *a0, R *a1, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 7));
   k_advection_combine<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, a0, a1);
 }
 template <typename R> void ns_slaved_update(const Grid &g, R *z0, R *z1, const R *a0, const R *a1, double nu, double dt, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 6));
   k_ns_slaved<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, a0, a1, (R)(-nu * dt), (R)(1. / nu));
 }
 template <typename R> void solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 6));
   k_solenoidal<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2);
 }
 template <typename R> void grad_k(const Grid &g, const R *a, R *d0, R *d1, R *d2, R scale, bool shift, const double *e_ext_n, cudaStream_t s) {
   const int ext = e_ext_n ? 1 : 0;
   const R ex0 = ext ? (R)e_ext_n[0] : R(0), ex1 = ext ? (R)e_ext_n[1] : R(0), ex2 = ext ? (R)e_ext_n[2] : R(0);
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_grad<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, d0, d1, d2, scale, shift ? 1 : 0, ext, ex0, ex1, ex2);
 }
 template <typename R> void div_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *div, bool shift, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_div<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, div, shift ? 1 : 0);
 }
 template <typename R> void euler_update(const Grid &g, R *z0, R *z1, R *r0, R *r1, R *c0, R *c1, const R *cr0, const R *cr1, double nu, double dt, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 12));
   k_euler<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, r0, r1, c0, c1, cr0, cr1, (R)nu, (R)dt);
 }
 template <typename R> void inv_laplace_k(const Grid &g, R *a, double eps_ref, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 2));
   k_inv_laplace<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, (R)(1.0 / eps_ref));
 }
 template <typename R> void scale_copy(const Grid &g, const R *x, R *y, R a, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 2));
   k_scale_copy<R><<<div_up(g.nf(), TPB), TPB, 0, s>>>(g.nf(), x, y, a);
 }
 template <typename R> void advection_products(const Grid &g, R *u0, R *u1, R *u2, R *a0, R *a1, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 8));
   k_adv_products<R><<<nblk_real(g), TPB, 0, s>>>(g, u0, u1, u2, a0, a1);
 }
 template <typename R> void phi_clip(const Grid &g, const R *phs, R *phi, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 2));
   k_phi_clip<R><<<nblk_real(g), TPB, 0, s>>>(g, phs, phi);
 }
 template <typename R> void f_nonsole(const Grid &g, R *const *f, R *const *up, const R *phi, R *const *u, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 10));
   k_f_nonsole<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(f), v3(up), phi, v3(u));
 }
 template <typename R> void add_vec(const Grid &g, R *const *u, R *const *f, R a, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 9));
   k_add_vec<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(u), v3(f), a);
 }
 template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_sin, const R *eps_w, double ef, double ep, double dc, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 3));
   k_eps_from_profile<R><<<nblk_real(g), TPB, 0, s>>>(g, eps, phi_sin, eps_w, (R)(ef * dc), (R)dc, (R)((ep - ef) * dc));
 }
 template <typename R> void eps_janus(const Grid &g, R *eps, const R *phi_sin, const R *eps_j, double ef, double dc, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 3));
   k_eps_janus<R><<<nblk_real(g), TPB, 0, s>>>(g, eps, phi_sin, eps_j, (R)ef, (R)dc);
 }
 template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, first ? 3.0 : 4.0));
   k_charge_add<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c, phi, (R)ze, first ? 1 : 0);
 }
 template <typename R>
 void solute_charge(const Grid &g, R *out, const R *c0, const R *c1, const R *phi, double ze0, double ze1, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_solute_charge<R><<<nblk_real(g), TPB, 0, s>>>(g, out, c0, c1, phi, (R)ze0, (R)ze1);
 }
 template <typename R> void eps_face_mul(const Grid &g, R *w0, R *w1, R *w2, const R *eps, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 7));
   k_eps_face_mul<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps);
 }
 template <typename R> void eps_face_E(const Grid &g, R *w0, R *w1, R *w2, const R *eps, double e0, double e1, double e2, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_eps_face_E<R><<<nblk_real(g), TPB, 0, s>>>(g, w0, w1, w2, eps, (R)e0, (R)e1, (R)e2);
 }
 template <typename R> void axpby_real(const Grid &g, const R *x, R *y, R a, R b, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 3));
   k_axpby_real<R><<<nblk_real(g), TPB, 0, s>>>(g, x, y, a, b);
 }
 template <typename R> void interp_normal(const Grid &g, R *const *out, R *const *in, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 6));
   k_interp_normal<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(out), v3(in));
 }
 template <typename R> void maxwell_e2(const Grid &g, const R *f0, const R *f1, const R *f2, R *w1, double e0, double e1, double e2, int ext, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_maxwell_e2<R><<<nblk_real(g), TPB, 0, s>>>(g, f0, f1, f2, w1, (R)e0, (R)e1, (R)e2, ext);
 }
 template <typename R> void maxwell_face(const Grid &g, R *const *force, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 11));
   k_maxwell_face<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(force), rho, w1, v3(ge), (R)e0, (R)e1, (R)e2, ext);
 }
 template <typename R> void np_flux_electric(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 7));
   k_np_flux_electric<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(gp), (R)L_ze);
 }
 template <typename R> void np_impermeability(const Grid &g, R *const *flux, R *const *sn, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 9));
   k_np_imperm<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), v3(sn));
 }
 template <typename R> void np_flux_advection(const Grid &g, R *const *flux, const R *c, R *const *u, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 10));
   k_np_flux_adv<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(u));
 }
 template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 1));
   k_fill_real<R><<<nblk_real(g), TPB, 0, s>>>(g, a, v);
 }
 

@@ -15,6 +15,7 @@
 
 namespace icep {
 unsigned long long g_kernel_launches = 0;
+unsigned long long g_alg_bytes = 0;
 
 // Host ranges pinned through icep_pin_host, registered as mapped: the
 // drop-in calls read and write them from kernels over the CPU-GPU link.
@@ -246,6 +247,7 @@ int icep_phase_times(icep_ctx *c, double *ms, int n) {
   return wrap(c, c->e->phase_times(ms, n));
 }
 unsigned long long icep_kernel_launches(void) { return __atomic_load_n(&icep::g_kernel_launches, __ATOMIC_RELAXED); }
+unsigned long long icep_algorithmic_bytes(void) { return __atomic_load_n(&icep::g_alg_bytes, __ATOMIC_RELAXED); }
 int icep_pin_host(void *p, size_t bytes) {
   if (!p || !bytes) return ICEP_ERR_ARG;
   if (cudaHostRegister(p, bytes, cudaHostRegisterMapped) != cudaSuccess) return ICEP_ERR_CUDA;

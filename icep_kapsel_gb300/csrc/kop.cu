@@ -556,12 +556,15 @@ struct RPlane {
   static constexpr int NT = H * TY;
   static constexpr int RZ = NY * TZ / NT;
   static constexpr int BUF = NY * (H + 1);  // complex values: the plane, [j][kz]
-  static_assert(PY >= TY && PZ >= TZ && RZ >= 1 && NY * TZ == RZ * NT, "register plane shape");
+  static constexpr int ER = NY < 64 ? NY : 64;  // rows of the z phase's first round (0..ER-1)
+  static constexpr int EBUF = ER * (H + 1);     // their face permittivities, float pairs
+  static_assert(PY >= TY && PZ >= TZ && RZ >= 1 && RZ <= 2 && NY * TZ == RZ * NT, "register plane shape");
   static_assert(H <= NY, "the y exchange regions fit in the plane buffer");
 };
 template <int NY, int H>
 __host__ __device__ constexpr size_t rplane_smem() {
-  return ((size_t)RPlane<NY, H>::BUF + NY + H + (H + 1)) * sizeof(cf) + 2 * sizeof(unsigned long long);
+  return ((size_t)RPlane<NY, H>::BUF + RPlane<NY, H>::EBUF + NY + H + (H + 1)) * sizeof(cf) +
+         2 * sizeof(unsigned long long);
 }
 
 // Row j of the z phase for warp w, lane group jr, round p: rows of a
@@ -593,7 +596,8 @@ __global__ void __launch_bounds__(H * 8, (H >= 64) ? 2 : 4)
   constexpr int TY = S::TY, PY = S::PY, TZ = S::TZ, PZ = S::PZ, RS = H + 1;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   cf *buf = reinterpret_cast<cf *>(smem_raw);
-  cf *sty = buf + S::BUF;
+  float2 *estage = reinterpret_cast<float2 *>(buf + S::BUF);  // eps_face rows 0..ER-1
+  cf *sty = reinterpret_cast<cf *>(estage + S::EBUF);
   cf *stz = sty + NY;
   cf *spost = stz + H;
   unsigned long long *mb = reinterpret_cast<unsigned long long *>(spost + H + 1);
@@ -603,30 +607,45 @@ __global__ void __launch_bounds__(H * 8, (H >= 64) ? 2 : 4)
   cf *cplane = reinterpret_cast<cf *>(data) + (long)i * S::BUF;
   const float2 *efp = reinterpret_cast<const float2 *>(ef) + (long)i * S::BUF;  // [j][NZ_] floats as float2
   const int lin = threadIdx.x, lane = lin & 31, w = lin >> 5;
-  constexpr uint32_t BYTES = S::BUF * sizeof(cf);
-  const uint32_t mb0 = smem_addr(&mb[0]);
+  constexpr uint32_t BYTES = S::BUF * sizeof(cf), EBYTES = S::EBUF * sizeof(float2);
+  const uint32_t mb0 = smem_addr(&mb[0]), mb1 = smem_addr(&mb[1]);
   if (lin == 0) {
     mbar_init(mb0, 1);
+    mbar_init(mb1, 1);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
   if (lin == 0) {
     if (test_wait) {
-      mbar_expect_tx(mb0, 16);  // a transaction that nothing will complete
+      mbar_expect_tx(mb0, 16);  // transactions that nothing will complete
+      mbar_expect_tx(mb1, 16);
     } else {
       mbar_expect_tx(mb0, BYTES);
       bulk_g2s(smem_addr(buf), cplane, BYTES, mb0);
+      // the face permittivities of the z phase's first round of rows, which
+      // land while the y transforms run
+      mbar_expect_tx(mb1, EBYTES);
+      bulk_g2s(smem_addr(estage), efp, EBYTES, mb1);
     }
+  }
+  // the rows of the second round go to L2 meanwhile (one 128-byte line per thread)
+  if (S::RZ > 1 && !test_wait) {
+    constexpr int LINES = (NY - S::ER) * (H + 1) * (int)sizeof(float2) / 128;
+    for (int q = lin; q < LINES; q += S::NT)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(reinterpret_cast<const char *>(efp + S::EBUF) + 128 * q));
   }
   for (int q = lin; q < NY; q += S::NT) sty[q] = twy[q];
   for (int q = lin; q < H; q += S::NT) stz[q] = twz[q];
   for (int q = lin; q <= H; q += S::NT) spost[q] = post[q];
-  const bool ok = mbar_wait_for(mb0, 0, test_wait ? KOP_TEST_WAIT_NS : KOP_WAIT_NS);
-  if (__syncthreads_or(!ok)) {
-    // the copy did not land: report it, let a copy still in flight finish
+  const unsigned long long lim = test_wait ? KOP_TEST_WAIT_NS : KOP_WAIT_NS;
+  if (__syncthreads_or(!mbar_wait_for(mb0, 0, lim))) {
+    // a copy did not land: report it, let copies still in flight finish
     // before the block's shared memory is released, and leave
     if (lin == 0) atomicExch(err, 1);
-    if (!test_wait) mbar_wait_for(mb0, 0, KOP_WAIT_NS);
+    if (!test_wait) {
+      mbar_wait_for(mb0, 0, KOP_WAIT_NS);
+      mbar_wait_for(mb1, 0, KOP_WAIT_NS);
+    }
     return;
   }
   // ---- y inverse: thread (column k, t), rows t + 8m
@@ -656,17 +675,26 @@ __global__ void __launch_bounds__(H * 8, (H >= 64) ? 2 : 4)
   __syncthreads();  // every column's exchange is read
 #pragma unroll
   for (int r = 0; r < PY; r++) buf[(t + 8 * r) * RS + k] = a[r];
-  __syncthreads();
+  if (__syncthreads_or(!mbar_wait_for(mb1, 0, KOP_WAIT_NS))) {
+    if (lin == 0) atomicExch(err, 1);
+    mbar_wait_for(mb1, 0, KOP_WAIT_NS);
+    return;
+  }
   // ---- z: merge, inverse, times the scaled face permittivity, forward
   {
     const int tz = lane & (TZ - 1), jr = lane / TZ;
-#pragma unroll 1
+    // second-round permittivities from L2 into registers, in flight while
+    // the first round runs on the staged ones
+    float2 enext[PZ];
+    if (S::RZ > 1) {
+      const int j1 = rplane_row<TZ>(w, jr, 1);
+#pragma unroll
+      for (int m = 0; m < PZ; m++) enext[m] = __ldg(efp + j1 * RS + tz + TZ * m);
+    }
+#pragma unroll
     for (int p = 0; p < S::RZ; p++) {
       const int j = rplane_row<TZ>(w, jr, p);
       cf *row = buf + j * RS;
-      float2 e2[PZ];
-#pragma unroll
-      for (int m = 0; m < PZ; m++) e2[m] = __ldg(efp + j * RS + tz + TZ * m);
       cf z[PZ];
 #pragma unroll
       for (int m = 0; m < PZ; m++) {
@@ -686,7 +714,11 @@ __global__ void __launch_bounds__(H * 8, (H >= 64) ? 2 : 4)
       const int rpar = (j >> 3) & 1;
       reg_dft<TZ, PZ>(z, tz, row, rpar, stz, true);
 #pragma unroll
-      for (int m = 0; m < PZ; m++) z[m] = cf{(z[m].x * scale) * e2[m].x, (z[m].y * scale) * e2[m].y};
+      for (int m = 0; m < PZ; m++) {
+        // first round: the staged rows, read only now; second: the registers
+        const float2 e = (p == 0) ? estage[j * RS + tz + TZ * m] : enext[m];
+        z[m] = cf{(z[m].x * scale) * e.x, (z[m].y * scale) * e.y};
+      }
       __syncwarp();
       reg_dft<TZ, PZ>(z, tz, row, rpar, stz, false);
       __syncwarp();
@@ -939,7 +971,7 @@ void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, c
       cudaFuncSetAttribute(k_kop_plane_r<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       attr = true;
     }
-    count_launch();
+    count_launch(fld<float>(p.g, 9));
     probe_begin(PROBE_KOP_PLANE, s);
     k_kop_plane_r<NY, H><<<dim3(p.g.nx, 3), RPlane<NY, H>::NT, sm, s>>>(
         p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z, p.tw_post, scale, err, test_wait);
@@ -952,7 +984,7 @@ void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, c
       cudaFuncSetAttribute(k_kop_plane<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
       attr = true;
     }
-    count_launch();
+    count_launch(fld<float>(p.g, 9));
     probe_begin(PROBE_KOP_PLANE, s);
     k_kop_plane<NY, H><<<dim3(p.g.nx, 3), 1024, sm, s>>>(p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z,
                                                                p.tw_post, scale, err);
@@ -980,7 +1012,7 @@ bool kop_supported(const Grid &g) {
 int kop_pencil_blocks(const Grid &g) { return (int)div_up((long)g.ny * g.hnz, KW); }
 
 void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, float *ef2, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<float>(g, 4));
   k_kop_eps_faces<<<div_up(g.nreal(), 256), 256, 0, s>>>(g, eps, ef0, ef1, ef2);
 }
 
@@ -990,7 +1022,7 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
   const Grid &g = p.g;
   const unsigned nb = (unsigned)kop_pencil_blocks(g);
   const float ieps = (float)(1.0 / eps_ref);
-  count_launch();
+  count_launch(fld<float>(g, mode == KOP_P ? 7.0 : mode == KOP_S ? 6.0 : 4.0));
   probe_begin(PROBE_KOP_XINV, s);
 #define KOP_XINV(N)                                                                                        \
   case N:                                                                                                  \
@@ -1035,7 +1067,7 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const f
               const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s) {
   const Grid &g = p.g;
   const unsigned nb = (unsigned)kop_pencil_blocks(g);
-  count_launch();
+  count_launch(fld<float>(g, mode == KOP_NONE ? 4.0 : 5.0));
   probe_begin(PROBE_KOP_XFWD, s);
 #define KOP_XFWD(N)                                                                                                 \
   case N:                                                                                                           \
@@ -1061,7 +1093,7 @@ void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv,
             double rho, const double *fin1, const double *fin2, double *part3, double *fin3, unsigned *counter3,
             cudaStream_t s, double *ks, int maxit) {
   const unsigned nb = (unsigned)kop_xr_blocks(g);
-  count_launch();
+  count_launch(fld<float>(g, 7));
 #define KOP_XR(HH)                                                                                            \
   case HH:                                                                                                    \
     k_kop_xr<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, sv, t, r0, rho, fin1, fin2, part3, fin3, counter3, ks, \

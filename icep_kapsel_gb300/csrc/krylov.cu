@@ -209,62 +209,62 @@ __global__ void k_scale_d2f(Grid g, const double *x, float *y, double a) {
 template <typename R>
 void dots(const Grid &g, const R *a0, const R *b0, const R *a1, const R *b1, int n, double *partials, double *scal,
           int slot, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, ndistinct(a0, b0, n > 1 ? a1 : nullptr, n > 1 ? b1 : nullptr)));
   k_dots<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a0, b0, a1, b1, n, partials);
   count_launch();
   k_dots_final<<<1, 256, 0, s>>>(partials, DOT_BLOCKS, n, scal, slot);
 }
 template <typename R>
 void sum_real(const Grid &g, const R *a, double *partials, double *scal, int slot, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 1));
   k_sum<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a, partials, 0);
   count_launch();
   k_dots_final<<<1, 256, 0, s>>>(partials, DOT_BLOCKS, 1, scal, slot);
 }
 template <typename R>
 void sum_abs_real(const Grid &g, const R *a, double *partials, double *scal, int slot, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 1));
   k_sum<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a, partials, 1);
   count_launch();
   k_dots_final<<<1, 256, 0, s>>>(partials, DOT_BLOCKS, 1, scal, slot);
 }
 template <typename R>
 void bicg_p(const Grid &g, R *p, const R *r, const R *v, double beta, double w, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_bicg_p<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, p, r, v, (R)beta, (R)w);
 }
 template <typename R>
 void bicg_s(const Grid &g, R *sv, const R *r, const R *v, double rho, const double *scal, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 3));
   k_bicg_s<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, sv, r, v, rho, scal);
 }
 template <typename R>
 void bicg_xr(const Grid &g, R *x, R *r, const R *y, const R *z, const R *sv, const R *t, double rho,
              const double *scal, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 7));
   k_bicg_xr<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, x, r, y, z, sv, t, rho, scal);
 }
 template <typename R>
 void copy_real(const Grid &g, const R *x, R *y, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 2));
   k_copy_real<R><<<div_up(g.nf(), TPB), TPB, 0, s>>>(g, x, y);
 }
 template <typename R>
 void sub_real(const Grid &g, const R *b, const R *t, R *r, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 3));
   k_sub_real<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, b, t, r);
 }
 template <typename R>
 void sub_mean(const Grid &g, R *a, const double *scal, int slot, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 2));
   k_sub_mean<R><<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, a, scal, slot);
 }
 void convert_f2d(long n, const float *x, double *y, cudaStream_t s) {
-  count_launch();
+  count_launch(12.0 * n);
   k_f2d<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y);
 }
 void convert_d2f(long n, const double *x, float *y, cudaStream_t s) {
-  count_launch();
+  count_launch(12.0 * n);
   k_d2f<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y);
 }
 namespace {
@@ -278,13 +278,13 @@ unsigned link_blocks(long n2) {
 }  // namespace
 void link_d2f(long n, const double *x, float *y, cudaStream_t s) {
   if (!link_ok(n, x, y)) return convert_d2f(n, x, y, s);
-  count_launch();
+  count_launch(12.0 * n);
   k_d2f_link<<<link_blocks(n / 2), TPB, 0, s>>>(n / 2, reinterpret_cast<const double2 *>(x),
                                                  reinterpret_cast<float2 *>(y));
 }
 void link_f2d(long n, const float *x, double *y, cudaStream_t s) {
   if (!link_ok(n, x, y)) return convert_f2d(n, x, y, s);
-  count_launch();
+  count_launch(12.0 * n);
   k_f2d_link<<<link_blocks(n / 2), TPB, 0, s>>>(n / 2, reinterpret_cast<const float2 *>(x),
                                                  reinterpret_cast<double2 *>(y));
 }
@@ -293,28 +293,28 @@ void link_copy(long n, const double *x, double *y, cudaStream_t s) {
     cudaMemcpyAsync(y, x, sizeof(double) * n, cudaMemcpyDefault, s);
     return;
   }
-  count_launch();
+  count_launch(16.0 * n);
   k_copy_link<<<link_blocks(n / 2), TPB, 0, s>>>(n / 2, reinterpret_cast<const double2 *>(x),
                                                   reinterpret_cast<double2 *>(y));
 }
 void scale_d2f_all(long n, const double *x, float *y, double a, cudaStream_t s) {
-  count_launch();
+  count_launch(12.0 * n);
   k_scale_d2f_all<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y, a);
 }
 void add_f2d_all(long n, const float *x, double *y, double a, cudaStream_t s) {
-  count_launch();
+  count_launch(20.0 * n);
   k_add_f2d_all<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y, a);
 }
 void axpby_all(long n, const double *x, double *y, double a, double b, cudaStream_t s) {
-  count_launch();
+  count_launch(24.0 * n);
   k_axpby_all<<<div_up(n, TPB), TPB, 0, s>>>(n, x, y, a, b);
 }
 void add_f2d(const Grid &g, const float *x, double *y, double a, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<float>(g, 1) + fld<double>(g, 2));
   k_add_f2d<<<div_up(g.nreal(), TPB), TPB, 0, s>>>(g, x, y, a);
 }
 void scale_d2f(const Grid &g, const double *x, float *y, double a, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<double>(g, 1) + fld<float>(g, 1));
   k_scale_d2f<<<div_up(g.nf(), TPB), TPB, 0, s>>>(g, x, y, a);
 }
 

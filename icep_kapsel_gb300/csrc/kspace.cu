@@ -359,45 +359,45 @@ void kdots_finish(const double *partials, int nblocks, int n, double *scal, int 
 template <typename R>
 void kdots(const Grid &g, const R *a0, const R *b0, const R *a1, const R *b1, int n, double *partials, double *scal,
            int slot, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, ndistinct(a0, b0, n > 1 ? a1 : nullptr, n > 1 ? b1 : nullptr)));
   k_kdots<R><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, a0, b0, a1, b1, n, partials);
   count_launch();
   k_kdots_final<<<1, 256, 0, s>>>(partials, DOT_BLOCKS, n, scal, slot);
 }
 template <typename R>
 void kbicg_p(const Grid &g, R *p, const R *r, const R *v, double beta, double w, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_kbicg_p<R><<<nblk(g), TPB, 0, s>>>(g, p, r, v, (R)beta, (R)w);
 }
 template <typename R>
 void kbicg_s(const Grid &g, R *sv, const R *r, const R *v, double rho, const double *scal, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 3));
   k_kbicg_s<R><<<nblk(g), TPB, 0, s>>>(g, sv, r, v, rho, scal);
 }
 template <typename R>
 void kbicg_xr(const Grid &g, R *xt, R *r, const R *p, const R *sv, const R *t, double rho, const double *scal,
               cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 6));
   k_kbicg_xr<R><<<nblk(g), TPB, 0, s>>>(g, xt, r, p, sv, t, rho, scal);
 }
 template <typename R>
 void kgrad_pre(const Grid &g, const R *p, R *g0, R *g1, R *g2, double eps_ref, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_kgrad_pre<R><<<nblk(g), TPB, 0, s>>>(g, p, g0, g1, g2, (R)(1.0 / eps_ref));
 }
 template <typename R>
 void kdiv_post(const Grid &g, const R *w0, const R *w1, const R *w2, R *v, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 4));
   k_kdiv_post<R><<<nblk(g), TPB, 0, s>>>(g, w0, w1, w2, v);
 }
 template <typename R>
 void kprecond(const Grid &g, const R *x, R *y, double eps_ref, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<R>(g, 2));
   k_kprecond<R><<<nblk(g), TPB, 0, s>>>(g, x, y, (R)(1.0 / eps_ref));
 }
 
 void kmdot(const Grid &g, const KVecs &V, int nv, const float *w, double *partials, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<float>(g, nv + 1.0));
   k_kmdot<<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, V, nv, w, partials);
 }
 void kmdot_final(const double *partials, int nv, double *out, cudaStream_t s) {
@@ -405,19 +405,19 @@ void kmdot_final(const double *partials, int nv, double *out, cudaStream_t s) {
   k_kmdot_final<<<nv, 256, 0, s>>>(partials, DOT_BLOCKS, nv, out);
 }
 void kmaxpy(const Grid &g, float *w, const KVecs &V, int nv, const double *coef, double sign, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<float>(g, nv + 2.0));
   k_kmaxpy<<<nblk(g), TPB, 0, s>>>(g, w, V, nv, coef, (float)sign);
 }
 void kscale_by_norm(const Grid &g, const float *w, float *out, const double *nrm2, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<float>(g, 2));
   k_kscale_by_norm<<<nblk(g), TPB, 0, s>>>(g, w, out, nrm2);
 }
 void kadd(const Grid &g, const float *v, const float *z, float *xt, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<float>(g, 3));
   k_kadd<<<nblk(g), TPB, 0, s>>>(g, v, z, xt);
 }
 void ksub(const Grid &g, const float *b, const float *w, float *r, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<float>(g, 3));
   k_ksub<<<nblk(g), TPB, 0, s>>>(g, b, w, r);
 }
 

@@ -522,28 +522,28 @@ template <typename R>
 void scatter_profile(const PartParams &pp, const icep_particle *p, const int *sek, R *out, R *aux, int kind,
                      cudaStream_t s) {
   if (pp.np == 0) return;
-  count_launch();
+  count_launch((double)pp.np * pp.np_domain * sizeof(R) * (aux ? 4.0 : 2.0));
   k_scatter_profile<R><<<blocks_pts(pp), TPB, 0, s>>>(pp, p, sek, out, aux, kind);
 }
 template <typename R>
 void scatter_up(const PartParams &pp, const icep_particle *p, const int *sek, const R *phs, R *u0, R *u1, R *u2,
                 cudaStream_t s) {
   if (pp.np == 0) return;
-  count_launch();
+  count_launch((double)pp.np * pp.np_domain * sizeof(R) * 7.0);
   k_scatter_up<R><<<blocks_pts(pp), TPB, 0, s>>>(pp, p, sek, phs, u0, u1, u2);
 }
 template <typename R>
 void scatter_normal(const PartParams &pp, const icep_particle *p, const int *sek, R *s0, R *s1, R *s2,
                     cudaStream_t s) {
   if (pp.np == 0) return;
-  count_launch();
+  count_launch((double)pp.np * pp.np_domain * sizeof(R) * 6.0);
   k_scatter_normal<R><<<blocks_pts(pp), TPB, 0, s>>>(pp, p, sek, s0, s1, s2);
 }
 template <typename R>
 void f_hydro(const PartParams &pp, icep_particle *p, const int *sek, const R *phs, const R *u0, const R *u1,
              const R *u2, bool copy_to_1, cudaStream_t s) {
   if (pp.np == 0) return;
-  count_launch();
+  count_launch((double)pp.np * pp.np_domain * sizeof(R) * 4.0);
   k_f_hydro<R><<<pp.np, 256, 0, s>>>(pp, p, sek, phs, u0, u1, u2, copy_to_1 ? 1 : 0);
 }
 
@@ -558,21 +558,21 @@ int lj_force(const PartParams &pp, icep_particle *p, int *work, int work_ints, i
   if (ncell <= 0) return ICEP_ERR_UNSUPPORTED;
   if (work_ints < 2 * (ncell + 1) + pp.np) return ICEP_ERR_ARG;
   int *start = work, *fill = work + (ncell + 1), *list = work + 2 * (ncell + 1);
-  count_launch();
+  count_launch((double)pp.np * sizeof(icep_particle));
   k_lj_cells<<<1, 1024, 0, s>>>(pp, cg, p, start, fill, list, ncell);
-  count_launch();
+  count_launch(2.0 * pp.np * sizeof(icep_particle));
   k_lj_gather<<<div_up((long)pp.np * 32, 128), 128, 0, s>>>(pp, cg, p, start, list, pairs, max_pairs, n_pairs);
   return ICEP_OK;
 }
 
 void md_position(const PartParams &pp, icep_particle *p, bool ab2, cudaStream_t s) {
   if (pp.np == 0) return;
-  count_launch();
+  count_launch(2.0 * pp.np * sizeof(icep_particle));
   k_md_position<<<div_up(pp.np, 128), 128, 0, s>>>(pp, p, ab2 ? 1 : 0);
 }
 void md_velocity(const PartParams &pp, icep_particle *p, bool ab2, cudaStream_t s) {
   if (pp.np == 0) return;
-  count_launch();
+  count_launch(2.0 * pp.np * sizeof(icep_particle));
   k_md_velocity<<<div_up(pp.np, 128), 128, 0, s>>>(pp, p, ab2 ? 1 : 0);
 }
 

@@ -254,49 +254,54 @@ void RefineTables::free_all() {
 static RfTab tab_of(const RefineTables &t) { return RfTab{{t.gd[0], t.gd[1], t.gd[2]}}; }
 
 void rf_from_f32(long n, const float *a, dfl *out, cudaStream_t s) {
-  count_launch();
+  count_launch(12.0 * n);
   k_rf_from_f32<<<nblk(n), TPB, 0, s>>>(n, a, reinterpret_cast<float2 *>(out));
 }
 void rf_to_f32(long n, const dfl *a, float *out, double scale, cudaStream_t s) {
-  count_launch();
+  count_launch(12.0 * n);
   k_rf_to_f32<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const float2 *>(a), out, (float)scale);
 }
 void rf_differs(long n, const double *a, const double *b, int *flag, cudaStream_t s) {
   cudaMemsetAsync(flag, 0, sizeof(int), s);
-  count_launch();
+  count_launch(16.0 * n);
   k_rf_differs<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const unsigned long long *>(a),
                                        reinterpret_cast<const unsigned long long *>(b), flag);
 }
 void rf_to_f64(long n, const dfl *a, double *out, cudaStream_t s) {
-  count_launch();
+  count_launch(16.0 * n);
   k_rf_to_f64<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const float2 *>(a), out);
 }
 void rf_add_f32(long n, const float *d, dfl *x, double a, cudaStream_t s) {
-  count_launch();
+  count_launch(20.0 * n);
   k_rf_add_f32<<<nblk(n), TPB, 0, s>>>(n, d, reinterpret_cast<float2 *>(x), dfl::from_double(a));
 }
 void rf_extrapolate(long n, const dfl *x, dfl *y, cudaStream_t s) {
-  count_launch();
+  count_launch(24.0 * n);
   k_rf_extrapolate<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const float2 *>(x), reinterpret_cast<float2 *>(y));
 }
 void rf_grad(const Grid &g, const RefineTables &t, const dfl *x, dfl *w0, dfl *w1, dfl *w2, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<double>(g, 4));
   k_rf_grad<<<nblk(g.nmodes()), TPB, 0, s>>>(g, tab_of(t), reinterpret_cast<const float4 *>(x),
                                              reinterpret_cast<float4 *>(w0), reinterpret_cast<float4 *>(w1),
                                              reinterpret_cast<float4 *>(w2));
 }
 void rf_eps_face_mul(const Grid &g, dfl *w0, dfl *w1, dfl *w2, const float *eps, cudaStream_t s) {
-  count_launch();
+  count_launch(fld<double>(g, 6) + fld<float>(g, 1));
   k_rf_eps_face_mul<<<nblk(g.nreal()), TPB, 0, s>>>(g, reinterpret_cast<float2 *>(w0), reinterpret_cast<float2 *>(w1),
                                                     reinterpret_cast<float2 *>(w2), eps);
 }
 void rf_eps_face_e(const Grid &g, dfl *w0, dfl *w1, dfl *w2, const float *eps, const double *e, const bool *use,
                    cudaStream_t s) {
   const int u = (use[0] ? 1 : 0) | (use[1] ? 2 : 0) | (use[2] ? 4 : 0);
-  count_launch();
+  count_launch(fld<double>(g, 3) + fld<float>(g, 1));
   k_rf_eps_face_e<<<nblk(g.nreal()), TPB, 0, s>>>(g, reinterpret_cast<float2 *>(w0), reinterpret_cast<float2 *>(w1),
                                                   reinterpret_cast<float2 *>(w2), eps, dfl::from_double(e[0]),
                                                   dfl::from_double(e[1]), dfl::from_double(e[2]), u);
+}
+// fields the fused divergence pass reads and writes: the used components,
+// the base (when given) and the output
+static double mode_fields(int use_bits, const dfl *base) {
+  return (double)(((use_bits >> 0) & 1) + ((use_bits >> 1) & 1) + ((use_bits >> 2) & 1)) + (base ? 1.0 : 0.0) + 1.0;
 }
 void rf_div_combine(const Grid &g, const RefineTables &t, const dfl *w0, const dfl *w1, const dfl *w2,
                     const bool *use, const dfl *base, dfl *out, int mode, float prescale, bool acc64,
@@ -308,7 +313,7 @@ void rf_div_combine(const Grid &g, const RefineTables &t, const dfl *w0, const d
   float4 *o = reinterpret_cast<float4 *>(out);
   // post: 1/N, and 1/prescale^2 for the FP32 sums
   const double post = (acc64 ? 1.0 : 1.0 / ((double)prescale * (double)prescale)) / (double)g.nreal();
-  count_launch();
+  count_launch(fld<double>(g, mode_fields(u, base)));
   if (acc64)
     k_rf_div_combine<true>
         <<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, tab_of(t), a0, a1, a2, u, b, o, mode, prescale, post, partials);

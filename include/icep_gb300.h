@@ -345,6 +345,11 @@ int icep_phase_times(icep_ctx *ctx, double *ms, int n);
 int icep_selftest_wait(icep_ctx *ctx, int kernel);
 /* Kernels launched by this library so far (all contexts). */
 unsigned long long icep_kernel_launches(void);
+/* Algorithmic bytes of the kernels launched so far (all contexts): every
+ * launch adds its external inputs and outputs (grid fields read or written,
+ * one field per field and pass of a 3D transform, scatter/gather stencil
+ * traffic); a step's increase divided by its time is its roofline figure. */
+unsigned long long icep_algorithmic_bytes(void);
 /* Page-lock / release a caller's host buffer for the drop-in transfers. The
  * buffer is registered as mapped: icep_time_evolution and the field getters
  * and setters then read and write it from their conversion kernels over the

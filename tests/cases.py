@@ -179,3 +179,29 @@ def icep64_case(solver=abi.SOLVER_SPECTRAL, precision=abi.FP64, tol=1e-10):
     1e-10 true residual (the salt of icep_case)."""
     return icep_case(n=64, npart=16, minsep=12.0, seed=64, a=5.0, eps_f=80.0, eps_p=2.0,
                      e_ext=(0.0, 0.0, 0.1), tol=tol, solver=solver, precision=precision)
+
+
+def _rel(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / (nb if nb > 0 else 1.0))
+
+
+def mixed_vs_oracle_errors(m, o, nz, npart):
+    """Relative L2 error per field of a MIXED GPU state against the FP64
+    oracle's state (velocity from the vorticity by Zeta_k2u on both sides)."""
+    out = {}
+    for k in ("zeta0", "zeta1", "c0", "c1"):
+        out[k] = _rel(m.get(k), o.get(k))
+    a, b = m.get("pot")[:, :, :nz], o.get("pot")[:, :, :nz]
+    out["pot"] = _rel(a - a.mean(), b - b.mean())
+    out["phi"] = _rel(m.get("phi")[:, :, :nz], o.get("phi")[:, :, :nz])
+    m.call("zeta_k2u")
+    o.call("zeta_k2u")
+    out["u"] = float(np.sqrt(sum(np.linalg.norm(m.get("u%d" % d)[:, :, :nz] - o.get("u%d" % d)[:, :, :nz]) ** 2
+                                 for d in range(3)) /
+                             sum(np.linalg.norm(o.get("u%d" % d)[:, :, :nz]) ** 2 for d in range(3))))
+    pa = abi.particles_to_numpy(m.particles(), npart)
+    pb = abi.particles_to_numpy(o.particles(), npart)
+    for k in ("x", "v"):
+        out["particle_" + k] = _rel(pa[k], pb[k])
+    return out

@@ -65,6 +65,7 @@ class Params(C.Structure):
         ("salt_free", C.c_int),
         ("valency_counterion", C.c_double),
         ("onsager_counterion", C.c_double),
+        ("poisson_boltzmann", C.c_int),
     ]
 
 

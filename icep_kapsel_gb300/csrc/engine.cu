@@ -202,6 +202,14 @@ class Engine : public EngineBase {
       if (p.valency_counterion * p.surface_charge[0] >= 0.)
         return fail(ICEP_ERR_ARG, "counterion valency must be opposite to the surface charge");
     }
+    // INIT_profile Poisson_Boltzmann: with charged particles the reference
+    // relaxes the ion densities (Init_rho_ion, operate_electrolyte.cxx:
+    // 810-853); built here: the salt solution with more than one particle
+    // (Set_steadystate_ion_density); uncharged particles start uniform there
+    if (p.poisson_boltzmann && have_sc && (salt_free || n <= 1))
+      return fail(ICEP_ERR_UNSUPPORTED,
+                  "INIT_profile Poisson_Boltzmann: only the salt solution with more than one charged particle "
+                  "(Set_steadystate_ion_density) is built; the salt-free and single-particle relaxations are not");
     if (janus) {
       if (p.per_particle_eps) return fail(ICEP_ERR_ARG, "Janus particles with per-particle permittivity");
       for (int q = 0; q < n; q++)
@@ -1503,8 +1511,92 @@ class Engine : public EngineBase {
     return cuda_status("step");
   }
 
+  // Count_single_solute (solute_rhs.cxx:130-148) of a real field:
+  // sum (1 - phi) c DX^3, as sum c - sum phi c
+  double count_solute(const R *conc_x) {
+    sum_real<R>(g, conc_x, partials, scal, S_AUX0, s);
+    dots<R>(g, f[F_PHI], conc_x, nullptr, nullptr, 1, partials, scal, S_AUX1, s);
+    read_scal();
+    return (hscal[S_AUX0] - hscal[S_AUX1]) * P.dx * P.dx * P.dx;
+  }
+  // The Dielectric branch of Calc_free_energy_PB (operate_electrolyte.cxx:
+  // 302-421): `charge` is the array the reference accumulates into (its
+  // up[1]) and is modified as there; F_PHI holds the particle profile.
+  double free_energy_pb(R *charge) {
+    R *c0 = f[F_GE1], *c1 = f[F_GE2], *ideal = f[F_WV1], *es = f[F_WORK];
+    copy(F_GE1, F_C0);
+    copy(F_GE2, F_C1);
+    c2r(c0, c1);
+    pb_energy_terms<R>(g, c0, c1, f[F_PHI], charge, f[F_POT], valency_e[0], valency_e[1], ext_now, P.dx,
+                       P.external_field, ideal, es, s);
+    sum_real<R>(g, ideal, partials, scal, S_AUX0, s);
+    sum_real<R>(g, es, partials, scal, S_AUX1, s);
+    read_scal();
+    const double dx3 = P.dx * P.dx * P.dx;
+    return hscal[S_AUX0] * P.kbt * dx3 + hscal[S_AUX1] * dx3;
+  }
+  // Set_steadystate_ion_density (operate_electrolyte.cxx:424-457): the salt
+  // densities relaxed by Ion_diffusion_solver_Euler (fluid_solver.cxx:
+  // 293-316) -- the Nernst-Planck right-hand side with the fluid at rest and
+  // the potential as it is (zero before the first solve: the external field
+  // alone drives the ions), an Euler step of the densities on the 2/3 modes
+  // and Rescale_solute (solute_rhs.cxx:99-128) back to the initial totals --
+  // until the free energy changes by less than TOL = 1e-4
+  // (operate_electrolyte.h:22), at most 9999 steps. The free energy's charge
+  // array starts as the particle velocity field's y component (the
+  // reference's up[1]) and, inside the loop, as the last species' real
+  // density before its rescale (Rescale_solute's working array is up[1]).
+  int steadystate_ions(const double *total) {
+    R *charge = f[F_GE0], *tmp = f[F_U0];
+    copy(F_GE0, F_UP1);
+    double f_prev = free_energy_pb(charge);
+    for (int d = 0; d < 2; d++) {  // zero vorticity and its right-hand side for the density-only Euler step
+      zero(F_NS0_0 + d);
+      zero(F_NS1_0 + d);
+    }
+    pb_iterations = 0;
+    for (int m = 1; m < 10000; m++) {
+      copy(F_WV1, F_POT);
+      r2c(f[F_WV1]);
+      grad_k<R>(g, f[F_WV1], f[F_F0], f[F_F1], f[F_F2], R(1), true, P.external_field ? e_ext_nh : nullptr, s);
+      c2r(f[F_F0], f[F_F1], f[F_F2]);
+      for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
+      interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);
+      for (int d = 0; d < 3; d++) zero(F_SN0 + d);
+      scatter_normal<R>(pp, dp, dsek, f[F_SN0], f[F_SN1], f[F_SN2], s);
+      for (int n = 0; n < 2; n++) {
+        truncate_23<R>(g, batch(f[F_C0 + n]), s);
+        grad_k<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], (R)(P.kbt * onsager[n]), false, nullptr, s);
+        c2r(f[F_UP0], f[F_UP1], f[F_UP2]);
+        copy(F_CRHS0 + n, F_C0 + n);
+        c2r(f[F_CRHS0 + n]);
+        np_flux_electric<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_F0), onsager[n] * valency_e[n], s);
+        np_impermeability<R>(g, vec(F_UP0), vec(F_SN0), s);
+        r2c(f[F_UP0], f[F_UP1], f[F_UP2]);
+        div_k<R>(g, f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n], false, s);
+      }
+      euler_update<R>(g, f[F_NS0_0], f[F_NS0_1], f[F_NS1_0], f[F_NS1_1], f[F_C0], f[F_C1], f[F_CRHS0], f[F_CRHS1],
+                      nu, P.dt, s);
+      for (int n = 0; n < 2; n++) {  // Rescale_solute; tmp ends as species 1 before its rescale
+        cudaMemcpyAsync(tmp, f[F_C0 + n], sizeof(R) * g.nf(), cudaMemcpyDeviceToDevice, s);
+        c2r(tmp);
+        const double factor = total[n] / count_solute(tmp);
+        scale_copy<R>(g, f[F_C0 + n], f[F_C0 + n], (R)factor, s);
+      }
+      copy(F_GE0, F_U0);
+      const double f_now = free_energy_pb(charge);
+      pb_iterations = m;
+      if (!std::isfinite(f_now)) return fail(ICEP_ERR_NOT_CONVERGED, "Poisson-Boltzmann initialisation: non-finite free energy");
+      if (fabs(f_now - f_prev) < 1e-4) break;
+      f_prev = f_now;
+    }
+    for (int d = 0; d < 3; d++) zero(F_U0 + d);  // the reference leaves the velocity field reset
+    return cuda_status("steadystate_ions");
+  }
+  int pb_iterations = 0;
+
   // Init_rho_ion_dielectric without surface charge (operate_electrolyte.cxx:864-979)
-  void init_ions() {
+  int init_ions() {
     zero(F_PHI);
     scatter_profile<R>(pp, dp, dsek, f[F_PHI], nullptr, PROF_PHI, s);
     const double z0 = P.valency_pos, z1 = P.valency_neg;
@@ -1547,11 +1639,18 @@ class Engine : public EngineBase {
         cm = 0.0;
       }
     }
+    double total[2];
     for (int n = 0; n < 2; n++) {
       zero(F_C0 + n);
       fill_real<R>(g, f[F_C0 + n], (R)(n ? cm : cp), s);
+      total[n] = count_solute(f[F_C0 + n]);
       r2c(f[F_C0 + n]);
     }
+    // INIT_profile Poisson_Boltzmann with charged particles in the salt
+    // solution and more than one particle (Init_rho_ion,
+    // operate_electrolyte.cxx:834-853)
+    if (P.poisson_boltzmann && have_sc && !salt_free && np > 1) return steadystate_ions(total);
+    return ICEP_OK;
   }
 
   // ------------------------------------------------------------ interface
@@ -1578,7 +1677,8 @@ class Engine : public EngineBase {
       time = 0.0;  // Init_potential_dielectric runs at jikan.time = 0
       refresh_ext();
       for (int d = 0; d < 3; d++) zero(F_GE0 + d);
-      init_ions();
+      int st0 = init_ions();
+      if (st0) return st0;
       // Init_potential_dielectric (operate_dielectric.cxx:574-609)
       make_dielectric_field(F_GE2, F_WORK);
       int st = conc_k2charge(F_GE1, F_GE2, F_GE0);
@@ -2091,7 +2191,7 @@ class Engine : public EngineBase {
         break;
       case C_TRUNCATE: truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s); break;
       case C_CHARGE_FIELD: st = conc_k2charge(F_RHO, F_WORK, F_UP0); break;
-      case C_INIT_ION: init_ions(); break;
+      case C_INIT_ION: st = init_ions(); break;
       case C_APPLY_BK:
         if constexpr (std::is_same<R, float>::value) {
           if (!kop_supported(g)) return fail(ICEP_ERR_UNSUPPORTED, "apply_bk: no fused passes for this mesh");

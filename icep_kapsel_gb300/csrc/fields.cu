@@ -632,6 +632,29 @@ template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s) {
   k_fill_real<R><<<nblk_real(g), TPB, 0, s>>>(g, a, v);
 }
 
+template <typename R>
+__global__ void k_pb_energy(Grid g, const R *c0, const R *c1, const R *phi, R *charge, const R *pot, R ze0, R ze1,
+                            R ex, R ey, R ez, R dx, int ext, R *ideal, R *es) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R ph = phi[p.im], a = c0[p.im], b = c1[p.im];
+  ideal[p.im] = (1. - ph) * a * (log(a) - 1.) + (1. - ph) * b * (log(b) - 1.);
+  R q = charge[p.im];
+  q += ze0 * a * (1. - ph);
+  q += ze1 * b * (1. - ph);
+  charge[p.im] = q;
+  R pt = 0.5 * pot[p.im];
+  if (ext) pt -= (ex * (R)p.i + ey * (R)p.j + ez * (R)p.k) * dx;
+  es[p.im] = q * pt;
+}
+template <typename R>
+void pb_energy_terms(const Grid &g, const R *c0, const R *c1, const R *phi, R *charge, const R *pot, double ze0,
+                     double ze1, const double *e, double dx, int ext, R *ideal, R *es, cudaStream_t s) {
+  count_launch(fld<R>(g, 7));
+  k_pb_energy<R><<<nblk_real(g), TPB, 0, s>>>(g, c0, c1, phi, charge, pot, (R)ze0, (R)ze1, (R)e[0], (R)e[1], (R)e[2],
+                                              (R)dx, ext, ideal, es);
+}
+
 #define ICEP_INST(R)                                                                                                   \
   template void truncate_23<R>(const Grid &, const FieldBatch<R> &, cudaStream_t);                                    \
   template void zeta_k2u_k<R>(const Grid &, const R *, const R *, const double *, R *, R *, R *, cudaStream_t);        \
@@ -664,7 +687,9 @@ template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s) {
   template void np_flux_electric<R>(const Grid &, R *const *, const R *, R *const *, double, cudaStream_t);            \
   template void np_impermeability<R>(const Grid &, R *const *, R *const *, cudaStream_t);                              \
   template void np_flux_advection<R>(const Grid &, R *const *, const R *, R *const *, cudaStream_t);                   \
-  template void fill_real<R>(const Grid &, R *, R, cudaStream_t);
+  template void fill_real<R>(const Grid &, R *, R, cudaStream_t);                                                    \
+  template void pb_energy_terms<R>(const Grid &, const R *, const R *, const R *, R *, const R *, double, double,     \
+                                   const double *, double, int, R *, R *, cudaStream_t);
 
 ICEP_INST(double)
 ICEP_INST(float)

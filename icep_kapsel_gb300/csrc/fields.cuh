@@ -71,5 +71,13 @@ template <typename R> void np_impermeability(const Grid &g, R *const *flux, R *c
 template <typename R> void np_flux_advection(const Grid &g, R *const *flux, const R *c, R *const *u, cudaStream_t s);
 // real-space fill (k < NZ) of a constant
 template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s);
+// The per-point terms of the free energy of Calc_free_energy_PB's Dielectric
+// branch (operate_electrolyte.cxx:302-421) from the real densities c0, c1:
+// ideal = sum_n (1 - phi) c_n (log c_n - 1); charge += sum_n ze_n c_n (1 - phi)
+// (in place, species 0 first, as the reference accumulates); es = charge
+// (pot/2 - E.r dx) with E = e (0 when ext is 0).
+template <typename R>
+void pb_energy_terms(const Grid &g, const R *c0, const R *c1, const R *phi, R *charge, const R *pot, double ze0,
+                     double ze1, const double *e, double dx, int ext, R *ideal, R *es, cudaStream_t s);
 
 }  // namespace icep

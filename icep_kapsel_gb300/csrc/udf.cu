@@ -450,7 +450,11 @@ static bool fill(Bound &b, Result &r) {
   if (p.sw_eq == ICEP_ELECTROLYTE) {
     std::string v;
     if (!b.num(ce + "Dielectric_cst", p.dielectric_cst) || !b.str(ce + "INIT_profile", v)) return bad(r, b);
-    if (v != "Uniform") return unsupported(r, "INIT_profile " + v);
+    // INIT_profile (input.cxx:704-715); the engine refuses the relaxations
+    // it does not build (salt-free, a single particle in salt)
+    if (v == "Uniform") p.poisson_boltzmann = 0;
+    else if (v == "Poisson_Boltzmann") p.poisson_boltzmann = 1;
+    else return bad(r, b);
     if (!b.str(ce + "Dielectric_property.type", v)) return bad(r, b);
     if (v != "ON") return unsupported(r, "Electrolyte with Dielectric_property OFF");
     p.dielectric = 1;

@@ -125,6 +125,12 @@ typedef struct icep_params {
   int salt_free;
   double valency_counterion;
   double onsager_counterion;
+  /* constitutive_eq.Electrolyte.INIT_profile: 0 Uniform, 1 Poisson_Boltzmann
+   * (input.cxx:704-715). With charged particles in the salt solution and more
+   * than one particle, the uniform ion densities are relaxed towards their
+   * steady state before the first step (Set_steadystate_ion_density,
+   * operate_electrolyte.cxx:424-457). */
+  int poisson_boltzmann;
 } icep_params;
 
 /*

@@ -127,6 +127,7 @@ typedef struct {
   double last_error;
   long matvecs;
   double total_solute[2];
+  long pb_iterations; /* relaxation steps of the last Poisson-Boltzmann initialisation */
 } ko_ctx;
 
 #define IDX(c, i, j, k) (((long)(i) * (c)->ny + (j)) * (c)->nzp + (k))
@@ -1741,6 +1742,149 @@ static void set_salt_free_species(ko_ctx *c) {
   c->onsager[1] = 0.0;
 }
 
+/* Count_single_solute (solute_rhs.cxx:130-148): sum (1 - phi) c DX^3 of a
+ * real field */
+static double count_single_solute(const ko_ctx *c, const double *conc_x, const double *phi) {
+  double s = 0.;
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      for (int k = 0; k < c->nz; k++) s += (1. - phi[IDX(c, i, j, k)]) * conc_x[IDX(c, i, j, k)];
+  return s * c->dx3;
+}
+
+/* The Dielectric branch of Calc_free_energy_PB (operate_electrolyte.cxx:
+ * 302-421): kBT DX^3 sum (1 - phi) c (log c - 1) over the species plus
+ * DX^3 sum rho (Potential/2 - E.r DX) with rho = `charge` + sum z e c (1 - phi).
+ * `charge` is the array the reference accumulates into (its up[1]); it is
+ * modified here as there. phi is the particle profile. */
+static double free_energy_pb(ko_ctx *c, double *charge, const double *phi, double *tmp) {
+  double ideal = 0., es = 0.;
+  for (int n = 0; n < 2; n++) {
+    memcpy(tmp, c->f[F_C0 + n], sizeof(double) * c->nf);
+    fft_c2r(c, tmp);
+    for (int i = 0; i < c->nx; i++)
+      for (int j = 0; j < c->ny; j++)
+        for (int k = 0; k < c->nz; k++) {
+          const long im = IDX(c, i, j, k);
+          const double cc = tmp[im], ph = phi[im];
+          ideal += (1. - ph) * cc * (log(cc) - 1.);
+          charge[im] += c->valency_e[n] * cc * (1. - ph);
+        }
+  }
+  ideal *= c->P.kbt * c->dx3;
+  double ext[DIM];
+  for (int d = 0; d < DIM; d++)
+    ext[d] = c->P.e_ext[d] * (c->P.ac ? sin(2.0 * M_PI * c->P.frequency * c->time) : 1.0);
+  for (int i = 0; i < c->nx; i++)
+    for (int j = 0; j < c->ny; j++)
+      for (int k = 0; k < c->nz; k++) {
+        const long im = IDX(c, i, j, k);
+        double pot = 0.5 * c->f[F_POT][im];
+        if (c->P.external_field) pot -= (ext[0] * (double)i + ext[1] * (double)j + ext[2] * (double)k) * c->dx;
+        es += charge[im] * pot;
+      }
+  return ideal + es * c->dx3;
+}
+
+/* Set_steadystate_ion_density (operate_electrolyte.cxx:424-457): the salt
+ * densities relaxed by Ion_diffusion_solver_Euler (fluid_solver.cxx:293-316)
+ * -- the Nernst-Planck right-hand side of Rhs_NS_Nernst_Planck (:246-292)
+ * with the fluid at rest and the potential as it is (zero before the first
+ * solve: the external field alone drives the ions), an Euler step of the
+ * densities on the 2/3 modes and Rescale_solute (solute_rhs.cxx:99-128) back
+ * to the initial totals -- until the free energy changes by less than
+ * TOL = 1e-4 (operate_electrolyte.h:22), at most 9999 steps. The free
+ * energy's charge array starts as the reference's up[1] (here F_UP1, the
+ * particle velocity field) and, inside the loop, as the last species' real
+ * density before its rescale (Rescale_solute's working array is up[1]). */
+static void steadystate_ions(ko_ctx *c) {
+  double *phi = c->f[F_PHI];
+  double *gp[3] = {c->f[F_F0], c->f[F_F1], c->f[F_F2]};
+  double *flux[3] = {c->f[F_UP0], c->f[F_UP1], c->f[F_UP2]};
+  double *sn[3] = {c->f[F_SN0], c->f[F_SN1], c->f[F_SN2]};
+  double *crhs[2] = {c->f[F_CRHS0], c->f[F_CRHS1]};
+  double *charge = c->f[F_WV3_0], *tmp = c->f[F_WV3_1], *scratch = c->f[F_WV3_2];
+  double *pot = c->f[F_POT];
+  memcpy(charge, c->f[F_UP1], sizeof(double) * c->nf);
+  double f_prev = free_energy_pb(c, charge, phi, tmp);
+  c->pb_iterations = 0;
+  for (int m = 1; m < 10000; m++) {
+    /* grad potential on the staggered grid, minus E_ext at k = 0, to nodes */
+    fft_r2c(c, pot);
+    a_k2da_k(c, pot, gp);
+    shift_fw(c, gp);
+    fft_c2r(c, pot);
+    if (c->P.external_field) {
+      double amp = (double)c->nx * c->ny * c->nz;
+      if (c->P.ac) amp *= sin(2.0 * M_PI * c->P.frequency * c->time);
+      for (int d = 0; d < DIM; d++) gp[d][0] -= c->P.e_ext[d] * amp;
+    }
+    for (int d = 0; d < DIM; d++) fft_c2r(c, gp[d]);
+    interp_vec_normal(c, gp);
+    make_surface_normal(c);
+    for (int n = 0; n < 2; n++) {
+      double *conc = c->f[F_C0 + n];
+      truncate_23(c, conc);
+      const double kl = c->P.kbt * c->onsager[n];
+      for (long q = 0; q < c->nf; q++) scratch[q] = kl * conc[q];
+      a_k2da_k(c, scratch, flux);
+      for (int d = 0; d < DIM; d++) fft_c2r(c, flux[d]);
+      memcpy(crhs[n], conc, sizeof(double) * c->nf);
+      fft_c2r(c, crhs[n]);
+      const double ze = c->valency_e[n], L = c->onsager[n];
+      for (int i = 0; i < c->nx; i++)
+        for (int j = 0; j < c->ny; j++)
+          for (int k = 0; k < c->nz; k++) {
+            const long im = IDX(c, i, j, k);
+            const double cc = crhs[n][im];
+            for (int d = 0; d < DIM; d++) flux[d][im] += cc * (L * (gp[d][im] * ze));
+          }
+      for (int p = 0; p < c->np; p++) {  /* Solute_impermeability, as in nssolute_solver_euler */
+        pcell pc;
+        particle_cell(c, c->p[p].x, &pc);
+        for (int q = 0; q < c->np_domain; q++) {
+          double r[3], dist;
+          const long im = stencil_point(c, &pc, c->p[p].x, q, r, &dist);
+          double nv[3], n2 = 0.0;
+          for (int d = 0; d < DIM; d++) {
+            nv[d] = sn[d][im];
+            n2 += SQ(nv[d]);
+          }
+          if (n2 > 0.) {
+            double dd = 0.;
+            for (int d = 0; d < DIM; d++) dd += flux[d][im] * nv[d];
+            dd /= n2;
+            for (int d = 0; d < DIM; d++) flux[d][im] -= nv[d] * dd;
+          }
+        }
+      }
+      /* the fluid is at rest: the advection flux adds -0 */
+      for (int d = 0; d < DIM; d++) fft_r2c(c, flux[d]);
+      u_k2divergence_k(c, flux, crhs[n]);
+    }
+    const double dt = c->P.dt;
+    for (int i = 0; i < c->nx; i++)
+      for (int j = 0; j < c->ny; j++)
+        for (int k = 0; k < c->nzp; k++) {
+          if (!in_two_third(c, i, j, k / 2)) continue;
+          const long im = IDX(c, i, j, k);
+          c->f[F_C0][im] += dt * crhs[0][im];
+          c->f[F_C1][im] += dt * crhs[1][im];
+        }
+    /* Rescale_solute: charge ends as the last species' density before its rescale */
+    for (int n = 0; n < 2; n++) {
+      memcpy(charge, c->f[F_C0 + n], sizeof(double) * c->nf);
+      fft_c2r(c, charge);
+      const double factor = c->total_solute[n] / count_single_solute(c, charge, phi);
+      for (long q = 0; q < c->nf; q++) c->f[F_C0 + n][q] *= factor;
+    }
+    const double f_now = free_energy_pb(c, charge, phi, tmp);
+    c->pb_iterations = m;
+    if (fabs(f_now - f_prev) < 1e-4) break;
+    f_prev = f_now;
+  }
+}
+
 static void init_ions(ko_ctx *c) {
   const double z0 = c->P.valency_pos, z1 = c->P.valency_neg;
   c->valency_e[0] = z0 * c->P.elementary_charge;
@@ -1798,8 +1942,14 @@ static void init_ions(ko_ctx *c) {
     for (int i = 0; i < c->nx; i++)
       for (int j = 0; j < c->ny; j++)
         for (int k = 0; k < c->nz; k++) cf[IDX(c, i, j, k)] = 0.0 + val;
+    c->total_solute[n] = count_single_solute(c, cf, c->f[F_PHI]);
     fft_r2c(c, cf);
   }
+  /* INIT_profile Poisson_Boltzmann with charged particles in the salt
+   * solution, more than one particle (Init_rho_ion, operate_electrolyte.cxx:
+   * 834-853) */
+  if (c->P.poisson_boltzmann && c->P.surface_charge[0] != 0.0 && !c->P.salt_free && c->np > 1)
+    steadystate_ions(c);
 }
 
 /* main()'s initialisation after Init_Particle (sp_3d_ns.cxx:425-457) */
@@ -1934,6 +2084,7 @@ void ko_a2a_k(ko_ctx *c, double *a) { fft_r2c(c, a); }
 void ko_a_k2a(ko_ctx *c, double *a) { fft_c2r(c, a); }
 void ko_apply_A(ko_ctx *c, const double *x, double *y) { apply_A(c, x, y); }
 long ko_last_iterations(const ko_ctx *c) { return c->last_iters; }
+long ko_pb_iterations(const ko_ctx *c) { return c->pb_iterations; }
 double ko_last_error(const ko_ctx *c) { return c->last_error; }
 long ko_matvec_count(const ko_ctx *c) { return c->matvecs; }
 /* MaxIter_potential of later solves (lets a timing harness cap a solve) */

@@ -118,6 +118,8 @@ class Oracle(_Base):
         L.ko_set_uk_dc.argtypes = [C.c_void_p, _DP]
         L.ko_last_iterations.restype = C.c_long
         L.ko_last_iterations.argtypes = [C.c_void_p]
+        L.ko_pb_iterations.restype = C.c_long
+        L.ko_pb_iterations.argtypes = [C.c_void_p]
         L.ko_last_error.restype = C.c_double
         L.ko_last_error.argtypes = [C.c_void_p]
         L.ko_matvec_count.restype = C.c_long
@@ -201,6 +203,10 @@ class Oracle(_Base):
 
     def matvecs(self):
         return self.lib.ko_matvec_count(self.ctx)
+
+    def pb_iterations(self):
+        """Relaxation steps of the last Poisson-Boltzmann initialisation."""
+        return self.lib.ko_pb_iterations(self.ctx)
 
     def set_potential_iter(self, maxit):
         self.lib.ko_set_potential_iter(self.ctx, int(maxit))

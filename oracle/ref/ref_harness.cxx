@@ -372,7 +372,7 @@ static void set_globals(const icep_params *q) {
   N_spec = q->salt_free ? 1 : 2;  // Add_salt saltfree / salt (input.cxx:751-770)
   Valency_counterion = q->valency_counterion;
   Onsager_coeff_counterion = q->onsager_counterion;
-  Poisson_Boltzmann = 0;
+  Poisson_Boltzmann = q->poisson_boltzmann;  // INIT_profile (input.cxx:704-715)
   Rigid_Number = 0;
   degree_oblique = 0.0;
 }

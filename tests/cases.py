@@ -148,6 +148,15 @@ def charged_case(n=32, npart=4, seed=2, charges=(-5.0,), tol=1e-7, solver=abi.SO
     return p, abi.make_particles(x, spec=[i % len(charges) for i in range(npart)])
 
 
+def pb_case(precision=abi.FP64, solver=abi.SOLVER_REF, tol=1e-7):
+    """Charged particles in the salt solution with INIT_profile
+    Poisson_Boltzmann and a DC field E0 = (0, 0, 0.1): the ion densities are
+    relaxed towards their steady state in the field before the first solve."""
+    p, parts = charged_case(e_ext=(0.0, 0.0, 0.1), precision=precision, solver=solver, tol=tol)
+    p.poisson_boltzmann = 1
+    return p, parts
+
+
 def saltfree_case(n=32, npart=4, seed=2, charges=(-5.0, -3.0), tol=1e-7, solver=abi.SOLVER_REF,
                   precision=abi.FP64, valency=1.0, onsager=7.24):
     """Charged particles with their counterions only (Add_salt saltfree,

@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-CASES = ["fft16", "ops16", "ns32", "icep32", "icep32_bicgstab", "icep64_200", "lj32", "ax32", "janus32", "charged32", "ac32", "out32", "avs16", "saltfree32"]
+CASES = ["fft16", "ops16", "ns32", "icep32", "icep32_bicgstab", "icep64_200", "lj32", "ax32", "janus32", "charged32", "charged32_pb", "ac32", "out32", "avs16", "saltfree32"]
 
 
 def small_case(potential_tol=1e-10):
@@ -272,6 +272,18 @@ def run_case(name, out):
         r.call("charge_field")
         data["rho"] = r.get("rho")[:, :, :32]
         data["phi_p"] = r.get("work")[:, :, :32]
+    elif name == "charged32_pb":
+        # INIT_profile Poisson_Boltzmann with charged particles in the salt
+        # solution: Init_rho_ion relaxes the uniform densities in the external
+        # field (Set_steadystate_ion_density) before the initial solve
+        p, parts = cases.pb_case()
+        r = pyoracle.RefKapsel(p, parts)
+        r.init_state()
+        meta["init_iterations"] = int(r.last_iterations())
+        meta["init_error"] = float(r.last_error())
+        for k in ("c0", "c1"):
+            data[k] = r.get(k)
+        data["pot"] = r.get("pot")[:, :, :32]
     elif name == "ac32":
         # an AC field: zero at t = 0 (initial solve and first step), then
         # E_ext sin(2 pi f t) in the Poisson right-hand side, the ions' flux

@@ -1,7 +1,7 @@
 """An AC external field, E_ext sin(2 pi f t) (Electric_field.ON.AC), on the GPU.
 
 * FP64 with the reference's solver against the reference-generated golden
-  fixture ac32 (the tolerances of the DC fixture icep32): the field is zero at
+  fixture ac32 (the tolerances of the DC fixture icep32_bicgstab): the field is zero at
   t = 0, so the first step's potential is exactly zero, and the next two steps
   run with the field at t = dt and 2 dt.
 * FP64 with the spectral solver against the oracle over four steps (1e-8).

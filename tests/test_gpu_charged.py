@@ -9,6 +9,9 @@ branch of Init_potential_dielectric and Make_Maxwell_force_x_on_fluid).
 * FP64 with the spectral solver against the oracle for two steps (1e-8).
 * MIXED against FP64 (the tolerances of test_gpu_mixed.py).
 * Charged and uncharged species together are refused.
+* INIT_profile Poisson_Boltzmann: the relaxed initial densities against the
+  reference's relaxation (tests/golden/charged32_pb, 1e-12); the branches that
+  are not built are refused.
 """
 import numpy as np
 import pytest
@@ -89,3 +92,41 @@ def test_mixed_charged_and_neutral_species_refused(Sim):
     p, parts = cases.charged_case(charges=(-5.0, 0.0))
     with pytest.raises(IcepError):
         Sim(p, parts)
+
+
+def test_poisson_boltzmann_init_against_reference_golden(Sim):
+    """INIT_profile Poisson_Boltzmann (Init_rho_ion -> Set_steadystate_ion_density,
+    operate_electrolyte.cxx:424-457, 834-853): FP64 GPU relaxation of the salt
+    densities in the external field against the reference's own relaxation
+    (tests/golden/charged32_pb): the densities within 1e-12 (the relaxation
+    stops at the same step of its free-energy test), the initial potential
+    within the reference BiCGSTAB's 1e-7 tolerance (2e-5); the relaxed
+    densities differ from the uniform start."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "charged32_pb.npz"))
+    p, parts = cases.pb_case()
+    s = Sim(p, parts)
+    s.init_state()
+    for k in ("c0", "c1"):
+        assert rel(s.get(k), g[k]) < 1e-12, k
+    a = s.get("pot")[:, :, :32]
+    assert rel(a - a.mean(), g["pot"] - g["pot"].mean()) < 2e-5
+    u, uparts = cases.charged_case(e_ext=(0.0, 0.0, 0.1))
+    uni = Sim(u, uparts)
+    uni.init_state()
+    assert rel(uni.get("c0"), g["c0"]) > 1e-3
+    s.step(2)  # the step runs on from the relaxed state
+    assert np.isfinite(s.get("c0")).all()
+
+
+def test_poisson_boltzmann_unbuilt_branches_refused(Sim):
+    """The salt-free and single-particle relaxations are refused, not run."""
+    from icep_kapsel_gb300.runtime import IcepError
+    p, parts = cases.saltfree_case()
+    p.poisson_boltzmann = 1
+    with pytest.raises(IcepError):
+        Sim(p, parts)
+    q, qparts = cases.charged_case(npart=1)
+    q.poisson_boltzmann = 1
+    with pytest.raises(IcepError):
+        Sim(q, qparts)

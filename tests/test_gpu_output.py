@@ -3,7 +3,7 @@ Output_dielectric_charge_field_data, output.cxx:262-320) and
 icep_output_avs (the reference's AVS frames of the context's state).
 
 * FP64 against the reference-generated fixture out32 (the charged case after
-  its initial solve, with zeta from icep32 and a mean flow): u 1e-12, phi and
+  its initial solve, with zeta from icep32_bicgstab and a mean flow): u 1e-12, phi and
   the surface charge 1e-13 (scatter atomics add in another order), the
   solute charge 1e-12, eps 1e-13; the potential is the context's own.
 * MIXED against the same fixture at FP32 tolerances (2e-6; the solute
@@ -46,7 +46,7 @@ def Sim():
 
 
 def out32_state(Sim, precision):
-    ic = np.load(os.path.join(GOLD, "icep32.npz"))
+    ic = np.load(os.path.join(GOLD, "icep32_bicgstab.npz"))
     p, parts = cases.charged_case()
     p.precision = precision
     p.solver = abi.SOLVER_SPECTRAL

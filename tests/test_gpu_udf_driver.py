@@ -56,7 +56,7 @@ def test_driver_matches_api(rt, tmp_path):
 
 def test_driver_refuses_unsupported(rt, tmp_path):
     from icep_kapsel_gb300.build import BIN
-    src = open(FIX).read().replace('"Uniform",', '"Poisson_Boltzmann",')
+    src = open(FIX).read().replace('{"ON", {1000, 1.0e-8, 80.0, 5.0, 2.0}}', '{"OFF", {1000, 1.0e-8, 80.0, 5.0, 2.0}}')
     d = tmp_path / "u"
     d.mkdir()
     (d / "define_small.udf").write_text(open(os.path.join(os.path.dirname(FIX), "define_small.udf")).read())
@@ -64,4 +64,4 @@ def test_driver_refuses_unsupported(rt, tmp_path):
     r = subprocess.run([BIN, "-I", str(d / "input.udf"), "-O", str(tmp_path / "o")], capture_output=True, text=True,
                        timeout=120)
     assert r.returncode == 3  # ICEP_ERR_UNSUPPORTED
-    assert "Poisson_Boltzmann" in r.stderr
+    assert "Dielectric_property OFF" in r.stderr

@@ -319,3 +319,18 @@ def test_saltfree32(oracle_so):
     assert rel(a - a.mean(), g["pot"] - g["pot"].mean()) < 2e-5
     o.call("charge_field")
     assert rel(o.get("rho")[:, :, :32], g["rho"]) < 1e-12
+
+
+def test_charged32_pb(oracle_so):
+    """INIT_profile Poisson_Boltzmann (Set_steadystate_ion_density): the
+    relaxed ion densities at rounding level -- the relaxation stops at the same
+    step (its free-energy test) and every step agrees."""
+    g, meta = load("charged32_pb")
+    p, parts = cases.pb_case()
+    o = pyoracle.Oracle(p, parts, so=oracle_so)
+    o.init_state()
+    assert o.pb_iterations() > 10
+    for k in ("c0", "c1"):
+        assert rel(o.get(k), g[k]) < 1e-12, k
+    a = o.get("pot")[:, :, :32]
+    assert rel(a - a.mean(), g["pot"] - g["pot"].mean()) < 2e-5

@@ -119,8 +119,17 @@ def test_saltfree(rt, tmp_path):
     assert p.salt_free == 0
 
 
+def test_init_profile(rt, tmp_path):
+    """INIT_profile (input.cxx:704-715): Uniform -> 0, Poisson_Boltzmann -> 1;
+    any other word is an error."""
+    p, _, _, _ = rt.udf_read(FIX)
+    assert p.poisson_boltzmann == 0
+    p, _, _, _ = rt.udf_read(rewrite(tmp_path, '"Uniform",', '"Poisson_Boltzmann",'))
+    assert p.poisson_boltzmann == 1
+
+
 @pytest.mark.parametrize("old,new", [
-    ('"Uniform",', '"Poisson_Boltzmann",'),
+    ('{"ON", {1000, 1.0e-8, 80.0, 5.0, 2.0}}', '{"OFF", {1000, 1.0e-8, 80.0, 5.0, 2.0}}'),
     ('{"user_specify",\n', '{"uniform_random",\n'),  # fine: placement by rand()
 ])
 def test_unsupported_or_changed(rt, tmp_path, old, new):

@@ -309,21 +309,7 @@ class Engine : public EngineBase {
     pp.eps_f = p.eps_fluid;
     pp.dt = p.dt;
     pp.rho = p.rho;
-    pp.lj_eps = p.lj_epsilon;
-    pp.lj_dia = 2.0 * radius;
-    pp.lj_powers = p.lj_powers;
-    double arc;
-    if (p.lj_truncate > 0)
-      arc = (p.lj_powers == 0) ? pow(2., 1. / 6.) : (p.lj_powers == 1) ? pow(2., 1. / 12.) : pow(2., 1. / 18.);
-    else if (p.lj_truncate == 0) {
-      int nmin = N[0] < N[1] ? N[0] : N[1];
-      nmin = nmin < N[2] ? nmin : N[2];
-      arc = nmin * p.dx * .5 / pp.lj_dia;
-      if (arc > 2.5) arc = 2.5;
-    } else
-      arc = 0.;
-    pp.r_cutoff = arc * pp.lj_dia;
-    pp.lj_on = p.lj_truncate >= 0;
+    lj_params_from(p, pp);
     pp.n_species = p.n_species;
     for (int q = 0; q < ICEP_MAX_SPECIES; q++) {
       const double mass = p.mass_ratio[q] * p.rho * 4. / 3. * M_PI * radius * radius * radius;
@@ -1120,6 +1106,8 @@ class Engine : public EngineBase {
     if (!learned) return unsupported_learned();
     if (configs < 1 || steps < 1 || !(lr > 0)) return fail(ICEP_ERR_ARG, "learned_train arguments");
     std::vector<icep_particle> keep(np > 0 ? np : 1);
+    std::vector<float> snap(net.nparams);  // the parameters before this training
+    cudaMemcpyAsync(snap.data(), net.params, sizeof(float) * net.nparams, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
     memcpy(keep.data(), hp, sizeof(icep_particle) * np);
@@ -1138,7 +1126,12 @@ class Engine : public EngineBase {
         st = fail(ICEP_ERR_ARG, "cannot place the training particles");
         break;
       }
-      for (int q = 0; q < np; q++) hp[q].eps_p = P.per_particle_eps ? 1.0 + 9.0 * u(rng) : P.eps_particle_top;
+      // eps_p uniform in [1, 10]; with per-particle permittivities a
+      // configuration also draws how many particles it has (np/4 .. np): the
+      // others take the fluid's permittivity and are absent from eps
+      const int active = P.per_particle_eps ? np / 4 + (int)(u(rng) * (np - np / 4 + 1)) : np;
+      for (int q = 0; q < np; q++)
+        hp[q].eps_p = !P.per_particle_eps ? P.eps_particle_top : (q < active ? 1.0 + 9.0 * u(rng) : P.eps_fluid);
       cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
       double e[3] = {nd(rng), nd(rng), nd(rng)};
       const double en = sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]);
@@ -1165,9 +1158,26 @@ class Engine : public EngineBase {
     cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
     make_dielectric_field(F_WORK, F_WV1);
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
-    if (st == ICEP_OK) net_trained = true;
-    return st;
+    if (st != ICEP_OK) return st;
+    // keep the trained parameters only if they lower the one-step loss on
+    // the context's own residuals (configurations it was not trained on);
+    // otherwise restore the parameters it had before
+    net_trained = true;
+    double ls = 0.0, ll = 0.0;
+    if ((st = learned_eval(2, &ls, &ll))) return st;
+    if (!(ll < ls)) {
+      // not better than the spectral preconditioner alone: the network is
+      // not applied (as before any training), its earlier parameters back
+      cudaMemcpyAsync(net.params, snap.data(), sizeof(float) * net.nparams, cudaMemcpyHostToDevice, s);
+      net.pack(s);
+      net_trained = false;
+      kept_training = false;
+    } else {
+      kept_training = true;
+    }
+    return cuda_status("learned_train");
   }
+  bool kept_training = false;
   int learned_enable(int on) override {
     if (!learned) return unsupported_learned();
     net_use = on != 0;

@@ -80,6 +80,10 @@ extern "C" int icep_Calc_f_Lennard_Jones_noalloc(const icep_params *params, icep
       return reject(ICEP_ERR_UNSUPPORTED, "mesh sizes must be powers of two in [16, 256]");
   if (!(params->dx > 0.0)) return reject(ICEP_ERR_ARG, "non-positive DX");
   if (n_particles == 0) return ICEP_OK;
+  // an error left pending by the caller's earlier work is reported, not
+  // taken over (and not cleared)
+  if (cudaPeekAtLastError() != cudaSuccess)
+    return reject(ICEP_ERR_CUDA, "a CUDA error is pending from earlier work");
   int *scratch = nullptr;
   if (scratch_for_current_device(&scratch) != ICEP_OK)
     return reject(ICEP_ERR_CUDA, "cannot look up the device scratch array");
@@ -95,21 +99,7 @@ extern "C" int icep_Calc_f_Lennard_Jones_noalloc(const icep_params *params, icep
     pp.N[d] = N[d];
   }
   pp.np = n_particles;
-  pp.lj_eps = params->lj_epsilon;
-  pp.lj_dia = 2.0 * pp.radius;
-  pp.lj_powers = params->lj_powers;
-  double arc;
-  if (params->lj_truncate > 0)
-    arc = (params->lj_powers == 0) ? pow(2., 1. / 6.) : (params->lj_powers == 1) ? pow(2., 1. / 12.) : pow(2., 1. / 18.);
-  else if (params->lj_truncate == 0) {
-    int nmin = N[0] < N[1] ? N[0] : N[1];
-    nmin = nmin < N[2] ? nmin : N[2];
-    arc = nmin * params->dx * .5 / pp.lj_dia;
-    if (arc > 2.5) arc = 2.5;
-  } else
-    arc = 0.;
-  pp.r_cutoff = arc * pp.lj_dia;
-  pp.lj_on = params->lj_truncate >= 0;
+  lj_params_from(*params, pp);
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // fr accumulates in the gather: it starts from zero. The cell counters in
@@ -118,11 +108,13 @@ extern "C" int icep_Calc_f_Lennard_Jones_noalloc(const icep_params *params, icep
   // the scratch by an earlier call is used.
   count_launch();
   k_clear_fr<<<div_up(n_particles, 128), 128, 0, s>>>(d_particles, n_particles);
+  cudaError_t e = cudaGetLastError();  // nothing was pending: this is the launch's own status
+  if (e != cudaSuccess) return reject(ICEP_ERR_CUDA, cudaGetErrorString(e));
   if (pp.lj_on) {
     const int st = lj_force(pp, d_particles, scratch, kScratchInts, nullptr, 0, nullptr, s);
     if (st != ICEP_OK) return reject(st, "cell list does not fit the scratch array");
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return reject(ICEP_ERR_CUDA, cudaGetErrorString(e));
   }
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return reject(ICEP_ERR_CUDA, cudaGetErrorString(e));
   return ICEP_OK;
 }

@@ -570,6 +570,24 @@ void md_position(const PartParams &pp, icep_particle *p, bool ab2, cudaStream_t 
   count_launch(2.0 * pp.np * sizeof(icep_particle));
   k_md_position<<<div_up(pp.np, 128), 128, 0, s>>>(pp, p, ab2 ? 1 : 0);
 }
+void lj_params_from(const icep_params &p, PartParams &pp) {
+  pp.lj_eps = p.lj_epsilon;
+  pp.lj_dia = 2.0 * pp.radius;
+  pp.lj_powers = p.lj_powers;
+  double arc;
+  if (p.lj_truncate > 0) {
+    arc = (p.lj_powers == 0) ? pow(2., 1. / 6.) : (p.lj_powers == 1) ? pow(2., 1. / 12.) : pow(2., 1. / 18.);
+  } else if (p.lj_truncate == 0) {
+    int nmin = pp.N[0] < pp.N[1] ? pp.N[0] : pp.N[1];
+    nmin = nmin < pp.N[2] ? nmin : pp.N[2];
+    arc = nmin * pp.dx * .5 / pp.lj_dia;
+    if (arc > 2.5) arc = 2.5;
+  } else {
+    arc = 0.;
+  }
+  pp.r_cutoff = arc * pp.lj_dia;
+  pp.lj_on = p.lj_truncate >= 0;
+}
 void md_velocity(const PartParams &pp, icep_particle *p, bool ab2, cudaStream_t s) {
   if (pp.np == 0) return;
   count_launch(2.0 * pp.np * sizeof(icep_particle));

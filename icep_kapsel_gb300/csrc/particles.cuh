@@ -36,6 +36,13 @@ struct PartParams {
   double qe[ICEP_MAX_SPECIES];
 };
 
+// The Lennard-Jones constants of Set_global_parameters (input.cxx:404-440)
+// into pp: lj_eps, lj_dia = 2 a, lj_powers, the cutoff (2^(1/6), 2^(1/12)
+// or 2^(1/18) diameters for LJ_truncate ON; half the smallest box edge, at
+// most 2.5 diameters, for OFF; none for NONE) and lj_on. Needs pp.radius,
+// pp.dx and pp.N set; shared by contexts and the context-free entry point.
+void lj_params_from(const icep_params &p, PartParams &pp);
+
 // Profile scatters over the integration stencil (Particle_domain stencil,
 // profile.cxx:25-74), one thread per (particle, stencil point), atomics:
 //   PROF_PHI:     out += Phi (Make_phi_particle_sum, make_phi.cxx:229-275)

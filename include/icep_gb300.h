@@ -286,12 +286,18 @@ int icep_batch_step(icep_batch *batch, int nsteps);
  * decides convergence as for the plain solver. Before training (or with
  * icep_learned_enable(ctx, 0)) the network is not applied. */
 /* Train on the GPU: `configs` random particle configurations (the context's
- * particle count and radius, new positions, eps_p uniform in [1, 10] when
- * per-particle permittivity is on, a random direction of E_ext), each for
- * `steps_per_config` Adam steps along the chain of residuals r -> r - A P(r)
- * starting from the right-hand side; loss |r - A P(r)|^2 / |r|^2 with
- * P(r) = M^-1 (r + rms(r) prolong(net(eps, r))). The
- * context's particles and field are restored afterwards. */
+ * radius, new positions, a random direction of E_ext; with per-particle
+ * permittivity on, eps_p uniform in [1, 10] and between a quarter of the
+ * context's particle count and all of it present -- the others take the
+ * fluid's permittivity), each for `steps_per_config` Adam steps along the
+ * chain of residuals r -> r - A P(r) starting from the right-hand side; loss
+ * |r - A P(r)|^2 / |r|^2 with P(r) = M^-1 (r + rms(r) prolong(net(eps, r))).
+ * The context's particles and field are restored afterwards. The trained
+ * parameters are kept only if they lower the one-step loss on the context's
+ * own residuals (icep_learned_eval with chain 2, configurations not trained
+ * on) below the spectral preconditioner's; otherwise the earlier parameters
+ * come back and the network is not applied until icep_learned_enable(ctx, 1)
+ * or a later training that is kept. */
 int icep_learned_train(icep_ctx *ctx, int configs, int steps_per_config, unsigned seed, double lr, double *loss_first,
                        double *loss_last);
 /* 1: apply the network in the preconditioner, 0: spectral part only. */

@@ -85,11 +85,10 @@ def test_learned_solve_matches_plain():
     ls1, ll1 = lrn.learned_eval(4)
     print("\none-step loss on the context's residuals: spectral %.4f, learned before %.4f after %.4f"
           % (ls1, ll0, ll1))
-    # the trained correction does not make the preconditioner worse than the
-    # spectral one alone by more than training noise (Adam on gradients
-    # summed with atomics: the loss after training varies by ~1% between
-    # runs; on this problem the network gains little, see bench.py's numbers)
-    assert ll1 <= ls1 * 1.02
+    # training keeps its parameters only when they lower the one-step loss on
+    # these residuals (the context's own, not trained on) below the spectral
+    # preconditioner's: the learned preconditioner is never worse here
+    assert ll1 <= ls1
     plain.step(3)
     lrn.step(3)
     it_plain, err_plain, _ = plain.solver_stats()

@@ -77,8 +77,32 @@ def test_no_alloc_matches_context_entry_point_twice():
         np.testing.assert_allclose(got, ref, rtol=RTOL, atol=RTOL * np.abs(ref).max())
 
 
+@pytest.mark.parametrize("truncate", [0, -1])
+def test_no_alloc_matches_other_cutoffs(truncate):
+    """LJ_truncate OFF (cutoff at half the smallest box edge, at most 2.5
+    diameters) and NONE (no Lennard-Jones force: fr comes back zero), both
+    entry points deriving the cutoff from the same parameters."""
+    lib = _lib()
+    p, parts = cases.lj_dense_case()
+    p.lj_truncate = truncate
+    for q in range(p.n_particles):
+        parts[q].fr[1] = -7.0  # stale input
+    ref = _with_context(lib, p, parts)
+    got = _no_alloc(lib, p, parts)
+    if truncate < 0:
+        assert np.abs(ref).max() == 0.0 and np.abs(got).max() == 0.0
+    else:
+        assert np.abs(ref).max() > 0.0
+        np.testing.assert_allclose(got, ref, rtol=RTOL, atol=RTOL * np.abs(ref).max())
+
+
 def test_no_alloc_rejects_oversize():
     lib = _lib()
     p, _ = cases.lj_dense_case()
     st = lib.icep_Calc_f_Lennard_Jones_noalloc(C.byref(p), C.c_void_p(16), MAX_PARTICLES + 1, None)
     assert st == ERR_UNSUPPORTED
+    for n in (48, 512):  # not a power of two; more than 16 cells of 16 DX per side
+        q, _ = cases.lj_dense_case()
+        q.nx = n
+        st = lib.icep_Calc_f_Lennard_Jones_noalloc(C.byref(q), C.c_void_p(16), 4, None)
+        assert st == ERR_UNSUPPORTED, n

@@ -114,8 +114,58 @@ class Engine : public EngineBase {
   bool x64_valid = false;
   bool xp_valid = false;  // D_XP holds the potential of the previous solve
 
+  // The step's two fixed kernel sequences (before and after the Poisson
+  // solve, whose host-side iteration control stays outside) captured once as
+  // CUDA graphs and replayed each step: one launch each instead of ~100
+  // kernel launches, which is what bounds small replicas. Used when no
+  // kernel argument changes between steps (no AC field; no surface charges,
+  // whose charge normalisation reads a sum on the host; no phase profiling)
+  // from the second step on (the first uses the Euler integrators); disabled
+  // by ICEP_GRAPHS=0 and, for the context, by any capture failure (the step
+  // then runs eagerly).
+  bool use_graphs = false;
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  unsigned long long glaunch[2] = {0, 0}, gbytes[2] = {0, 0};
+  template <class Body>
+  int run_segment(int k, Body body) {
+    if (!use_graphs || ts == 0) return body();
+    if (!gexec[k]) {
+      const unsigned long long l0 = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
+      const unsigned long long b0 = __atomic_load_n(&g_alg_bytes, __ATOMIC_RELAXED);
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        use_graphs = false;
+        return body();
+      }
+      const int st = body();
+      cudaGraph_t graph = nullptr;
+      cudaError_t e = cudaStreamEndCapture(s, &graph);
+      const unsigned long long dl = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED) - l0;
+      const unsigned long long db = __atomic_load_n(&g_alg_bytes, __ATOMIC_RELAXED) - b0;
+      // nothing captured has run: its counts come with each replay
+      __atomic_fetch_sub(&g_kernel_launches, dl, __ATOMIC_RELAXED);
+      __atomic_fetch_sub(&g_alg_bytes, db, __ATOMIC_RELAXED);
+      if (e == cudaSuccess && st == ICEP_OK) e = cudaGraphInstantiate(&gexec[k], graph, 0);
+      if (graph) cudaGraphDestroy(graph);
+      if (st != ICEP_OK || e != cudaSuccess || !gexec[k]) {
+        cudaGetLastError();
+        gexec[k] = nullptr;
+        use_graphs = false;
+        return body();  // the sequence runs eagerly from now on
+      }
+      glaunch[k] = dl;
+      gbytes[k] = db;
+    }
+    if (cudaGraphLaunch(gexec[k], s) != cudaSuccess) return cuda_status("graph launch");
+    __atomic_fetch_add(&g_kernel_launches, glaunch[k], __ATOMIC_RELAXED);
+    __atomic_fetch_add(&g_alg_bytes, gbytes[k], __ATOMIC_RELAXED);
+    return ICEP_OK;
+  }
+
   ~Engine() override {
     if (s) cudaStreamSynchronize(s);
+    for (int k = 0; k < 2; k++)
+      if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
     for (int i = 0; i < F_COUNT; i++) cudaFree(f[i]);
     fft_plan_free(fft);
     for (int i = 0; i < D_COUNT; i++) cudaFree(d64[i]);
@@ -376,6 +426,8 @@ class Engine : public EngineBase {
       phase_on = true;
       for (int k = 0; k <= NPH; k++) cudaEventCreate(&ph_ev[k]);
     }
+    const char *ge = getenv("ICEP_GRAPHS");
+    use_graphs = !(ge && ge[0] == '0') && !phase_on && !p.ac && !have_sc;
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("setup");
     return cuda_status("setup");
   }
@@ -1465,49 +1517,65 @@ class Engine : public EngineBase {
   // Time_evolution_hydro (sp_3d_ns.cxx:24-186)
   int time_evolution_hydro() {
     int st;
-    mark(0);
-    if (!electrolyte) ns_solver_slaved_euler();
-    else nssolute_solver_euler();
-    for (int d = 0; d < 3; d++)  // FIX_CELL: time-dependent mean pressure gradient (sp_3d_ns.cxx:30-36)
-      if ((P.fix_cell >> d) & 1) cudaMemsetAsync(ukdc + d, 0, sizeof(double), s);
-    mark(1);
-    truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
-    zeta_k2u();
-    if (!P.fixed_particle) md_position(pp, dp, ts != 0, s);
-    make_phi_particle_sum();
-    mark(2);
-    if (electrolyte) {
-      for (int d = 0; d < 3; d++) {
-        zero(F_UP0 + d);
-        zero(F_F0 + d);
+    // the sequence before the Poisson solve
+    st = run_segment(0, [&]() -> int {
+      mark(0);
+      if (!electrolyte) ns_solver_slaved_euler();
+      else nssolute_solver_euler();
+      for (int d = 0; d < 3; d++)  // FIX_CELL: time-dependent mean pressure gradient (sp_3d_ns.cxx:30-36)
+        if ((P.fix_cell >> d) & 1) cudaMemsetAsync(ukdc + d, 0, sizeof(double), s);
+      mark(1);
+      truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
+      zeta_k2u();
+      if (!P.fixed_particle) md_position(pp, dp, ts != 0, s);
+      make_phi_particle_sum();
+      mark(2);
+      if (electrolyte) {
+        for (int d = 0; d < 3; d++) {
+          zero(F_UP0 + d);
+          zero(F_F0 + d);
+        }
+        f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], true, s);
+        make_dielectric_field(F_F0, F_WORK);
+        return conc_k2charge(F_UP0, F_F0, F_F1);
       }
-      f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], true, s);
-      make_dielectric_field(F_F0, F_WORK);
-      if ((st = conc_k2charge(F_UP0, F_F0, F_F1))) return st;
+      return ICEP_OK;
+    });
+    if (st) return st;
+    if (electrolyte) {
       mark(3);
       if ((st = solve_potential(F_UP0, F_POT, F_F2))) return st;
       mark(4);
-      maxwell_stress(F_UP0);
-      mark(5);
-      add_vec<R>(g, vec(F_U0), vec(F_F0), (R)(P.dt / P.rho), s);
-      solenoidal_u(F_U0);
     } else {
       mark(3);
       mark(4);
-      mark(5);
     }
-    mark(6);
-    f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], false, s);
-    if (!P.fixed_particle) {
-      if ((st = lj_into_fr())) return fail(st, "LJ cell list");
-      md_velocity(pp, dp, ts != 0, s);
-    }
-    mark(7);
-    make_u_particle_sum();
-    f_particle_sole_and_add();
-    mark(8);
-    r2c(f[F_U0], f[F_U1], f[F_U2]);
-    u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
+    // the sequence after it
+    st = run_segment(1, [&]() -> int {
+      if (electrolyte) {
+        maxwell_stress(F_UP0);
+        mark(5);
+        add_vec<R>(g, vec(F_U0), vec(F_F0), (R)(P.dt / P.rho), s);
+        solenoidal_u(F_U0);
+      } else {
+        mark(5);
+      }
+      mark(6);
+      f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], false, s);
+      if (!P.fixed_particle) {
+        const int s2 = lj_into_fr();
+        if (s2) return fail(s2, "LJ cell list");
+        md_velocity(pp, dp, ts != 0, s);
+      }
+      mark(7);
+      make_u_particle_sum();
+      f_particle_sole_and_add();
+      mark(8);
+      r2c(f[F_U0], f[F_U1], f[F_U2]);
+      u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
+      return ICEP_OK;
+    });
+    if (st) return st;
     mark(9);
     mark(10);
     if (phase_on) {

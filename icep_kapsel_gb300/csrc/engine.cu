@@ -17,6 +17,7 @@
 #include "fields.cuh"
 #include "krylov.cuh"
 #include "kop.cuh"
+#include "probe.cuh"
 #include "kspace.cuh"
 #include "refine.cuh"
 #include "unet.cuh"
@@ -124,11 +125,17 @@ class Engine : public EngineBase {
   // by ICEP_GRAPHS=0 and, for the context, by any capture failure (the step
   // then runs eagerly).
   bool use_graphs = false;
-  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-  unsigned long long glaunch[2] = {0, 0}, gbytes[2] = {0, 0};
+  cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+  unsigned long long glaunch[3] = {0, 0, 0}, gbytes[3] = {0, 0, 0};
   template <class Body>
   int run_segment(int k, Body body) {
     if (!use_graphs || ts == 0) return body();
+    return run_graph(k, body);
+  }
+  // body() captured once into graph slot k (0, 1: the step's sequences; 2:
+  // one iteration of the fused Poisson solve), then replayed
+  template <class Body>
+  int run_graph(int k, Body body) {
     if (!gexec[k]) {
       const unsigned long long l0 = __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED);
       const unsigned long long b0 = __atomic_load_n(&g_alg_bytes, __ATOMIC_RELAXED);
@@ -164,7 +171,7 @@ class Engine : public EngineBase {
 
   ~Engine() override {
     if (s) cudaStreamSynchronize(s);
-    for (int k = 0; k < 2; k++)
+    for (int k = 0; k < 3; k++)
       if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
     for (int i = 0; i < F_COUNT; i++) cudaFree(f[i]);
     fft_plan_free(fft);
@@ -829,18 +836,27 @@ class Engine : public EngineBase {
       hks[KS_ITERS] = 0.0;
       hks[KS_RR] = bsq;
       hks[KS_RESTART] = eps2 * bsq;
+      hks[KS_IEPS] = 1.0 / eps_ref;
       cudaMemcpyAsync(kst, hks, sizeof(double) * KS_COUNT, cudaMemcpyHostToDevice, s);
+      // one iteration: every argument is a fixed pointer or constant (the
+      // scalars, 1/eps_ref and the stop flag live in kst), so it is captured
+      // once as a CUDA graph and replayed (not while a probe times launches)
+      auto iteration = [&]() -> int {
+        kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, s, kst);
+        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
+        kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s);
+        kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, s, kst);
+        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
+        kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s);
+        kop_xr(g, xt, r, p, sv, t, r0, 0.0, F1, F2, P3, F3, kcnt + 2, s, kst, maxit);
+        return ICEP_OK;
+      };
+      const bool graph_iter = use_graphs && g_probe_kind == PROBE_NONE;
       while (i < maxit && rr > tol2) {
         int chunk = (i == 0 && kf_pred > 2) ? kf_pred - 2 : 1;
         if (chunk > maxit - i) chunk = maxit - i;
         for (int q = 0; q < chunk; q++) {
-          kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, s, kst);
-          kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-          kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s);
-          kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, s, kst);
-          kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-          kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s);
-          kop_xr(g, xt, r, p, sv, t, r0, 0.0, F1, F2, P3, F3, kcnt + 2, s, kst, maxit);
+          if ((st = graph_iter ? run_graph(2, iteration) : iteration())) return st;
         }
         cudaMemcpyAsync(hkpart, kfin, sizeof(double) * (7 + KS_COUNT), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fused k-space iteration");
@@ -1135,7 +1151,8 @@ class Engine : public EngineBase {
     double ls = 0, ll = 0;
     for (int k = 0; k < chain; k++) {
       double l[2];
-      for (int use = 1; use >= 0; use--) {
+      // without a trained network both are the spectral preconditioner
+      for (int use = net_trained ? 1 : 0; use >= 0; use--) {
         copy_real<R>(g, f[F_KB], f[F_KR], s);
         learned_precond_real(eref, use == 1 && net_trained);
         apply_A(f[F_KZ], f[F_KT]);
@@ -1144,6 +1161,7 @@ class Engine : public EngineBase {
         if ((st = read_scal())) return st;
         l[use] = hscal[S_AUX0];
       }
+      if (!net_trained) l[1] = l[0];
       ls += l[0];
       ll += l[1];
       // next residual of the spectral chain (F_KS holds it after use = 0)

@@ -141,6 +141,7 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
     beta = (float)__ldcg(ks + KS_BETA);
     omega = (float)__ldcg(ks + KS_OMEGA);
     rho = __ldcg(ks + KS_RHO);
+    ieps = (float)__ldcg(ks + KS_IEPS);
   }
   extern __shared__ unsigned char smem_raw[];
   const int sw = KW + 1;

@@ -34,7 +34,9 @@ bool kop_supported(const Grid &g);
 // and sets KS_DONE (1: converged, non-finite or at the iteration limit; 2: a
 // restart for the host). The host then enqueues several iterations between
 // synchronisations.
-enum { KS_RHO = 0, KS_BETA, KS_OMEGA, KS_TOL2, KS_DONE, KS_ITERS, KS_RR, KS_RESTART, KS_COUNT };
+// KS_IEPS: 1/eps_ref of the solve's preconditioner (read by kop_xinv in place
+// of its argument when a state pointer is given).
+enum { KS_RHO = 0, KS_BETA, KS_OMEGA, KS_TOL2, KS_DONE, KS_ITERS, KS_RR, KS_RESTART, KS_IEPS, KS_COUNT };
 // number of x-pencil blocks (= partial sums written by kop_xfwd)
 int kop_pencil_blocks(const Grid &g);
 // ef_d = 0.5 (eps + eps at the next point along d), real points

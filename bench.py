@@ -225,13 +225,18 @@ def run_reference(args, world, rank, dist):
     o.step(1)
     t_step = time.perf_counter() - t0
     m_step, it_step, err_step = o.matvecs() - m_init, o.last_iterations(), o.last_error()
-    need_min = (args.steps + args.warmup) * t_step / 60.0
+    # from the sixth step on the solve stagnates above the tolerance and runs
+    # both MaxIter attempts: 2 * (MaxIter + 1) operator applications
+    t_stagnant = t_step * 2.0 * (args.maxit + 1) / max(m_step, 1)
+    need_min = (min(args.steps + args.warmup, 5) * t_step + max(args.steps + args.warmup - 5, 0) * t_stagnant) / 60.0
     line = {"impl": "reference", "metric": METRIC, "unit": UNIT, "higher_is_better": True, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
             "unavailable": ("a full reference step of the %d^3 / %d-sphere workload took %.1f s on %d host cores "
-                            "(%d operator applications; later steps stagnate above the tolerance and run both "
-                            "MaxIter attempts), so --steps %d --warmup %d would take more than %.0f min"
-                            % (args.n, args.np, t_step, cores, m_step, args.steps, args.warmup, need_min)),
+                            "(%d operator applications); from the sixth step on its solve stagnates above the "
+                            "tolerance and runs both MaxIter attempts (~%.0f s a step at the same rate), so "
+                            "--steps %d --warmup %d would take about %.0f min"
+                            % (args.n, args.np, t_step, cores, m_step, t_stagnant, args.steps, args.warmup,
+                               need_min)),
             "config": workload_config(args, "fp64", "reference BiCGSTAB (identity)"),
             "one_full_step": {"seconds": t_step, "steps_per_s": 1.0 / t_step, "cores": cores, "kind": "port",
                               "iterations": int(it_step), "operator_applications": int(m_step),

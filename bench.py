@@ -265,6 +265,13 @@ def run_gpu(args, world, rank, local, dist):
     precision = abi.MIXED if args.precision == "mixed" else abi.FP64
     p, parts = workload(args, precision, abi.SOLVER_SPECTRAL)
     sim = Simulation(p, parts)
+    tiles = None
+    if precision == abi.MIXED:
+        picks, us = sim.autotune_picks()
+        tiles = {"xinv_pencils_per_block": picks[0], "xfwd_pencils_per_block": picks[1],
+                 "plane_kernel": "shared-memory" if picks[2] else "register-resident",
+                 "us_per_launch": {"xinv_8_16_32": list(us[0:3]), "xfwd_8_16_32": list(us[3:6]),
+                                   "plane_register_shared": list(us[6:8])}}
     sim.init_state()
     for _ in range(args.warmup):
         sim.step(1)
@@ -356,7 +363,7 @@ def run_gpu(args, world, rank, local, dist):
                                   "definition": "every kernel of the step adds its external inputs and outputs "
                                                 "(icep_algorithmic_bytes), summed over the timed steps, divided "
                                                 "by the steps' device time"}},
-            "cpu_baseline": base}
+            "cpu_baseline": base, "autotune": tiles}
     if fp64_error is not None:
         line["fp64_oracle_error"] = fp64_error
     if learned is not None:

@@ -75,6 +75,9 @@ class Engine : public EngineBase {
   int kf_pred = 0;            // iterations of the last fused solve (the first batch of the next)
   unsigned *kcnt = nullptr;   // last-block counters of the dot passes
   int kop_npb = 0;
+  KopTiles kop_tiles;        // the autotuner's picks for this mesh
+  bool kop_tuned = false;
+  double kop_tune_us[8] = {0};
   // learned preconditioner and its flexible GMRES (solver LEARNED)
   static constexpr int FG_M = 20;  // restart length
   bool learned = false;
@@ -405,6 +408,22 @@ class Engine : public EngineBase {
       kfin = kpart + nk - 7 - KS_COUNT;
       kerr = reinterpret_cast<int *>(kfin + 6);
       kst = kfin + 7;
+      // tile choices of the fused passes (cached per mesh); ICEP_AUTOTUNE=0
+      // keeps the defaults, ICEP_KOP_TILES="xinv,xfwd,plane" sets them
+      const char *at = getenv("ICEP_AUTOTUNE");
+      const char *force = getenv("ICEP_KOP_TILES");
+      int fi = 0, ff = 0, fp = 0;
+      if (force && sscanf(force, "%d,%d,%d", &fi, &ff, &fp) == 3) {
+        kop_tiles.xinv_kw = fi;
+        kop_tiles.xfwd_kw = ff;
+        kop_tiles.plane_smem = fp;
+      } else if constexpr (std::is_same<R, float>::value) {
+        if (!(at && at[0] == '0')) {
+          kop_tiles = kop_autotune(fft, f[F_KP], f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2],
+                                   f[F_KV], kerr, s, kop_tune_us);
+          kop_tuned = true;
+        }
+      }
     }
     if (p.solver == ICEP_SOLVER_LEARNED) {
       if (!mixed || !electrolyte || !kpart || p.nx != p.ny || p.nx != p.nz || p.nx < 32)
@@ -842,12 +861,12 @@ class Engine : public EngineBase {
       // scalars, 1/eps_ref and the stop flag live in kst), so it is captured
       // once as a CUDA graph and replayed (not while a probe times launches)
       auto iteration = [&]() -> int {
-        kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, s, kst);
-        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-        kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s);
-        kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, s, kst);
-        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-        kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s);
+        kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, s, kst, kop_tiles);
+        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
+        kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s, kop_tiles);
+        kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, s, kst, kop_tiles);
+        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
+        kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s, kop_tiles);
         kop_xr(g, xt, r, p, sv, t, r0, 0.0, F1, F2, P3, F3, kcnt + 2, s, kst, maxit);
         return ICEP_OK;
       };
@@ -916,9 +935,10 @@ class Engine : public EngineBase {
   void apply_Bk(float *xt, float *out) {
     if constexpr (std::is_same<R, float>::value) {
       kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, mean_eps_cached, f[F_WV3_0], f[F_WV3_1],
-               f[F_WV3_2], s);
-      kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], kerr, s);
-      kop_xfwd(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], out, KOP_NONE, nullptr, nullptr, nullptr, nullptr, s);
+               f[F_WV3_2], s, nullptr, kop_tiles);
+      kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
+      kop_xfwd(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], out, KOP_NONE, nullptr, nullptr, nullptr, nullptr, s,
+               kop_tiles);
       matvecs++;
     }
   }
@@ -2210,6 +2230,16 @@ class Engine : public EngineBase {
   int phase_times(double *ms, int n) override {
     for (int k = 0; k < n && k < NPH; k++) ms[k] = ph_ms[k];
     return phase_on ? ICEP_OK : ICEP_ERR_STATE;
+  }
+
+  int tile_picks(int *picks, double *us) override {
+    if (!kop_tuned) return fail(ICEP_ERR_STATE, "no tuned fused passes in this context (MIXED electrolyte, NX <= 128)");
+    picks[0] = kop_tiles.xinv_kw;
+    picks[1] = kop_tiles.xfwd_kw;
+    picks[2] = kop_tiles.plane_smem;
+    if (us)
+      for (int k = 0; k < 8; k++) us[k] = kop_tune_us[k];
+    return ICEP_OK;
   }
 
   int selftest_wait(int kernel) override {

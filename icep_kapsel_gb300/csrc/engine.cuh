@@ -57,6 +57,11 @@ struct EngineBase {
     return unsupported_learned();
   }
   virtual int learned_backward(const double *gy, double *grad) { return unsupported_learned(); }
+  // the tile autotuner's picks for the fused Poisson passes (see kop.cuh)
+  virtual int tile_picks(int *picks, double *us) {
+    err = "no tuned fused passes in this context";
+    return ICEP_ERR_STATE;
+  }
   // launch one kernel whose bounded wait must run out (1: fused plane pass,
   // 2: tcgen05 convolution) and return the status a solve would return
   virtual int selftest_wait(int kernel) {

@@ -271,6 +271,9 @@ int icep_unpin_host(void *p) {
   return cudaHostUnregister(p) == cudaSuccess ? ICEP_OK : ICEP_ERR_CUDA;
 }
 
+int icep_autotune_picks(icep_ctx *c, int *picks, double *us) {
+  return (ok(c) && picks) ? wrap(c, c->e->tile_picks(picks, us)) : ICEP_ERR_ARG;
+}
 int icep_selftest_wait(icep_ctx *c, int kernel) { return ok(c) ? wrap(c, c->e->selftest_wait(kernel)) : ICEP_ERR_ARG; }
 
 /* generic dispatch used by the Python layer (same numbering as the oracle) */

@@ -1,4 +1,9 @@
 // kop.cu -- see kop.cuh.
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 #include "fft_blocks.cuh"
 #include "kop.cuh"
 #include "krylov.cuh"
@@ -86,10 +91,11 @@ __device__ int block_partials_final(float s0, float s1, double scale, double *pa
   return 1;
 }
 
-// (j, kz) of pencils q0 .. q0 + KW - 1 into shared arrays (synchronised by the caller)
+// (j, kz) of pencils q0 .. q0 + W - 1 into shared arrays (synchronised by the caller)
+template <int W>
 __device__ __forceinline__ void pencil_coords(const Grid &g, int q0, int *pj, int *pkz) {
   const int lin = threadIdx.y * blockDim.x + threadIdx.x;
-  if (lin < KW) {
+  if (lin < W) {
     const int q = q0 + lin;
     pj[lin] = q / g.hnz;
     pkz[lin] = q - (q / g.hnz) * g.hnz;
@@ -131,7 +137,7 @@ struct SrcGradXInv {
   }
 };
 
-template <int N>
+template <int N, int KWT>
 __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, const float *r, const float *v,
                                                   float beta, float omega, double rho, const double *fin,
                                                   float ieps, float *w0, float *w1, float *w2,
@@ -144,34 +150,34 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
     ieps = (float)__ldcg(ks + KS_IEPS);
   }
   extern __shared__ unsigned char smem_raw[];
-  const int sw = KW + 1;
+  const int sw = KWT + 1;
   cf *tws = reinterpret_cast<cf *>(smem_raw);
   cf *raw = tws + N;
   cf *ta = raw + N * sw;
   cf *tb = ta + N * sw;
   const int nq = g.ny * g.hnz;
-  const int q0 = blockIdx.x * KW;
-  const int nvalid = nq - q0 < KW ? nq - q0 : KW;
+  const int q0 = blockIdx.x * KWT;
+  const int nvalid = nq - q0 < KWT ? nq - q0 : KWT;
   const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  __shared__ int pj[KW], pkz[KW];
+  __shared__ int pj[KWT], pkz[KWT];
   load_table(tws, twx, N);
-  pencil_coords(g, q0, pj, pkz);
+  pencil_coords<KWT>(g, q0, pj, pkz);
   __syncthreads();
   __shared__ float salpha;  // one FP64 division per block
   if (mode == KOP_S && lin == 0) salpha = (float)(rho / fin[0]);
   __syncthreads();
   const float alpha = (mode == KOP_S) ? salpha : 0.f;
   // vector update at the read modes of this block's pencils: xblock gives
-  // KW * N/8 threads, so every thread has XPT = 8 items; the loads of a batch
+  // KWT * N/8 threads, so every thread has XPT = 8 items; the loads of a batch
   // of XB items are issued together before any update is computed or stored
-  static_assert(N / 8 <= 512 / KW, "xblock(N) = KW x N/8 threads");
+  static_assert(N / 8 <= 512 / KWT, "xblock(N) = KWT x N/8 threads");
   constexpr int XPT = 8, XB = 4;
   for (int u0 = 0; u0 < XPT; u0 += XB) {
     cf lr[XB], lv[XB], lp[XB];
 #pragma unroll
     for (int u = 0; u < XB; u++) {
       const int it = lin + (u0 + u) * nthr;
-      const int w = it % KW, e = it / KW;
+      const int w = it % KWT, e = it / KWT;
       lr[u] = lv[u] = lp[u] = cf{0.f, 0.f};
       if (w >= nvalid) continue;
       const long idx = (long)e * nq + q0 + w;
@@ -187,7 +193,7 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
 #pragma unroll
     for (int u = 0; u < XB; u++) {
       const int it = lin + (u0 + u) * nthr;
-      const int w = it % KW, e = it / KW;
+      const int w = it % KWT, e = it / KWT;
       if (w >= nvalid) {
         raw[e * sw + w] = cf{0.f, 0.f};
         continue;
@@ -210,13 +216,13 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
     }
   }
   __syncthreads();
-  block_fft<float, N, KW>(SrcGradXInv<0>{raw, pj, pkz, sw, nvalid, g},
+  block_fft<float, N, KWT>(SrcGradXInv<0>{raw, pj, pkz, sw, nvalid, g},
                           GPencils<float>{reinterpret_cast<cf *>(w0), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
-  block_fft<float, N, KW>(SrcGradXInv<1>{raw, pj, pkz, sw, nvalid, g},
+  block_fft<float, N, KWT>(SrcGradXInv<1>{raw, pj, pkz, sw, nvalid, g},
                           GPencils<float>{reinterpret_cast<cf *>(w1), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
-  block_fft<float, N, KW>(SrcGradXInv<2>{raw, pj, pkz, sw, nvalid, g},
+  block_fft<float, N, KWT>(SrcGradXInv<2>{raw, pj, pkz, sw, nvalid, g},
                           GPencils<float>{reinterpret_cast<cf *>(w2), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
 }
@@ -793,38 +799,38 @@ struct DivAcc {
   }
 };
 
-template <int N>
+template <int N, int KWT>
 __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const float *w1, const float *w2,
                                                   float *out, int mode, const float *other, double *partials,
                                                   double *finals, unsigned *counter, const cf *__restrict__ twx) {
   extern __shared__ unsigned char smem_raw[];
-  const int sw = KW + 1;
+  const int sw = KWT + 1;
   cf *tws = reinterpret_cast<cf *>(smem_raw);
   cf *acc = tws + N;
   cf *ta = acc + N * sw;
   cf *tb = ta + N * sw;
   const int nq = g.ny * g.hnz;
-  const int q0 = blockIdx.x * KW;
-  const int nvalid = nq - q0 < KW ? nq - q0 : KW;
+  const int q0 = blockIdx.x * KWT;
+  const int nvalid = nq - q0 < KWT ? nq - q0 : KWT;
   const int lin = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
-  __shared__ int pj[KW], pkz[KW];
+  __shared__ int pj[KWT], pkz[KWT];
   load_table(tws, twx, N);
-  pencil_coords(g, q0, pj, pkz);
+  pencil_coords<KWT>(g, q0, pj, pkz);
   __syncthreads();
-  block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w0)), (long)q0, 1, (long)nq, nvalid},
+  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w0)), (long)q0, 1, (long)nq, nvalid},
                           DivAcc<0>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
-  block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w1)), (long)q0, 1, (long)nq, nvalid},
+  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w1)), (long)q0, 1, (long)nq, nvalid},
                           DivAcc<1>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
-  block_fft<float, N, KW>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w2)), (long)q0, 1, (long)nq, nvalid},
+  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w2)), (long)q0, 1, (long)nq, nvalid},
                           DivAcc<2>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
   float s0 = 0.f, s1 = 0.f;  // the thread's few terms in FP32; blocks and their sum in FP64
-  static_assert(N / 8 <= 512 / KW, "xblock(N) = KW x N/8 threads");
+  static_assert(N / 8 <= 512 / KWT, "xblock(N) = KWT x N/8 threads");
   constexpr int XPT = 8;
   cf lo[XPT];  // the dot operands, all loads in flight before use
 #pragma unroll
   for (int u = 0; u < XPT; u++) {
     const int it = lin + u * nthr;
-    const int w = it % KW, e = it / KW;
+    const int w = it % KWT, e = it / KWT;
     lo[u] = cf{0.f, 0.f};
     if (mode == KOP_NONE || w >= nvalid) continue;
     lo[u] = ldw(other, (long)e * nq + q0 + w, read_weight(g, e, pj[w], pkz[w]));
@@ -832,7 +838,7 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
 #pragma unroll
   for (int u = 0; u < XPT; u++) {
     const int it = lin + u * nthr;
-    const int w = it % KW, e = it / KW;
+    const int w = it % KWT, e = it / KWT;
     if (w >= nvalid) continue;
     const int wt = read_weight(g, e, pj[w], pkz[w]);
     if (wt == 0) continue;
@@ -940,19 +946,40 @@ __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1
   ef2[im] = 0.5f * (eps[gidx(g, i, j, (k + 1) % g.nz)] + e0);
 }
 
-size_t xpass_smem(int n) { return ((size_t)n + 3 * (size_t)n * (KW + 1)) * sizeof(cf); }
+size_t xpass_smem(int n, int kw) { return ((size_t)n + 3 * (size_t)n * (kw + 1)) * sizeof(cf); }
 size_t plane_smem_f(int ny, int h) { return kplane_smem(ny, h); }
 constexpr size_t KOP_PLANE_SMEM_MAX = 220 * 1024;
 
-dim3 xblock(int n) { return dim3(KW, n / 8 < 512 / KW ? n / 8 : 512 / KW); }
+dim3 xblock(int n, int kw) { return dim3(kw, n / 8 < 512 / kw ? n / 8 : 512 / kw); }
 
-template <int N>
+template <int N, int KWT>
 void set_x_attr() {
   static bool attr = false;  // one attribute call per instantiation
   if (attr) return;
-  cudaFuncSetAttribute(k_kop_xinv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xpass_smem(N));
-  cudaFuncSetAttribute(k_kop_xfwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xpass_smem(N));
+  cudaFuncSetAttribute(k_kop_xinv<N, KWT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xpass_smem(N, KWT));
+  cudaFuncSetAttribute(k_kop_xfwd<N, KWT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xpass_smem(N, KWT));
   attr = true;
+}
+
+// pencils per block of the x passes that a mesh edge N offers the tuner
+// (N/8 threads per pencil, at most 512 threads per block)
+inline bool xkw_ok(int n, int kw) { return (kw == 8 || kw == 16 || kw == 32) && n / 8 * kw <= 512 && (n == 64 || n == 128 || kw == 16); }
+
+template <int N, int KWT>
+void launch_xinv(const Grid &g, int mode, float *vec, const float *r, const float *v, double beta, double omega,
+                 double rho, const double *fin, float ieps, float *w0, float *w1, float *w2, const cf *twx,
+                 const double *ks, cudaStream_t s) {
+  set_x_attr<N, KWT>();
+  k_kop_xinv<N, KWT><<<div_up((long)g.ny * g.hnz, KWT), xblock(N, KWT), xpass_smem(N, KWT), s>>>(
+      g, mode, vec, r, v, (float)beta, (float)omega, rho, fin, ieps, w0, w1, w2, twx, ks);
+}
+template <int N, int KWT>
+void launch_xfwd(const Grid &g, const float *w0, const float *w1, const float *w2, float *out, int mode,
+                 const float *other, double *partials, double *finals, unsigned *counter, const cf *twx,
+                 cudaStream_t s) {
+  set_x_attr<N, KWT>();
+  k_kop_xfwd<N, KWT><<<div_up((long)g.ny * g.hnz, KWT), xblock(N, KWT), xpass_smem(N, KWT), s>>>(
+      g, w0, w1, w2, out, mode, other, partials, finals, counter, twx);
 }
 
 // the register plane pass covers NY in {64, 128} and NZ/2 in {32, 64}
@@ -963,22 +990,26 @@ constexpr bool rplane_ok() {
 
 template <int NY, int H>
 void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-                     const float *ef2, int *err, cudaStream_t s, int test_wait = 0) {
+                     const float *ef2, int *err, cudaStream_t s, int test_wait = 0, bool smem_kernel = false) {
   const float scale = (float)(1.0 / ((double)p.g.nx * p.g.ny * p.g.nz));
   if constexpr (rplane_ok<NY, H>()) {
-    constexpr size_t sm = rplane_smem<NY, H>();
-    static bool attr = false;  // one attribute call per instantiation
-    if (!attr) {
-      cudaFuncSetAttribute(k_kop_plane_r<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-      attr = true;
+    if (!smem_kernel) {
+      constexpr size_t sm = rplane_smem<NY, H>();
+      static bool attr = false;  // one attribute call per instantiation
+      if (!attr) {
+        cudaFuncSetAttribute(k_kop_plane_r<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        attr = true;
+      }
+      count_launch(fld<float>(p.g, 9));
+      probe_begin(PROBE_KOP_PLANE, s);
+      k_kop_plane_r<NY, H><<<dim3(p.g.nx, 3), RPlane<NY, H>::NT, sm, s>>>(
+          p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z, p.tw_post, scale, err, test_wait);
+      // algorithmic bytes: per field the half spectrum in and out and eps_face_d in
+      probe_end(PROBE_KOP_PLANE, 3.0 * 3.0 * sizeof(float) * (double)p.g.nreal(), s);
+      return;
     }
-    count_launch(fld<float>(p.g, 9));
-    probe_begin(PROBE_KOP_PLANE, s);
-    k_kop_plane_r<NY, H><<<dim3(p.g.nx, 3), RPlane<NY, H>::NT, sm, s>>>(
-        p.g, w0, w1, w2, ef0, ef1, ef2, p.tw_y, p.tw_z, p.tw_post, scale, err, test_wait);
-    // algorithmic bytes: per field the half spectrum in and out and eps_face_d in
-    probe_end(PROBE_KOP_PLANE, 3.0 * 3.0 * sizeof(float) * (double)p.g.nreal(), s);
-  } else {
+  }
+  {
     const size_t sm = plane_smem_f(NY, H);
     static bool attr = false;  // one attribute call per instantiation
     if (!attr) {
@@ -995,12 +1026,12 @@ void launch_plane_nh(const FFTPlan<float> &p, float *w0, float *w1, float *w2, c
 
 template <int NY>
 void launch_plane_n(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-                    const float *ef2, int *err, cudaStream_t s) {
+                    const float *ef2, int *err, cudaStream_t s, bool smem_kernel) {
   switch (p.g.nz / 2) {
-    case 8: launch_plane_nh<NY, 8>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
-    case 16: launch_plane_nh<NY, 16>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
-    case 32: launch_plane_nh<NY, 32>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
-    default: launch_plane_nh<NY, 64>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
+    case 8: launch_plane_nh<NY, 8>(p, w0, w1, w2, ef0, ef1, ef2, err, s, 0, smem_kernel); break;
+    case 16: launch_plane_nh<NY, 16>(p, w0, w1, w2, ef0, ef1, ef2, err, s, 0, smem_kernel); break;
+    case 32: launch_plane_nh<NY, 32>(p, w0, w1, w2, ef0, ef1, ef2, err, s, 0, smem_kernel); break;
+    default: launch_plane_nh<NY, 64>(p, w0, w1, w2, ef0, ef1, ef2, err, s, 0, smem_kernel); break;
   }
 }
 
@@ -1010,7 +1041,8 @@ bool kop_supported(const Grid &g) {
   return g.ny <= 128 && g.nz <= 128 && plane_smem_f(g.ny, g.nz / 2) <= KOP_PLANE_SMEM_MAX;
 }
 
-int kop_pencil_blocks(const Grid &g) { return (int)div_up((long)g.ny * g.hnz, KW); }
+// (an upper bound over the x-pass variants: at least 8 pencils per block)
+int kop_pencil_blocks(const Grid &g) { return (int)div_up((long)g.ny * g.hnz, 8); }
 
 void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, float *ef2, cudaStream_t s) {
   count_launch(fld<float>(g, 4));
@@ -1019,24 +1051,27 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
               double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
-              cudaStream_t s, const double *ks) {
+              cudaStream_t s, const double *ks, const KopTiles &t) {
   const Grid &g = p.g;
-  const unsigned nb = (unsigned)kop_pencil_blocks(g);
   const float ieps = (float)(1.0 / eps_ref);
+  const int kw = xkw_ok(g.nx, t.xinv_kw) ? t.xinv_kw : 16;
   count_launch(fld<float>(g, mode == KOP_P ? 7.0 : mode == KOP_S ? 6.0 : 4.0));
   probe_begin(PROBE_KOP_XINV, s);
-#define KOP_XINV(N)                                                                                        \
-  case N:                                                                                                  \
-    set_x_attr<N>();                                                                                       \
-    k_kop_xinv<N><<<nb, xblock(N), xpass_smem(N), s>>>(g, mode, vec, r, v, (float)beta, (float)omega, rho, \
-                                                       fin, ieps, w0, w1, w2, p.tw_x, ks);                 \
-    break;
+#define KOP_XINV(N, W) launch_xinv<N, W>(g, mode, vec, r, v, beta, omega, rho, fin, ieps, w0, w1, w2, p.tw_x, ks, s)
   switch (g.nx) {
-    KOP_XINV(16)
-    KOP_XINV(32)
-    KOP_XINV(64)
-    KOP_XINV(128)
-    KOP_XINV(256)
+    case 16: KOP_XINV(16, 16); break;
+    case 32: KOP_XINV(32, 16); break;
+    case 64:
+      if (kw == 8) KOP_XINV(64, 8);
+      else if (kw == 32) KOP_XINV(64, 32);
+      else KOP_XINV(64, 16);
+      break;
+    case 128:
+      if (kw == 8) KOP_XINV(128, 8);
+      else if (kw == 32) KOP_XINV(128, 32);
+      else KOP_XINV(128, 16);
+      break;
+    case 256: KOP_XINV(256, 16); break;
   }
 #undef KOP_XINV
   // algorithmic bytes: r, v (and p) in, the updated vector and 3 fields out
@@ -1044,13 +1079,81 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
 }
 
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-               const float *ef2, int *err, cudaStream_t s) {
+               const float *ef2, int *err, cudaStream_t s, const KopTiles &t) {
+  const bool smem = t.plane_smem != 0;
   switch (p.g.ny) {
-    case 16: launch_plane_n<16>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
-    case 32: launch_plane_n<32>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
-    case 64: launch_plane_n<64>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
-    default: launch_plane_n<128>(p, w0, w1, w2, ef0, ef1, ef2, err, s); break;
+    case 16: launch_plane_n<16>(p, w0, w1, w2, ef0, ef1, ef2, err, s, smem); break;
+    case 32: launch_plane_n<32>(p, w0, w1, w2, ef0, ef1, ef2, err, s, smem); break;
+    case 64: launch_plane_n<64>(p, w0, w1, w2, ef0, ef1, ef2, err, s, smem); break;
+    default: launch_plane_n<128>(p, w0, w1, w2, ef0, ef1, ef2, err, s, smem); break;
   }
+}
+
+KopTiles kop_autotune(const FFTPlan<float> &p, float *vec, float *w0, float *w1, float *w2, const float *ef0,
+                      const float *ef1, const float *ef2, float *out, int *err, cudaStream_t s, double *us) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int>, std::pair<KopTiles, std::vector<double>>> cache;
+  const Grid &g = p.g;
+  const auto key = std::make_tuple(g.nx, g.ny, g.nz);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      if (us)
+        for (int k = 0; k < 8; k++) us[k] = it->second.second[k];
+      return it->second.first;
+    }
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto time_us = [&](auto launch) -> double {
+    launch();
+    cudaEventRecord(e0, s);
+    for (int r = 0; r < 5; r++) launch();
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return 1000.0 * ms / 5.0;
+  };
+  std::vector<double> t(8, 0.0);
+  const int kws[3] = {8, 16, 32};
+  KopTiles best;
+  double bi = 1e30, bf = 1e30;
+  for (int c = 0; c < 3; c++) {
+    KopTiles v;
+    v.xinv_kw = v.xfwd_kw = kws[c];
+    if (!xkw_ok(g.nx, kws[c])) continue;
+    t[c] = time_us([&]() {
+      kop_xinv(p, KOP_NONE, vec, nullptr, nullptr, 0, 0, 0, nullptr, 1.0, w0, w1, w2, s, nullptr, v);
+    });
+    t[3 + c] = time_us([&]() { kop_xfwd(p, w0, w1, w2, out, KOP_NONE, nullptr, nullptr, nullptr, nullptr, s, v); });
+    if (t[c] < bi) {
+      bi = t[c];
+      best.xinv_kw = kws[c];
+    }
+    if (t[3 + c] < bf) {
+      bf = t[3 + c];
+      best.xfwd_kw = kws[c];
+    }
+  }
+  KopTiles reg, sh;
+  sh.plane_smem = 1;
+  const bool has_reg = (g.ny == 64 || g.ny == 128) && (g.nz / 2 == 32 || g.nz / 2 == 64) && g.nz / 2 <= g.ny;
+  if (has_reg) t[6] = time_us([&]() { kop_plane(p, w0, w1, w2, ef0, ef1, ef2, err, s, reg); });
+  t[7] = time_us([&]() { kop_plane(p, w0, w1, w2, ef0, ef1, ef2, err, s, sh); });
+  best.plane_smem = (has_reg && t[6] <= t[7]) ? 0 : 1;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaMemsetAsync(err, 0, sizeof(int), s);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = std::make_pair(best, t);
+  }
+  if (us)
+    for (int k = 0; k < 8; k++) us[k] = t[k];
+  return best;
 }
 
 bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0,
@@ -1065,23 +1168,27 @@ bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2
 }
 
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
-              const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s) {
+              const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s,
+              const KopTiles &t) {
   const Grid &g = p.g;
-  const unsigned nb = (unsigned)kop_pencil_blocks(g);
+  const int kw = xkw_ok(g.nx, t.xfwd_kw) ? t.xfwd_kw : 16;
   count_launch(fld<float>(g, mode == KOP_NONE ? 4.0 : 5.0));
   probe_begin(PROBE_KOP_XFWD, s);
-#define KOP_XFWD(N)                                                                                                 \
-  case N:                                                                                                           \
-    set_x_attr<N>();                                                                                                \
-    k_kop_xfwd<N><<<nb, xblock(N), xpass_smem(N), s>>>(g, w0, w1, w2, out, mode, other, partials, finals, \
-                                                       counter, p.tw_x);                                    \
-    break;
+#define KOP_XFWD(N, W) launch_xfwd<N, W>(g, w0, w1, w2, out, mode, other, partials, finals, counter, p.tw_x, s)
   switch (g.nx) {
-    KOP_XFWD(16)
-    KOP_XFWD(32)
-    KOP_XFWD(64)
-    KOP_XFWD(128)
-    KOP_XFWD(256)
+    case 16: KOP_XFWD(16, 16); break;
+    case 32: KOP_XFWD(32, 16); break;
+    case 64:
+      if (kw == 8) KOP_XFWD(64, 8);
+      else if (kw == 32) KOP_XFWD(64, 32);
+      else KOP_XFWD(64, 16);
+      break;
+    case 128:
+      if (kw == 8) KOP_XFWD(128, 8);
+      else if (kw == 32) KOP_XFWD(128, 32);
+      else KOP_XFWD(128, 16);
+      break;
+    case 256: KOP_XFWD(256, 16); break;
   }
 #undef KOP_XFWD
   // algorithmic bytes: 3 fields and the dot operand in, the output vector out

@@ -26,6 +26,23 @@ enum { KOP_P = 0, KOP_S = 1, KOP_NONE = 2 };
 
 // true if the fused passes cover this grid (an x-plane fits in shared memory)
 bool kop_supported(const Grid &g);
+
+// Tile choices of the fused passes: x pencils per block of the inverse and
+// forward x passes (8, 16 or 32 for NX in {64, 128}; 16 otherwise), and the
+// plane pass's implementation (0: the register-resident kernel where the
+// mesh has one, 1: the shared-memory kernel).
+struct KopTiles {
+  int xinv_kw = 16, xfwd_kw = 16, plane_smem = 0;
+};
+// The tile autotuner: times every candidate of each pass (5 launches each
+// after one warm-up, CUDA events on s) on the given scratch fields -- any
+// values: the operator runs without vector update or dots -- and returns the
+// fastest; `us` (optional, 8 values) receives the times per launch in the
+// order xinv 8/16/32, xfwd 8/16/32, plane register/shared (0 where a
+// candidate does not exist for the mesh). The picks are cached per mesh for
+// the process, so later contexts of the same mesh take them untimed.
+KopTiles kop_autotune(const FFTPlan<float> &p, float *vec, float *w0, float *w1, float *w2, const float *ef0,
+                      const float *ef1, const float *ef2, float *out, int *err, cudaStream_t s, double *us);
 // Device-side BiCGSTAB iteration state (doubles). With a state pointer
 // kop_xinv takes beta, omega and rho from it instead of its arguments, and
 // kop_xr returns without touching x and r once KS_DONE is set (the other
@@ -37,7 +54,7 @@ bool kop_supported(const Grid &g);
 // KS_IEPS: 1/eps_ref of the solve's preconditioner (read by kop_xinv in place
 // of its argument when a state pointer is given).
 enum { KS_RHO = 0, KS_BETA, KS_OMEGA, KS_TOL2, KS_DONE, KS_ITERS, KS_RR, KS_RESTART, KS_IEPS, KS_COUNT };
-// number of x-pencil blocks (= partial sums written by kop_xfwd)
+// an upper bound on the x-pencil blocks (= partial sums written by kop_xfwd)
 int kop_pencil_blocks(const Grid &g);
 // ef_d = 0.5 (eps + eps at the next point along d), real points
 void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, float *ef2, cudaStream_t s);
@@ -46,11 +63,11 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 // mode KOP_NONE: vec is used as it is (r, v, fin unused).
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
               double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
-              cudaStream_t s, const double *ks = nullptr);
+              cudaStream_t s, const double *ks = nullptr, const KopTiles &t = KopTiles());
 // err: device word set to 1 if a bulk copy into shared memory did not
 // complete within the kernel's wait limit (checked by the caller)
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-               const float *ef2, int *err, cudaStream_t s);
+               const float *ef2, int *err, cudaStream_t s, const KopTiles &t = KopTiles());
 // Bounded-wait self-test of the plane pass: the register plane kernel
 // launched so that its copy-arrival wait runs out (no copy is issued), which
 // sets *err; false when the grid has no register plane kernel.
@@ -62,7 +79,8 @@ bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2
 // to finish (counter: a device word at zero, left at zero);
 // mode KOP_NONE: no dot products (other, partials, finals unused).
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
-              const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s);
+              const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s,
+              const KopTiles &t = KopTiles());
 // alpha = rho / fin1[0]; omega = fin2[1] / fin2[0];
 // part3[2b] = (r0, r), part3[2b+1] = (r, r) over kop_xr_blocks(g) blocks,
 // fin3 their sums (counter3 as for kop_xfwd).

@@ -111,6 +111,7 @@ def load_library(path=None):
     L.icep_learned_backward.argtypes = [V, _DP, _DP]
     L.icep_learned_stats.argtypes = [V, C.POINTER(I), C.POINTER(I)]
     L.icep_selftest_wait.argtypes = [V, I]
+    L.icep_autotune_picks.argtypes = [V, C.POINTER(I), _DP]
     _lib = L
     return L
 
@@ -196,6 +197,15 @@ class Simulation:
 
     def call(self, name):
         self._check(self.lib.icep_call(self.ctx, CALL_ID[name]), name)
+
+    def autotune_picks(self):
+        """The tile autotuner's picks (xinv pencils per block, xfwd pencils per
+        block, plane kernel 0 register / 1 shared memory) and its timings (us
+        per launch: xinv 8/16/32, xfwd 8/16/32, plane register/shared)."""
+        picks = (C.c_int * 3)()
+        us = np.zeros(8)
+        self._check(self.lib.icep_autotune_picks(self.ctx, picks, _dp(us)), "autotune_picks")
+        return list(picks), us
 
     def selftest_wait(self, kernel):
         """icep_selftest_wait: the status (ICEP_ERR_TIMEOUT expected) and the

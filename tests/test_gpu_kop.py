@@ -119,3 +119,39 @@ def test_bounded_wait_convolution(Sim):
     _, err, _ = s.solver_stats()
     assert err <= 1e-8
     s.close()
+
+
+def test_autotune_picks_and_every_tile_shape(Sim, monkeypatch):
+    """The tile autotuner times every candidate at context creation and keeps
+    the fastest; every candidate tile shape computes the same operator
+    (ICEP_KOP_TILES sets the tiles for a context)."""
+    p, parts = cases.icep_case(n=64, npart=8, minsep=10.0, seed=7, eps_f=80.0, eps_p=2.0, e_ext=(0.0, 0.0, 0.1),
+                               tol=1e-8, solver=abi.SOLVER_SPECTRAL, precision=abi.MIXED)
+    s = Sim(p, parts)
+    picks, us = s.autotune_picks()
+    assert picks[0] in (8, 16, 32) and picks[1] in (8, 16, 32) and picks[2] in (0, 1)
+    assert np.all(us[:6] > 0) and us[6] > 0 and us[7] > 0
+    idx = {8: 0, 16: 1, 32: 2}
+    assert us[idx[picks[0]]] == min(us[0:3]) and us[3 + idx[picks[1]]] == min(us[3:6])
+    assert picks[2] == (0 if us[6] <= us[7] else 1)
+    s.close()
+    rng = np.random.default_rng(3)
+    ph = np.fft.rfftn(rng.standard_normal((64, 64, 64)))
+    buf = np.zeros((64, 64, 66))
+    buf[:, :, 0::2] = ph.real
+    buf[:, :, 1::2] = ph.imag
+    outs = []
+    for tiles in ("8,8,0", "16,16,1", "32,32,0", "16,32,1"):
+        monkeypatch.setenv("ICEP_KOP_TILES", tiles)
+        q = Sim(p, parts)
+        q.call("dielectric_field")
+        q.set("wv1", buf)
+        q.call("apply_bk")
+        outs.append(q.get("work"))
+        q.close()
+    wt = read_weight(64, 32)
+    for o in outs[1:]:
+        a = o[:, :, 0::2] + 1j * o[:, :, 1::2]
+        b = outs[0][:, :, 0::2] + 1j * outs[0][:, :, 1::2]
+        d = np.where(wt > 0, np.abs(a - b), 0.0)
+        assert float(np.linalg.norm(d) / np.linalg.norm(np.where(wt > 0, np.abs(b), 0.0))) < 2e-6

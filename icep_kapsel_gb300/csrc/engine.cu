@@ -509,6 +509,12 @@ class Engine : public EngineBase {
     zeta_k2u_k<R>(g, f[F_ZETA0], f[F_ZETA1], ukdc, f[F_U0], f[F_U1], f[F_U2], s);
     c2r(f[F_U0], f[F_U1], f[F_U2]);
   }
+  // Truncate_vector_two_third_rule of zeta then Zeta_k2u, the truncation
+  // fused into the k-space pass (fluid_solver.cxx:342-343; sp_3d_ns.cxx:37-38)
+  void truncate_zeta_k2u() {
+    zeta_k2u_trunc<R>(g, f[F_ZETA0], f[F_ZETA1], ukdc, f[F_U0], f[F_U1], f[F_U2], s);
+    c2r(f[F_U0], f[F_U1], f[F_U2]);
+  }
   // U2advection_k (operate_omega.cxx:12-98) on real u into adv0/adv1
   void u2advection_k(int a0, int a1) {
     advection_products<R>(g, f[F_U0], f[F_U1], f[F_U2], f[a0], f[a1], s);
@@ -518,14 +524,12 @@ class Engine : public EngineBase {
   // Solenoidal_u (operate_omega.h:109-116)
   void solenoidal_u(int id0) {
     r2c(f[id0], f[id0 + 1], f[id0 + 2]);
-    truncate_23<R>(g, batch(f[id0], f[id0 + 1], f[id0 + 2]), s);
-    solenoidal_uk<R>(g, f[id0], f[id0 + 1], f[id0 + 2], s);
+    truncate_solenoidal_uk<R>(g, f[id0], f[id0 + 1], f[id0 + 2], s);
     c2r(f[id0], f[id0 + 1], f[id0 + 2]);
   }
   // NS_solver_slavedEuler (fluid_solver.cxx:340-366)
   void ns_solver_slaved_euler() {
-    truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
-    zeta_k2u();
+    truncate_zeta_k2u();
     u2advection_k(F_NS0_0, F_NS0_1);
     ns_slaved_update<R>(g, f[F_ZETA0], f[F_ZETA1], f[F_NS0_0], f[F_NS0_1], nu, P.dt, s);
   }
@@ -541,11 +545,16 @@ class Engine : public EngineBase {
     for (int d = 0; d < 3; d++) zero(F_UP0 + d);
     scatter_up<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_UP0], f[F_UP1], f[F_UP2], s);
   }
-  // Make_f_particle_dt_sole + Add_f_particle (f_particle.h:37-95)
-  void f_particle_sole_and_add() {
+  // Make_f_particle_dt_sole + Add_f_particle (f_particle.h:37-95) + U2zeta_k
+  // (operate_omega.h:212-215): f = up - phi u, then f and u to spectra and
+  // one k-space pass (u += P T f, the vorticity and mean flow of the sum).
+  // Leaves u as its spectrum, as U2zeta_k does, and f as the spectrum of the
+  // non-solenoidal force.
+  void f_particle_sole_add_to_zeta() {
     f_nonsole<R>(g, vec(F_F0), vec(F_UP0), f[F_PHI], vec(F_U0), s);
-    solenoidal_u(F_F0);
-    add_vec<R>(g, vec(F_U0), vec(F_F0), R(1), s);
+    r2c(f[F_F0], f[F_F1], f[F_F2]);
+    r2c(f[F_U0], f[F_U1], f[F_U2]);
+    sole_add_zeta<R>(g, vec(F_F0), vec(F_U0), f[F_ZETA0], f[F_ZETA1], ukdc, s);
   }
   // Make_dielectric_field (operate_dielectric.cxx:270-309): phi_sin into
   // phi_id; per-particle permittivity (extension) accumulates into aux_id.
@@ -1250,11 +1259,12 @@ class Engine : public EngineBase {
     if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("learned_train");
     if (st != ICEP_OK) return st;
     // keep the trained parameters only if they lower the one-step loss on
-    // the context's own residuals (configurations it was not trained on);
+    // the context's own residuals (configurations it was not trained on),
+    // over the chain of four residuals that learned_eval(4) reports;
     // otherwise restore the parameters it had before
     net_trained = true;
     double ls = 0.0, ll = 0.0;
-    if ((st = learned_eval(2, &ls, &ll))) return st;
+    if ((st = learned_eval(4, &ls, &ll))) return st;
     if (!(ll < ls)) {
       // not better than the spectral preconditioner alone: the network is
       // not applied (as before any training), its earlier parameters back
@@ -1504,15 +1514,18 @@ class Engine : public EngineBase {
   }
   // the part of Make_Maxwell_force_x_on_fluid after the Poisson solve
   // (operate_dielectric.cxx:651-763)
+  // (the force on the fluid into F_F0..2 and a copy into F_GE0..2)
   void maxwell_stress(int rho_id) {
+    maxwell_face_force(rho_id);
+    interp_normal_to<R>(g, vec(F_WV3_0), vec(F_F0), vec(F_GE0), nullptr, R(0), s);
+  }
+  // the face force into F_WV3_0..2 (operate_dielectric.cxx:651-755)
+  void maxwell_face_force(int rho_id) {
     staggered_grad(F_EPS, F_GE0, F_WV1);
     staggered_grad(F_POT, F_F0, F_WV1);
     maxwell_e2<R>(g, f[F_F0], f[F_F1], f[F_F2], f[F_WV1], ext_now[0], ext_now[1], ext_now[2], P.external_field, s);
-    maxwell_face<R>(g, vec(F_F0), f[rho_id], f[F_WV1], vec(F_GE0), ext_now[0], ext_now[1], ext_now[2],
+    maxwell_face<R>(g, vec(F_F0), vec(F_WV3_0), f[rho_id], f[F_WV1], vec(F_GE0), ext_now[0], ext_now[1], ext_now[2],
                     P.external_field, s);
-    for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
-    interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);
-    for (int d = 0; d < 3; d++) copy(F_GE0 + d, F_F0 + d);
   }
 
   // NSsolute_solver_Euler (fluid_solver.cxx:318-338), Dielectric branch of
@@ -1521,21 +1534,17 @@ class Engine : public EngineBase {
     // staggered grad of the potential minus E_ext, interpolated to nodes
     copy(F_WV1, F_POT);
     r2c(f[F_WV1]);
-    grad_k<R>(g, f[F_WV1], f[F_F0], f[F_F1], f[F_F2], R(1), true, P.external_field ? e_ext_nh : nullptr, s);
-    c2r(f[F_F0], f[F_F1], f[F_F2]);
-    for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
+    grad_k<R>(g, f[F_WV1], f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], R(1), true, P.external_field ? e_ext_nh : nullptr, s);
+    c2r(f[F_WV3_0], f[F_WV3_1], f[F_WV3_2]);
     interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);
-    truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
-    zeta_k2u();
+    truncate_zeta_k2u();
     for (int d = 0; d < 3; d++) zero(F_SN0 + d);
     scatter_normal<R>(pp, dp, dsek, f[F_SN0], f[F_SN1], f[F_SN2], s);
     for (int n = 0; n < (salt_free ? 1 : 2); n++) {  // F_CRHS1 stays zero without a second species
-      truncate_23<R>(g, batch(f[F_C0 + n]), s);
-      // Diffusion_flux_single: grad(kBT L c)
-      grad_k<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], (R)(P.kbt * onsager[n]), false, nullptr, s);
-      c2r(f[F_UP0], f[F_UP1], f[F_UP2]);
-      copy(F_CRHS0 + n, F_C0 + n);
-      c2r(f[F_CRHS0 + n]);
+      // truncation, Diffusion_flux_single's grad(kBT L c) and the copy of c
+      // whose real values the electric and advective fluxes take, one pass
+      grad_trunc_copy<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n], (R)(P.kbt * onsager[n]), s);
+      c2r(f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n]);
       np_flux_electric<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_F0), onsager[n] * valency_e[n], s);
       np_impermeability<R>(g, vec(F_UP0), vec(F_SN0), s);
       np_flux_advection<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_U0), s);
@@ -1563,8 +1572,7 @@ class Engine : public EngineBase {
       for (int d = 0; d < 3; d++)  // FIX_CELL: time-dependent mean pressure gradient (sp_3d_ns.cxx:30-36)
         if ((P.fix_cell >> d) & 1) cudaMemsetAsync(ukdc + d, 0, sizeof(double), s);
       mark(1);
-      truncate_23<R>(g, batch(f[F_ZETA0], f[F_ZETA1]), s);
-      zeta_k2u();
+      truncate_zeta_k2u();
       if (!P.fixed_particle) md_position(pp, dp, ts != 0, s);
       make_phi_particle_sum();
       mark(2);
@@ -1591,9 +1599,10 @@ class Engine : public EngineBase {
     // the sequence after it
     st = run_segment(1, [&]() -> int {
       if (electrolyte) {
-        maxwell_stress(F_UP0);
+        maxwell_face_force(F_UP0);
         mark(5);
-        add_vec<R>(g, vec(F_U0), vec(F_F0), (R)(P.dt / P.rho), s);
+        // the force to nodes, kept in F_GE0..2 and added as u += dt/rho f
+        interp_normal_to<R>(g, vec(F_WV3_0), nullptr, vec(F_GE0), vec(F_U0), (R)(P.dt / P.rho), s);
         solenoidal_u(F_U0);
       } else {
         mark(5);
@@ -1607,10 +1616,8 @@ class Engine : public EngineBase {
       }
       mark(7);
       make_u_particle_sum();
-      f_particle_sole_and_add();
       mark(8);
-      r2c(f[F_U0], f[F_U1], f[F_U2]);
-      u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
+      f_particle_sole_add_to_zeta();
       return ICEP_OK;
     });
     if (st) return st;
@@ -1674,18 +1681,14 @@ class Engine : public EngineBase {
     for (int m = 1; m < 10000; m++) {
       copy(F_WV1, F_POT);
       r2c(f[F_WV1]);
-      grad_k<R>(g, f[F_WV1], f[F_F0], f[F_F1], f[F_F2], R(1), true, P.external_field ? e_ext_nh : nullptr, s);
-      c2r(f[F_F0], f[F_F1], f[F_F2]);
-      for (int d = 0; d < 3; d++) copy(F_WV3_0 + d, F_F0 + d);
+      grad_k<R>(g, f[F_WV1], f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], R(1), true, P.external_field ? e_ext_nh : nullptr, s);
+      c2r(f[F_WV3_0], f[F_WV3_1], f[F_WV3_2]);
       interp_normal<R>(g, vec(F_F0), vec(F_WV3_0), s);
       for (int d = 0; d < 3; d++) zero(F_SN0 + d);
       scatter_normal<R>(pp, dp, dsek, f[F_SN0], f[F_SN1], f[F_SN2], s);
       for (int n = 0; n < 2; n++) {
-        truncate_23<R>(g, batch(f[F_C0 + n]), s);
-        grad_k<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], (R)(P.kbt * onsager[n]), false, nullptr, s);
-        c2r(f[F_UP0], f[F_UP1], f[F_UP2]);
-        copy(F_CRHS0 + n, F_C0 + n);
-        c2r(f[F_CRHS0 + n]);
+        grad_trunc_copy<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n], (R)(P.kbt * onsager[n]), s);
+        c2r(f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n]);
         np_flux_electric<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_F0), onsager[n] * valency_e[n], s);
         np_impermeability<R>(g, vec(F_UP0), vec(F_SN0), s);
         r2c(f[F_UP0], f[F_UP1], f[F_UP2]);
@@ -1785,9 +1788,7 @@ class Engine : public EngineBase {
     make_phi_particle_sum();
     make_u_particle_sum();
     zeta_k2u();
-    f_particle_sole_and_add();
-    r2c(f[F_U0], f[F_U1], f[F_U2]);
-    u_k2zeta_k<R>(g, f[F_U0], f[F_U1], f[F_U2], f[F_ZETA0], f[F_ZETA1], ukdc, s);
+    f_particle_sole_add_to_zeta();
     cudaMemsetAsync(ukdc, 0, sizeof(double) * 3, s);
     if (electrolyte) {
       time = 0.0;  // Init_potential_dielectric runs at jikan.time = 0

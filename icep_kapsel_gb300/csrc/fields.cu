@@ -65,6 +65,12 @@ __device__ __forceinline__ float exp_t(float a) { return expf(a); }
 
 #define TID ((long)blockIdx.x * blockDim.x + threadIdx.x)
 
+// three component fields passed by value
+template <typename R>
+struct V3 {
+  R *p[3];
+};
+
 // ---------------------------------------------------------------- k-space
 template <typename R>
 __global__ void k_truncate(FieldBatch<R> fb, Grid g) {
@@ -76,16 +82,14 @@ __global__ void k_truncate(FieldBatch<R> fb, Grid g) {
   a[m.im + 1] = R(0);
 }
 
+// u(k) of one mode from its two stored vorticity components (a, b):
+// v[0..5] = u0 re, im, u1 re, im, u2 re, im
 template <typename R>
-__global__ void k_zeta_k2u_k(Grid g, const R *z0, const R *z1, const double *ukdc, R *u0, R *u1, R *u2) {
-  Mode m;
-  if (!mode_of(g, TID, m)) return;
+__device__ __forceinline__ void zeta_mode_to_u(const Grid &g, const Mode &m, R a_r, R a_i, R b_r, R b_i, R *v) {
   const int KX = kx_of(g, m.i), KY = ky_of(g, m.j);
   R kx = wave_of<R>(g, 0) * (R)KX, ky = wave_of<R>(g, 1) * (R)KY, kz = wave_of<R>(g, 2) * (R)m.kz;
   const R k2 = kx * kx + ky * ky + kz * kz;
   const R ik2 = (k2 > R(0)) ? R(1) / k2 : R(0);
-  const R a_r = z0[m.im], a_i = z0[m.im + 1];
-  const R b_r = z1[m.im], b_i = z1[m.im + 1];
   R wr0, wi0, wr1, wi1, wr2, wi2;
   if (KX != 0) {
     const R ikx = R(1) / kx;
@@ -104,14 +108,22 @@ __global__ void k_zeta_k2u_k(Grid g, const R *z0, const R *z1, const double *ukd
     wr2 = R(0); wi2 = R(0);
   }
   kx *= ik2; ky *= ik2; kz *= ik2;
-  R v0r = -(ky * wi2 - kz * wi1), v0i = (ky * wr2 - kz * wr1);
-  R v1r = -(kz * wi0 - kx * wi2), v1i = (kz * wr0 - kx * wr2);
-  R v2r = -(kx * wi1 - ky * wi0), v2i = (kx * wr1 - ky * wr0);
+  v[0] = -(ky * wi2 - kz * wi1); v[1] = (ky * wr2 - kz * wr1);
+  v[2] = -(kz * wi0 - kx * wi2); v[3] = (kz * wr0 - kx * wr2);
+  v[4] = -(kx * wi1 - ky * wi0); v[5] = (kx * wr1 - ky * wr0);
+}
+
+template <typename R>
+__global__ void k_zeta_k2u_k(Grid g, const R *z0, const R *z1, const double *ukdc, R *u0, R *u1, R *u2) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R v[6];
+  zeta_mode_to_u(g, m, z0[m.im], z0[m.im + 1], z1[m.im], z1[m.im + 1], v);
   // the k = 0 mode takes uk_dc (k_set_k0), written after this kernel so that
   // no warp issues the FP64 conversions under a predicate
-  u0[m.im] = v0r; u0[m.im + 1] = v0i;
-  u1[m.im] = v1r; u1[m.im + 1] = v1i;
-  u2[m.im] = v2r; u2[m.im + 1] = v2i;
+  u0[m.im] = v[0]; u0[m.im + 1] = v[1];
+  u1[m.im] = v[2]; u1[m.im + 1] = v[3];
+  u2[m.im] = v[4]; u2[m.im + 1] = v[5];
 }
 
 // u_d(k = 0) = uk_dc[d] (Zeta_k2u_k's mean flow, fft_wrapper.cxx:614-711)
@@ -122,15 +134,38 @@ __global__ void k_set_k0(R *u0, R *u1, R *u2, const double *ukdc) {
   u2[0] = (R)ukdc[2];
 }
 
+// Truncate_two_third_rule_k of the vorticity (in place) followed by
+// Zeta_k2u_k, in one pass: a mode outside the 2/3 cube is zeroed in zeta and
+// u; the k = 0 mode takes uk_dc
 template <typename R>
-__global__ void k_u_k2zeta_k(Grid g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *ukdc) {
+__global__ void k_zeta_k2u_trunc(Grid g, R *z0, R *z1, const double *ukdc, R *u0, R *u1, R *u2) {
   Mode m;
   if (!mode_of(g, TID, m)) return;
-  R k[3];
-  kvec(g, m, k);
-  const R a0r = u0[m.im], a0i = u0[m.im + 1];
-  const R a1r = u1[m.im], a1i = u1[m.im + 1];
-  const R a2r = u2[m.im], a2i = u2[m.im + 1];
+  R v[6];
+  if (!in_two_third(g, m.i, m.j, m.kz)) {
+    z0[m.im] = R(0); z0[m.im + 1] = R(0);
+    z1[m.im] = R(0); z1[m.im + 1] = R(0);
+#pragma unroll
+    for (int c = 0; c < 6; c++) v[c] = R(0);
+  } else {
+    zeta_mode_to_u(g, m, z0[m.im], z0[m.im + 1], z1[m.im], z1[m.im + 1], v);
+    if (m.im == 0) {
+      v[0] = (R)ukdc[0];
+      v[2] = (R)ukdc[1];
+      v[4] = (R)ukdc[2];
+    }
+  }
+  u0[m.im] = v[0]; u0[m.im + 1] = v[1];
+  u1[m.im] = v[2]; u1[m.im + 1] = v[3];
+  u2[m.im] = v[4]; u2[m.im + 1] = v[5];
+}
+
+template <typename R>
+__device__ __forceinline__ void u_mode_to_zeta(const Grid &g, const Mode &m, const R *k, const R *v, R *z0, R *z1,
+                                               double *ukdc) {
+  const R a0r = v[0], a0i = v[1];
+  const R a1r = v[2], a1i = v[3];
+  const R a2r = v[4], a2i = v[5];
   R wr[3], wi[3];
   wr[0] = -(k[1] * a2i - k[2] * a1i); wi[0] = (k[1] * a2r - k[2] * a1r);
   wr[1] = -(k[2] * a0i - k[0] * a2i); wi[1] = (k[2] * a0r - k[0] * a2r);
@@ -144,6 +179,56 @@ __global__ void k_u_k2zeta_k(Grid g, const R *u0, const R *u1, const R *u2, R *z
   if (m.im == 0) {
     ukdc[0] = a0r; ukdc[1] = a1r; ukdc[2] = a2r;
   }
+}
+
+template <typename R>
+__global__ void k_u_k2zeta_k(Grid g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *ukdc) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R k[3];
+  kvec(g, m, k);
+  const R v[6] = {u0[m.im], u0[m.im + 1], u1[m.im], u1[m.im + 1], u2[m.im], u2[m.im + 1]};
+  u_mode_to_zeta(g, m, k, v, z0, z1, ukdc);
+}
+
+// The end of the step in k-space, one pass: the particle force f (spectrum)
+// truncated to the 2/3 cube and made solenoidal (Make_f_particle_dt_sole,
+// f_particle.h:67-78, through Solenoidal_u, operate_omega.h:109-116) is added
+// to u (Add_f_particle, f_particle.h:79-95) and the sum becomes the vorticity
+// and mean flow (U2zeta_k, operate_omega.h:212-215).
+// u + f is added spectrally rather than in real space: the same sum, since
+// the truncated, projected f keeps the Hermitian symmetry of a real field and
+// has no Nyquist modes. u keeps the spectrum of the sum, as after U2zeta_k.
+template <typename R>
+__global__ void k_sole_add_zeta(Grid g, V3<R> f, V3<R> u, R *z0, R *z1, double *ukdc) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R k[3];
+  kvec(g, m, k);
+  R v[6];
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    v[2 * c] = u.p[c][m.im];
+    v[2 * c + 1] = u.p[c][m.im + 1];
+  }
+  if (in_two_third(g, m.i, m.j, m.kz)) {
+    const R k2 = k2_of(k);
+    const R ik2 = (k2 > R(0)) ? R(1) / k2 : R(0);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const R a = f.p[0][m.im + h], b = f.p[1][m.im + h], d = f.p[2][m.im + h];
+      const R r = ik2 * (a * k[0] + b * k[1] + d * k[2]);
+      v[h] += a - r * k[0];
+      v[2 + h] += b - r * k[1];
+      v[4 + h] += d - r * k[2];
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    u.p[c][m.im] = v[2 * c];
+    u.p[c][m.im + 1] = v[2 * c + 1];
+  }
+  u_mode_to_zeta(g, m, k, v, z0, z1, ukdc);
 }
 
 template <typename R>
@@ -194,10 +279,18 @@ __global__ void k_ns_slaved(Grid g, R *z0, R *z1, const R *a0, const R *a1, R mn
   }
 }
 
+// Truncate_two_third_rule of each component then Solenoidal_uk, the k-space
+// part of Solenoidal_u (operate_omega.h:109-116), in one pass
 template <typename R>
 __global__ void k_solenoidal(Grid g, R *u0, R *u1, R *u2) {
   Mode m;
   if (!mode_of(g, TID, m)) return;
+  if (!in_two_third(g, m.i, m.j, m.kz)) {
+    u0[m.im] = R(0); u0[m.im + 1] = R(0);
+    u1[m.im] = R(0); u1[m.im + 1] = R(0);
+    u2[m.im] = R(0); u2[m.im + 1] = R(0);
+    return;
+  }
   R k[3];
   kvec(g, m, k);
   const R k2 = k2_of(k);
@@ -235,6 +328,38 @@ __global__ void k_grad(Grid g, const R *a, R *d0, R *d1, R *d2, R scale, int shi
     if (ext && m.im == 0) gr -= (c == 0) ? ex0 : (c == 1) ? ex1 : ex2;
     d[c][m.im] = gr;
     d[c][m.im + 1] = gi;
+  }
+}
+
+// Truncate_two_third_rule of a concentration spectrum (in place), its
+// unshifted gradient scale i k a and a copy of the truncated spectrum, in one
+// pass (the start of each species' flux in Rhs_NS_Nernst_Planck,
+// fluid_solver.cxx:246-292)
+template <typename R>
+__global__ void k_grad_trunc_copy(Grid g, R *a, R *d0, R *d1, R *d2, R *cp, R scale) {
+  Mode m;
+  if (!mode_of(g, TID, m)) return;
+  R *d[3] = {d0, d1, d2};
+  if (!in_two_third(g, m.i, m.j, m.kz)) {
+    a[m.im] = R(0); a[m.im + 1] = R(0);
+    cp[m.im] = R(0); cp[m.im + 1] = R(0);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      d[c][m.im] = R(0);
+      d[c][m.im + 1] = R(0);
+    }
+    return;
+  }
+  const R ar = a[m.im], ai = a[m.im + 1];
+  cp[m.im] = ar;
+  cp[m.im + 1] = ai;
+  R k[3];
+  kvec(g, m, k);
+  const R re = scale * ar, im = scale * ai;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    d[c][m.im] = -k[c] * im;
+    d[c][m.im + 1] = k[c] * re;
   }
 }
 
@@ -334,25 +459,12 @@ __global__ void k_phi_clip(Grid g, const R *phs, R *phi) {
 }
 
 template <typename R>
-struct V3 {
-  R *p[3];
-};
-
-template <typename R>
 __global__ void k_f_nonsole(Grid g, V3<R> f, V3<R> up, const R *phi, V3<R> u) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
   const R ph = phi[p.im];
 #pragma unroll
   for (int d = 0; d < 3; d++) f.p[d][p.im] = up.p[d][p.im] - ph * u.p[d][p.im];
-}
-
-template <typename R>
-__global__ void k_add_vec(Grid g, V3<R> u, V3<R> f, R a) {
-  Pt p;
-  if (!pt_of(g, TID, p)) return;
-#pragma unroll
-  for (int d = 0; d < 3; d++) u.p[d][p.im] += f.p[d][p.im] * a;
 }
 
 template <typename R>
@@ -418,13 +530,22 @@ __global__ void k_axpby_real(Grid g, const R *x, R *y, R a, R b) {
   y[p.im] = a * x[p.im] + b * y[p.im];
 }
 
+// face values to nodes; the result goes to out and, where given, to out2,
+// and acc += a * result where acc is given (null pointers skip a target)
 template <typename R>
-__global__ void k_interp_normal(Grid g, V3<R> out, V3<R> in) {
+__global__ void k_interp_normal(Grid g, V3<R> out, V3<R> in, V3<R> out2, V3<R> acc, R a) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
-  out.p[0][p.im] = R(0.5) * in.p[0][p.im] + R(0.5) * in.p[0][wrapi(g, p.i - 1, p.j, p.k)];
-  out.p[1][p.im] = R(0.5) * in.p[1][p.im] + R(0.5) * in.p[1][wrapi(g, p.i, p.j - 1, p.k)];
-  out.p[2][p.im] = R(0.5) * in.p[2][p.im] + R(0.5) * in.p[2][wrapi(g, p.i, p.j, p.k - 1)];
+  R t[3];
+  t[0] = R(0.5) * in.p[0][p.im] + R(0.5) * in.p[0][wrapi(g, p.i - 1, p.j, p.k)];
+  t[1] = R(0.5) * in.p[1][p.im] + R(0.5) * in.p[1][wrapi(g, p.i, p.j - 1, p.k)];
+  t[2] = R(0.5) * in.p[2][p.im] + R(0.5) * in.p[2][wrapi(g, p.i, p.j, p.k - 1)];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (out.p[0]) out.p[d][p.im] = t[d];
+    if (out2.p[0]) out2.p[d][p.im] = t[d];
+    if (acc.p[0]) acc.p[d][p.im] += t[d] * a;
+  }
 }
 
 template <typename R>
@@ -444,18 +565,19 @@ __global__ void k_maxwell_e2(Grid g, const R *f0, const R *f1, const R *f2, R *w
 }
 
 template <typename R>
-__global__ void k_maxwell_face(Grid g, V3<R> force, const R *rho, const R *w1, V3<R> ge, R e0, R e1, R e2, int ext) {
+__global__ void k_maxwell_face(Grid g, V3<R> grad_pot, V3<R> out, const R *rho, const R *w1, V3<R> ge, R e0, R e1, R e2,
+                               int ext) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
   const R E[3] = {e0, e1, e2};
 #pragma unroll
   for (int d = 0; d < 3; d++) {
     const long ip = wrapi(g, p.i + (d == 0), p.j + (d == 1), p.k + (d == 2));
-    R efw = -force.p[d][p.im];
+    R efw = -grad_pot.p[d][p.im];
     if (ext) efw += E[d];
     const R rf = R(0.5) * rho[ip] + R(0.5) * rho[p.im];
     const R e2v = R(0.5) * w1[p.im] + R(0.5) * w1[ip];
-    force.p[d][p.im] = rf * efw - e2v * ge.p[d][p.im] / R(2);
+    out.p[d][p.im] = rf * efw - e2v * ge.p[d][p.im] / R(2);
   }
 }
 
@@ -520,9 +642,17 @@ template <typename R> void zeta_k2u_k(const Grid &g, const R *z0, const R *z1, c
   count_launch();
   k_set_k0<R><<<1, 1, 0, s>>>(u0, u1, u2, uk_dc);
 }
+template <typename R> void zeta_k2u_trunc(const Grid &g, R *z0, R *z1, const double *uk_dc, R *u0, R *u1, R *u2, cudaStream_t s) {
+  count_launch(fld<R>(g, 7));
+  k_zeta_k2u_trunc<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, uk_dc, u0, u1, u2);
+}
 template <typename R> void u_k2zeta_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *uk_dc, cudaStream_t s) {
   count_launch(fld<R>(g, 5));
   k_u_k2zeta_k<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2, z0, z1, uk_dc);
+}
+template <typename R> void sole_add_zeta(const Grid &g, R *const *f, R *const *u, R *z0, R *z1, double *uk_dc, cudaStream_t s) {
+  count_launch(fld<R>(g, 11));
+  k_sole_add_zeta<R><<<nblk_modes(g), TPB, 0, s>>>(g, v3(f), v3(u), z0, z1, uk_dc);
 }
 template <typename R> void advection_combine(const Grid &g, R *u0, R *u1, R *u2, R *a0, R *a1, cudaStream_t s) {
   count_launch(fld<R>(g, 7));
@@ -532,7 +662,7 @@ template <typename R> void ns_slaved_update(const Grid &g, R *z0, R *z1, const R
   count_launch(fld<R>(g, 6));
   k_ns_slaved<R><<<nblk_modes(g), TPB, 0, s>>>(g, z0, z1, a0, a1, (R)(-nu * dt), (R)(1. / nu));
 }
-template <typename R> void solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s) {
+template <typename R> void truncate_solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s) {
   count_launch(fld<R>(g, 6));
   k_solenoidal<R><<<nblk_modes(g), TPB, 0, s>>>(g, u0, u1, u2);
 }
@@ -541,6 +671,10 @@ template <typename R> void grad_k(const Grid &g, const R *a, R *d0, R *d1, R *d2
   const R ex0 = ext ? (R)e_ext_n[0] : R(0), ex1 = ext ? (R)e_ext_n[1] : R(0), ex2 = ext ? (R)e_ext_n[2] : R(0);
   count_launch(fld<R>(g, 4));
   k_grad<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, d0, d1, d2, scale, shift ? 1 : 0, ext, ex0, ex1, ex2);
+}
+template <typename R> void grad_trunc_copy(const Grid &g, R *a, R *d0, R *d1, R *d2, R *cp, R scale, cudaStream_t s) {
+  count_launch(fld<R>(g, 6));
+  k_grad_trunc_copy<R><<<nblk_modes(g), TPB, 0, s>>>(g, a, d0, d1, d2, cp, scale);
 }
 template <typename R> void div_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *div, bool shift, cudaStream_t s) {
   count_launch(fld<R>(g, 4));
@@ -569,10 +703,6 @@ template <typename R> void phi_clip(const Grid &g, const R *phs, R *phi, cudaStr
 template <typename R> void f_nonsole(const Grid &g, R *const *f, R *const *up, const R *phi, R *const *u, cudaStream_t s) {
   count_launch(fld<R>(g, 10));
   k_f_nonsole<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(f), v3(up), phi, v3(u));
-}
-template <typename R> void add_vec(const Grid &g, R *const *u, R *const *f, R a, cudaStream_t s) {
-  count_launch(fld<R>(g, 9));
-  k_add_vec<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(u), v3(f), a);
 }
 template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_sin, const R *eps_w, double ef, double ep, double dc, cudaStream_t s) {
   count_launch(fld<R>(g, 3));
@@ -605,15 +735,21 @@ template <typename R> void axpby_real(const Grid &g, const R *x, R *y, R a, R b,
 }
 template <typename R> void interp_normal(const Grid &g, R *const *out, R *const *in, cudaStream_t s) {
   count_launch(fld<R>(g, 6));
-  k_interp_normal<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(out), v3(in));
+  k_interp_normal<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(out), v3(in), V3<R>{}, V3<R>{}, R(0));
+}
+template <typename R> void interp_normal_to(const Grid &g, R *const *in, R *const *out, R *const *out2, R *const *acc, R a, cudaStream_t s) {
+  const V3<R> none{};
+  count_launch(fld<R>(g, 3.0 + (out ? 3 : 0) + (out2 ? 3 : 0) + (acc ? 6 : 0)));
+  k_interp_normal<R><<<nblk_real(g), TPB, 0, s>>>(g, out ? v3(out) : none, v3(in), out2 ? v3(out2) : none,
+                                                   acc ? v3(acc) : none, a);
 }
 template <typename R> void maxwell_e2(const Grid &g, const R *f0, const R *f1, const R *f2, R *w1, double e0, double e1, double e2, int ext, cudaStream_t s) {
   count_launch(fld<R>(g, 4));
   k_maxwell_e2<R><<<nblk_real(g), TPB, 0, s>>>(g, f0, f1, f2, w1, (R)e0, (R)e1, (R)e2, ext);
 }
-template <typename R> void maxwell_face(const Grid &g, R *const *force, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s) {
+template <typename R> void maxwell_face(const Grid &g, R *const *grad_pot, R *const *out, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s) {
   count_launch(fld<R>(g, 11));
-  k_maxwell_face<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(force), rho, w1, v3(ge), (R)e0, (R)e1, (R)e2, ext);
+  k_maxwell_face<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(grad_pot), v3(out), rho, w1, v3(ge), (R)e0, (R)e1, (R)e2, ext);
 }
 template <typename R> void np_flux_electric(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, cudaStream_t s) {
   count_launch(fld<R>(g, 7));
@@ -659,9 +795,13 @@ void pb_energy_terms(const Grid &g, const R *c0, const R *c1, const R *phi, R *c
   template void truncate_23<R>(const Grid &, const FieldBatch<R> &, cudaStream_t);                                    \
   template void zeta_k2u_k<R>(const Grid &, const R *, const R *, const double *, R *, R *, R *, cudaStream_t);        \
   template void u_k2zeta_k<R>(const Grid &, const R *, const R *, const R *, R *, R *, double *, cudaStream_t);        \
+  template void zeta_k2u_trunc<R>(const Grid &, R *, R *, const double *, R *, R *, R *, cudaStream_t);                \
+  template void sole_add_zeta<R>(const Grid &, R *const *, R *const *, R *, R *, double *, cudaStream_t);              \
+  template void grad_trunc_copy<R>(const Grid &, R *, R *, R *, R *, R *, R, cudaStream_t);                            \
+  template void interp_normal_to<R>(const Grid &, R *const *, R *const *, R *const *, R *const *, R, cudaStream_t);   \
   template void advection_combine<R>(const Grid &, R *, R *, R *, R *, R *, cudaStream_t);                             \
   template void ns_slaved_update<R>(const Grid &, R *, R *, const R *, const R *, double, double, cudaStream_t);       \
-  template void solenoidal_uk<R>(const Grid &, R *, R *, R *, cudaStream_t);                                           \
+  template void truncate_solenoidal_uk<R>(const Grid &, R *, R *, R *, cudaStream_t);                                  \
   template void grad_k<R>(const Grid &, const R *, R *, R *, R *, R, bool, const double *, cudaStream_t);              \
   template void div_k<R>(const Grid &, const R *, const R *, const R *, R *, bool, cudaStream_t);                      \
   template void euler_update<R>(const Grid &, R *, R *, R *, R *, R *, R *, const R *, const R *, double, double,      \
@@ -671,7 +811,6 @@ void pb_energy_terms(const Grid &g, const R *c0, const R *c1, const R *phi, R *c
   template void advection_products<R>(const Grid &, R *, R *, R *, R *, R *, cudaStream_t);                            \
   template void phi_clip<R>(const Grid &, const R *, R *, cudaStream_t);                                               \
   template void f_nonsole<R>(const Grid &, R *const *, R *const *, const R *, R *const *, cudaStream_t);               \
-  template void add_vec<R>(const Grid &, R *const *, R *const *, R, cudaStream_t);                                     \
   template void eps_from_profile<R>(const Grid &, R *, const R *, const R *, double, double, double, cudaStream_t);    \
   template void eps_janus<R>(const Grid &, R *, const R *, const R *, double, double, cudaStream_t);                   \
   template void charge_add<R>(const Grid &, R *, const R *, const R *, double, bool, cudaStream_t);                    \
@@ -682,7 +821,8 @@ void pb_energy_terms(const Grid &g, const R *c0, const R *c1, const R *phi, R *c
   template void interp_normal<R>(const Grid &, R *const *, R *const *, cudaStream_t);                                  \
   template void maxwell_e2<R>(const Grid &, const R *, const R *, const R *, R *, double, double, double, int,         \
                               cudaStream_t);                                                                           \
-  template void maxwell_face<R>(const Grid &, R *const *, const R *, const R *, R *const *, double, double, double,    \
+  template void maxwell_face<R>(const Grid &, R *const *, R *const *, const R *, const R *, R *const *, double, double, \
+                                double,                                                                                \
                                 int, cudaStream_t);                                                                    \
   template void np_flux_electric<R>(const Grid &, R *const *, const R *, R *const *, double, cudaStream_t);            \
   template void np_impermeability<R>(const Grid &, R *const *, R *const *, cudaStream_t);                              \

@@ -10,19 +10,31 @@ namespace icep {
 template <typename R> void truncate_23(const Grid &g, const FieldBatch<R> &fb, cudaStream_t s);
 // Zeta_k2u_k (fft_wrapper.cxx:614-711); uk_dc: device double[3]
 template <typename R> void zeta_k2u_k(const Grid &g, const R *z0, const R *z1, const double *uk_dc, R *u0, R *u1, R *u2, cudaStream_t s);
+// Truncate_two_third_rule of zeta (in place) then Zeta_k2u_k, one pass
+template <typename R> void zeta_k2u_trunc(const Grid &g, R *z0, R *z1, const double *uk_dc, R *u0, R *u1, R *u2, cudaStream_t s);
 // U_k2zeta_k (fft_wrapper.cxx:428-497); writes uk_dc (device double[3])
 template <typename R> void u_k2zeta_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *z0, R *z1, double *uk_dc, cudaStream_t s);
+// The end of the step on spectra, one pass: u += P T f with T the 2/3
+// truncation and P the solenoidal projection (the k-space part of
+// Make_f_particle_dt_sole and Add_f_particle, f_particle.h:67-95), then
+// U_k2zeta_k of the sum; f and u are spectra, u keeps the sum's spectrum
+template <typename R> void sole_add_zeta(const Grid &g, R *const *f, R *const *u, R *z0, R *z1, double *uk_dc, cudaStream_t s);
 // k-space half of U2advection_k (operate_omega.cxx:61-96) + Omega_k2zeta_k (fft_wrapper.cxx:248-284)
 template <typename R> void advection_combine(const Grid &g, R *u0, R *u1, R *u2, R *a0, R *a1, cudaStream_t s);
 // NS_solver_slavedEuler update (fluid_solver.cxx:345-365)
 template <typename R> void ns_slaved_update(const Grid &g, R *z0, R *z1, const R *a0, const R *a1, double nu, double dt, cudaStream_t s);
-// Solenoidal_uk (operate_omega.cxx:187-220)
-template <typename R> void solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s);
+// Truncate_two_third_rule of each component then Solenoidal_uk
+// (operate_omega.cxx:187-220): the k-space part of Solenoidal_u
+// (operate_omega.h:109-116), one pass
+template <typename R> void truncate_solenoidal_uk(const Grid &g, R *u0, R *u1, R *u2, cudaStream_t s);
 // A_k2da_k (fft_wrapper.cxx:214-237), optionally * Shift (Shift_vec_fw_imag,
 // fft_wrapper.h:841-858), optionally minus e_ext*N at k = 0
 // (Add_constant_field_k, fluid_solver.cxx:231-244; e_ext_n: a HOST array of
 // the three values, or null); a may alias nothing.
 template <typename R> void grad_k(const Grid &g, const R *a, R *d0, R *d1, R *d2, R scale, bool shift, const double *e_ext_n, cudaStream_t s);
+// Truncate_two_third_rule of a (in place), d = scale i k a (unshifted) and
+// cp = a, one pass (each species' diffusion flux, fluid_solver.cxx:246-292)
+template <typename R> void grad_trunc_copy(const Grid &g, R *a, R *d0, R *d1, R *d2, R *cp, R scale, cudaStream_t s);
 // U_k2divergence_k (fft_wrapper.cxx:896-920) / U_k2divergence_k_shift (fft_wrapper.h:879-900)
 template <typename R> void div_k(const Grid &g, const R *u0, const R *u1, const R *u2, R *div, bool shift, cudaStream_t s);
 // Add_zeta_viscous_term + Field_solver_Euler over the 2/3 region
@@ -41,8 +53,6 @@ template <typename R> void advection_products(const Grid &g, R *u0, R *u1, R *u2
 template <typename R> void phi_clip(const Grid &g, const R *phs, R *phi, cudaStream_t s);
 // f = up - phi u (Make_f_particle_dt_nonsole, f_particle.h:37-60)
 template <typename R> void f_nonsole(const Grid &g, R *const *f, R *const *up, const R *phi, R *const *u, cudaStream_t s);
-// u += a f (Add_f_particle, f_particle.h:79-95; sp_3d_ns.cxx:83-94)
-template <typename R> void add_vec(const Grid &g, R *const *u, R *const *f, R a, cudaStream_t s);
 // eps = ef*dc + (ep - ef)*dc*phi_sin, or eps = ef*dc + dc*eps_w (per particle)
 // (Make_dielectric_field, operate_dielectric.cxx:298-307)
 template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_sin, const R *eps_w, double ef, double ep, double dc, cudaStream_t s);
@@ -62,9 +72,15 @@ template <typename R> void eps_face_E(const Grid &g, R *w0, R *w1, R *w2, const 
 template <typename R> void axpby_real(const Grid &g, const R *x, R *y, R a, R b, cudaStream_t s);
 // out_d(i) = 0.5 in_d(i) + 0.5 in_d(i - e_d) (Interpolate_vec_on_normal_grid, operate_dielectric.cxx:32-55)
 template <typename R> void interp_normal(const Grid &g, R *const *out, R *const *in, cudaStream_t s);
+// the same interpolation of in, written to out and out2 and added as
+// acc += a * result (null targets skipped): the Maxwell force's copies and
+// its Euler step u += dt/rho f (sp_3d_ns.cxx:83-94) in one pass
+template <typename R> void interp_normal_to(const Grid &g, R *const *in, R *const *out, R *const *out2, R *const *acc, R a, cudaStream_t s);
 // Maxwell stress terms (operate_dielectric.cxx:670-762)
 template <typename R> void maxwell_e2(const Grid &g, const R *f0, const R *f1, const R *f2, R *w1, double e0, double e1, double e2, int ext, cudaStream_t s);
-template <typename R> void maxwell_face(const Grid &g, R *const *force, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s);
+// out = face force from the staggered potential gradient grad_pot, the face
+// charge and |E|^2 and the staggered permittivity gradient ge
+template <typename R> void maxwell_face(const Grid &g, R *const *grad_pot, R *const *out, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s);
 // Nernst-Planck fluxes (solute_rhs.cxx:150-210, 42-97)
 template <typename R> void np_flux_electric(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, cudaStream_t s);
 template <typename R> void np_impermeability(const Grid &g, R *const *flux, R *const *sn, cudaStream_t s);

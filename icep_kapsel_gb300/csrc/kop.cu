@@ -817,16 +817,10 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
   load_table(tws, twx, N);
   pencil_coords<KWT>(g, q0, pj, pkz);
   __syncthreads();
-  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w0)), (long)q0, 1, (long)nq, nvalid},
-                          DivAcc<0>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
-  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w1)), (long)q0, 1, (long)nq, nvalid},
-                          DivAcc<1>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
-  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w2)), (long)q0, 1, (long)nq, nvalid},
-                          DivAcc<2>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
   float s0 = 0.f, s1 = 0.f;  // the thread's few terms in FP32; blocks and their sum in FP64
   static_assert(N / 8 <= 512 / KWT, "xblock(N) = KWT x N/8 threads");
   constexpr int XPT = 8;
-  cf lo[XPT];  // the dot operands, all loads in flight before use
+  cf lo[XPT];  // the dot operands: loaded first, in flight during the transforms
 #pragma unroll
   for (int u = 0; u < XPT; u++) {
     const int it = lin + u * nthr;
@@ -835,6 +829,12 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
     if (mode == KOP_NONE || w >= nvalid) continue;
     lo[u] = ldw(other, (long)e * nq + q0 + w, read_weight(g, e, pj[w], pkz[w]));
   }
+  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w0)), (long)q0, 1, (long)nq, nvalid},
+                          DivAcc<0>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
+  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w1)), (long)q0, 1, (long)nq, nvalid},
+                          DivAcc<1>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
+  block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w2)), (long)q0, 1, (long)nq, nvalid},
+                          DivAcc<2>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
 #pragma unroll
   for (int u = 0; u < XPT; u++) {
     const int it = lin + u * nthr;

@@ -294,7 +294,7 @@ int icep_batch_step(icep_batch *batch, int nsteps);
  * |r - A P(r)|^2 / |r|^2 with P(r) = M^-1 (r + rms(r) prolong(net(eps, r))).
  * The context's particles and field are restored afterwards. The trained
  * parameters are kept only if they lower the one-step loss on the context's
- * own residuals (icep_learned_eval with chain 2, configurations not trained
+ * own residuals (icep_learned_eval with chain 4, configurations not trained
  * on) below the spectral preconditioner's; otherwise the earlier parameters
  * come back and the network is not applied until icep_learned_enable(ctx, 1)
  * or a later training that is kept. */
@@ -337,8 +337,9 @@ int icep_step_timed(icep_ctx *ctx, int nsteps, double *ms);
  * phase boundaries): 0 fluid/solute update, 1 velocity + particle positions
  * + profile, 2 hydrodynamic force + permittivity + free charge, 3 Poisson
  * solve, 4 Maxwell stress, 5 Maxwell force on the fluid + projection,
- * 6 particle forces and velocities, 7 rigidity force, 8 back to vorticity,
- * 9 unused. Returns ICEP_ERR_STATE when profiling is off. */
+ * 6 particle forces and velocities, 7 particle velocity field, 8 rigidity
+ * force and back to vorticity, 9 unused. Returns ICEP_ERR_STATE when
+ * profiling is off. */
 int icep_phase_times(icep_ctx *ctx, double *ms, int n);
 /* The tile autotuner of the fused Poisson passes (no counterpart in the
  * reference): at context creation (MIXED electrolyte on a mesh the fused

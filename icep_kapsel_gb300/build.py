@@ -20,7 +20,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libicep_gb300.so")
 BIN = os.path.join(HERE, "icep_kapsel")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["fft_df.cu", "fft.cu", "fields.cu", "particles.cu", "krylov.cu", "kspace.cu", "kop.cu", "unet.cu", "engine.cu", "icep_abi.cu", "lj_noalloc.cu", "probe.cu", "refine.cu", "udf.cu", "avs.cpp"]
+SOURCES = ["fft_df.cu", "fft.cu", "fields.cu", "particles.cu", "krylov.cu", "kspace.cu", "kop.cu", "unet.cu", "engine.cu", "icep_abi.cu", "lj_noalloc.cu", "probe.cu", "refine.cu", "solve_graph.cu", "udf.cu", "avs.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

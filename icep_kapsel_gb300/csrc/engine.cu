@@ -20,6 +20,7 @@
 #include "probe.cuh"
 #include "kspace.cuh"
 #include "refine.cuh"
+#include "solve_graph.cuh"
 #include "unet.cuh"
 #include <type_traits>
 
@@ -56,6 +57,7 @@ class Engine : public EngineBase {
   // E_ext at the current time (times sin(2 pi f t) for an AC field) and the
   // same times NX*NY*NZ (the k = 0 term of Add_constant_field_k)
   double ext_now[3] = {0, 0, 0}, e_ext_nh[3] = {0, 0, 0};
+  void refresh_field() override { refresh_ext(); }
   void refresh_ext() {
     const double f = P.ac ? sin(2.0 * M_PI * P.frequency * time) : 1.0;
     const double amp = (double)P.nx * P.ny * P.nz * f;
@@ -172,10 +174,206 @@ class Engine : public EngineBase {
     return ICEP_OK;
   }
 
+  // ---- the whole step as one CUDA graph -------------------------------
+  // With the MIXED fused solver the solve's loops run on the device
+  // (solve_graph.cuh): the step -- the two fixed sequences, the solve with
+  // its sweep and iteration loops as conditional WHILE nodes, and a copy of
+  // the solve's status to pinned host memory -- is captured once and
+  // replayed as one launch, and the host waits once per step. Used where the
+  // segment graphs are (use_graphs), for an electrolyte on the fused passes
+  // once the potential's float-float history is in place (from the second
+  // step after init_state, or after a change of the potential), without the
+  // learned preconditioner or a kernel probe; otherwise, and after any
+  // capture failure, the step runs as before.
+  double *sc = nullptr;         // SC_COUNT doubles, then SCF_COUNT floats (solve_graph.cuh)
+  float *scf = nullptr;
+  double *hstat = nullptr;      // pinned: sc, then kfin's 7 + KS_COUNT doubles
+  cudaGraphExec_t step_exec = nullptr;
+  bool step_graph_failed = false;
+  // kernel launches and algorithmic bytes of the captured step: outside the
+  // loops, per sweep body (outside the inner loop), per inner iteration
+  unsigned long long sg_l[3] = {0, 0, 0}, sg_b[3] = {0, 0, 0};
+  static unsigned long long launches_now() { return __atomic_load_n(&g_kernel_launches, __ATOMIC_RELAXED); }
+  static unsigned long long bytes_now() { return __atomic_load_n(&g_alg_bytes, __ATOMIC_RELAXED); }
+
+  bool whole_step_ok() const override {
+    return use_graphs && ts != 0 && mixed && electrolyte && kpart && sc && !learned && x64_valid && xp_valid &&
+           g_probe_kind == PROBE_NONE && !step_graph_failed;
+  }
+
+  // Appends this context's step to graph gr after the nodes deps (deps
+  // receives the step's last nodes). Nothing captured runs: the kernel
+  // counters and the host-side counts are restored, and come with each
+  // replay (step_graph_done).
+  int capture_step(cudaGraph_t gr, std::vector<cudaGraphNode_t> &deps) override {
+    if constexpr (!std::is_same<R, float>::value) {
+      return ICEP_ERR_UNSUPPORTED;
+    } else {
+      const long nf = g.nf();
+      const double eps2 = DBL_EPSILON * DBL_EPSILON, nreal = (double)g.nreal(), tol = P.potential_tol;
+      const int maxit = P.potential_iter;
+      const long mv0 = matvecs;
+      float *r = f[F_KR], *r0 = f[F_KR0], *p = f[F_KP], *v = f[F_KV];
+      const float *prescale = scf + SCF_PRESCALE;
+      cudaGraphConditionalHandle hs = 0, hi = 0;
+      cudaGraphNode_t ns = nullptr, ni = nullptr;
+      cudaGraph_t bs = nullptr, bi = nullptr;
+      std::vector<cudaGraphNode_t> sdeps, ideps;
+      int st = ICEP_OK;
+      cudaError_t e = cudaSuccess;
+      unsigned long long cl[3] = {0, 0, 0}, cb[3] = {0, 0, 0};
+      // one stream capture appended to `into` after `after` (leaf back in after)
+      auto seg = [&](int part, cudaGraph_t into, std::vector<cudaGraphNode_t> &after, auto body) {
+        if (e != cudaSuccess || st != ICEP_OK) return;
+        const unsigned long long l0 = launches_now(), b0 = bytes_now();
+        e = cap_begin(s, into, after);
+        if (e != cudaSuccess) return;
+        st = body();
+        const cudaError_t e2 = cap_end(s, after);
+        if (e == cudaSuccess) e = e2;
+        cl[part] += launches_now() - l0;
+        cb[part] += bytes_now() - b0;
+      };
+      const bool use[3] = {ext_now[0] != 0.0, ext_now[1] != 0.0, ext_now[2] != 0.0};
+      e = cudaGraphConditionalHandleCreate(&hs, gr, 0, cudaGraphCondAssignDefault);
+      // the sequence before the solve, the right-hand side, the first true
+      // residual and the sweep loop's first decision
+      seg(0, gr, deps, [&]() -> int {
+        int q = pre_solve();
+        if (q) return q;
+        rf_extrapolate_shift(nf, df(D_X), df(D_XP), s);
+        dfl *w[3] = {df(D_W3_0), df(D_W3_1), df(D_W3_2)};
+        rf_eps_face_e(g, w[0], w[1], w[2], (const float *)f[F_EPS], ext_now, use, s);
+        FieldBatch<dfl> nz{};
+        for (int d = 0; d < 3; d++)
+          if (use[d]) nz.p[nz.n++] = w[d];
+        if (nz.n) fft_r2c(fftdf, nz, s);
+        rf_from_f32(nf, (const float *)f[F_UP0], df(D_R), s);
+        fft_r2c(fftdf, batch(df(D_R)), s);
+        rf_div_combine(g, rtab, df(D_W3_0), df(D_W3_1), df(D_W3_2), use, df(D_R), df(D_B), RF_RHS, 1.f, true,
+                       partials, scal, S_BB, s);
+        sum_real<R>(g, f[F_EPS], partials, scal, S_AUX1, s);
+        solve_begin(scal, S_BB, S_AUX1, sc, scf, kst, tol, nreal, s);
+        kop_eps_faces(g, f[F_EPS], f[F_EF0], f[F_EF1], f[F_EF2], s);
+        residual_df(1.f, prescale);
+        sweep_cond(hs, scal, S_RR, sc, scf, kst, tol, nreal, 30, false, s);
+        return ICEP_OK;
+      });
+      if (e == cudaSuccess && st == ICEP_OK) e = add_while(gr, deps, hs, &ns, &bs);
+      if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&hi, bs, 0, cudaGraphCondAssignDefault);
+      // a sweep: the FP32 correction problem on the normalised residual
+      seg(1, bs, sdeps, [&]() -> int {
+        rf_to_f32(nf, df(D_R), r, scf + SCF_INVRN, s);
+        cudaMemsetAsync(r, 0, 2 * sizeof(R), s);  // k = 0: the mean
+        cudaMemcpyAsync(r0, r, sizeof(R) * nf, cudaMemcpyDeviceToDevice, s);
+        kdots<R>(g, r, r, r, r, 1, partials, scal, S_RR, s);
+        zero(F_KY);
+        zero(F_KV);
+        zero(F_KP);
+        inner_prep(hi, scal, S_RR, sc, kst, eps2, s);
+        return ICEP_OK;
+      });
+      if (e == cudaSuccess && st == ICEP_OK) e = add_while(bs, sdeps, hi, &ni, &bi);
+      sdeps.assign(1, ni);
+      seg(2, bi, ideps, [&]() -> int {
+        kf_iteration(1.0, maxit);
+        inner_cond(hi, kst, r, r0, v, p, nf, maxit, sc, eps2, s);
+        return ICEP_OK;
+      });
+      // the correction added, the next true residual and decision
+      seg(1, bs, sdeps, [&]() -> int {
+        kprecond<R>(g, f[F_KY], f[F_KX], kst + KS_IEPS, s);
+        rf_add_f32(nf, f[F_KX], df(D_X), reinterpret_cast<const float2 *>(scf + SCF_RN), s);
+        residual_df(1.f, prescale);
+        sweep_cond(hs, scal, S_RR, sc, scf, kst, tol, nreal, 30, true, s);
+        return ICEP_OK;
+      });
+      deps.assign(1, ns);
+      // the potential, the sequence after the solve, the status to the host
+      seg(0, gr, deps, [&]() -> int {
+        rf_zero_if(nf, df(D_X), sc + SC_ZERO_RHS, s);
+        rf_to_f32(nf, df(D_X), (float *)f[F_POT], 1.0, s);
+        c2r(f[F_POT]);
+        const int q = post_solve();
+        if (q) return q;
+        cudaMemcpyAsync(hstat, sc, sizeof(double) * SC_COUNT, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hstat + SC_COUNT, kfin, sizeof(double) * (7 + KS_COUNT), cudaMemcpyDeviceToHost, s);
+        return ICEP_OK;
+      });
+      matvecs = mv0;
+      __atomic_fetch_sub(&g_kernel_launches, cl[0] + cl[1] + cl[2], __ATOMIC_RELAXED);
+      __atomic_fetch_sub(&g_alg_bytes, cb[0] + cb[1] + cb[2], __ATOMIC_RELAXED);
+      for (int k = 0; k < 3; k++) {
+        sg_l[k] = cl[k];
+        sg_b[k] = cb[k];
+      }
+      if (st != ICEP_OK) return st;
+      if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ICEP_ERR_CUDA, (std::string("capture of the step graph: ") + cudaGetErrorString(e)).c_str());
+      }
+      return ICEP_OK;
+    }
+  }
+  // After a replay of the captured step (the stream synchronised): the
+  // solve's status and counts, and with `advance` the step's time advance.
+  int step_graph_done(bool advance) override {
+    const double *h = hstat;
+    const double *hks = h + SC_COUNT + 7;
+    const double sweeps = h[SC_SWEEPS], inner = h[SC_INNER];
+    __atomic_fetch_add(&g_kernel_launches,
+                       sg_l[0] + (unsigned long long)sweeps * sg_l[1] + (unsigned long long)inner * sg_l[2],
+                       __ATOMIC_RELAXED);
+    __atomic_fetch_add(&g_alg_bytes,
+                       sg_b[0] + (unsigned long long)sweeps * sg_b[1] + (unsigned long long)inner * sg_b[2],
+                       __ATOMIC_RELAXED);
+    matvecs += (long)(sweeps + 1.0) + 2 * (long)inner;
+    last_iters = (int)inner;
+    last_error = h[SC_REL];
+    last_fallbacks = 0;
+    last_precond_apps = 0;
+    kf_pred = (int)hks[KS_ITERS];
+    pot_export_valid = false;
+    graph_steps++;
+    if (*reinterpret_cast<const int *>(h + SC_COUNT + 6))
+      return fail(ICEP_ERR_TIMEOUT, "fused plane pass: a bulk copy did not complete within the wait limit");
+    if (h[SC_STATUS] != (double)ICEP_OK)
+      return fail((int)h[SC_STATUS], "Poisson solve: non-finite right-hand side or residual");
+    if (h[SC_GUARD] != 0.0) return fail(ICEP_ERR_NOT_CONVERGED, "Poisson solve: inner loop guard reached");
+    if (advance) {
+      time += P.dt;
+      ts++;
+    }
+    return cuda_status("step");
+  }
+  int run_step_graph() {
+    if (!step_exec) {
+      cudaGraph_t gr = nullptr;
+      std::vector<cudaGraphNode_t> deps;
+      int st = cudaGraphCreate(&gr, 0) == cudaSuccess ? capture_step(gr, deps) : ICEP_ERR_CUDA;
+      if (st == ICEP_OK && cudaGraphInstantiate(&step_exec, gr, 0) != cudaSuccess) st = ICEP_ERR_CUDA;
+      if (gr) cudaGraphDestroy(gr);
+      if (st != ICEP_OK) {
+        cudaGetLastError();
+        if (step_exec) cudaGraphExecDestroy(step_exec);
+        step_exec = nullptr;
+        step_graph_failed = true;  // this context steps as before from now on
+        err.clear();
+        return time_evolution_hydro();
+      }
+    }
+    if (cudaGraphLaunch(step_exec, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+      return cuda_status("step graph");
+    return step_graph_done(false);  // step() advances time and ts
+  }
+
   ~Engine() override {
     if (s) cudaStreamSynchronize(s);
     for (int k = 0; k < 3; k++)
       if (gexec[k]) cudaGraphExecDestroy(gexec[k]);
+    if (step_exec) cudaGraphExecDestroy(step_exec);
+    cudaFree(sc);
+    cudaFreeHost(hstat);
     for (int i = 0; i < F_COUNT; i++) cudaFree(f[i]);
     fft_plan_free(fft);
     for (int i = 0; i < D_COUNT; i++) cudaFree(d64[i]);
@@ -408,6 +606,13 @@ class Engine : public EngineBase {
       kfin = kpart + nk - 7 - KS_COUNT;
       kerr = reinterpret_cast<int *>(kfin + 6);
       kst = kfin + 7;
+      // the device-side control of the solve for step graphs, and its status
+      // copy on the host
+      if (cudaMalloc(&sc, sizeof(double) * SC_COUNT + sizeof(float) * SCF_COUNT) != cudaSuccess ||
+          cudaMallocHost(&hstat, sizeof(double) * (SC_COUNT + 7 + KS_COUNT)) != cudaSuccess)
+        return fail(ICEP_ERR_CUDA, "allocation of the solve's control state failed");
+      scf = reinterpret_cast<float *>(sc + SC_COUNT);
+      cudaMemsetAsync(sc, 0, sizeof(double) * SC_COUNT + sizeof(float) * SCF_COUNT, s);
       // tile choices of the fused passes (cached per mesh); ICEP_AUTOTUNE=0
       // keeps the defaults, ICEP_KOP_TILES="xinv,xfwd,plane" sets them
       const char *at = getenv("ICEP_AUTOTUNE");
@@ -817,16 +1022,31 @@ class Engine : public EngineBase {
    * one update kernel, one host synchronisation. FP32 engine on grids whose
    * x-planes fit in shared memory.
    */
-  int bicgstab_kf(double tol, int maxit, double eps_ref, int *iters, double *rel_err, bool kspace_io = false) {
-    if constexpr (!std::is_same<R, float>::value) {
-      return bicgstab_k(tol, maxit, eps_ref, iters, rel_err);
-    } else {
+  // One iteration of the fused k-space BiCGSTAB (B x~ = A M^-1 x~ by the
+  // fused passes), its scalars in kst; eps_ref is used where kst does not
+  // give it.
+  void kf_iteration(double eps_ref, int maxit) {
+    if constexpr (std::is_same<R, float>::value) {
       float *r = f[F_KR], *r0 = f[F_KR0], *p = f[F_KP], *v = f[F_KV];
       float *sv = f[F_KS], *t = f[F_KT], *xt = f[F_KY];
       float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2];
       const int nb = kop_npb;
       double *P1 = kpart, *P2 = kpart + 2 * nb, *P3 = kpart + 4 * nb;
       double *F1 = kfin, *F2 = kfin + 2, *F3 = kfin + 4;  // final sums; kfin[6] holds the error word
+      kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, s, kst, kop_tiles);
+      kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
+      kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s, kop_tiles);
+      kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, s, kst, kop_tiles);
+      kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
+      kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s, kop_tiles);
+      kop_xr(g, xt, r, p, sv, t, r0, 0.0, F1, F2, P3, F3, kcnt + 2, s, kst, maxit);
+    }
+  }
+  int bicgstab_kf(double tol, int maxit, double eps_ref, int *iters, double *rel_err, bool kspace_io = false) {
+    if constexpr (!std::is_same<R, float>::value) {
+      return bicgstab_k(tol, maxit, eps_ref, iters, rel_err);
+    } else {
+      float *r = f[F_KR], *r0 = f[F_KR0], *xt = f[F_KY];
       if (!kspace_io) {  // right-hand side from the real field F_KB, else already in F_KR
         copy_real<R>(g, f[F_KB], r, s);
         r2c(r);
@@ -870,13 +1090,7 @@ class Engine : public EngineBase {
       // scalars, 1/eps_ref and the stop flag live in kst), so it is captured
       // once as a CUDA graph and replayed (not while a probe times launches)
       auto iteration = [&]() -> int {
-        kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, s, kst, kop_tiles);
-        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
-        kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s, kop_tiles);
-        kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, s, kst, kop_tiles);
-        kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
-        kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s, kop_tiles);
-        kop_xr(g, xt, r, p, sv, t, r0, 0.0, F1, F2, P3, F3, kcnt + 2, s, kst, maxit);
+        kf_iteration(eps_ref, maxit);
         return ICEP_OK;
       };
       const bool graph_iter = use_graphs && g_probe_kind == PROBE_NONE;
@@ -1341,7 +1555,7 @@ class Engine : public EngineBase {
   // r^ = b^ - A x^ in float-float and |r^|^2 / N into hscal[S_RR] after the
   // next read_scal (A: Ax, operate_dielectric.cxx:485-522, on the FP32
   // permittivity; 6 float-float FFTs)
-  void residual_df(float prescale) {
+  void residual_df(float prescale, const float *prescale_dev = nullptr) {
     const bool all[3] = {true, true, true};
     dfl *w0 = df(D_W3_0), *w1 = df(D_W3_1), *w2 = df(D_W3_2);
     rf_grad(g, rtab, df(D_X), w0, w1, w2, s);
@@ -1349,7 +1563,7 @@ class Engine : public EngineBase {
     rf_eps_face_mul(g, w0, w1, w2, (const float *)f[F_EPS], s);
     fft_r2c(fftdf, batch(w0, w1, w2), s);
     rf_div_combine(g, rtab, w0, w1, w2, all, df(D_B), df(D_R), RF_RESIDUAL, prescale, false, partials, scal, S_RR,
-                   s);
+                   s, prescale_dev);
     matvecs++;
   }
 
@@ -1382,8 +1596,7 @@ class Engine : public EngineBase {
     // last two solves (the reference starts from the last potential; both
     // are converged to the same true-residual tolerance)
     if (xp_valid) {
-      rf_extrapolate(nf, df(D_X), df(D_XP), s);
-      std::swap(d64[D_X], d64[D_XP]);
+      rf_extrapolate_shift(nf, df(D_X), df(D_XP), s);
     } else {
       cudaMemcpyAsync(d64[D_XP], d64[D_X], sizeof(double) * nf, cudaMemcpyDeviceToDevice, s);
     }
@@ -1561,32 +1774,59 @@ class Engine : public EngineBase {
     return lj_force(pp, dp, ljwork, ljwork_ints, nullptr, 0, nullptr, s);
   }
 
-  // Time_evolution_hydro (sp_3d_ns.cxx:24-186)
-  int time_evolution_hydro() {
-    int st;
-    // the sequence before the Poisson solve
-    st = run_segment(0, [&]() -> int {
-      mark(0);
-      if (!electrolyte) ns_solver_slaved_euler();
-      else nssolute_solver_euler();
-      for (int d = 0; d < 3; d++)  // FIX_CELL: time-dependent mean pressure gradient (sp_3d_ns.cxx:30-36)
-        if ((P.fix_cell >> d) & 1) cudaMemsetAsync(ukdc + d, 0, sizeof(double), s);
-      mark(1);
-      truncate_zeta_k2u();
-      if (!P.fixed_particle) md_position(pp, dp, ts != 0, s);
-      make_phi_particle_sum();
-      mark(2);
-      if (electrolyte) {
-        for (int d = 0; d < 3; d++) {
-          zero(F_UP0 + d);
-          zero(F_F0 + d);
-        }
-        f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], true, s);
-        make_dielectric_field(F_F0, F_WORK);
-        return conc_k2charge(F_UP0, F_F0, F_F1);
+  // Time_evolution_hydro (sp_3d_ns.cxx:24-186): the sequence before the
+  // Poisson solve
+  int pre_solve() {
+    mark(0);
+    if (!electrolyte) ns_solver_slaved_euler();
+    else nssolute_solver_euler();
+    for (int d = 0; d < 3; d++)  // FIX_CELL: time-dependent mean pressure gradient (sp_3d_ns.cxx:30-36)
+      if ((P.fix_cell >> d) & 1) cudaMemsetAsync(ukdc + d, 0, sizeof(double), s);
+    mark(1);
+    truncate_zeta_k2u();
+    if (!P.fixed_particle) md_position(pp, dp, ts != 0, s);
+    make_phi_particle_sum();
+    mark(2);
+    if (electrolyte) {
+      for (int d = 0; d < 3; d++) {
+        zero(F_UP0 + d);
+        zero(F_F0 + d);
       }
-      return ICEP_OK;
-    });
+      f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], true, s);
+      make_dielectric_field(F_F0, F_WORK);
+      return conc_k2charge(F_UP0, F_F0, F_F1);
+    }
+    return ICEP_OK;
+  }
+  // the sequence after it
+  int post_solve() {
+    if (electrolyte) {
+      maxwell_face_force(F_UP0);
+      mark(5);
+      // the force to nodes, kept in F_GE0..2 and added as u += dt/rho f
+      interp_normal_to<R>(g, vec(F_WV3_0), nullptr, vec(F_GE0), vec(F_U0), (R)(P.dt / P.rho), s);
+      solenoidal_u(F_U0);
+    } else {
+      mark(5);
+    }
+    mark(6);
+    f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], false, s);
+    if (!P.fixed_particle) {
+      const int s2 = lj_into_fr();
+      if (s2) return fail(s2, "LJ cell list");
+      md_velocity(pp, dp, ts != 0, s);
+    }
+    mark(7);
+    make_u_particle_sum();
+    mark(8);
+    f_particle_sole_add_to_zeta();
+    return ICEP_OK;
+  }
+
+  int time_evolution_hydro() {
+    if (whole_step_ok()) return run_step_graph();
+    int st;
+    st = run_segment(0, [&]() -> int { return pre_solve(); });
     if (st) return st;
     if (electrolyte) {
       mark(3);
@@ -1596,30 +1836,7 @@ class Engine : public EngineBase {
       mark(3);
       mark(4);
     }
-    // the sequence after it
-    st = run_segment(1, [&]() -> int {
-      if (electrolyte) {
-        maxwell_face_force(F_UP0);
-        mark(5);
-        // the force to nodes, kept in F_GE0..2 and added as u += dt/rho f
-        interp_normal_to<R>(g, vec(F_WV3_0), nullptr, vec(F_GE0), vec(F_U0), (R)(P.dt / P.rho), s);
-        solenoidal_u(F_U0);
-      } else {
-        mark(5);
-      }
-      mark(6);
-      f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], false, s);
-      if (!P.fixed_particle) {
-        const int s2 = lj_into_fr();
-        if (s2) return fail(s2, "LJ cell list");
-        md_velocity(pp, dp, ts != 0, s);
-      }
-      mark(7);
-      make_u_particle_sum();
-      mark(8);
-      f_particle_sole_add_to_zeta();
-      return ICEP_OK;
-    });
+    st = run_segment(1, [&]() -> int { return post_solve(); });
     if (st) return st;
     mark(9);
     mark(10);

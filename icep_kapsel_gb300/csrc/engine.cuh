@@ -2,6 +2,7 @@
 // sequence of Time_evolution_hydro (sp_3d_ns.cxx:24-186) and its phases.
 #pragma once
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "fft.cuh"
@@ -68,6 +69,21 @@ struct EngineBase {
     err = "the wait self-test needs a MIXED context (kernel 1) or solver LEARNED (kernel 2)";
     return ICEP_ERR_UNSUPPORTED;
   }
+  // The step as one CUDA graph (MIXED electrolytes on the fused passes):
+  // whether the next step can run so; its capture appended to a graph after
+  // the given nodes (which receive its last nodes); and, after a replay has
+  // finished, the solve's status read back (advance: time and step count
+  // advanced as step() does). A batch captures all its replicas into one
+  // graph.
+  virtual bool whole_step_ok() const { return false; }
+  virtual int capture_step(cudaGraph_t gr, std::vector<cudaGraphNode_t> &deps) {
+    err = "no step graph for this context";
+    return ICEP_ERR_UNSUPPORTED;
+  }
+  virtual int step_graph_done(bool advance) { return ICEP_ERR_UNSUPPORTED; }
+  long graph_steps = 0;  // steps run as one graph (alone or in a batch graph)
+  // E_ext at the context's current time (an AC field's phase)
+  virtual void refresh_field() {}
   int unsupported_learned() {
     err = "the learned preconditioner needs precision MIXED and solver LEARNED";
     return ICEP_ERR_UNSUPPORTED;

@@ -84,6 +84,12 @@ int icep_step(icep_ctx *c, int n) {
   return wrap(c, c->e->step(n));
 }
 
+int icep_step_graphs(icep_ctx *c, long *n) {
+  if (!ok(c) || !n) return ICEP_ERR_ARG;
+  *n = c->e->graph_steps;
+  return ICEP_OK;
+}
+
 int icep_get_field(icep_ctx *c, int field, double *host) {
   if (!ok(c) || !host) return ICEP_ERR_ARG;
   return wrap(c, c->e->get_field(field, host));
@@ -315,6 +321,11 @@ int icep_learned_stats(icep_ctx *c, int *fallbacks, int *precond_apps) {
 struct icep_batch {
   std::vector<icep_ctx *> ctx;
   std::string err;
+  // all replicas' steps captured into one CUDA graph (built at the first step
+  // that every replica can take as a graph) and its failure, after which the
+  // batch steps from the thread pool
+  cudaGraphExec_t exec = nullptr;
+  bool graph_failed = false;
 };
 
 namespace {
@@ -371,6 +382,7 @@ icep_batch *icep_batch_create(int n, const icep_params *params, const icep_parti
 }
 void icep_batch_destroy(icep_batch *b) {
   if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
   for (icep_ctx *c : b->ctx) icep_destroy(c);
   delete b;
 }
@@ -382,12 +394,74 @@ const char *icep_batch_last_error(const icep_batch *b) { return b ? b->err.c_str
 int icep_batch_init_state(icep_batch *b) {
   return b ? batch_run(b, [](icep_ctx *c) { return icep_init_state(c); }) : ICEP_ERR_ARG;
 }
+namespace {
+// One step of every replica as one graph launch: each replica's captured step
+// is an independent branch of the batch graph, so the replicas' kernels run
+// concurrently with one launch and one host wait per batch step. Returns -1
+// when some replica cannot step as a graph now (the caller steps the batch
+// from the thread pool instead).
+int batch_graph_step(icep_batch *b) {
+  if (b->graph_failed) return -1;
+  for (icep_ctx *c : b->ctx)
+    if (!c->e->whole_step_ok()) return -1;
+  cudaStream_t s = b->ctx[0]->e->stream();
+  if (!b->exec) {
+    cudaGraph_t gr = nullptr;
+    int st = cudaGraphCreate(&gr, 0) == cudaSuccess ? ICEP_OK : ICEP_ERR_CUDA;
+    for (size_t i = 0; i < b->ctx.size() && st == ICEP_OK; i++) {
+      std::vector<cudaGraphNode_t> deps;
+      st = b->ctx[i]->e->capture_step(gr, deps);
+    }
+    if (st == ICEP_OK && cudaGraphInstantiate(&b->exec, gr, 0) != cudaSuccess) st = ICEP_ERR_CUDA;
+    if (gr) cudaGraphDestroy(gr);
+    if (st != ICEP_OK) {
+      cudaGetLastError();
+      if (b->exec) cudaGraphExecDestroy(b->exec);
+      b->exec = nullptr;
+      b->graph_failed = true;
+      return -1;
+    }
+  }
+  for (icep_ctx *c : b->ctx) c->e->refresh_field();
+  // the replicas' streams may still hold earlier work (e.g. their first step)
+  for (icep_ctx *c : b->ctx)
+    if (cudaStreamSynchronize(c->e->stream()) != cudaSuccess) return ICEP_ERR_CUDA;
+  if (cudaGraphLaunch(b->exec, s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+    b->err = std::string("batch step graph: ") + cudaGetErrorString(cudaGetLastError());
+    return ICEP_ERR_CUDA;
+  }
+  int first = ICEP_OK;
+  for (size_t i = 0; i < b->ctx.size(); i++) {
+    const int st = wrap(b->ctx[i], b->ctx[i]->e->step_graph_done(true));
+    if (st != ICEP_OK && first == ICEP_OK) {
+      first = st;
+      b->err = "replica " + std::to_string(i) + ": " + b->ctx[i]->err;
+    }
+  }
+  return first;
+}
+}  // namespace
+
 int icep_batch_step(icep_batch *b, int nsteps) {
   if (!b || nsteps < 0) return ICEP_ERR_ARG;
-  return batch_run(b, [nsteps](icep_ctx *c) {
-    const int st = icep_step(c, nsteps);
-    return st != ICEP_OK ? st : icep_synchronize(c);
-  });
+  for (int k = 0; k < nsteps;) {
+    int st = batch_graph_step(b);
+    int done = 1;
+    if (st < 0) {
+      // from the thread pool: one step while a replica takes its first (after
+      // which the graph may become possible), else all that remain
+      bool first = false;
+      for (icep_ctx *c : b->ctx) first = first || c->e->ts == 0;
+      done = first ? 1 : nsteps - k;
+      st = batch_run(b, [done](icep_ctx *c) {
+        const int q = icep_step(c, done);
+        return q != ICEP_OK ? q : icep_synchronize(c);
+      });
+    }
+    if (st != ICEP_OK) return st;
+    k += done;
+  }
+  return ICEP_OK;
 }
 
 }  // extern "C"

@@ -221,10 +221,12 @@ __global__ void k_kdiv_post(Grid g, const R *w0, const R *w1, const R *w2, R *v)
   v[m.im + 1] = sr;
 }
 
+// ieps_dev (if given: 1/eps_ref as a device double) replaces ieps
 template <typename R>
-__global__ void k_kprecond(Grid g, const R *x, R *y, R ieps) {
+__global__ void k_kprecond(Grid g, const R *x, R *y, R ieps, const double *ieps_dev) {
   KMode m;
   if (!kmode(g, KTID, m)) return;
+  if (ieps_dev) ieps = (R)*ieps_dev;
   const int wt = kweight(g, m);
   if (wt == 0) return;
   R k[3];
@@ -393,7 +395,12 @@ void kdiv_post(const Grid &g, const R *w0, const R *w1, const R *w2, R *v, cudaS
 template <typename R>
 void kprecond(const Grid &g, const R *x, R *y, double eps_ref, cudaStream_t s) {
   count_launch(fld<R>(g, 2));
-  k_kprecond<R><<<nblk(g), TPB, 0, s>>>(g, x, y, (R)(1.0 / eps_ref));
+  k_kprecond<R><<<nblk(g), TPB, 0, s>>>(g, x, y, (R)(1.0 / eps_ref), nullptr);
+}
+template <typename R>
+void kprecond(const Grid &g, const R *x, R *y, const double *ieps_dev, cudaStream_t s) {
+  count_launch(fld<R>(g, 2));
+  k_kprecond<R><<<nblk(g), TPB, 0, s>>>(g, x, y, R(0), ieps_dev);
 }
 
 void kmdot(const Grid &g, const KVecs &V, int nv, const float *w, double *partials, cudaStream_t s) {
@@ -430,7 +437,8 @@ void ksub(const Grid &g, const float *b, const float *w, float *r, cudaStream_t 
                             cudaStream_t);                                                                         \
   template void kgrad_pre<R>(const Grid &, const R *, R *, R *, R *, double, cudaStream_t);                        \
   template void kdiv_post<R>(const Grid &, const R *, const R *, const R *, R *, cudaStream_t);                    \
-  template void kprecond<R>(const Grid &, const R *, R *, double, cudaStream_t);
+  template void kprecond<R>(const Grid &, const R *, R *, double, cudaStream_t);                                      \
+  template void kprecond<R>(const Grid &, const R *, R *, const double *, cudaStream_t);
 
 KS_INST(double)
 KS_INST(float)

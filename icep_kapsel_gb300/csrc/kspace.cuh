@@ -47,6 +47,9 @@ void kdiv_post(const Grid &g, const R *w0, const R *w1, const R *w2, R *v, cudaS
 // y = m(k) P(x) (the preconditioner applied to the iterate)
 template <typename R>
 void kprecond(const Grid &g, const R *x, R *y, double eps_ref, cudaStream_t s);
+// the same with 1/eps_ref read from device memory
+template <typename R>
+void kprecond(const Grid &g, const R *x, R *y, const double *ieps_dev, cudaStream_t s);
 
 // ---- vectors of the flexible GMRES (k-space, read modes) ------------------
 constexpr int KVEC_MAX = 34;

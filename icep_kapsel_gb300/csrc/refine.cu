@@ -32,11 +32,14 @@ __global__ void k_rf_from_f32(long n, const float *__restrict__ a, float2 *__res
   if (t < n) out[t] = make_float2(a[t], 0.f);
 }
 
-__global__ void k_rf_to_f32(long n, const float2 *__restrict__ a, float *__restrict__ out, float scale) {
+// scale_dev (if given) replaces scale: a factor formed on the device
+__global__ void k_rf_to_f32(long n, const float2 *__restrict__ a, float *__restrict__ out, float scale,
+                            const float *scale_dev) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) {
+    const float sc = scale_dev ? *scale_dev : scale;
     const float2 v = a[t];
-    out[t] = __fadd_rn(v.x, v.y) * scale;
+    out[t] = __fadd_rn(v.x, v.y) * sc;
   }
 }
 
@@ -48,22 +51,32 @@ __global__ void k_rf_to_f64(long n, const float2 *__restrict__ a, double *__rest
   }
 }
 
-__global__ void k_rf_add_f32(long n, const float *__restrict__ d, float2 *__restrict__ x, dfl a) {
+// a_dev (if given: hi, lo) replaces a
+__global__ void k_rf_add_f32(long n, const float *__restrict__ d, float2 *__restrict__ x, dfl a,
+                             const float2 *a_dev) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) {
+    if (a_dev) a = dfl(a_dev->x, a_dev->y);
     const float2 v = x[t];
     const dfl r = dfl(v.x, v.y) + a * d[t];
     x[t] = make_float2(r.hi, r.lo);
   }
 }
 
-__global__ void k_rf_extrapolate(long n, const float2 *__restrict__ x, float2 *__restrict__ y) {
+// x <- 2 x - xp (the linear extrapolation in time) and xp <- x, in place
+__global__ void k_rf_extrapolate_shift(long n, float2 *__restrict__ x, float2 *__restrict__ xp) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n) {
-    const float2 a = x[t], b = y[t];
+    const float2 a = x[t], b = xp[t];
     const dfl r = dfl(2.f * a.x, 2.f * a.y) - dfl(b.x, b.y);
-    y[t] = make_float2(r.hi, r.lo);
+    x[t] = make_float2(r.hi, r.lo);
+    xp[t] = a;
   }
+}
+
+__global__ void k_rf_zero_if(long n, float2 *__restrict__ x, const double *flag) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n && *flag != 0.0) x[t] = make_float2(0.f, 0.f);
 }
 
 struct RfTab {
@@ -152,7 +165,12 @@ __global__ void __launch_bounds__(DOT_TPB) k_rf_div_combine(Grid g, RfTab tab, c
                                                              const float4 *__restrict__ w1, const float4 *__restrict__ w2,
                                                              int use, const float4 *__restrict__ base,
                                                              float4 *__restrict__ out, int mode, float prescale,
-                                                             double post, double *__restrict__ partials) {
+                                                             double post, double *__restrict__ partials,
+                                                             const float *prescale_dev) {
+  if (!ACC64 && prescale_dev) {  // the prescale formed on the device, post as the host forms it
+    prescale = *prescale_dev;
+    post = (1.0 / ((double)prescale * (double)prescale)) / (double)g.nreal();
+  }
   const unsigned N = (unsigned)g.nmodes();
   const float4 *w[3] = {w0, w1, w2};
   float acc = 0.f;
@@ -259,7 +277,11 @@ void rf_from_f32(long n, const float *a, dfl *out, cudaStream_t s) {
 }
 void rf_to_f32(long n, const dfl *a, float *out, double scale, cudaStream_t s) {
   count_launch(12.0 * n);
-  k_rf_to_f32<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const float2 *>(a), out, (float)scale);
+  k_rf_to_f32<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const float2 *>(a), out, (float)scale, nullptr);
+}
+void rf_to_f32(long n, const dfl *a, float *out, const float *scale_dev, cudaStream_t s) {
+  count_launch(12.0 * n);
+  k_rf_to_f32<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const float2 *>(a), out, 1.f, scale_dev);
 }
 void rf_differs(long n, const double *a, const double *b, int *flag, cudaStream_t s) {
   cudaMemsetAsync(flag, 0, sizeof(int), s);
@@ -273,11 +295,19 @@ void rf_to_f64(long n, const dfl *a, double *out, cudaStream_t s) {
 }
 void rf_add_f32(long n, const float *d, dfl *x, double a, cudaStream_t s) {
   count_launch(20.0 * n);
-  k_rf_add_f32<<<nblk(n), TPB, 0, s>>>(n, d, reinterpret_cast<float2 *>(x), dfl::from_double(a));
+  k_rf_add_f32<<<nblk(n), TPB, 0, s>>>(n, d, reinterpret_cast<float2 *>(x), dfl::from_double(a), nullptr);
 }
-void rf_extrapolate(long n, const dfl *x, dfl *y, cudaStream_t s) {
-  count_launch(24.0 * n);
-  k_rf_extrapolate<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<const float2 *>(x), reinterpret_cast<float2 *>(y));
+void rf_add_f32(long n, const float *d, dfl *x, const float2 *a_dev, cudaStream_t s) {
+  count_launch(20.0 * n);
+  k_rf_add_f32<<<nblk(n), TPB, 0, s>>>(n, d, reinterpret_cast<float2 *>(x), dfl(0), a_dev);
+}
+void rf_extrapolate_shift(long n, dfl *x, dfl *xp, cudaStream_t s) {
+  count_launch(32.0 * n);
+  k_rf_extrapolate_shift<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<float2 *>(x), reinterpret_cast<float2 *>(xp));
+}
+void rf_zero_if(long n, dfl *x, const double *flag, cudaStream_t s) {
+  count_launch();
+  k_rf_zero_if<<<nblk(n), TPB, 0, s>>>(n, reinterpret_cast<float2 *>(x), flag);
 }
 void rf_grad(const Grid &g, const RefineTables &t, const dfl *x, dfl *w0, dfl *w1, dfl *w2, cudaStream_t s) {
   count_launch(fld<double>(g, 4));
@@ -305,7 +335,7 @@ static double mode_fields(int use_bits, const dfl *base) {
 }
 void rf_div_combine(const Grid &g, const RefineTables &t, const dfl *w0, const dfl *w1, const dfl *w2,
                     const bool *use, const dfl *base, dfl *out, int mode, float prescale, bool acc64,
-                    double *partials, double *scal, int slot, cudaStream_t s) {
+                    double *partials, double *scal, int slot, cudaStream_t s, const float *prescale_dev) {
   const int u = (use[0] ? 1 : 0) | (use[1] ? 2 : 0) | (use[2] ? 4 : 0);
   const float4 *a0 = reinterpret_cast<const float4 *>(w0), *a1 = reinterpret_cast<const float4 *>(w1),
                *a2 = reinterpret_cast<const float4 *>(w2);
@@ -316,10 +346,10 @@ void rf_div_combine(const Grid &g, const RefineTables &t, const dfl *w0, const d
   count_launch(fld<double>(g, mode_fields(u, base)));
   if (acc64)
     k_rf_div_combine<true>
-        <<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, tab_of(t), a0, a1, a2, u, b, o, mode, prescale, post, partials);
+        <<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, tab_of(t), a0, a1, a2, u, b, o, mode, prescale, post, partials, nullptr);
   else
-    k_rf_div_combine<false>
-        <<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, tab_of(t), a0, a1, a2, u, b, o, mode, prescale, post, partials);
+    k_rf_div_combine<false><<<DOT_BLOCKS, DOT_TPB, 0, s>>>(g, tab_of(t), a0, a1, a2, u, b, o, mode, prescale, post,
+                                                          partials, prescale_dev);
   kdots_finish(partials, DOT_BLOCKS, 1, scal, slot, s);
 }
 

@@ -32,14 +32,20 @@ struct RefineTables {
 void rf_from_f32(long n, const float *a, dfl *out, cudaStream_t s);
 // out = (float)(a * scale)
 void rf_to_f32(long n, const dfl *a, float *out, double scale, cudaStream_t s);
+// the same with the FP32 factor read from device memory
+void rf_to_f32(long n, const dfl *a, float *out, const float *scale_dev, cudaStream_t s);
 // out = (double)a
 void rf_to_f64(long n, const dfl *a, double *out, cudaStream_t s);
 // *flag = 1 if the n doubles a and b differ in any bit, else 0 (device int)
 void rf_differs(long n, const double *a, const double *b, int *flag, cudaStream_t s);
 // x += a * d (a a host double, d FP32)
 void rf_add_f32(long n, const float *d, dfl *x, double a, cudaStream_t s);
-// y = 2 x - y (linear extrapolation in time)
-void rf_extrapolate(long n, const dfl *x, dfl *y, cudaStream_t s);
+// the same with a read from device memory as a float-float pair (hi, lo)
+void rf_add_f32(long n, const float *d, dfl *x, const float2 *a_dev, cudaStream_t s);
+// x <- 2 x - xp and xp <- x in place (linear extrapolation in time)
+void rf_extrapolate_shift(long n, dfl *x, dfl *xp, cudaStream_t s);
+// x = 0 if *flag (a device double) is non-zero
+void rf_zero_if(long n, dfl *x, const double *flag, cudaStream_t s);
 // w_d = D^+_d x^ (k-space, d = 0..2)
 void rf_grad(const Grid &g, const RefineTables &t, const dfl *x, dfl *w0, dfl *w1, dfl *w2, cudaStream_t s);
 // w_d *= eps_face_d (real points; eps is the FP32 permittivity)
@@ -57,8 +63,10 @@ void rf_eps_face_e(const Grid &g, dfl *w0, dfl *w1, dfl *w2, const float *eps, c
 // no square under- or overflows), per thread, then in FP64 across threads;
 // acc64 sums them in FP64 instead (no prescale needed).
 enum { RF_RESIDUAL = 0, RF_RHS = 1 };
+// prescale_dev (if given, FP32 sums only) replaces prescale by a value
+// formed on the device.
 void rf_div_combine(const Grid &g, const RefineTables &t, const dfl *w0, const dfl *w1, const dfl *w2,
                     const bool *use, const dfl *base, dfl *out, int mode, float prescale, bool acc64,
-                    double *partials, double *scal, int slot, cudaStream_t s);
+                    double *partials, double *scal, int slot, cudaStream_t s, const float *prescale_dev = nullptr);
 
 }  // namespace icep

@@ -87,6 +87,7 @@ def load_library(path=None):
     L.icep_MD_solver_velocity.argtypes = [V, I]
     L.icep_Charge_field2potential_dielectric.argtypes = [V, C.POINTER(I), _DP]
     L.icep_solver_stats.argtypes = [V, C.POINTER(I), _DP, C.POINTER(C.c_long)]
+    L.icep_step_graphs.argtypes = [V, C.POINTER(C.c_long)]
     L.icep_time_evolution.argtypes = [V, _DP, _DP, _DP, _DP, _DP, _DP, V, I]
     L.icep_stream.restype = V
     L.icep_stream.argtypes = [V]
@@ -301,6 +302,12 @@ class Simulation:
         mv = C.c_long(0)
         self._check(self.lib.icep_solver_stats(self.ctx, C.byref(it), C.byref(er), C.byref(mv)), "stats")
         return it.value, er.value, mv.value
+
+    def step_graphs(self):
+        """Steps taken as one CUDA graph so far (icep_step_graphs)."""
+        n = C.c_long(0)
+        self._check(self.lib.icep_step_graphs(self.ctx, C.byref(n)), "step_graphs")
+        return n.value
 
     def last_iterations(self):
         return self.solver_stats()[0]

@@ -254,6 +254,13 @@ int icep_Charge_field2potential_dielectric(icep_ctx *ctx, int *iterations, doubl
 int icep_Make_Maxwell_force_x_on_fluid(icep_ctx *ctx);
 /* Statistics of the last Poisson solve of the context. */
 int icep_solver_stats(icep_ctx *ctx, int *iterations, double *error, long *matvecs);
+/* Steps of the context taken as one CUDA graph so far (no reference
+ * counterpart): with precision ICEP_MIXED, an electrolyte and the fused
+ * Poisson passes, a step from the second on is captured once -- the Poisson
+ * solve's refinement sweeps and iterations as device-side loops -- and
+ * replayed, alone (icep_step) or with the other replicas of a batch
+ * (icep_batch_step); ICEP_GRAPHS=0 at context creation turns this off. */
+int icep_step_graphs(icep_ctx *ctx, long *n);
 /* Generic phase dispatch (ids of the step's phases, numbered as in the
  * checker used by the tests). */
 int icep_call(icep_ctx *ctx, int fn);
@@ -261,9 +268,14 @@ int icep_call(icep_ctx *ctx, int fn);
 /* ---- batches of independent replicas (no reference counterpart) ---------
  * The reference runs one system per process; an ensemble there is many
  * processes. A batch holds n contexts (any mix of meshes, particle counts and
- * parameters), each with its own CUDA stream; icep_batch_step advances all of
- * them from a pool of host threads so that their kernels run concurrently on
- * the GPU, and returns when every replica has finished. */
+ * parameters), each with its own CUDA stream. icep_batch_step advances all
+ * of them and returns when every replica has finished: once every replica
+ * can take its step as a CUDA graph (MIXED electrolytes on the fused Poisson
+ * passes, from their second step on), all replicas' steps are captured into
+ * one graph -- independent branches, the Poisson solves' loops on the device
+ * -- and each batch step is one graph launch and one host wait; otherwise the
+ * replicas step from a pool of host threads, their kernels running
+ * concurrently on their streams. */
 typedef struct icep_batch icep_batch;
 /* params[i], particles[i] (params[i].n_particles entries) for replica i. */
 icep_batch *icep_batch_create(int n, const icep_params *params, const icep_particle *const *particles, int *status);

@@ -281,11 +281,13 @@ def run_gpu(args, world, rank, local, dist):
     ms = C.c_double(0)
     launches0 = lib.icep_kernel_launches()
     abytes0 = lib.icep_algorithmic_bytes()
+    graphs0 = sim.step_graphs()
     with ClockSampler(0) as clk:
         st = lib.icep_step_timed(sim.ctx, args.steps, C.byref(ms))
     if st != 0:
         raise RuntimeError("timed steps failed: %d" % st)
     launches = int(lib.icep_kernel_launches() - launches0)
+    graph_steps = sim.step_graphs() - graphs0
     step_bytes = float(lib.icep_algorithmic_bytes() - abytes0) / args.steps
     # the dominant kernel's launches timed with CUDA events on their stream
     # over further steps (the probe's events run the solver's iterations as
@@ -352,6 +354,10 @@ def run_gpu(args, world, rank, local, dist):
             "clocks": clk.summary(),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": io_bytes, "d2h_bytes_per_step": io_bytes},
             "gpu_launches": launches,
+            # the timed launches' positions in the process's launch sequence
+            # (for slicing a profiler's launch list to the timed steps)
+            "timed_launch_range": [int(launches0), int(launches0) + launches],
+            "steps_as_one_graph": graph_steps,
             "grid_point_steps_per_s": value * args.n ** 3,
             "roofline": {"bound": "hbm", "kernel": PROBE_KERNEL, "achieved": achieved, "peak": peak,
                          "peak_kind": peak_kind + " (hbm_gbs, copy)", "unit": "GB/s",
@@ -396,16 +402,25 @@ def run_batch(args, n_replicas=64, seed=4242):
                                     precision=abi.MIXED))
         points += n ** 3
     b = Batch(reps)
+    lib = b.lib
+    lib.icep_kernel_launches.restype = C.c_ulonglong
     b.init_state()
     b.step(args.warmup)
+    g0 = [b.replica(i).step_graphs() for i in range(n_replicas)]
+    l0 = lib.icep_kernel_launches()
     t0 = time.perf_counter()
     b.step(args.steps)
     dt = time.perf_counter() - t0
+    l1 = lib.icep_kernel_launches()
+    # batch steps taken as one graph launch: every replica's step replayed
+    graph_steps = min(b.replica(i).step_graphs() - g0[i] for i in range(n_replicas))
     b.close()
     return {"replicas": n_replicas, "meshes": "32^3 / 64^3", "value": n_replicas * args.steps / dt,
             "unit": "replica-steps/s", "grid_point_steps_per_s": points * args.steps / dt,
-            "ms_per_batch_step": 1000.0 * dt / args.steps, "timing": "host wall clock around icep_batch_step "
-            "(returns after every replica's stream has finished)"}
+            "ms_per_batch_step": 1000.0 * dt / args.steps,
+            "batch_steps_as_one_graph_launch": graph_steps,
+            "kernel_launches_per_batch_step": (l1 - l0) / args.steps,
+            "timing": "host wall clock around icep_batch_step (returns after every replica has finished)"}
 
 
 def dense_positions(n, L, minsep, seed, max_tries=2000000):

@@ -622,6 +622,7 @@ class Engine : public EngineBase {
         kop_tiles.xinv_kw = fi;
         kop_tiles.xfwd_kw = ff;
         kop_tiles.plane_smem = fp;
+        kop_tuned = true;  // picks set by hand: reported with no timings
       } else if constexpr (std::is_same<R, float>::value) {
         if (!(at && at[0] == '0')) {
           kop_tiles = kop_autotune(fft, f[F_KP], f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2],

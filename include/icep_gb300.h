@@ -357,11 +357,12 @@ int icep_phase_times(icep_ctx *ctx, double *ms, int n);
  * reference): at context creation (MIXED electrolyte on a mesh the fused
  * passes cover) every candidate tile shape is timed on scratch fields and the
  * fastest kept, per mesh for the process (ICEP_AUTOTUNE=0 keeps the
- * defaults). picks[3] receives the x pencils per block of the inverse and
- * forward x passes and the plane pass's kernel (0 register-resident, 1
- * shared-memory); us[8] (optional) the measured times per launch: xinv 8/16/32,
- * xfwd 8/16/32, plane register/shared (0 for candidates the mesh lacks).
- * ICEP_ERR_STATE for contexts without tuned passes. */
+ * defaults; ICEP_KOP_TILES="xinv,xfwd,plane" sets the picks, untimed).
+ * picks[3] receives the x pencils per block of the inverse and forward x
+ * passes and the plane pass's kernel (0 register-resident, 1 shared-memory);
+ * us[8] (optional) the measured times per launch: xinv 8/16/32, xfwd
+ * 8/16/32, plane register/shared (0 for candidates the mesh lacks or picks
+ * set by hand). ICEP_ERR_STATE for contexts without tuned passes. */
 int icep_autotune_picks(icep_ctx *ctx, int *picks, double *us);
 /* Check of the bounded device waits (no counterpart in the reference):
  * launches one kernel in a mode that issues no asynchronous copy or MMA, so

@@ -7,8 +7,9 @@ xi = 2 (volume fraction 6.5%) at seeded random positions with minimum
 separation 10; per-particle permittivity uniform in [1, 5] (seeded),
 eps_fluid = 80; uniform field E0 = (0, 0, 0.1); salt z = +-1, Onsager 7.24,
 Debye length 10 a, kBT = 1; dt = 0.01; Poisson solved to 1e-8 relative true
-residual with the plain spectral-preconditioned BiCGSTAB. Synthetic inputs
-only (no dataset is involved).
+residual: float-float iterative refinement around the plain spectral-
+preconditioned inner solve (CG; BiCGSTAB with ICEP_INNER=bicgstab). Synthetic
+inputs only (no dataset is involved).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -54,6 +55,14 @@ def workload(args, precision, solver):
                                e_ext=(0.0, 0.0, 0.1), tol=args.tol, maxit=args.maxit, dt=0.01,
                                per_particle_eps=(1.0, 5.0), solver=solver, precision=precision)
     return p, parts
+
+
+def solver_label(precision):
+    from icep_kapsel_gb300 import abi
+    if precision == abi.FP64:
+        return "spectral-preconditioned BiCGSTAB, FP64 (plain)"
+    inner = "BiCGSTAB" if os.environ.get("ICEP_INNER") == "bicgstab" else "CG"
+    return "spectral-preconditioned %s inner solve, float-float true-residual refinement (plain)" % inner
 
 
 def workload_config(args, precision_name, solver_name):
@@ -348,7 +357,7 @@ def run_gpu(args, world, rank, local, dist):
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if precision == abi.FP64 else "f32 (fields, FFTs, inner Krylov) + f64 (particles, k=0, residual)",
             "data": "synthetic",
-            "config": dict(workload_config(args, args.precision, "spectral-preconditioned BiCGSTAB (plain)"),
+            "config": dict(workload_config(args, args.precision, solver_label(precision)),
                            parallelism="replicas" if world > 1 else "single GPU"),
             "poisson": {"iterations_last_solve": iters, "relative_true_residual": err},
             "clocks": clk.summary(),

@@ -802,7 +802,8 @@ struct DivAcc {
 template <int N, int KWT>
 __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const float *w1, const float *w2,
                                                   float *out, int mode, const float *other, double *partials,
-                                                  double *finals, unsigned *counter, const cf *__restrict__ twx) {
+                                                  double *finals, unsigned *counter, const cf *__restrict__ twx,
+                                                  const double *ks) {
   extern __shared__ unsigned char smem_raw[];
   const int sw = KWT + 1;
   cf *tws = reinterpret_cast<cf *>(smem_raw);
@@ -817,6 +818,8 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
   load_table(tws, twx, N);
   pencil_coords<KWT>(g, q0, pj, pkz);
   __syncthreads();
+  // KOP_CG: the dot is weighted by the preconditioner m(k) (1/eps_ref from ks)
+  const float ieps = (mode == KOP_CG) ? (float)__ldcg(ks + KS_IEPS) : 0.f;
   float s0 = 0.f, s1 = 0.f;  // the thread's few terms in FP32; blocks and their sum in FP64
   static_assert(N / 8 <= 512 / KWT, "xblock(N) = KWT x N/8 threads");
   constexpr int XPT = 8;
@@ -851,6 +854,8 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
     const cf o = lo[u];
     if (mode == KOP_P) {
       s0 += fw * (o.x * vr + o.y * vi);
+    } else if (mode == KOP_CG) {
+      s0 += fw * precond_m(g, e, pj[w], pkz[w], ieps) * (o.x * vr + o.y * vi);
     } else {
       s0 += fw * (vr * vr + vi * vi);
       s1 += fw * (vr * o.x + vi * o.y);
@@ -931,6 +936,69 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float 
   }
 }
 
+// Update kernel of the preconditioned CG (the inner solve's alternative to
+// BiCGSTAB: the operator is symmetric, A = -(D+)^* eps D+, and so is the
+// spectral preconditioner m(k)). In the x~ form p = M^-1 p~, x = M^-1 x~:
+// alpha = rho / (M^-1 p~, q) with q = B p~ (fin_pq, from k_kop_xfwd's KOP_CG
+// dot); x~ += alpha p~; r -= alpha q; then rho' = (r, M^-1 r) and |r|^2,
+// and the last block forms beta = rho'/rho (k_kop_xinv's KOP_P update with
+// omega = 0 makes p~ = r + beta p~) and the stop test. init: no update, only
+// rho and |r|^2 of the starting residual (beta = 0: p~ = r).
+template <int H>
+__global__ void __launch_bounds__(KOP_XR_TPB) k_kop_cg(Grid g, float *xt, float *r, const float *p, const float *q,
+                                                     const double *fin_pq, double *part, double *fin,
+                                                     unsigned *counter, double *ks, int maxit, int init) {
+  const int lin = threadIdx.x;
+  __shared__ float sc[2];  // alpha, 1/eps_ref
+  __shared__ int stop;     // the solve is done: this launch leaves x and r alone
+  if (lin == 0) {
+    stop = (__ldcg(ks + KS_DONE) != 0.0) ? 1 : 0;
+    sc[0] = init ? 0.f : (float)(__ldcg(ks + KS_RHO) / __ldcg(fin_pq));
+    sc[1] = (float)__ldcg(ks + KS_IEPS);
+  }
+  __syncthreads();
+  if (stop) return;
+  const float alpha = sc[0], ieps = sc[1];
+  constexpr int RL = H + 1;  // modes per z row
+  const long nm = g.nmodes();
+  const long base = (long)blockIdx.x * (KOP_XR_TPB * KOP_XR_MPT);
+  const int lny = __ffs(g.ny) - 1;
+  float s0 = 0.f, s1 = 0.f;
+#pragma unroll
+  for (int k = 0; k < KOP_XR_MPT; k++) {
+    const long idx = base + k * KOP_XR_TPB + lin;
+    if (idx >= nm) break;
+    const int row = (int)(idx / RL), kz = (int)(idx - (long)row * RL);
+    const int i = row >> lny, j = row & (g.ny - 1);
+    const int wt = read_weight(g, i, j, kz);
+    if (wt == 0) continue;
+    cf nr = ldw(r, idx, wt);
+    if (!init) {
+      const cf pp = ldw(p, idx, wt), qq = ldw(q, idx, wt), xx = ldw(xt, idx, wt);
+      nr = cf{nr.x - alpha * qq.x, nr.y - alpha * qq.y};
+      reinterpret_cast<float2 *>(xt)[idx] = make_float2(xx.x + alpha * pp.x, xx.y + alpha * pp.y);
+      reinterpret_cast<float2 *>(r)[idx] = make_float2(nr.x, nr.y);
+    }
+    const float fw = (float)wt, n2 = nr.x * nr.x + nr.y * nr.y;
+    s0 += fw * precond_m(g, i, j, kz, ieps) * n2;
+    s1 += fw * n2;
+  }
+  const int last = block_partials_final(s0, s1, 1.0 / (double)g.nreal(), part, fin, counter);
+  if (last) {
+    __syncthreads();
+    if (lin == 0) {
+      const double rho_new = __ldcg(fin), rr = __ldcg(fin + 1);
+      const double it = ks[KS_ITERS] + (init ? 0.0 : 1.0);
+      ks[KS_BETA] = init ? 0.0 : rho_new / ks[KS_RHO];
+      ks[KS_OMEGA] = 0.0;
+      ks[KS_RHO] = rho_new;
+      ks[KS_ITERS] = it;
+      ks[KS_RR] = rr;
+      ks[KS_DONE] = (!(rr > ks[KS_TOL2]) || !isfinite(rr) || !isfinite(rho_new) || it >= (double)maxit) ? 1.0 : 0.0;
+    }
+  }
+}
+
 __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2) {
   const long tl = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tl >= g.nreal()) return;
@@ -976,10 +1044,10 @@ void launch_xinv(const Grid &g, int mode, float *vec, const float *r, const floa
 template <int N, int KWT>
 void launch_xfwd(const Grid &g, const float *w0, const float *w1, const float *w2, float *out, int mode,
                  const float *other, double *partials, double *finals, unsigned *counter, const cf *twx,
-                 cudaStream_t s) {
+                 const double *ks, cudaStream_t s) {
   set_x_attr<N, KWT>();
   k_kop_xfwd<N, KWT><<<div_up((long)g.ny * g.hnz, KWT), xblock(N, KWT), xpass_smem(N, KWT), s>>>(
-      g, w0, w1, w2, out, mode, other, partials, finals, counter, twx);
+      g, w0, w1, w2, out, mode, other, partials, finals, counter, twx, ks);
 }
 
 // the register plane pass covers NY in {64, 128} and NZ/2 in {32, 64}
@@ -1169,12 +1237,12 @@ bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2
 
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
               const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s,
-              const KopTiles &t) {
+              const KopTiles &t, const double *ks) {
   const Grid &g = p.g;
   const int kw = xkw_ok(g.nx, t.xfwd_kw) ? t.xfwd_kw : 16;
   count_launch(fld<float>(g, mode == KOP_NONE ? 4.0 : 5.0));
   probe_begin(PROBE_KOP_XFWD, s);
-#define KOP_XFWD(N, W) launch_xfwd<N, W>(g, w0, w1, w2, out, mode, other, partials, finals, counter, p.tw_x, s)
+#define KOP_XFWD(N, W) launch_xfwd<N, W>(g, w0, w1, w2, out, mode, other, partials, finals, counter, p.tw_x, ks, s)
   switch (g.nx) {
     case 16: KOP_XFWD(16, 16); break;
     case 32: KOP_XFWD(32, 16); break;
@@ -1215,6 +1283,24 @@ void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv,
     KOP_XR(128)
   }
 #undef KOP_XR
+}
+
+void kop_cg(const Grid &g, float *xt, float *r, const float *p, const float *q, const double *fin_pq, double *part,
+            double *fin, unsigned *counter, cudaStream_t s, double *ks, int maxit, bool init) {
+  const unsigned nb = (unsigned)kop_xr_blocks(g);
+  count_launch(fld<float>(g, init ? 1.0 : 6.0));
+#define KOP_CG(HH)                                                                                             \
+  case HH:                                                                                                     \
+    k_kop_cg<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, q, fin_pq, part, fin, counter, ks, maxit, init ? 1 : 0); \
+    break;
+  switch (g.nz / 2) {
+    KOP_CG(8)
+    KOP_CG(16)
+    KOP_CG(32)
+    KOP_CG(64)
+    KOP_CG(128)
+  }
+#undef KOP_CG
 }
 
 }  // namespace icep

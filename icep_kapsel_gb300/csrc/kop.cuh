@@ -22,7 +22,7 @@
 
 namespace icep {
 
-enum { KOP_P = 0, KOP_S = 1, KOP_NONE = 2 };
+enum { KOP_P = 0, KOP_S = 1, KOP_NONE = 2, KOP_CG = 3 };
 
 // true if the fused passes cover this grid (an x-plane fits in shared memory)
 bool kop_supported(const Grid &g);
@@ -77,10 +77,12 @@ bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2
 // mode KOP_S: partials[2b] = (out, out), partials[2b+1] = (out, other) with other = s;
 // finals[c] = sum over blocks of partials[2b + c], summed by the last block
 // to finish (counter: a device word at zero, left at zero);
+// mode KOP_CG: partials[2b] = (M^-1 other, out) = sum m(k) other^* out with
+// the preconditioner m(k) (1/eps_ref from ks[KS_IEPS]): the CG denominator;
 // mode KOP_NONE: no dot products (other, partials, finals unused).
 void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
               const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s,
-              const KopTiles &t = KopTiles());
+              const KopTiles &t = KopTiles(), const double *ks = nullptr);
 // alpha = rho / fin1[0]; omega = fin2[1] / fin2[0];
 // part3[2b] = (r0, r), part3[2b+1] = (r, r) over kop_xr_blocks(g) blocks,
 // fin3 their sums (counter3 as for kop_xfwd).
@@ -88,5 +90,14 @@ int kop_xr_blocks(const Grid &g);
 void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv, const float *t, const float *r0,
             double rho, const double *fin1, const double *fin2, double *part3, double *fin3, unsigned *counter3,
             cudaStream_t s, double *ks = nullptr, int maxit = 0);
+// The preconditioned CG's update (the operator and preconditioner are
+// symmetric): alpha = ks[KS_RHO] / fin_pq[0]; x~ += alpha p~; r -= alpha q;
+// part[2b] = (r, M^-1 r), part[2b+1] = (r, r) over kop_xr_blocks(g) blocks,
+// fin their sums; the last block sets KS_RHO, KS_BETA (rho'/rho, 0 with
+// init), KS_OMEGA = 0, KS_ITERS, KS_RR and KS_DONE (1: converged, non-finite
+// or at maxit). init: no update (the starting residual's sums only). Returns
+// without touching x and r once KS_DONE is set.
+void kop_cg(const Grid &g, float *xt, float *r, const float *p, const float *q, const double *fin_pq, double *part,
+            double *fin, unsigned *counter, cudaStream_t s, double *ks, int maxit, bool init);
 
 }  // namespace icep

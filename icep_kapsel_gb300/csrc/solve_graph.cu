@@ -66,7 +66,7 @@ __global__ void k_sweep_cond(cudaGraphConditionalHandle h, const double *scal, i
 }
 
 __global__ void k_inner_prep(cudaGraphConditionalHandle h, const double *scal, int slot_rr, double *sc, double *ks,
-                             double eps2) {
+                             double eps2, int cg) {
   const double bsq = scal[slot_rr];
   sc[SC_LOOPS] = 0.0;
   ks[KS_ITERS] = 0.0;
@@ -76,13 +76,15 @@ __global__ void k_inner_prep(cudaGraphConditionalHandle h, const double *scal, i
     return;
   }
   const double tol = sc[SC_INNER_TOL];
-  ks[KS_RHO] = bsq;  // iteration 0: rho = (r0, r), p = v = 0
-  ks[KS_BETA] = 1.0;
-  ks[KS_OMEGA] = 1.0;
+  // BiCGSTAB iteration 0: rho = (r0, r), p = v = 0; CG: p = r (beta = 0,
+  // omega = 0), rho formed by kop_cg's starting pass
+  ks[KS_RHO] = bsq;
+  ks[KS_BETA] = cg ? 0.0 : 1.0;
+  ks[KS_OMEGA] = cg ? 0.0 : 1.0;
   ks[KS_TOL2] = tol * tol * bsq;
   ks[KS_DONE] = 0.0;
   ks[KS_RR] = bsq;
-  ks[KS_RESTART] = eps2 * bsq;
+  ks[KS_RESTART] = cg ? 0.0 : eps2 * bsq;
   cudaGraphSetConditional(h, bsq > ks[KS_TOL2] ? 1u : 0u);
 }
 
@@ -137,9 +139,9 @@ void sweep_cond(cudaGraphConditionalHandle h, const double *scal, int slot_rr, d
   k_sweep_cond<<<1, 1, 0, s>>>(h, scal, slot_rr, sc, scf, ks, tol, nreal, max_sweeps, add_inner ? 1 : 0);
 }
 void inner_prep(cudaGraphConditionalHandle h, const double *scal, int slot_rr, double *sc, double *ks, double eps2,
-                cudaStream_t s) {
+                bool cg, cudaStream_t s) {
   count_launch();
-  k_inner_prep<<<1, 1, 0, s>>>(h, scal, slot_rr, sc, ks, eps2);
+  k_inner_prep<<<1, 1, 0, s>>>(h, scal, slot_rr, sc, ks, eps2, cg ? 1 : 0);
 }
 void inner_cond(cudaGraphConditionalHandle h, double *ks, float *r, float *r0, float *v, float *p, long nf,
                 int maxit, double *sc, double eps2, cudaStream_t s) {

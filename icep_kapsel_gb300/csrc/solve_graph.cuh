@@ -47,9 +47,10 @@ void solve_begin(const double *scal, int slot_bb, int slot_eps, double *sc, floa
 void sweep_cond(cudaGraphConditionalHandle h, const double *scal, int slot_rr, double *sc, float *scf,
                 const double *ks, double tol, double nreal, int max_sweeps, bool add_inner, cudaStream_t s);
 // After |r|^2 of the sweep's normalised residual (scal[slot_rr]): the inner
-// iteration's starting state in ks and the inner loop's condition.
+// iteration's starting state in ks (BiCGSTAB, or with cg the preconditioned
+// CG) and the inner loop's condition.
 void inner_prep(cudaGraphConditionalHandle h, const double *scal, int slot_rr, double *sc, double *ks, double eps2,
-                cudaStream_t s);
+                bool cg, cudaStream_t s);
 // End of an inner loop body: a restart that kop_xr asked for (r0 = r, v = p
 // = 0, the scalars reset) or the stop, as the host loop does it; nf floats
 // per vector.

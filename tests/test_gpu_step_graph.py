@@ -106,3 +106,37 @@ def test_step_graph_zero_right_hand_side():
         assert rel(g.get(name), h.get(name)) < 1e-5, name
     g.close()
     h.close()
+
+
+def with_inner(solver, p, parts):
+    """A context whose MIXED inner solve is `solver` (ICEP_INNER at creation)."""
+    old = os.environ.get("ICEP_INNER")
+    os.environ["ICEP_INNER"] = solver
+    try:
+        return Simulation(p, parts)
+    finally:
+        if old is None:
+            del os.environ["ICEP_INNER"]
+        else:
+            os.environ["ICEP_INNER"] = old
+
+
+def test_inner_cg_and_bicgstab_agree():
+    """The inner correction solve by preconditioned CG (the default) or by
+    BiCGSTAB: both sweeps end at the same true-residual criterion, so the
+    steps agree to the solve tolerance; CG takes one operator application
+    per iteration, BiCGSTAB two."""
+    sims = {k: with_inner(k, *replica(64, 20, 2, 0.1)) for k in ("cg", "bicgstab")}
+    for s in sims.values():
+        s.init_state()
+        s.step(4)
+    a, b = sims["cg"], sims["bicgstab"]
+    for name in ("zeta0", "zeta1", "c0", "phi"):
+        assert rel(a.get(name), b.get(name)) < 1e-5, name
+    assert rel(a.get("pot"), b.get("pot")) < 2e-5
+    ita, era, mva = a.solver_stats()
+    itb, erb, mvb = b.solver_stats()
+    assert era <= 1e-8 and erb <= 1e-8
+    assert 0 < ita <= 2 * itb + 2, (ita, itb)
+    for s in sims.values():
+        s.close()

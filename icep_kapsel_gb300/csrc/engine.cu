@@ -342,7 +342,7 @@ class Engine : public EngineBase {
     pot_export_valid = false;
     graph_steps++;
     if (*reinterpret_cast<const int *>(h + SC_COUNT + 6))
-      return fail(ICEP_ERR_TIMEOUT, "fused plane pass: a bulk copy did not complete within the wait limit");
+      return fail(ICEP_ERR_TIMEOUT, "plane pass: a bulk copy did not complete within the wait limit");
     if (h[SC_STATUS] != (double)ICEP_OK)
       return fail((int)h[SC_STATUS], "Poisson solve: non-finite right-hand side or residual");
     if (h[SC_GUARD] != 0.0) return fail(ICEP_ERR_NOT_CONVERGED, "Poisson solve: inner loop guard reached");
@@ -612,6 +612,9 @@ class Engine : public EngineBase {
       kfin = kpart + nk - 7 - KS_COUNT;
       kerr = reinterpret_cast<int *>(kfin + 6);
       kst = kfin + 7;
+      // the FP32 transforms' register-resident plane passes report a copy
+      // that did not land through the same word
+      fft.err = kerr;
       // the device-side control of the solve for step graphs, and its status
       // copy on the host
       if (cudaMalloc(&sc, sizeof(double) * SC_COUNT + sizeof(float) * SCF_COUNT) != cudaSuccess ||
@@ -1141,7 +1144,7 @@ class Engine : public EngineBase {
         cudaMemcpyAsync(hkpart, kfin, sizeof(double) * (7 + KS_COUNT), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fused k-space iteration");
         if (*reinterpret_cast<const int *>(hkpart + 6))
-          return fail(ICEP_ERR_TIMEOUT, "fused plane pass: a bulk copy did not complete within the wait limit");
+          return fail(ICEP_ERR_TIMEOUT, "plane pass: a bulk copy did not complete within the wait limit");
         const int now = (int)hks[KS_ITERS];
         matvecs += (cg ? 1 : 2) * (now - i);
         i = now;
@@ -1329,7 +1332,7 @@ class Engine : public EngineBase {
         cudaMemcpyAsync(&herr[0], kerr, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (net.err) cudaMemcpyAsync(&herr[1], net.err, sizeof(int), cudaMemcpyDeviceToHost, s);
         if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("fgmres");
-        if (herr[0]) return fail(ICEP_ERR_TIMEOUT, "fused plane pass: a bulk copy did not complete within the wait limit");
+        if (herr[0]) return fail(ICEP_ERR_TIMEOUT, "plane pass: a bulk copy did not complete within the wait limit");
         if (herr[1])
           return fail(ICEP_ERR_TIMEOUT, "network convolution: tensor-core completion did not arrive within the wait limit");
       }

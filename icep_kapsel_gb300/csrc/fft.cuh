@@ -21,6 +21,10 @@ struct FFTPlan {
   cplx<R> *tw_y = nullptr;    // exp(-2 pi i m / NY)
   cplx<R> *tw_z = nullptr;    // exp(-2 pi i m / (NZ/2))
   cplx<R> *tw_post = nullptr; // exp(-2 pi i k / NZ), k <= NZ/2
+  // device error word of the kernels with bounded waits (the FP32
+  // register-resident plane passes run only when it is set; the owner
+  // checks it)
+  int *err = nullptr;
 };
 
 template <typename R>

@@ -21,6 +21,7 @@
 
 #include "fft.cuh"
 #include "fft_blocks.cuh"
+#include "kop.cuh"
 
 namespace icep {
 
@@ -295,6 +296,9 @@ bool use_plane(const Grid &g) {
 
 template <typename R, int NY, int H>
 void launch_plane_nh(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, cudaStream_t s) {
+  if constexpr (std::is_same<R, float>::value) {
+    if (fft_plane_r(p, fb, inverse, s)) return;  // the register-resident kernels (kop.cu)
+  }
   const size_t sm = plane_smem<R>(NY, H);
   count_launch(fld<R>(p.g, 1.0 * fb.n));
   if (!inverse) {

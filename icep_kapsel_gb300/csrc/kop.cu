@@ -778,6 +778,220 @@ __global__ void __launch_bounds__(H * 8, (H >= 64) ? 2 : 4)
   if (lin == 0) bulk_s2g_wait(cplane, smem_addr(buf), BYTES);
 }
 
+// ---- register-resident plane passes of the plain 3D transforms -----------
+//
+// The two halves of k_kop_plane_r as the plane pass of the ordinary FP32
+// transforms (fft.cuh): C2R (y inverse with the j-direction half of the
+// Hermitian completion, then the z rows merged and inverse-transformed to the
+// real row, scaled) and R2C (z rows forward, then the real split and the y
+// forward). One block per (x-plane, field of the batch); the plane arrives by
+// one bulk copy and leaves by one (a real plane of NY rows of NZ+2 floats has
+// the byte size of the half-spectrum plane). A copy that does not land within
+// the wait limit sets *err (checked by the host as for the fused passes).
+
+// field f of a batch with constant indices (no local copy of the parameter)
+__device__ __forceinline__ float *batch_field(const FieldBatch<float> &fb, int f) {
+  float *q = fb.p[0];
+#pragma unroll
+  for (int c = 1; c < 5; c++)
+    if (f == c) q = fb.p[c];
+  return q;
+}
+
+template <int NY, int H>
+__global__ void __launch_bounds__(H * 8, (H >= 64) ? 2 : 4)
+    k_plane_c2r_r(FieldBatch<float> fb, const cf *__restrict__ twy, const cf *__restrict__ twz,
+                  const cf *__restrict__ post, float scale, int *err) {
+  using S = RPlane<NY, H>;
+  constexpr int TY = S::TY, PY = S::PY, TZ = S::TZ, PZ = S::PZ, RS = H + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cf *buf = reinterpret_cast<cf *>(smem_raw);
+  cf *sty = buf + S::BUF;
+  cf *stz = sty + NY;
+  cf *spost = stz + H;
+  unsigned long long *mb = reinterpret_cast<unsigned long long *>(spost + H + 1);
+  const int i = blockIdx.x;
+  cf *cplane = reinterpret_cast<cf *>(batch_field(fb, blockIdx.y)) + (long)i * S::BUF;
+  const int lin = threadIdx.x, lane = lin & 31, w = lin >> 5;
+  constexpr uint32_t BYTES = S::BUF * sizeof(cf);
+  const uint32_t mb0 = smem_addr(&mb[0]);
+  if (lin == 0) {
+    mbar_init(mb0, 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (lin == 0) {
+    mbar_expect_tx(mb0, BYTES);
+    bulk_g2s(smem_addr(buf), cplane, BYTES, mb0);
+  }
+  for (int q = lin; q < NY; q += S::NT) sty[q] = twy[q];
+  for (int q = lin; q < H; q += S::NT) stz[q] = twz[q];
+  for (int q = lin; q <= H; q += S::NT) spost[q] = post[q];
+  if (__syncthreads_or(!mbar_wait_for(mb0, 0, KOP_WAIT_NS))) {
+    if (lin == 0) atomicExch(err, 1);
+    mbar_wait_for(mb0, 0, KOP_WAIT_NS);
+    return;
+  }
+  // ---- y inverse: thread (column k, t), rows t + 8m (as in k_kop_plane_r)
+  const int t = lane & 7, kc = lane >> 3;
+  const int k = (w & 7) + 8 * kc + 32 * (w >> 3);
+  const int par = (k >> 3) & 1;
+  cf a[PY];
+  if (k == 0) {
+#pragma unroll
+    for (int m = 0; m < PY; m++) {
+      const int j = t + 8 * m, jm = (NY - j) & (NY - 1);
+      const bool low = (j >= 1 && j < NY / 2), high = (j > NY / 2);
+      const cf x0 = high ? cconj(buf[jm * RS]) : buf[j * RS];
+      const cf xh = low ? cconj(buf[jm * RS + H]) : buf[j * RS + H];
+      a[m] = cf{x0.x - xh.y, x0.y + xh.x};
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < PY; m++) a[m] = buf[(t + 8 * m) * RS + k];
+  }
+  __syncthreads();
+  reg_dft<TY, PY>(a, t, buf + k * (NY + 1), par, sty, true);
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < PY; r++) buf[(t + 8 * r) * RS + k] = a[r];
+  __syncthreads();
+  // ---- z: merge and inverse to the real row, scaled; its padding zeroed
+  {
+    const int tz = lane & (TZ - 1), jr = lane / TZ;
+#pragma unroll
+    for (int p = 0; p < S::RZ; p++) {
+      const int j = rplane_row<TZ>(w, jr, p);
+      cf *row = buf + j * RS;
+      cf z[PZ];
+#pragma unroll
+      for (int m = 0; m < PZ; m++) {
+        const int n = tz + TZ * m;
+        cf x, c;
+        if (n == 0) {
+          const cf zz = row[0];
+          x = cf{zz.x, 0.f};
+          c = cf{zz.y, 0.f};
+        } else {
+          x = row[n];
+          c = row[H - n];
+        }
+        z[m] = merge_inv(x, cconj(c), spost[n]);
+      }
+      __syncwarp();
+      reg_dft<TZ, PZ>(z, tz, row, (j >> 3) & 1, stz, true);
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < PZ; m++) row[tz + TZ * m] = cf{z[m].x * scale, z[m].y * scale};
+      if (tz == 0) row[H] = cf{0.f, 0.f};
+    }
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  if (lin == 0) bulk_s2g_wait(cplane, smem_addr(buf), BYTES);
+}
+
+template <int NY, int H>
+__global__ void __launch_bounds__(H * 8, (H >= 64) ? 2 : 4)
+    k_plane_r2c_r(FieldBatch<float> fb, const cf *__restrict__ twy, const cf *__restrict__ twz,
+                  const cf *__restrict__ post, int *err) {
+  using S = RPlane<NY, H>;
+  constexpr int TY = S::TY, PY = S::PY, TZ = S::TZ, PZ = S::PZ, RS = H + 1;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  cf *buf = reinterpret_cast<cf *>(smem_raw);
+  cf *sty = buf + S::BUF;
+  cf *stz = sty + NY;
+  cf *spost = stz + H;
+  unsigned long long *mb = reinterpret_cast<unsigned long long *>(spost + H + 1);
+  const int i = blockIdx.x;
+  cf *cplane = reinterpret_cast<cf *>(batch_field(fb, blockIdx.y)) + (long)i * S::BUF;
+  const int lin = threadIdx.x, lane = lin & 31, w = lin >> 5;
+  constexpr uint32_t BYTES = S::BUF * sizeof(cf);
+  const uint32_t mb0 = smem_addr(&mb[0]);
+  if (lin == 0) {
+    mbar_init(mb0, 1);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (lin == 0) {
+    mbar_expect_tx(mb0, BYTES);
+    bulk_g2s(smem_addr(buf), cplane, BYTES, mb0);
+  }
+  for (int q = lin; q < NY; q += S::NT) sty[q] = twy[q];
+  for (int q = lin; q < H; q += S::NT) stz[q] = twz[q];
+  for (int q = lin; q <= H; q += S::NT) spost[q] = post[q];
+  if (__syncthreads_or(!mbar_wait_for(mb0, 0, KOP_WAIT_NS))) {
+    if (lin == 0) atomicExch(err, 1);
+    mbar_wait_for(mb0, 0, KOP_WAIT_NS);
+    return;
+  }
+  // ---- z forward of each real row as an H-point complex row, in place
+  {
+    const int tz = lane & (TZ - 1), jr = lane / TZ;
+#pragma unroll
+    for (int p = 0; p < S::RZ; p++) {
+      const int j = rplane_row<TZ>(w, jr, p);
+      cf *row = buf + j * RS;
+      cf z[PZ];
+#pragma unroll
+      for (int m = 0; m < PZ; m++) z[m] = row[tz + TZ * m];
+      __syncwarp();
+      reg_dft<TZ, PZ>(z, tz, row, (j >> 3) & 1, stz, false);
+      __syncwarp();
+#pragma unroll
+      for (int m = 0; m < PZ; m++) row[tz + TZ * m] = z[m];
+    }
+  }
+  __syncthreads();
+  // ---- y forward of the split half spectrum (as in k_kop_plane_r)
+  const int t = lane & 7, kc = lane >> 3;
+  const int k = (w & 7) + 8 * kc + 32 * (w >> 3);
+  const int par = (k >> 3) & 1;
+  cf a[PY];
+  if (k == 0) {
+#pragma unroll
+    for (int m = 0; m < PY; m++) {
+      const cf z0 = buf[(t + 8 * m) * RS], c0 = cconj(z0);
+      a[m] = cf{split_fwd(z0, c0, spost[0]).x, split_fwd(z0, c0, spost[H]).x};
+    }
+  } else {
+#pragma unroll
+    for (int m = 0; m < PY; m++) {
+      const int j = t + 8 * m;
+      a[m] = split_fwd(buf[j * RS + k], cconj(buf[j * RS + H - k]), spost[k]);
+    }
+  }
+  __syncthreads();
+  reg_dft<TY, PY>(a, t, buf + k * (NY + 1), par, sty, false);
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int r = 0; r < PY; r++) {
+      const int src = (lane & ~7) | ((8 - t) & 7);
+      cf zm{__shfl_sync(0xffffffffu, a[PY - 1 - r].x, src), __shfl_sync(0xffffffffu, a[PY - 1 - r].y, src)};
+      if (t == 0) zm = a[(PY - r) & (PY - 1)];
+      if (k == 0) {
+        const cf z = a[r], zc = cconj(zm);
+        const int j = t + 8 * r;
+        buf[j * RS] = cf{0.5f * (z.x + zc.x), 0.5f * (z.y + zc.y)};
+        buf[j * RS + H] = cf{0.5f * (z.y - zc.y), -0.5f * (z.x - zc.x)};
+      }
+    }
+  }
+  if (k != 0) {
+#pragma unroll
+    for (int r = 0; r < PY; r++) buf[(t + 8 * r) * RS + k] = a[r];
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  __syncthreads();
+  if (lin == 0) bulk_s2g_wait(cplane, smem_addr(buf), BYTES);
+}
+
+template <int NY, int H>
+constexpr size_t rplane_fft_smem() {
+  return ((size_t)RPlane<NY, H>::BUF + NY + H + (H + 1)) * sizeof(cf) + sizeof(unsigned long long);
+}
+
 // Last-stage sink of the forward x transforms: acc += k_D exp(-i dx k_D/2) X_D
 template <int D>
 struct DivAcc {
@@ -1104,6 +1318,40 @@ void launch_plane_n(const FFTPlan<float> &p, float *w0, float *w1, float *w2, co
 }
 
 }  // namespace
+
+template <int NY, int H>
+bool launch_rplane_fft(const FFTPlan<float> &p, const FieldBatch<float> &fb, bool inverse, int *err, cudaStream_t s) {
+  if constexpr (!rplane_ok<NY, H>()) {
+    return false;
+  } else {
+    constexpr size_t sm = rplane_fft_smem<NY, H>();
+    static bool attr = false;  // one attribute call per instantiation
+    if (!attr) {
+      cudaFuncSetAttribute(k_plane_c2r_r<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      cudaFuncSetAttribute(k_plane_r2c_r<NY, H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      attr = true;
+    }
+    count_launch(fld<float>(p.g, 1.0 * fb.n));
+    if (inverse) {
+      const float scale = (float)(1.0 / ((double)p.g.nx * p.g.ny * p.g.nz));
+      k_plane_c2r_r<NY, H><<<dim3(p.g.nx, fb.n), RPlane<NY, H>::NT, sm, s>>>(fb, p.tw_y, p.tw_z, p.tw_post, scale,
+                                                                            err);
+    } else {
+      k_plane_r2c_r<NY, H><<<dim3(p.g.nx, fb.n), RPlane<NY, H>::NT, sm, s>>>(fb, p.tw_y, p.tw_z, p.tw_post, err);
+    }
+    return true;
+  }
+}
+
+bool fft_plane_r(const FFTPlan<float> &p, const FieldBatch<float> &fb, bool inverse, cudaStream_t s) {
+  if (!p.err || fb.n < 1) return false;
+  const int ny = p.g.ny, h = p.g.nz / 2;
+  if (ny == 128 && h == 64) return launch_rplane_fft<128, 64>(p, fb, inverse, p.err, s);
+  if (ny == 128 && h == 32) return launch_rplane_fft<128, 32>(p, fb, inverse, p.err, s);
+  if (ny == 64 && h == 64) return launch_rplane_fft<64, 64>(p, fb, inverse, p.err, s);
+  if (ny == 64 && h == 32) return launch_rplane_fft<64, 32>(p, fb, inverse, p.err, s);
+  return false;
+}
 
 bool kop_supported(const Grid &g) {
   return g.ny <= 128 && g.nz <= 128 && plane_smem_f(g.ny, g.nz / 2) <= KOP_PLANE_SMEM_MAX;

@@ -26,6 +26,11 @@ enum { KOP_P = 0, KOP_S = 1, KOP_NONE = 2, KOP_CG = 3 };
 
 // true if the fused passes cover this grid (an x-plane fits in shared memory)
 bool kop_supported(const Grid &g);
+// The plane pass of the plain FP32 3D transforms (fft.cuh) by the
+// register-resident kernels (C2R with `inverse`, else R2C) when the plan has
+// an error word (p.err) and the plane has a register kernel (NY in {64, 128},
+// NZ/2 in {32, 64}, NZ/2 <= NY); false (nothing launched) otherwise.
+bool fft_plane_r(const FFTPlan<float> &p, const FieldBatch<float> &fb, bool inverse, cudaStream_t s);
 
 // Tile choices of the fused passes: x pencils per block of the inverse and
 // forward x passes (8, 16 or 32 for NX in {64, 128}; 16 otherwise), and the

@@ -155,3 +155,31 @@ def test_autotune_picks_and_every_tile_shape(Sim, monkeypatch):
         b = outs[0][:, :, 0::2] + 1j * outs[0][:, :, 1::2]
         d = np.where(wt > 0, np.abs(a - b), 0.0)
         assert float(np.linalg.norm(d) / np.linalg.norm(np.where(wt > 0, np.abs(b), 0.0))) < 2e-6
+
+
+@pytest.mark.parametrize("n", [64, 128])
+def test_register_plane_fft_against_fp64(Sim, n):
+    """The plain FP32 3D transforms of a MIXED context run their plane pass on
+    the register-resident kernels (R2C: z rows forward, split, y forward; C2R:
+    y inverse with the Hermitian completion, z rows inverse): both against the
+    FP64 context's transforms of the same field, to FP32 accuracy, and the
+    round trip."""
+    pm, xm = cases.icep_case(n=n, npart=4, minsep=12.0, seed=3, precision=abi.MIXED,
+                             solver=abi.SOLVER_SPECTRAL)
+    pd, xd = cases.icep_case(n=n, npart=4, minsep=12.0, seed=3, precision=abi.FP64,
+                             solver=abi.SOLVER_SPECTRAL)
+    m, d = Sim(pm, xm), Sim(pd, xd)
+    rng = np.random.default_rng(n)
+    a = np.zeros((n, n, n + 2))
+    a[:, :, :n] = rng.standard_normal((n, n, n))
+    fm, fd = m.fft_r2c(a.copy()), d.fft_r2c(a.copy())
+    err = np.linalg.norm(fm - fd) / np.linalg.norm(fd)
+    assert err < 2e-6, err
+    bm, bd = m.fft_c2r(fd.copy()), d.fft_c2r(fd.copy())
+    err = np.linalg.norm(bm[:, :, :n] - bd[:, :, :n]) / np.linalg.norm(bd[:, :, :n])
+    assert err < 2e-6, err
+    assert np.abs(bm[:, :, n:]).max() == 0.0  # the padding of the real rows
+    back = m.fft_c2r(m.fft_r2c(a.copy()))
+    assert np.linalg.norm(back[:, :, :n] - a[:, :, :n]) / np.linalg.norm(a) < 2e-6
+    m.close()
+    d.close()

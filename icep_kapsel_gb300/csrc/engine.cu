@@ -562,6 +562,7 @@ class Engine : public EngineBase {
     // particle parameters (Set_global_parameters, input.cxx:286-300, 404-440)
     memset(&pp, 0, sizeof(pp));
     pp.dx = p.dx; pp.radius = radius; pp.xi = xi; pp.hxi = hxi;
+    set_band_bounds(pp);
     for (int d = 0; d < 3; d++) {
       pp.L[d] = N[d] * p.dx;
       pp.N[d] = N[d];

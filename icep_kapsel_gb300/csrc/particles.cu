@@ -220,14 +220,35 @@ __global__ void k_scatter_up(PartParams pp, const icep_particle *__restrict__ p,
 template <typename R>
 __global__ void k_scatter_normal(PartParams pp, const icep_particle *__restrict__ p, const int *__restrict__ sek, R *s0,
                                  R *s1, R *s2) {
-  // FP64 geometry in both precisions: the surface band |r - a| < xi/2 has a
-  // sharp edge, which FP32 distances would move
+  // the band |r - a| < xi/2 has a sharp edge, which FP32 distances would
+  // move: the decision is FP64's for every point near the edge
   int n, m;
-  chunk_cell(pp, p, n, m);
+  const PCell &pc = chunk_cell(pp, p, n, m);
   if (m >= pp.np_domain) return;
+  if constexpr (std::is_same<R, float>::value) {
+    // MIXED: FP32 offsets from the particle's cell (distance error < 1e-6)
+    // decide the points further than 1e-4 from the band's edges; the normal
+    // of a point inside is the FP32 unit vector
+    float r[3], dist;
+    const long im = stencil_pt<float>(pp, p[n].x, pc, sek, m, r, &dist);
+    const float off = fabsf(dist - (float)pp.radius), h = (float)pp.hxi;
+    if (off > h + 1e-4f) return;
+    if (off < h - 1e-4f) {
+      const float ir = 1.f / dist;
+      atomicAdd(s0 + im, r[0] * ir);
+      atomicAdd(s1 + im, r[1] * ir);
+      atomicAdd(s2 + im, r[2] * ir);
+      return;
+    }
+  }
   double r[3], dist;
   const long im = stencil_point(pp, p[n].x, sek, m, r, &dist);
-  const double dr = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  const double dr2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  // a conservative test on the squared distance skips the points far from
+  // the band before the FP64 square root and division (the exact test below
+  // decides every point that passes it)
+  if (dr2 < pp.band_lo2 || dr2 > pp.band_hi2) return;
+  const double dr = sqrt(dr2);
   if (fabs(dr - pp.radius) < pp.hxi) {
     const double ir = 1. / dr;
     atomicAdd(s0 + im, (R)(r[0] * ir));

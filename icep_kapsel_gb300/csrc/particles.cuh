@@ -34,7 +34,16 @@ struct PartParams {
   double eps_ave, eps_delta, sharp;
   // surface charge e Q of each species (Make_phi_qq_particle)
   double qe[ICEP_MAX_SPECIES];
+  // squared distances outside which no point is in the surface band
+  // |r - radius| < hxi (margins far above the rounding of the exact test)
+  double band_lo2, band_hi2;
 };
+// the band bounds of pp from pp.radius and pp.hxi
+inline void set_band_bounds(PartParams &pp) {
+  const double lo = pp.radius - pp.hxi, hi = pp.radius + pp.hxi;
+  pp.band_lo2 = lo > 0.0 ? lo * lo * (1.0 - 1e-12) : 0.0;
+  pp.band_hi2 = hi * hi * (1.0 + 1e-12);
+}
 
 // The Lennard-Jones constants of Set_global_parameters (input.cxx:404-440)
 // into pp: lj_eps, lj_dia = 2 a, lj_powers, the cutoff (2^(1/6), 2^(1/12)

@@ -796,7 +796,9 @@ class Engine : public EngineBase {
   // with surface charges Conc_k2charge_field (operate_electrolyte.cxx:45-74):
   // phi_id becomes the sum of Phi and rho starts from the surface charge of
   // Make_phi_qq_particle (operate_electrolyte.cxx:179-243)
-  int conc_k2charge(int rho_id, int phi_id, int tmp_id) {
+  // (tmp2_id, if given, lets both species' densities go to real space in
+  // one batched transform)
+  int conc_k2charge(int rho_id, int phi_id, int tmp_id, int tmp2_id = -1) {
     if (have_sc) {
       zero(phi_id);
       zero(rho_id);
@@ -807,6 +809,14 @@ class Engine : public EngineBase {
       // volume of the surface section normalised to sum_n |e Q_n|
       const double rescale = abs_total_qe / (hscal[S_AUX1] * P.dx * P.dx * P.dx);
       scale_copy<R>(g, f[rho_id], f[rho_id], (R)rescale, s);
+    }
+    if (tmp2_id >= 0) {
+      copy(tmp_id, F_C0);
+      copy(tmp2_id, F_C1);
+      c2r(f[tmp_id], f[tmp2_id]);
+      charge_add<R>(g, f[rho_id], f[tmp_id], f[phi_id], valency_e[0], !have_sc, s);
+      charge_add<R>(g, f[rho_id], f[tmp2_id], f[phi_id], valency_e[1], false, s);
+      return ICEP_OK;
     }
     for (int n = 0; n < 2; n++) {
       copy(tmp_id, F_C0 + n);
@@ -1749,18 +1759,10 @@ class Engine : public EngineBase {
     return ICEP_OK;
   }
 
-  // staggered gradient of a real field (R2C, i k, shift, C2R), the field kept
-  void staggered_grad(int a_id, int g0, int tmp) {
-    copy(tmp, a_id);
-    r2c(f[tmp]);
-    grad_k<R>(g, f[tmp], f[g0], f[g0 + 1], f[g0 + 2], R(1), true, nullptr, s);
-    c2r(f[g0], f[g0 + 1], f[g0 + 2]);
-  }
-
   // Make_Maxwell_force_x_on_fluid (operate_dielectric.cxx:611-764)
   int maxwell_force(int rho_id) {
     make_dielectric_field(F_F0, F_WORK);
-    int st = conc_k2charge(rho_id, F_F0, F_F1);
+    int st = conc_k2charge(rho_id, F_F0, F_F1, F_F2);
     if (st) return st;
     st = solve_potential(rho_id, F_POT, F_F2);
     if (st) return st;
@@ -1776,8 +1778,16 @@ class Engine : public EngineBase {
   }
   // the face force into F_WV3_0..2 (operate_dielectric.cxx:651-755)
   void maxwell_face_force(int rho_id) {
-    staggered_grad(F_EPS, F_GE0, F_WV1);
-    staggered_grad(F_POT, F_F0, F_WV1);
+    // the staggered gradients of eps (F_GE0..2) and of the potential
+    // (F_F0..2), both spectra from one batched transform (F_KT is free after
+    // the solve)
+    copy(F_WV1, F_EPS);
+    copy(F_KT, F_POT);
+    r2c(f[F_WV1], f[F_KT]);
+    grad_k<R>(g, f[F_WV1], f[F_GE0], f[F_GE1], f[F_GE2], R(1), true, nullptr, s);
+    grad_k<R>(g, f[F_KT], f[F_F0], f[F_F1], f[F_F2], R(1), true, nullptr, s);
+    c2r(f[F_GE0], f[F_GE1], f[F_GE2]);
+    c2r(f[F_F0], f[F_F1], f[F_F2]);
     maxwell_e2<R>(g, f[F_F0], f[F_F1], f[F_F2], f[F_WV1], ext_now[0], ext_now[1], ext_now[2], P.external_field, s);
     maxwell_face<R>(g, vec(F_F0), vec(F_WV3_0), f[rho_id], f[F_WV1], vec(F_GE0), ext_now[0], ext_now[1], ext_now[2],
                     P.external_field, s);
@@ -1836,7 +1846,7 @@ class Engine : public EngineBase {
       }
       f_hydro<R>(pp, dp, dsek, f[F_PHI_SUM], f[F_U0], f[F_U1], f[F_U2], true, s);
       make_dielectric_field(F_F0, F_WORK);
-      return conc_k2charge(F_UP0, F_F0, F_F1);
+      return conc_k2charge(F_UP0, F_F0, F_F1, F_F2);
     }
     return ICEP_OK;
   }

@@ -1213,6 +1213,22 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_cg(Grid g, float *xt, float 
   }
 }
 
+// w_d *= ef_d at the real points (the product of the split plane step)
+__global__ void k_kop_eps_mul(Grid g, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
+                              const float *ef2) {
+  const long tl = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tl >= g.nreal()) return;
+  const unsigned t = (unsigned)tl;
+  const unsigned plane = (unsigned)g.ny * (unsigned)g.nz;
+  const int i = (int)(t / plane);
+  const unsigned rem = t - (unsigned)i * plane;
+  const int j = (int)(rem / (unsigned)g.nz), k = (int)(rem - (unsigned)j * (unsigned)g.nz);
+  const long im = gidx(g, i, j, k);
+  w0[im] *= ef0[im];
+  w1[im] *= ef1[im];
+  w2[im] *= ef2[im];
+}
+
 __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2) {
   const long tl = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tl >= g.nreal()) return;
@@ -1353,8 +1369,14 @@ bool fft_plane_r(const FFTPlan<float> &p, const FieldBatch<float> &fb, bool inve
   return false;
 }
 
-bool kop_supported(const Grid &g) {
+// an x-plane of the three fields fits in one block's shared memory
+bool kop_plane_fits(const Grid &g) {
   return g.ny <= 128 && g.nz <= 128 && plane_smem_f(g.ny, g.nz / 2) <= KOP_PLANE_SMEM_MAX;
+}
+bool kop_supported(const Grid &g) {
+  // larger planes (up to 256^2) take the split plane step: the plain
+  // transform's separate y-pencil and z-row passes around the product
+  return kop_plane_fits(g) || (g.nx <= 256 && g.ny <= 256 && g.nz <= 256);
 }
 
 // (an upper bound over the x-pass variants: at least 8 pencils per block)
@@ -1396,6 +1418,20 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
 
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
                const float *ef2, int *err, cudaStream_t s, const KopTiles &t) {
+  if (!kop_plane_fits(p.g)) {
+    // the split plane step: inverse y and z transforms (scaled), the face
+    // permittivity product in real space, forward z and y transforms
+    FieldBatch<float> fb{};
+    fb.p[0] = w0;
+    fb.p[1] = w1;
+    fb.p[2] = w2;
+    fb.n = 3;
+    fft_pass(p, fb, 3, s);
+    count_launch(fld<float>(p.g, 9));
+    k_kop_eps_mul<<<(unsigned)div_up(p.g.nreal(), 256), 256, 0, s>>>(p.g, w0, w1, w2, ef0, ef1, ef2);
+    fft_pass(p, fb, 0, s);
+    return;
+  }
   const bool smem = t.plane_smem != 0;
   switch (p.g.ny) {
     case 16: launch_plane_n<16>(p, w0, w1, w2, ef0, ef1, ef2, err, s, smem); break;

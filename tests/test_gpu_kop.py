@@ -66,8 +66,10 @@ def apply_b_fp64(ph, eps, n):
     return out
 
 
-@pytest.mark.parametrize("n", [32, 64, 128])
+@pytest.mark.parametrize("n", [32, 64, 128, 256])
 def test_fused_operator_against_fp64(Sim, n):
+    """The fused operator B = A M^-1 against an FP64 restatement; 256^3 takes
+    the split plane step (its x-plane does not fit in shared memory)."""
     p, parts = cases.icep_case(n=n, npart=max(4, n // 8), minsep=10.0, seed=7, eps_f=80.0, eps_p=2.0,
                                e_ext=(0.0, 0.0, 0.1), tol=1e-8, solver=abi.SOLVER_SPECTRAL,
                                precision=abi.MIXED)

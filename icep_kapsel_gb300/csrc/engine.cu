@@ -814,8 +814,7 @@ class Engine : public EngineBase {
       copy(tmp_id, F_C0);
       copy(tmp2_id, F_C1);
       c2r(f[tmp_id], f[tmp2_id]);
-      charge_add<R>(g, f[rho_id], f[tmp_id], f[phi_id], valency_e[0], !have_sc, s);
-      charge_add<R>(g, f[rho_id], f[tmp2_id], f[phi_id], valency_e[1], false, s);
+      charge_add2<R>(g, f[rho_id], f[tmp_id], f[tmp2_id], f[phi_id], valency_e[0], valency_e[1], !have_sc, s);
       return ICEP_OK;
     }
     for (int n = 0; n < 2; n++) {
@@ -1810,9 +1809,7 @@ class Engine : public EngineBase {
       // whose real values the electric and advective fluxes take, one pass
       grad_trunc_copy<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n], (R)(P.kbt * onsager[n]), s);
       c2r(f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n]);
-      np_flux_electric<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_F0), onsager[n] * valency_e[n], s);
-      np_impermeability<R>(g, vec(F_UP0), vec(F_SN0), s);
-      np_flux_advection<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_U0), s);
+      np_flux<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_F0), onsager[n] * valency_e[n], vec(F_SN0), vec(F_U0), s);
       r2c(f[F_UP0], f[F_UP1], f[F_UP2]);
       div_k<R>(g, f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n], false, s);
     }
@@ -1958,8 +1955,7 @@ class Engine : public EngineBase {
       for (int n = 0; n < 2; n++) {
         grad_trunc_copy<R>(g, f[F_C0 + n], f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n], (R)(P.kbt * onsager[n]), s);
         c2r(f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n]);
-        np_flux_electric<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_F0), onsager[n] * valency_e[n], s);
-        np_impermeability<R>(g, vec(F_UP0), vec(F_SN0), s);
+        np_flux<R>(g, vec(F_UP0), f[F_CRHS0 + n], vec(F_F0), onsager[n] * valency_e[n], vec(F_SN0), nullptr, s);
         r2c(f[F_UP0], f[F_UP1], f[F_UP2]);
         div_k<R>(g, f[F_UP0], f[F_UP1], f[F_UP2], f[F_CRHS0 + n], false, s);
       }

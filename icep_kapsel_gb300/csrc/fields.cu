@@ -493,6 +493,16 @@ __global__ void k_charge_add(Grid g, R *rho, const R *c, const R *phi, R ze, int
   rho[p.im] = first ? v : rho[p.im] + v;
 }
 
+// both species in one pass, the sums in the order of two k_charge_add passes
+template <typename R>
+__global__ void k_charge_add2(Grid g, R *rho, const R *c0, const R *c1, const R *phi, R ze0, R ze1, int first) {
+  Pt p;
+  if (!pt_of(g, TID, p)) return;
+  const R ph = R(1) - phi[p.im];
+  const R v0 = ze0 * c0[p.im] * ph, v1 = ze1 * c1[p.im] * ph;
+  rho[p.im] = (first ? v0 : rho[p.im] + v0) + v1;
+}
+
 // the solute charge of the field output (output.cxx:286-297):
 // (e z_0 c_0 + e z_1 c_1) (1 - phi)
 template <typename R>
@@ -581,36 +591,34 @@ __global__ void k_maxwell_face(Grid g, V3<R> grad_pot, V3<R> out, const R *rho, 
   }
 }
 
+// One species' flux in one pass, the flux held in registers between the
+// terms: the diffusion flux (read) plus the electric term L z e c grad(pot)
+// (Solute_solver_rhs_nonlinear_x_single, solute_rhs.cxx:150-189), the normal
+// component removed where the surface normal is non-zero
+// (Solute_impermeability, :42-97), then the advective flux -c u
+// (Add_advection_flux, :190-210) when u is given.
 template <typename R>
-__global__ void k_np_flux_electric(Grid g, V3<R> flux, const R *c, V3<R> gp, R lz) {
+__global__ void k_np_flux(Grid g, V3<R> flux, const R *c, V3<R> gp, R lz, V3<R> sn, V3<R> u) {
   Pt p;
   if (!pt_of(g, TID, p)) return;
   const R cc = c[p.im];
+  R f[3];
 #pragma unroll
-  for (int d = 0; d < 3; d++) flux.p[d][p.im] = flux.p[d][p.im] + cc * (gp.p[d][p.im] * lz);
-}
-
-template <typename R>
-__global__ void k_np_imperm(Grid g, V3<R> flux, V3<R> sn) {
-  Pt p;
-  if (!pt_of(g, TID, p)) return;
+  for (int d = 0; d < 3; d++) f[d] = flux.p[d][p.im] + cc * (gp.p[d][p.im] * lz);
   const R n0 = sn.p[0][p.im], n1 = sn.p[1][p.im], n2 = sn.p[2][p.im];
   const R nn = n0 * n0 + n1 * n1 + n2 * n2;
-  if (!(nn > R(0))) return;
-  const R f0 = flux.p[0][p.im], f1 = flux.p[1][p.im], f2 = flux.p[2][p.im];
-  const R dd = (f0 * n0 + f1 * n1 + f2 * n2) / nn;
-  flux.p[0][p.im] = f0 - n0 * dd;
-  flux.p[1][p.im] = f1 - n1 * dd;
-  flux.p[2][p.im] = f2 - n2 * dd;
-}
-
-template <typename R>
-__global__ void k_np_flux_adv(Grid g, V3<R> flux, const R *c, V3<R> u) {
-  Pt p;
-  if (!pt_of(g, TID, p)) return;
-  const R cc = c[p.im];
+  if (nn > R(0)) {
+    const R dd = (f[0] * n0 + f[1] * n1 + f[2] * n2) / nn;
+    f[0] = f[0] - n0 * dd;
+    f[1] = f[1] - n1 * dd;
+    f[2] = f[2] - n2 * dd;
+  }
+  if (u.p[0]) {
 #pragma unroll
-  for (int d = 0; d < 3; d++) flux.p[d][p.im] += cc * -u.p[d][p.im];
+    for (int d = 0; d < 3; d++) f[d] += cc * -u.p[d][p.im];
+  }
+#pragma unroll
+  for (int d = 0; d < 3; d++) flux.p[d][p.im] = f[d];
 }
 
 template <typename R>
@@ -716,6 +724,10 @@ template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R
   count_launch(fld<R>(g, first ? 3.0 : 4.0));
   k_charge_add<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c, phi, (R)ze, first ? 1 : 0);
 }
+template <typename R> void charge_add2(const Grid &g, R *rho, const R *c0, const R *c1, const R *phi, double ze0, double ze1, bool first, cudaStream_t s) {
+  count_launch(fld<R>(g, first ? 4.0 : 5.0));
+  k_charge_add2<R><<<nblk_real(g), TPB, 0, s>>>(g, rho, c0, c1, phi, (R)ze0, (R)ze1, first ? 1 : 0);
+}
 template <typename R>
 void solute_charge(const Grid &g, R *out, const R *c0, const R *c1, const R *phi, double ze0, double ze1, cudaStream_t s) {
   count_launch(fld<R>(g, 4));
@@ -751,17 +763,9 @@ template <typename R> void maxwell_face(const Grid &g, R *const *grad_pot, R *co
   count_launch(fld<R>(g, 11));
   k_maxwell_face<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(grad_pot), v3(out), rho, w1, v3(ge), (R)e0, (R)e1, (R)e2, ext);
 }
-template <typename R> void np_flux_electric(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, cudaStream_t s) {
-  count_launch(fld<R>(g, 7));
-  k_np_flux_electric<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(gp), (R)L_ze);
-}
-template <typename R> void np_impermeability(const Grid &g, R *const *flux, R *const *sn, cudaStream_t s) {
-  count_launch(fld<R>(g, 9));
-  k_np_imperm<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), v3(sn));
-}
-template <typename R> void np_flux_advection(const Grid &g, R *const *flux, const R *c, R *const *u, cudaStream_t s) {
-  count_launch(fld<R>(g, 10));
-  k_np_flux_adv<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(u));
+template <typename R> void np_flux(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, R *const *sn, R *const *u, cudaStream_t s) {
+  count_launch(fld<R>(g, u ? 13.0 : 10.0));
+  k_np_flux<R><<<nblk_real(g), TPB, 0, s>>>(g, v3(flux), c, v3(gp), (R)L_ze, v3(sn), u ? v3(u) : V3<R>{});
 }
 template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s) {
   count_launch(fld<R>(g, 1));
@@ -814,6 +818,7 @@ void pb_energy_terms(const Grid &g, const R *c0, const R *c1, const R *phi, R *c
   template void eps_from_profile<R>(const Grid &, R *, const R *, const R *, double, double, double, cudaStream_t);    \
   template void eps_janus<R>(const Grid &, R *, const R *, const R *, double, double, cudaStream_t);                   \
   template void charge_add<R>(const Grid &, R *, const R *, const R *, double, bool, cudaStream_t);                    \
+  template void charge_add2<R>(const Grid &, R *, const R *, const R *, const R *, double, double, bool, cudaStream_t); \
   template void solute_charge<R>(const Grid &, R *, const R *, const R *, const R *, double, double, cudaStream_t);     \
   template void eps_face_mul<R>(const Grid &, R *, R *, R *, const R *, cudaStream_t);                                 \
   template void eps_face_E<R>(const Grid &, R *, R *, R *, const R *, double, double, double, cudaStream_t);           \
@@ -824,9 +829,8 @@ void pb_energy_terms(const Grid &g, const R *c0, const R *c1, const R *phi, R *c
   template void maxwell_face<R>(const Grid &, R *const *, R *const *, const R *, const R *, R *const *, double, double, \
                                 double,                                                                                \
                                 int, cudaStream_t);                                                                    \
-  template void np_flux_electric<R>(const Grid &, R *const *, const R *, R *const *, double, cudaStream_t);            \
-  template void np_impermeability<R>(const Grid &, R *const *, R *const *, cudaStream_t);                              \
-  template void np_flux_advection<R>(const Grid &, R *const *, const R *, R *const *, cudaStream_t);                   \
+  template void np_flux<R>(const Grid &, R *const *, const R *, R *const *, double, R *const *, R *const *,          \
+                           cudaStream_t);                                                                              \
   template void fill_real<R>(const Grid &, R *, R, cudaStream_t);                                                    \
   template void pb_energy_terms<R>(const Grid &, const R *, const R *, const R *, R *, const R *, double, double,     \
                                    const double *, double, int, R *, R *, cudaStream_t);

@@ -61,6 +61,8 @@ template <typename R> void eps_from_profile(const Grid &g, R *eps, const R *phi_
 template <typename R> void eps_janus(const Grid &g, R *eps, const R *phi_sin, const R *eps_j, double ef, double dc, cudaStream_t s);
 // rho += ze c (1 - phi) (Conc_k2charge_field_no_surfase_charge, operate_dielectric.cxx:135-160)
 template <typename R> void charge_add(const Grid &g, R *rho, const R *c, const R *phi, double ze, bool first, cudaStream_t s);
+// both species at once: rho (= or +=) ze0 c0 (1 - phi) then + ze1 c1 (1 - phi)
+template <typename R> void charge_add2(const Grid &g, R *rho, const R *c0, const R *c1, const R *phi, double ze0, double ze1, bool first, cudaStream_t s);
 // out = (ze0 c0 + ze1 c1) (1 - phi) (real points): the solute charge of the field output
 template <typename R>
 void solute_charge(const Grid &g, R *out, const R *c0, const R *c1, const R *phi, double ze0, double ze1, cudaStream_t s);
@@ -81,10 +83,10 @@ template <typename R> void maxwell_e2(const Grid &g, const R *f0, const R *f1, c
 // out = face force from the staggered potential gradient grad_pot, the face
 // charge and |E|^2 and the staggered permittivity gradient ge
 template <typename R> void maxwell_face(const Grid &g, R *const *grad_pot, R *const *out, const R *rho, const R *w1, R *const *ge, double e0, double e1, double e2, int ext, cudaStream_t s);
-// Nernst-Planck fluxes (solute_rhs.cxx:150-210, 42-97)
-template <typename R> void np_flux_electric(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, cudaStream_t s);
-template <typename R> void np_impermeability(const Grid &g, R *const *flux, R *const *sn, cudaStream_t s);
-template <typename R> void np_flux_advection(const Grid &g, R *const *flux, const R *c, R *const *u, cudaStream_t s);
+// Nernst-Planck flux of one species in place: flux (the diffusion flux) + L_ze c gp, its
+// component along the surface normal sn removed where sn != 0, then - c u
+// when u is given (solute_rhs.cxx:150-210, 42-97)
+template <typename R> void np_flux(const Grid &g, R *const *flux, const R *c, R *const *gp, double L_ze, R *const *sn, R *const *u, cudaStream_t s);
 // real-space fill (k < NZ) of a constant
 template <typename R> void fill_real(const Grid &g, R *a, R v, cudaStream_t s);
 // The per-point terms of the free energy of Calc_free_energy_PB's Dielectric

@@ -124,11 +124,14 @@ struct GPencilsXInv {
   __device__ __forceinline__ cplx<R> load(int w, int e) const {
     if (w >= g.nvalid) return cplx<R>{0, 0};
     const long q = g.base + w;  // pencil index j*hnz + kz
-    const int j = (int)(q / hnz), kz = (int)(q - (long)j * hnz);
     const cplx<R> v = g.data[q + e * g.estride];
-    if ((j == 0 || j == ny / 2) && (kz == 0 || kz == hnz - 1)) {
+    // the four special pencils by their indices (no division per load):
+    // kz = 0 at q = 0 and (NY/2) hnz, kz = NZ/2 at hnz - 1 and (NY/2) hnz + hnz - 1
+    const long qh = (long)(ny / 2) * hnz;
+    const bool kz0 = (q == 0 || q == qh), kzh = (q == hnz - 1 || q == qh + hnz - 1);
+    if (kz0 || kzh) {
       if (e == 0 || e == nx / 2) return cplx<R>{v.x, R(0)};
-      const bool kept = (kz == 0) ? (e <= nx / 2) : (e > nx / 2);
+      const bool kept = kz0 ? (e <= nx / 2) : (e > nx / 2);
       if (!kept) return cconj(g.data[q + (nx - e) * g.estride]);
     }
     return v;

@@ -545,12 +545,14 @@ __device__ __forceinline__ void reg_dft(cf *x, int t, cf *reg, int par, const cf
 }
 
 // shared -> global bulk copy of `bytes` from this CTA (16-byte aligned
-// addresses, size a multiple of 16), waited for before the CTA goes on
+// addresses, size a multiple of 16) as the CTA's last step: waited for until
+// the shared memory has been read (the writes complete with the grid), so
+// the CTA's slot is released without waiting for them
 __device__ __forceinline__ void bulk_s2g_wait(void *dst, uint32_t src, uint32_t bytes) {
   asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
                : "memory");
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
 
 // Thread shapes of the register plane pass: y transforms on TY = 8 threads

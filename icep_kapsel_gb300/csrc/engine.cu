@@ -1610,9 +1610,8 @@ class Engine : public EngineBase {
     const bool all[3] = {true, true, true};
     dfl *w0 = df(D_W3_0), *w1 = df(D_W3_1), *w2 = df(D_W3_2);
     rf_grad(g, rtab, df(D_X), w0, w1, w2, s);
-    fft_c2r(fftdf, batch(w0, w1, w2), s);
-    rf_eps_face_mul(g, w0, w1, w2, (const float *)f[F_EPS], s);
-    fft_r2c(fftdf, batch(w0, w1, w2), s);
+    // inverse transforms, times the face permittivity, forward transforms
+    fft_c2r_eps_r2c(fftdf, batch(w0, w1, w2), (const float *)f[F_EPS], s);
     rf_div_combine(g, rtab, w0, w1, w2, all, df(D_B), df(D_R), RF_RESIDUAL, prescale, false, partials, scal, S_RR,
                    s, prescale_dev);
     matvecs++;

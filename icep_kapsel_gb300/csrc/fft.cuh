@@ -38,6 +38,15 @@ void fft_r2c(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s);
 template <typename R>
 void fft_c2r(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s);
 
+// The float-float residual's operator core in one sequence: the inverse
+// transform of the three fields of fb, each field d times the face
+// permittivity 0.5 (eps + eps at the next point along d) (eps: the FP32
+// permittivity, real layout), and the forward transform; the z-row passes
+// and the product run as one kernel. The same results as fft_c2r, the
+// product and fft_r2c (instantiated for the float-float type).
+template <typename R>
+void fft_c2r_eps_r2c(const FFTPlan<R> &p, const FieldBatch<R> &fb, const float *eps, cudaStream_t s);
+
 // Single passes of the 3D transforms: 0 = z rows + y pencils forward (one
 // plane kernel when an x-plane fits in shared memory), 1 = x pencils forward,
 // 2 = x pencils inverse, 3 = y pencils + z rows inverse.

@@ -10,5 +10,6 @@ template int fft_plan_init<dfl>(FFTPlan<dfl> &, const Grid &, cudaStream_t);
 template void fft_plan_free<dfl>(FFTPlan<dfl> &);
 template void fft_r2c<dfl>(const FFTPlan<dfl> &, const FieldBatch<dfl> &, cudaStream_t);
 template void fft_c2r<dfl>(const FFTPlan<dfl> &, const FieldBatch<dfl> &, cudaStream_t);
+template void fft_c2r_eps_r2c<dfl>(const FFTPlan<dfl> &, const FieldBatch<dfl> &, const float *, cudaStream_t);
 
 }  // namespace icep

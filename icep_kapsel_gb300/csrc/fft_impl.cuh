@@ -224,6 +224,87 @@ __global__ void __launch_bounds__(512) k_rows(FieldBatch<R> fb, Grid g, const cp
   }
 }
 
+// The residual's z rows in one pass for the three gradient components of the
+// float-float operator (blockIdx.y = d): the inverse row transform as k_rows,
+// scaled, times the face permittivity 0.5 (eps + eps at the next point along
+// d) (the product of refine.cu's eps-face pass, same arithmetic), and the
+// forward row transform as k_rows: the real rows stay in shared memory.
+template <typename R, int H, int W>
+__global__ void __launch_bounds__(512) k_rows_eps(FieldBatch<R> fb, Grid g, const cplx<R> *__restrict__ tw,
+                                                  const cplx<R> *__restrict__ post, R scale,
+                                                  const float *__restrict__ eps) {
+  extern __shared__ unsigned char smem_raw[];
+  const int sw = W + 1;
+  cplx<R> *tws = reinterpret_cast<cplx<R> *>(smem_raw);
+  cplx<R> *spost = tws + H;
+  cplx<R> *A = spost + (H + 1);
+  cplx<R> *B = A + (H + 2) * sw;
+  const int d = blockIdx.y;
+  R *data = fb.p[0];
+#pragma unroll
+  for (int c = 1; c < 3; c++)
+    if (d == c) data = fb.p[c];
+  const long nrows = (long)g.nx * g.ny;
+  const long row0 = (long)blockIdx.x * W;
+  const int nthr = blockDim.x * blockDim.y, lin = threadIdx.y * blockDim.x + threadIdx.x;
+  load_table(tws, tw, H);
+  load_table(spost, post, H + 1);
+  constexpr int st = Plan<H>::nstages;
+  // inverse, as k_rows
+  for (int q = lin; q < W * (H + 1); q += nthr) {
+    const int w = q / (H + 1), k = q - w * (H + 1);
+    const long row = row0 + w;
+    cplx<R> v{0, 0};
+    if (row < nrows) {
+      const R *rp = data + row * g.nzp;
+      v = cplx<R>{rp[2 * k], (k == 0 || k == H) ? R(0) : rp[2 * k + 1]};
+    }
+    B[k * sw + w] = v;
+  }
+  __syncthreads();
+  for (int q = lin; q < W * H; q += nthr) {
+    const int w = q / H, k = q - w * H;
+    A[k * sw + w] = merge_inv(B[k * sw + w], cconj(B[(H - k) * sw + w]), spost[k]);
+  }
+  __syncthreads();
+  cplx<R> *X = (st & 1) ? B : A;
+  block_fft<R, H, W>(SmemT<R>{A, sw}, SmemT<R>{X, sw}, A, B, sw, tws, true);
+  // the real row values (2m, 2m+1) at X[m], scaled and times the face
+  // permittivity of component d
+  for (int q = lin; q < W * H; q += nthr) {
+    const int w = q / H, m = q - w * H;
+    const long row = row0 + w;
+    if (row >= nrows) continue;
+    const int i = (int)(row / g.ny), j = (int)(row - (long)i * g.ny);
+    const cplx<R> v = X[m * sw + w];
+    R x[2] = {v.x * scale, v.y * scale};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int k = 2 * m + h;
+      const long im = gidx(g, i, j, k);
+      const long nb = (d == 0) ? gidx(g, (i + 1) & (g.nx - 1), j, k)
+                               : (d == 1) ? gidx(g, i, (j + 1) & (g.ny - 1), k) : gidx(g, i, j, (k + 1) & (g.nz - 1));
+      x[h] = x[h] * half_of(two_sum(eps[im], eps[nb]));
+    }
+    X[m * sw + w] = cplx<R>{x[0], x[1]};
+  }
+  __syncthreads();
+  // forward, as k_rows, from X (the other tile the ping-pong partner)
+  cplx<R> *Y = (X == A) ? B : A;
+  cplx<R> *Z = (st & 1) ? Y : X;
+  block_fft<R, H, W>(SmemT<R>{X, sw}, SmemT<R>{Z, sw}, X, Y, sw, tws, false);
+  for (int q = lin; q < W * (H + 1); q += nthr) {
+    const int w = q / (H + 1), k = q - w * (H + 1);
+    const long row = row0 + w;
+    if (row >= nrows) continue;
+    const int k1 = (k == H) ? 0 : k, k2 = (k == 0) ? 0 : H - k;
+    const cplx<R> xo = split_fwd(Z[k1 * sw + w], cconj(Z[k2 * sw + w]), spost[k]);
+    R *rp = data + row * g.nzp;
+    rp[2 * k] = xo.x;
+    rp[2 * k + 1] = xo.y;
+  }
+}
+
 template <typename R>
 constexpr int pencil_width() {
   return (sizeof(R) == 8) ? 8 : 16;
@@ -367,6 +448,23 @@ void launch_rows_n(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, c
   else k_rows<R, H, false, W><<<grid, block, row_smem<R>(H), s>>>(fb, g, p.tw_z, p.tw_post, scale);
 }
 
+template <typename R, int H>
+void launch_rows_eps_n(const FFTPlan<R> &p, const FieldBatch<R> &fb, const float *eps, cudaStream_t s) {
+  const Grid &g = p.g;
+  constexpr int W = row_width<R>();
+  static bool attr = false;  // one attribute call per instantiation
+  if (!attr) {
+    cudaFuncSetAttribute(k_rows_eps<R, H, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)row_smem<R>(H));
+    attr = true;
+  }
+  const dim3 grid(div_up((long)g.nx * g.ny, W), 3);
+  const dim3 block(W, H / 8 < 512 / W ? H / 8 : 512 / W);
+  const R scale = from_double<R>(1.0 / ((double)g.nx * g.ny * g.nz));
+  // the two half passes of each field and the permittivity read
+  count_launch(fld<R>(g, 3.0) + fld<float>(g, 1.0));
+  k_rows_eps<R, H, W><<<grid, block, row_smem<R>(H), s>>>(fb, g, p.tw_z, p.tw_post, scale, eps);
+}
+
 template <typename R>
 void launch_rows(const FFTPlan<R> &p, const FieldBatch<R> &fb, bool inverse, cudaStream_t s) {
   switch (p.g.nz / 2) {
@@ -465,6 +563,22 @@ template <typename R>
 void fft_c2r(const FFTPlan<R> &p, const FieldBatch<R> &fb, cudaStream_t s) {
   fft_pass(p, fb, 2, s);
   fft_pass(p, fb, 3, s);
+}
+
+template <typename R>
+void fft_c2r_eps_r2c(const FFTPlan<R> &p, const FieldBatch<R> &fb, const float *eps, cudaStream_t s) {
+  launch_pencils(p, fb, 0, true, s);  // x inverse
+  launch_herm_columns(p, fb, s);
+  launch_pencils(p, fb, 1, true, s);  // y inverse
+  switch (p.g.nz / 2) {               // z rows inverse, the product, z rows forward
+    case 8: launch_rows_eps_n<R, 8>(p, fb, eps, s); break;
+    case 16: launch_rows_eps_n<R, 16>(p, fb, eps, s); break;
+    case 32: launch_rows_eps_n<R, 32>(p, fb, eps, s); break;
+    case 64: launch_rows_eps_n<R, 64>(p, fb, eps, s); break;
+    default: launch_rows_eps_n<R, 128>(p, fb, eps, s); break;
+  }
+  launch_pencils(p, fb, 1, false, s);  // y forward
+  launch_pencils(p, fb, 0, false, s);  // x forward
 }
 
 template <typename R>

@@ -141,6 +141,8 @@ enum FieldId {
   F_KR, F_KR0, F_KP, F_KV, F_KS, F_KT, F_KX, F_KB, F_KY, F_KZ,
   // face permittivities of the fused k-space operator
   F_EF0, F_EF1, F_EF2,
+  // the fused operator's fourth work field (its z component)
+  F_WV3_3,
   F_COUNT
 };
 

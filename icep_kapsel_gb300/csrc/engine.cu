@@ -635,7 +635,7 @@ class Engine : public EngineBase {
         kop_tuned = true;  // picks set by hand: reported with no timings
       } else if constexpr (std::is_same<R, float>::value) {
         if (!(at && at[0] == '0')) {
-          kop_tiles = kop_autotune(fft, f[F_KP], f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2],
+          kop_tiles = kop_autotune(fft, f[F_KP], f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_WV3_3], f[F_EF0], f[F_EF1], f[F_EF2],
                                    f[F_KV], kerr, s, kop_tune_us);
           kop_tuned = true;
         }
@@ -1051,16 +1051,16 @@ class Engine : public EngineBase {
     if constexpr (std::is_same<R, float>::value) {
       float *r = f[F_KR], *r0 = f[F_KR0], *p = f[F_KP], *v = f[F_KV];
       float *sv = f[F_KS], *t = f[F_KT], *xt = f[F_KY];
-      float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2];
+      float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2], *w3 = f[F_WV3_3];
       const int nb = kop_npb;
       double *P1 = kpart, *P2 = kpart + 2 * nb, *P3 = kpart + 4 * nb;
       double *F1 = kfin, *F2 = kfin + 2, *F3 = kfin + 4;  // final sums; kfin[6] holds the error word
-      kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, s, kst, kop_tiles);
-      kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
-      kop_xfwd(fft, w0, w1, w2, v, KOP_P, r0, P1, F1, kcnt, s, kop_tiles);
-      kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, s, kst, kop_tiles);
-      kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
-      kop_xfwd(fft, w0, w1, w2, t, KOP_S, sv, P2, F2, kcnt + 1, s, kop_tiles);
+      kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, s, kst, kop_tiles);
+      kop_plane(fft, w0, w1, w2, w3, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
+      kop_xfwd(fft, w0, w2, w3, v, KOP_P, r0, P1, F1, kcnt, s, kop_tiles);
+      kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, s, kst, kop_tiles);
+      kop_plane(fft, w0, w1, w2, w3, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
+      kop_xfwd(fft, w0, w2, w3, t, KOP_S, sv, P2, F2, kcnt + 1, s, kop_tiles);
       kop_xr(g, xt, r, p, sv, t, r0, 0.0, F1, F2, P3, F3, kcnt + 2, s, kst, maxit);
     }
   }
@@ -1071,13 +1071,13 @@ class Engine : public EngineBase {
   void kf_cg_iteration(int maxit) {
     if constexpr (std::is_same<R, float>::value) {
       float *r = f[F_KR], *p = f[F_KP], *v = f[F_KV], *xt = f[F_KY];
-      float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2];
+      float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2], *w3 = f[F_WV3_3];
       const int nb = kop_npb;
       double *P1 = kpart, *P3 = kpart + 4 * nb;
       double *F1 = kfin, *F3 = kfin + 4;
-      kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, 1.0, w0, w1, w2, s, kst, kop_tiles);
-      kop_plane(fft, w0, w1, w2, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
-      kop_xfwd(fft, w0, w1, w2, v, KOP_CG, p, P1, F1, kcnt, s, kop_tiles, kst);
+      kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, 1.0, w0, w1, s, kst, kop_tiles);
+      kop_plane(fft, w0, w1, w2, w3, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
+      kop_xfwd(fft, w0, w2, w3, v, KOP_CG, p, P1, F1, kcnt, s, kop_tiles, kst);
       kop_cg(g, xt, r, p, v, F1, P3, F3, kcnt + 2, s, kst, maxit, false);
     }
   }
@@ -1208,10 +1208,11 @@ class Engine : public EngineBase {
   // out = B x~ through the fused passes (no vector update, no dots)
   void apply_Bk(float *xt, float *out) {
     if constexpr (std::is_same<R, float>::value) {
-      kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, mean_eps_cached, f[F_WV3_0], f[F_WV3_1],
-               f[F_WV3_2], s, nullptr, kop_tiles);
-      kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
-      kop_xfwd(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], out, KOP_NONE, nullptr, nullptr, nullptr, nullptr, s,
+      kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, mean_eps_cached, f[F_WV3_0], f[F_WV3_1], s,
+               nullptr, kop_tiles);
+      kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_WV3_3], f[F_EF0], f[F_EF1], f[F_EF2], kerr, s,
+                kop_tiles);
+      kop_xfwd(fft, f[F_WV3_0], f[F_WV3_2], f[F_WV3_3], out, KOP_NONE, nullptr, nullptr, nullptr, nullptr, s,
                kop_tiles);
       matvecs++;
     }
@@ -2513,7 +2514,7 @@ class Engine : public EngineBase {
       if (kernel == 1) {
         word = kerr;
         cudaMemsetAsync(word, 0, sizeof(int), s);
-        if (!kop_plane_selftest(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_EF0], f[F_EF1], f[F_EF2], word, s))
+        if (!kop_plane_selftest(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_WV3_3], f[F_EF0], f[F_EF1], f[F_EF2], word, s))
           return fail(ICEP_ERR_UNSUPPORTED, "wait self-test: no register plane kernel for this mesh");
       } else if (kernel == 2 && learned) {
         word = net.err;

@@ -2,16 +2,21 @@
 // three FFT passes, with the BiCGSTAB vector updates and dot products folded
 // into them (FP32, the inner solver of MIXED precision).
 //
-//   kop_xinv : vector update (p or s) at the read modes, then for d = 0..2 the
-//              gradient multiplier m(k) i k_d exp(i dx k_d/2) and the inverse
-//              x transform, into w_d (one read of the vector, three writes)
-//   kop_plane: per x-plane and field: inverse y/z transform, multiplication
-//              by the face permittivity eps_face_d (the reference's
-//              0.5 (eps + eps shifted along d), operate_dielectric.cxx:485-522),
-//              forward z/y transform -- the real field never leaves shared memory
-//   kop_xfwd : forward x transforms of w_0..2 and the staggered divergence
-//              sum_d i k_d exp(-i dx k_d/2) w_d into the output vector, with the
-//              dot products the iteration needs next as per-block partials
+//   kop_xinv : vector update (p or s) at the read modes, then the inverse x
+//              transforms of the x gradient m(k) i k_x exp(i dx k_x/2) p into
+//              w0 and of M = m(k) p into w1 (the y and z gradient multipliers
+//              depend on (j, kz) only and commute with the x transform)
+//   kop_plane: per x-plane and component d: the y or z gradient factor on M
+//              (d = 1, 2), inverse y/z transform, multiplication by the face
+//              permittivity eps_face_d (the reference's 0.5 (eps + eps
+//              shifted along d), operate_dielectric.cxx:485-522), forward z/y
+//              transform, the divergence factor k_d exp(-i dx k_d/2) (d = 1,
+//              2) -- into w0 (d = 0, in place), w2 and w3; the real field
+//              never leaves shared memory
+//   kop_xfwd : forward x transforms of w0 (times k_x exp(-i dx k_x/2)) and of
+//              w2 + w3, their sum times i into the output vector (the
+//              staggered divergence), with the dot products the iteration
+//              needs next as per-block partials
 //   kop_xr   : x~ += alpha p + omega s, r = s - omega t and the dot products
 //              (r0, r), (r, r)
 // Vectors follow kspace.cuh (read modes only). Dot partials are FP64, one or
@@ -42,12 +47,15 @@ struct KopTiles {
 // The tile autotuner: times every candidate of each pass (5 launches each
 // after one warm-up, CUDA events on s) on the given scratch fields -- any
 // values: the operator runs without vector update or dots -- and returns the
-// fastest; `us` (optional, 8 values) receives the times per launch in the
+// faster plane kernel and, per x pass, the default 16 pencils unless a
+// candidate is more than 3% faster (then the fastest); `us` (optional, 8
+// values) receives the times per launch in the
 // order xinv 8/16/32, xfwd 8/16/32, plane register/shared (0 where a
 // candidate does not exist for the mesh). The picks are cached per mesh for
 // the process, so later contexts of the same mesh take them untimed.
-KopTiles kop_autotune(const FFTPlan<float> &p, float *vec, float *w0, float *w1, float *w2, const float *ef0,
-                      const float *ef1, const float *ef2, float *out, int *err, cudaStream_t s, double *us);
+KopTiles kop_autotune(const FFTPlan<float> &p, float *vec, float *w0, float *w1, float *w2, float *w3,
+                      const float *ef0, const float *ef1, const float *ef2, float *out, int *err, cudaStream_t s,
+                      double *us);
 // Device-side BiCGSTAB iteration state (doubles). With a state pointer
 // kop_xinv takes beta, omega and rho from it instead of its arguments, and
 // kop_xr returns without touching x and r once KS_DONE is set (the other
@@ -67,16 +75,16 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 // mode KOP_S: vec = s <- P(r) - alpha P(v), alpha = rho / fin[0];
 // mode KOP_NONE: vec is used as it is (r, v, fin unused).
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
-              double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
+              double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1,
               cudaStream_t s, const double *ks = nullptr, const KopTiles &t = KopTiles());
 // err: device word set to 1 if a bulk copy into shared memory did not
 // complete within the kernel's wait limit (checked by the caller)
-void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0, const float *ef1,
-               const float *ef2, int *err, cudaStream_t s, const KopTiles &t = KopTiles());
+void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, float *w3, const float *ef0,
+               const float *ef1, const float *ef2, int *err, cudaStream_t s, const KopTiles &t = KopTiles());
 // Bounded-wait self-test of the plane pass: the register plane kernel
 // launched so that its copy-arrival wait runs out (no copy is issued), which
 // sets *err; false when the grid has no register plane kernel.
-bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2, const float *ef0,
+bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2, float *w3, const float *ef0,
                         const float *ef1, const float *ef2, int *err, cudaStream_t s);
 // mode KOP_P: partials[2b] = (other, out) with other = r0;
 // mode KOP_S: partials[2b] = (out, out), partials[2b+1] = (out, other) with other = s;
@@ -85,7 +93,7 @@ bool kop_plane_selftest(const FFTPlan<float> &p, float *w0, float *w1, float *w2
 // mode KOP_CG: partials[2b] = (M^-1 other, out) = sum m(k) other^* out with
 // the preconditioner m(k) (1/eps_ref from ks[KS_IEPS]): the CG denominator;
 // mode KOP_NONE: no dot products (other, partials, finals unused).
-void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *w1, const float *w2, float *out, int mode,
+void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *wa, const float *wb, float *out, int mode,
               const float *other, double *partials, double *finals, unsigned *counter, cudaStream_t s,
               const KopTiles &t = KopTiles(), const double *ks = nullptr);
 // alpha = rho / fin1[0]; omega = fin2[1] / fin2[0];

@@ -123,9 +123,20 @@ def test_bounded_wait_convolution(Sim):
     s.close()
 
 
+def expected_pick(t):
+    """The x-pass pick from the times of 8, 16, 32 pencils per block: the
+    default 16 unless a candidate is more than 3% faster; then the fastest."""
+    b = 1
+    for c in range(3):
+        if 0 < t[c] < 0.97 * t[1] and t[c] < t[b]:
+            b = c
+    return (8, 16, 32)[b]
+
+
 def test_autotune_picks_and_every_tile_shape(Sim, monkeypatch):
     """The tile autotuner times every candidate at context creation and keeps
-    the fastest; every candidate tile shape computes the same operator
+    the default x tiles unless a candidate is clearly faster, and the faster
+    plane kernel; every candidate tile shape computes the same operator
     (ICEP_KOP_TILES sets the tiles for a context)."""
     p, parts = cases.icep_case(n=64, npart=8, minsep=10.0, seed=7, eps_f=80.0, eps_p=2.0, e_ext=(0.0, 0.0, 0.1),
                                tol=1e-8, solver=abi.SOLVER_SPECTRAL, precision=abi.MIXED)
@@ -133,8 +144,7 @@ def test_autotune_picks_and_every_tile_shape(Sim, monkeypatch):
     picks, us = s.autotune_picks()
     assert picks[0] in (8, 16, 32) and picks[1] in (8, 16, 32) and picks[2] in (0, 1)
     assert np.all(us[:6] > 0) and us[6] > 0 and us[7] > 0
-    idx = {8: 0, 16: 1, 32: 2}
-    assert us[idx[picks[0]]] == min(us[0:3]) and us[3 + idx[picks[1]]] == min(us[3:6])
+    assert picks[0] == expected_pick(us[0:3]) and picks[1] == expected_pick(us[3:6])
     assert picks[2] == (0 if us[6] <= us[7] else 1)
     s.close()
     rng = np.random.default_rng(3)

@@ -1065,7 +1065,7 @@ class Engine : public EngineBase {
     }
   }
   // One iteration of the fused preconditioned CG (the MIXED inner solve with
-  // inner_cg): p~ = r + beta p~ (k_kop_xinv's P update with omega = 0) and
+  // inner_cg): p~ = r + beta p~ (k_kop_xinv's KOP_PC update) and
   // the gradient of M^-1 p~; the plane pass; q = B p~ into F_KV with the
   // denominator (M^-1 p~, q); the update of x~ and r and the next scalars.
   void kf_cg_iteration(int maxit) {
@@ -1075,7 +1075,7 @@ class Engine : public EngineBase {
       const int nb = kop_npb;
       double *P1 = kpart, *P3 = kpart + 4 * nb;
       double *F1 = kfin, *F3 = kfin + 4;
-      kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, 1.0, w0, w1, s, kst, kop_tiles);
+      kop_xinv(fft, KOP_PC, p, r, nullptr, 0.0, 0.0, 0.0, nullptr, 1.0, w0, w1, s, kst, kop_tiles);
       kop_plane(fft, w0, w1, w2, w3, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
       kop_xfwd(fft, w0, w2, w3, v, KOP_CG, p, P1, F1, kcnt, s, kop_tiles, kst);
       kop_cg(g, xt, r, p, v, F1, P3, F3, kcnt + 2, s, kst, maxit, false);

@@ -206,8 +206,8 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
         continue;
       }
       lr[u] = ldw(r, idx, wt);
-      lv[u] = ldw(v, idx, wt);
-      if (mode == KOP_P) lp[u] = ldw(vec, idx, wt);
+      if (mode != KOP_PC) lv[u] = ldw(v, idx, wt);
+      if (mode == KOP_P || mode == KOP_PC) lp[u] = ldw(vec, idx, wt);
     }
 #pragma unroll
     for (int u = 0; u < XB; u++) {
@@ -226,6 +226,8 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
         nv = lp[u];
       } else if (mode == KOP_P) {
         nv = cf{lr[u].x + beta * (lp[u].x - omega * lv[u].x), lr[u].y + beta * (lp[u].y - omega * lv[u].y)};
+      } else if (mode == KOP_PC) {
+        nv = cf{lr[u].x + beta * lp[u].x, lr[u].y + beta * lp[u].y};
       } else {
         nv = cf{lr[u].x - alpha * lv[u].x, lr[u].y - alpha * lv[u].y};
       }
@@ -1258,8 +1260,8 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float 
 // spectral preconditioner m(k)). In the x~ form p = M^-1 p~, x = M^-1 x~:
 // alpha = rho / (M^-1 p~, q) with q = B p~ (fin_pq, from k_kop_xfwd's KOP_CG
 // dot); x~ += alpha p~; r -= alpha q; then rho' = (r, M^-1 r) and |r|^2,
-// and the last block forms beta = rho'/rho (k_kop_xinv's KOP_P update with
-// omega = 0 makes p~ = r + beta p~) and the stop test. init: no update, only
+// and the last block forms beta = rho'/rho (k_kop_xinv's KOP_PC update makes
+// p~ = r + beta p~) and the stop test. init: no update, only
 // rho and |r|^2 of the starting residual (beta = 0: p~ = r).
 template <int H>
 __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_cg(Grid g, float *xt, float *r, const float *p, const float *q,
@@ -1523,7 +1525,8 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
   const Grid &g = p.g;
   const float ieps = (float)(1.0 / eps_ref);
   const int kw = xkw_ok(g.nx, t.xinv_kw) ? t.xinv_kw : 16;
-  count_launch(fld<float>(g, mode == KOP_P ? 6.0 : mode == KOP_S ? 5.0 : 3.0));
+  const double nfld = mode == KOP_P ? 6.0 : (mode == KOP_S || mode == KOP_PC) ? 5.0 : 3.0;
+  count_launch(fld<float>(g, nfld));
   probe_begin(PROBE_KOP_XINV, s);
 #define KOP_XINV(N, W) launch_xinv<N, W>(g, mode, vec, r, v, beta, omega, rho, fin, ieps, w0, w1, p.tw_x, ks, s)
   switch (g.nx) {
@@ -1543,7 +1546,8 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
   }
 #undef KOP_XINV
   // algorithmic bytes: r, v (and p) in, the updated vector and 2 fields out
-  probe_end(PROBE_KOP_XINV, (mode == KOP_P ? 6.0 : mode == KOP_S ? 5.0 : 3.0) * sizeof(float) * (double)g.nreal(), s);
+  // (KOP_PC: r and p~ in)
+  probe_end(PROBE_KOP_XINV, nfld * sizeof(float) * (double)g.nreal(), s);
 }
 
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, float *w3, const float *ef0,

@@ -27,7 +27,7 @@
 
 namespace icep {
 
-enum { KOP_P = 0, KOP_S = 1, KOP_NONE = 2, KOP_CG = 3 };
+enum { KOP_P = 0, KOP_S = 1, KOP_NONE = 2, KOP_CG = 3, KOP_PC = 4 };
 
 // true if the fused passes cover this grid (an x-plane fits in shared memory)
 bool kop_supported(const Grid &g);
@@ -73,6 +73,7 @@ int kop_pencil_blocks(const Grid &g);
 void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, float *ef2, cudaStream_t s);
 // mode KOP_P: vec = p <- P(r) + beta (P(p) - omega P(v));
 // mode KOP_S: vec = s <- P(r) - alpha P(v), alpha = rho / fin[0];
+// mode KOP_PC (the CG): vec = p~ <- P(r) + beta P(p~) (v unused);
 // mode KOP_NONE: vec is used as it is (r, v, fin unused).
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
               double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1,

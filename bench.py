@@ -41,11 +41,11 @@ UNIT = "steps/s"
 
 # Dominant kernel of the step (largest share of device time in the ncu launch
 # list of this bench, profiles/launches_icep_step_128.txt) and its probe id.
-PROBE_KERNEL = "k_kop_plane_r<128,64> (fused plane pass of the k-space Poisson operator, 3 fields)"
+PROBE_KERNEL = "k_kop_plane_r<128,64> (fused plane pass of the k-space Poisson operator, 3 components)"
 PROBE_KIND = 1
 # DRAM bytes (read + write) per launch of that kernel from one ncu capture
 # (profiles/k_kop_plane_128.txt), keyed by (grid, precision, kernel).
-TRAFFIC = {(128, "mixed", PROBE_KERNEL): 51.19e6}
+TRAFFIC = {(128, "mixed", PROBE_KERNEL): 42.90e6}
 
 
 def workload(args, precision, solver):

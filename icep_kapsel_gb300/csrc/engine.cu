@@ -93,6 +93,7 @@ class Engine : public EngineBase {
   double *kcoef = nullptr, *hcoef = nullptr, *mpart = nullptr;
   enum { KC_H1 = 0, KC_H2 = KVEC_MAX, KC_NRM = 2 * KVEC_MAX, KC_Y = 2 * KVEC_MAX + 1, KC_COUNT = 3 * KVEC_MAX + 1 };
   double *hscal = nullptr;  // pinned
+  double *hukdc = nullptr;  // pinned: uk_dc on its way back to the drop-in call
   int *ljwork = nullptr;
   int ljwork_ints = 0;
   int *dpairs_n = nullptr;
@@ -406,6 +407,7 @@ class Engine : public EngineBase {
     cudaFreeHost(hcoef);
     cudaFree(mpart);
     cudaFreeHost(hscal);
+    cudaFreeHost(hukdc);
     cudaFree(ljwork);
     cudaFree(dpairs_n);
     if (phase_on)
@@ -2141,6 +2143,37 @@ class Engine : public EngineBase {
   // conversion kernels themselves over the CPU-GPU link (no staging copy);
   // others go through device staging buffers and the copy engines.
   int set_fields(const int *ids, const double *const *host, int n) override {
+    const int st = put_fields(ids, host, n);
+    if (st) return st;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_fields");
+    return ICEP_OK;
+  }
+  int get_fields(const int *ids, double *const *host, int n) override {
+    const int st = fetch_fields(ids, host, n);
+    if (st) return st;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_fields");
+    return ICEP_OK;
+  }
+  int time_evolution_host(const int *ids, double *const *host, int n, double *uk_dc, icep_particle *parts,
+                          int nsteps) override {
+    if (!hukdc && cudaMallocHost(&hukdc, sizeof(double) * 3) != cudaSuccess)
+      return fail(ICEP_ERR_CUDA, "pinned uk_dc buffer");
+    int st;
+    // a pageable source is consumed before cudaMemcpyAsync returns
+    cudaMemcpyAsync(ukdc, uk_dc, sizeof(double) * 3, cudaMemcpyHostToDevice, s);
+    if ((st = put_particles(parts)) || (st = put_fields(ids, host, n)) || (st = step(nsteps)) ||
+        (st = fetch_fields(ids, host, n)))
+      return st;
+    cudaMemcpyAsync(hukdc, ukdc, sizeof(double) * 3, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hp, dp, sizeof(icep_particle) * np, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("time_evolution");
+    for (int d = 0; d < 3; d++) uk_dc[d] = hukdc[d];
+    memcpy(parts, hp, sizeof(icep_particle) * np);
+    return ICEP_OK;
+  }
+  // set_fields / get_fields without the final synchronisation (the copies
+  // and conversion kernels queued on the context's stream)
+  int put_fields(const int *ids, const double *const *host, int n) {
     const long nf = g.nf();
     const double *pot_src = nullptr;
     for (int k = 0; k < n; k++) {
@@ -2160,10 +2193,9 @@ class Engine : public EngineBase {
       else link_d2f(nf, src, (float *)f[ids[k]], s);
     }
     if (pot_src) return import_potential(pot_src);  // synchronises
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_fields");
     return ICEP_OK;
   }
-  int get_fields(const int *ids, double *const *host, int n) override {
+  int fetch_fields(const int *ids, double *const *host, int n) {
     const long nf = g.nf();
     for (int k = 0; k < n; k++) {
       if (ids[k] < 0 || ids[k] >= F_COUNT) return fail(ICEP_ERR_ARG, "field id");
@@ -2187,7 +2219,6 @@ class Engine : public EngineBase {
         cudaMemcpyAsync(host[k], st, sizeof(double) * nf, cudaMemcpyDeviceToHost, s);
       }
     }
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("get_fields");
     return ICEP_OK;
   }
   // The fields of Output_dielectric_charge_field_data (output.cxx:262-320)
@@ -2390,6 +2421,14 @@ class Engine : public EngineBase {
     return ICEP_OK;
   }
   int set_particles(const icep_particle *h) override {
+    const int st = put_particles(h);
+    if (st) return st;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_particles");
+    return ICEP_OK;
+  }
+  // set_particles without the final synchronisation (the copy from the
+  // pinned staging array queued)
+  int put_particles(const icep_particle *h) {
     // species in range; the field stays Janus (every species with an axis) or
     // not (particle 0's species without one), as the context was created
     for (int q = 0; q < np; q++) {
@@ -2403,7 +2442,6 @@ class Engine : public EngineBase {
     if (!P.per_particle_eps)
       for (int q = 0; q < np; q++) hp[q].eps_p = P.eps_particle_top;
     cudaMemcpyAsync(dp, hp, sizeof(icep_particle) * np, cudaMemcpyHostToDevice, s);
-    if (cudaStreamSynchronize(s) != cudaSuccess) return cuda_status("set_particles");
     return ICEP_OK;
   }
   int get_uk_dc(double *v) override {

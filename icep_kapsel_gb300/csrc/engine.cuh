@@ -25,6 +25,12 @@ struct EngineBase {
   virtual int set_particles(const icep_particle *h) = 0;
   virtual int get_uk_dc(double *v) = 0;
   virtual int set_uk_dc(const double *v) = 0;
+  // The drop-in call (icep_time_evolution): uk_dc, the particles and the n
+  // fields up, nsteps steps, the same back into the same host arrays, with
+  // the copies queued and the stream synchronised only where the host needs
+  // a result (the potential's comparison, the steps' solver status, the end)
+  virtual int time_evolution_host(const int *ids, double *const *host, int n, double *uk_dc,
+                                  icep_particle *parts, int nsteps) = 0;
   virtual int fft_host(double *a, bool forward) = 0;
   virtual int call(int fn) = 0;
   virtual int apply_A_host(const double *x, double *y) = 0;

@@ -165,9 +165,9 @@ int icep_output_avs(icep_ctx *c, const char *out_dir, const char *out_name, int 
 int icep_time_evolution(icep_ctx *c, double *zeta0, double *zeta1, double *uk_dc, double *conc0, double *conc1,
                         double *potential, icep_particle *particles, int nsteps) {
   if (!ok(c) || !zeta0 || !zeta1 || !uk_dc || !particles || nsteps < 0) return ICEP_ERR_ARG;
-  int st;
   icep::EngineBase *e = c->e;
-  // the fields go as one batch each way (one synchronisation); a potential
+  // the fields go as one batch each way, queued with uk_dc and the particles
+  // (the stream synchronised where the host needs a result); a potential
   // passed back as this call returned it keeps the Poisson solver's state
   int ids[5] = {icep::F_ZETA0, icep::F_ZETA1};
   double *ptr[5] = {zeta0, zeta1};
@@ -175,12 +175,7 @@ int icep_time_evolution(icep_ctx *c, double *zeta0, double *zeta1, double *uk_dc
   if (conc0) { ids[n] = icep::F_C0; ptr[n++] = conc0; }
   if (conc1) { ids[n] = icep::F_C1; ptr[n++] = conc1; }
   if (potential) { ids[n] = icep::F_POT; ptr[n++] = potential; }
-  if ((st = e->set_uk_dc(uk_dc)) || (st = e->set_particles(particles)) || (st = e->set_fields(ids, ptr, n)))
-    return wrap(c, st);
-  if ((st = e->step(nsteps))) return wrap(c, st);
-  if ((st = e->get_fields(ids, ptr, n)) || (st = e->get_uk_dc(uk_dc)) || (st = e->get_particles(particles)))
-    return wrap(c, st);
-  return ICEP_OK;
+  return wrap(c, e->time_evolution_host(ids, ptr, n, uk_dc, particles, nsteps));
 }
 
 int icep_A2a_k(icep_ctx *c, double *a) { return ok(c) && a ? wrap(c, c->e->fft_host(a, true)) : ICEP_ERR_ARG; }
@@ -256,7 +251,10 @@ unsigned long long icep_kernel_launches(void) { return __atomic_load_n(&icep::g_
 unsigned long long icep_algorithmic_bytes(void) { return __atomic_load_n(&icep::g_alg_bytes, __ATOMIC_RELAXED); }
 int icep_pin_host(void *p, size_t bytes) {
   if (!p || !bytes) return ICEP_ERR_ARG;
-  if (cudaHostRegister(p, bytes, cudaHostRegisterMapped) != cudaSuccess) return ICEP_ERR_CUDA;
+  if (cudaHostRegister(p, bytes, cudaHostRegisterMapped) != cudaSuccess) {
+    cudaGetLastError();  // reported here: not left for the context's next call to find
+    return ICEP_ERR_CUDA;
+  }
   void *dev = nullptr;
   if (cudaHostGetDevicePointer(&dev, p, 0) == cudaSuccess && dev) {
     std::lock_guard<std::mutex> lk(icep::g_pin_mu);
@@ -274,7 +272,11 @@ int icep_unpin_host(void *p) {
       if (icep::g_pins[k].lo == (uintptr_t)p) icep::g_pins.erase(icep::g_pins.begin() + (long)k);
       else k++;
   }
-  return cudaHostUnregister(p) == cudaSuccess ? ICEP_OK : ICEP_ERR_CUDA;
+  if (cudaHostUnregister(p) != cudaSuccess) {
+    cudaGetLastError();
+    return ICEP_ERR_CUDA;
+  }
+  return ICEP_OK;
 }
 
 int icep_autotune_picks(icep_ctx *c, int *picks, double *us) {

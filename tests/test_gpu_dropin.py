@@ -119,3 +119,30 @@ def test_dropin_pinned_host_arrays(Sim):
     finally:
         for v in pinned.values():
             lib.icep_unpin_host(v.ctypes.data)
+
+
+def test_failed_pin_leaves_no_error_behind(Sim):
+    """icep_pin_host reports a failed registration itself (here: the array is
+    registered already) and leaves no CUDA error pending for the context's
+    next call, which steps normally."""
+    import ctypes as C
+    from icep_kapsel_gb300 import runtime
+    lib = runtime.load_library()
+    lib.icep_pin_host.argtypes = [C.c_void_p, C.c_size_t]
+    lib.icep_unpin_host.argtypes = [C.c_void_p]
+    p, parts = case(abi.MIXED)
+    a = Sim(p, parts)
+    a.init_state()
+    z = np.ascontiguousarray(a.get("zeta0"))
+    assert lib.icep_pin_host(z.ctypes.data, z.nbytes) == 0
+    try:
+        assert lib.icep_pin_host(z.ctypes.data, z.nbytes) != 0
+        keys = ("zeta1", "c0", "c1", "pot")
+        h = {k: np.ascontiguousarray(a.get(k)) for k in keys}
+        uk, hp = np.ascontiguousarray(a.uk_dc()), a.particles()
+        a.time_evolution(z, h["zeta1"], uk, hp, h["c0"], h["c1"], h["pot"], 1)
+        assert np.isfinite(z).all()
+    finally:
+        lib.icep_unpin_host(z.ctypes.data)
+    assert lib.icep_unpin_host(z.ctypes.data) != 0  # not registered any more
+    a.step(1)

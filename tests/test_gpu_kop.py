@@ -95,6 +95,73 @@ def test_fused_operator_against_fp64(Sim, n):
     s.close()
 
 
+def read_weight3(nx, ny, h):
+    """read_weight on an nx x ny x (h+1) half spectrum (NX != NY allowed)."""
+    i = np.arange(nx)[:, None, None]
+    j = np.arange(ny)[None, :, None]
+    kz = np.arange(h + 1)[None, None, :]
+    w = np.full((nx, ny, h + 1), 2, dtype=np.int8)
+    edge = (kz == 0) | (kz == h)
+    selfc = (((nx - i) % nx) == i) & (((ny - j) % ny) == j)
+    kept = np.where((j >= 1) & (j <= ny // 2 - 1), True, np.where((j == 0) | (j == ny // 2), i <= nx // 2, False))
+    kept = np.where(kz == h, ~kept, kept)
+    w = np.where(edge & selfc, 1, np.where(edge & ~kept, 0, w))
+    return np.broadcast_to(w, (nx, ny, h + 1))
+
+
+def apply_b_fp64_3(ph, eps, shape):
+    """apply_b_fp64 on an (nx, ny, nz) mesh."""
+    ns = shape
+    ks = []
+    for d, n in enumerate(ns):
+        kint = np.arange(n // 2 + 1) if d == 2 else np.where(np.arange(n) > n // 2, np.arange(n) - n, np.arange(n))
+        sh = [1, 1, 1]
+        sh[d] = -1
+        ks.append((kint * 2 * np.pi / n).reshape(sh))
+    k2 = ks[0] ** 2 + ks[1] ** 2 + ks[2] ** 2
+    m = np.where(k2 > 0, -1.0 / (eps.mean() * np.where(k2 > 0, k2, 1.0)), 0.0)
+    out = np.zeros(ph.shape, complex)
+    for d in range(3):
+        sh = np.exp(0.5j * ks[d])
+        w = np.fft.irfftn(m * 1j * ks[d] * sh * ph, s=ns, axes=(0, 1, 2))
+        ef = 0.5 * (eps + np.roll(eps, -1, axis=d))
+        out += 1j * ks[d] * np.conj(sh) * np.fft.rfftn(ef * w)
+    return out
+
+
+@pytest.mark.parametrize("shape", [(32, 64, 128), (128, 32, 64)])
+def test_fused_operator_noncubic(Sim, shape):
+    """The fused operator on meshes whose edges differ: the y and z gradient
+    and divergence factors of the plane pass index the y and z wavenumbers
+    of their own edges (32 x 64 x 128: the register plane kernel, NY = 64,
+    NZ/2 = 64; 128 x 32 x 64: the shared-memory one). Against the FP64
+    restatement, 2e-5 relative L2."""
+    nx, ny, nz = shape
+    p, parts = cases.icep_case(n=32, npart=4, minsep=10.0, seed=9, eps_f=80.0, eps_p=2.0,
+                               e_ext=(0.0, 0.0, 0.1), tol=1e-8, solver=abi.SOLVER_SPECTRAL, precision=abi.MIXED)
+    p.nx, p.ny, p.nz = nx, ny, nz
+    s = Sim(p, parts)
+    s.call("dielectric_field")
+    eps = s.get("eps")[:, :, :nz]
+    assert eps.min() < 10 and eps.max() > 70
+    rng = np.random.default_rng(nx + 3 * ny + 7 * nz)
+    ph = np.fft.rfftn(rng.standard_normal((nx, ny, nz)))
+    buf = np.zeros((nx, ny, nz + 2))
+    buf[:, :, 0::2] = ph.real
+    buf[:, :, 1::2] = ph.imag
+    s.set("wv1", buf)
+    s.call("apply_bk")
+    got = s.get("work")
+    gh = got[:, :, 0::2] + 1j * got[:, :, 1::2]
+    ref = apply_b_fp64_3(ph, eps, shape)
+    wt = read_weight3(nx, ny, nz // 2)
+    d2 = np.where(wt == 2, np.abs(gh - ref) ** 2, 0.0) + np.where(wt == 1, (gh.real - ref.real) ** 2, 0.0)
+    r2 = np.where(wt == 2, np.abs(ref) ** 2, 0.0) + np.where(wt == 1, ref.real ** 2, 0.0)
+    err = float(np.sqrt(d2.sum() / r2.sum()))
+    assert err < 2e-5, err
+    s.close()
+
+
 def test_bounded_wait_plane_pass(Sim):
     p, parts = cases.icep_case(n=64, npart=8, minsep=10.0, seed=5, eps_f=80.0, eps_p=2.0, e_ext=(0.0, 0.0, 0.1),
                                tol=1e-8, solver=abi.SOLVER_SPECTRAL, precision=abi.MIXED)

@@ -129,13 +129,15 @@ def apply_b_fp64_3(ph, eps, shape):
     return out
 
 
-@pytest.mark.parametrize("shape", [(32, 64, 128), (128, 32, 64)])
+@pytest.mark.parametrize("shape", [(32, 64, 128), (128, 32, 64), (64, 256, 128), (128, 64, 256)])
 def test_fused_operator_noncubic(Sim, shape):
     """The fused operator on meshes whose edges differ: the y and z gradient
     and divergence factors of the plane pass index the y and z wavenumbers
     of their own edges (32 x 64 x 128: the register plane kernel, NY = 64,
-    NZ/2 = 64; 128 x 32 x 64: the shared-memory one). Against the FP64
-    restatement, 2e-5 relative L2."""
+    NZ/2 = 64; 128 x 32 x 64: the shared-memory one; 64 x 256 x 128 and
+    128 x 64 x 256: the split plane step, whose factor kernels index the
+    half spectrum's rows and columns). Against the FP64 restatement, 2e-5
+    relative L2."""
     nx, ny, nz = shape
     p, parts = cases.icep_case(n=32, npart=4, minsep=10.0, seed=9, eps_f=80.0, eps_p=2.0,
                                e_ext=(0.0, 0.0, 0.1), tol=1e-8, solver=abi.SOLVER_SPECTRAL, precision=abi.MIXED)

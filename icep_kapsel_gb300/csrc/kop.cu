@@ -219,7 +219,7 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
       }
       const int j = pj[w], kz = pkz[w];
       // raw holds the vector times the preconditioner m(k), once per mode for
-      // the three gradient components
+      // the x gradient and M
       const float mk = precond_m(g, e, j, kz, ieps);
       cf nv;
       if (mode == KOP_NONE) {
@@ -1496,7 +1496,7 @@ bool fft_plane_r(const FFTPlan<float> &p, const FieldBatch<float> &fb, bool inve
   return false;
 }
 
-// an x-plane of the three fields fits in one block's shared memory
+// an x-plane of one component fits in one block's shared memory
 bool kop_plane_fits(const Grid &g) {
   return g.ny <= 128 && g.nz <= 128 && plane_smem_f(g.ny, g.nz / 2) <= KOP_PLANE_SMEM_MAX;
 }

@@ -9,7 +9,7 @@ namespace icep {
 // Kernel classes that can be probed (values of icep_probe_start's kind).
 enum ProbeKind {
   PROBE_NONE = 0,
-  PROBE_KOP_PLANE = 1,  // fused plane pass of the k-space operator (3 fields)
+  PROBE_KOP_PLANE = 1,  // fused plane pass of the k-space operator (3 components)
   PROBE_KOP_XINV = 2,   // fused inverse x pass (vector update + gradient)
   PROBE_KOP_XFWD = 3,   // fused forward x pass (divergence + dot partials)
 };

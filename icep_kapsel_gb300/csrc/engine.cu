@@ -1696,7 +1696,7 @@ class Engine : public EngineBase {
         // FP32 correction solve on the normalised residual
         const double rn = sqrt(rr / (double)G.nreal());
         rf_to_f32(nf, df(D_R), (float *)f[F_KR], 1.0 / rn, s);
-        double inner_tol = 0.5 * P.potential_tol * sqrt(bb / rr);
+        double inner_tol = INNER_MARGIN * P.potential_tol * sqrt(bb / rr);
         if (inner_tol < 2e-5) inner_tol = 2e-5;
         if (inner_tol > 0.5) inner_tol = 0.5;
         int it = 0;

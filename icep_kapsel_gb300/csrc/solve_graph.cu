@@ -54,7 +54,7 @@ __global__ void k_sweep_cond(cudaGraphConditionalHandle h, const double *scal, i
       const float hi = (float)rn;
       scf[SCF_RN] = hi;
       scf[SCF_RN + 1] = (float)(rn - (double)hi);
-      double inner_tol = 0.5 * tol * sqrt(sc[SC_BB] / rr);
+      double inner_tol = INNER_MARGIN * tol * sqrt(sc[SC_BB] / rr);
       if (inner_tol < 2e-5) inner_tol = 2e-5;
       if (inner_tol > 0.5) inner_tol = 0.5;
       sc[SC_INNER_TOL] = inner_tol;

@@ -18,6 +18,15 @@
 
 namespace icep {
 
+// A refinement sweep's inner tolerance: INNER_MARGIN tol |b| / |r| (clamped
+// to [2e-5, 0.5]), so that the sweep's true residual lands below tol with
+// room for the FP32 solve's deviation from it. Measured on GB300 at 128^3
+// (40 steps of the 512-sphere workload): margin 0.5 / 0.6 / 0.7 / 0.8 ->
+// 17.05 / 16.08 / 15.26 / 15.05 inner iterations per step, largest true
+// residual 4.9e-9 / 5.8e-9 / 7.0e-9 / 7.7e-9 at tol 1e-8, one sweep every
+// step; a sweep that misses tol is followed by another.
+constexpr double INNER_MARGIN = 0.7;
+
 // doubles of the control array
 enum {
   SC_BB = 0,     // |b^|^2 / N of the right-hand side

@@ -282,9 +282,12 @@ class Engine : public EngineBase {
       if (e == cudaSuccess && st == ICEP_OK) e = add_while(bs, sdeps, hi, &ni, &bi);
       sdeps.assign(1, ni);
       seg(2, bi, ideps, [&]() -> int {
-        if (inner_cg) kf_cg_iteration(maxit);
-        else kf_iteration(1.0, maxit);
-        inner_cond(hi, kst, r, r0, v, p, nf, maxit, sc, eps2, s);
+        if (inner_cg) {
+          kf_cg_iteration(maxit, hi);  // the CG update sets the loop's condition
+        } else {
+          kf_iteration(1.0, maxit);
+          inner_cond(hi, kst, r, r0, v, p, nf, maxit, sc, eps2, s);
+        }
         return ICEP_OK;
       });
       // the correction added, the next true residual and decision
@@ -1070,7 +1073,7 @@ class Engine : public EngineBase {
   // inner_cg): p~ = r + beta p~ (k_kop_xinv's KOP_PC update) and
   // the gradient of M^-1 p~; the plane pass; q = B p~ into F_KV with the
   // denominator (M^-1 p~, q); the update of x~ and r and the next scalars.
-  void kf_cg_iteration(int maxit) {
+  void kf_cg_iteration(int maxit, cudaGraphConditionalHandle h = 0) {
     if constexpr (std::is_same<R, float>::value) {
       float *r = f[F_KR], *p = f[F_KP], *v = f[F_KV], *xt = f[F_KY];
       float *w0 = f[F_WV3_0], *w1 = f[F_WV3_1], *w2 = f[F_WV3_2], *w3 = f[F_WV3_3];
@@ -1080,7 +1083,7 @@ class Engine : public EngineBase {
       kop_xinv(fft, KOP_PC, p, r, nullptr, 0.0, 0.0, 0.0, nullptr, 1.0, w0, w1, s, kst, kop_tiles);
       kop_plane(fft, w0, w1, w2, w3, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
       kop_xfwd(fft, w0, w2, w3, v, KOP_CG, p, P1, F1, kcnt, s, kop_tiles, kst);
-      kop_cg(g, xt, r, p, v, F1, P3, F3, kcnt + 2, s, kst, maxit, false);
+      kop_cg(g, xt, r, p, v, F1, P3, F3, kcnt + 2, s, kst, maxit, false, h);
     }
   }
   // the CG's starting pass: rho and |r|^2 of the starting residual

@@ -1266,7 +1266,8 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_xr(Grid g, float *xt, float 
 template <int H>
 __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_cg(Grid g, float *xt, float *r, const float *p, const float *q,
                                                      const double *fin_pq, double *part, double *fin,
-                                                     unsigned *counter, double *ks, int maxit, int init) {
+                                                     unsigned *counter, double *ks, int maxit, int init,
+                                                     cudaGraphConditionalHandle h) {
   const int lin = threadIdx.x;
   __shared__ float sc[2];  // alpha, 1/eps_ref
   __shared__ int stop;     // the solve is done: this launch leaves x and r alone
@@ -1276,7 +1277,12 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_cg(Grid g, float *xt, float 
     sc[1] = (float)__ldcg(ks + KS_IEPS);
   }
   __syncthreads();
-  if (stop) return;
+  if (stop) {
+    // inside the step graph's inner loop: a pass that finds the solve done
+    // ends the loop (every pass sets the loop's condition)
+    if (h && blockIdx.x == 0 && lin == 0) cudaGraphSetConditional(h, 0u);
+    return;
+  }
   const float alpha = sc[0], ieps = sc[1];
   constexpr int RL = H + 1;  // modes per z row
   const long nm = g.nmodes();
@@ -1313,7 +1319,11 @@ __global__ void __launch_bounds__(KOP_XR_TPB) k_kop_cg(Grid g, float *xt, float 
       ks[KS_RHO] = rho_new;
       ks[KS_ITERS] = it;
       ks[KS_RR] = rr;
-      ks[KS_DONE] = (!(rr > ks[KS_TOL2]) || !isfinite(rr) || !isfinite(rho_new) || it >= (double)maxit) ? 1.0 : 0.0;
+      const bool done = !(rr > ks[KS_TOL2]) || !isfinite(rr) || !isfinite(rho_new) || it >= (double)maxit;
+      ks[KS_DONE] = done ? 1.0 : 0.0;
+      // the step graph's inner loop continues while the solve is not done
+      // (at most maxit passes: KS_ITERS counts them)
+      if (h) cudaGraphSetConditional(h, done ? 0u : 1u);
     }
   }
 }
@@ -1713,12 +1723,13 @@ void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv,
 }
 
 void kop_cg(const Grid &g, float *xt, float *r, const float *p, const float *q, const double *fin_pq, double *part,
-            double *fin, unsigned *counter, cudaStream_t s, double *ks, int maxit, bool init) {
+            double *fin, unsigned *counter, cudaStream_t s, double *ks, int maxit, bool init,
+            cudaGraphConditionalHandle h) {
   const unsigned nb = (unsigned)kop_xr_blocks(g);
   count_launch(fld<float>(g, init ? 1.0 : 6.0));
 #define KOP_CG(HH)                                                                                             \
   case HH:                                                                                                     \
-    k_kop_cg<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, q, fin_pq, part, fin, counter, ks, maxit, init ? 1 : 0); \
+    k_kop_cg<HH><<<nb, KOP_XR_TPB, 0, s>>>(g, xt, r, p, q, fin_pq, part, fin, counter, ks, maxit, init ? 1 : 0, h); \
     break;
   switch (g.nz / 2) {
     KOP_CG(8)

@@ -110,8 +110,12 @@ void kop_xr(const Grid &g, float *xt, float *r, const float *p, const float *sv,
 // fin their sums; the last block sets KS_RHO, KS_BETA (rho'/rho, 0 with
 // init), KS_OMEGA = 0, KS_ITERS, KS_RR and KS_DONE (1: converged, non-finite
 // or at maxit). init: no update (the starting residual's sums only). Returns
-// without touching x and r once KS_DONE is set.
+// without touching x and r once KS_DONE is set. h (nonzero inside the step
+// graph's inner WHILE loop, not with init): every launch sets the loop's
+// condition, 1 while the solve is not done, 0 once it is (also when it finds
+// it done on entry).
 void kop_cg(const Grid &g, float *xt, float *r, const float *p, const float *q, const double *fin_pq, double *part,
-            double *fin, unsigned *counter, cudaStream_t s, double *ks, int maxit, bool init);
+            double *fin, unsigned *counter, cudaStream_t s, double *ks, int maxit, bool init,
+            cudaGraphConditionalHandle h = 0);
 
 }  // namespace icep

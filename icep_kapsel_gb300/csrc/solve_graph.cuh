@@ -60,9 +60,10 @@ void sweep_cond(cudaGraphConditionalHandle h, const double *scal, int slot_rr, d
 // CG) and the inner loop's condition.
 void inner_prep(cudaGraphConditionalHandle h, const double *scal, int slot_rr, double *sc, double *ks, double eps2,
                 bool cg, cudaStream_t s);
-// End of an inner loop body: a restart that kop_xr asked for (r0 = r, v = p
-// = 0, the scalars reset) or the stop, as the host loop does it; nf floats
-// per vector.
+// End of a BiCGSTAB inner loop body: a restart that kop_xr asked for (r0 =
+// r, v = p = 0, the scalars reset) or the stop, as the host loop does it; nf
+// floats per vector. (A CG body needs no such kernel: kop_cg's last block
+// sets the loop's condition.)
 void inner_cond(cudaGraphConditionalHandle h, double *ks, float *r, float *r0, float *v, float *p, long nf,
                 int maxit, double *sc, double eps2, cudaStream_t s);
 

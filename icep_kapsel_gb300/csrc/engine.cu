@@ -270,11 +270,13 @@ class Engine : public EngineBase {
       seg(1, bs, sdeps, [&]() -> int {
         rf_to_f32(nf, df(D_R), r, scf + SCF_INVRN, s);
         cudaMemsetAsync(r, 0, 2 * sizeof(R), s);  // k = 0: the mean
-        cudaMemcpyAsync(r0, r, sizeof(R) * nf, cudaMemcpyDeviceToDevice, s);
         kdots<R>(g, r, r, r, r, 1, partials, scal, S_RR, s);
         zero(F_KY);
-        zero(F_KV);
         zero(F_KP);
+        if (!inner_cg) {  // BiCGSTAB's shadow residual and v (CG writes q before reading it)
+          cudaMemcpyAsync(r0, r, sizeof(R) * nf, cudaMemcpyDeviceToDevice, s);
+          zero(F_KV);
+        }
         inner_prep(hi, scal, S_RR, sc, kst, eps2, inner_cg, s);
         if (inner_cg) kf_cg_start(maxit);
         return ICEP_OK;

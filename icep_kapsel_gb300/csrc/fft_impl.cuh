@@ -271,19 +271,25 @@ __global__ void __launch_bounds__(512) k_rows_eps(FieldBatch<R> fb, Grid g, cons
   block_fft<R, H, W>(SmemT<R>{A, sw}, SmemT<R>{X, sw}, A, B, sw, tws, true);
   // the real row values (2m, 2m+1) at X[m], scaled and times the face
   // permittivity of component d
+  // (i, j) of a row by shift and mask (the mesh edges are powers of two),
+  // the point and its neighbour along d as row bases plus k
+  const int lny = __ffs(g.ny) - 1;
   for (int q = lin; q < W * H; q += nthr) {
     const int w = q / H, m = q - w * H;
     const long row = row0 + w;
     if (row >= nrows) continue;
-    const int i = (int)(row / g.ny), j = (int)(row - (long)i * g.ny);
+    const int i = (int)(row >> lny), j = (int)row & (g.ny - 1);
+    const long base = row * g.nzp;
+    const long nbase = (d == 0)   ? ((long)(((i + 1) & (g.nx - 1)) << lny) + j) * g.nzp
+                       : (d == 1) ? ((long)(i << lny) + ((j + 1) & (g.ny - 1))) * g.nzp
+                                  : base;
     const cplx<R> v = X[m * sw + w];
     R x[2] = {v.x * scale, v.y * scale};
 #pragma unroll
     for (int h = 0; h < 2; h++) {
       const int k = 2 * m + h;
-      const long im = gidx(g, i, j, k);
-      const long nb = (d == 0) ? gidx(g, (i + 1) & (g.nx - 1), j, k)
-                               : (d == 1) ? gidx(g, i, (j + 1) & (g.ny - 1), k) : gidx(g, i, j, (k + 1) & (g.nz - 1));
+      const long im = base + k;
+      const long nb = nbase + ((d == 2) ? ((k + 1) & (g.nz - 1)) : k);
       x[h] = x[h] * half_of(two_sum(eps[im], eps[nb]));
     }
     X[m * sw + w] = cplx<R>{x[0], x[1]};

@@ -52,6 +52,23 @@ struct Grid {
 __host__ __device__ inline long gidx(const Grid &g, int i, int j, int k) {
   return ((long)i * g.ny + j) * g.nzp + k;
 }
+// real point t (row-major over nx x ny x nz) -> (i, j, k) by shifts and masks:
+// every mesh edge is a power of two (checked when a context is created)
+__device__ __forceinline__ void real_ijk(const Grid &g, unsigned t, int &i, int &j, int &k) {
+  const int lnz = __ffs(g.nz) - 1, lny = __ffs(g.ny) - 1;
+  k = (int)(t & (unsigned)(g.nz - 1));
+  j = (int)((t >> lnz) & (unsigned)(g.ny - 1));
+  i = (int)(t >> (lnz + lny));
+}
+// mode t of the half spectrum (row-major over nx x ny x hnz) -> (i, j, kz):
+// one division by hnz = nz/2 + 1 gives the row i ny + j, split by shift and
+// mask (ny a power of two)
+__device__ __forceinline__ void mode_ijk3(const Grid &g, unsigned t, int &i, int &j, int &kz) {
+  const unsigned row = t / (unsigned)g.hnz;
+  kz = (int)(t - row * (unsigned)g.hnz);
+  j = (int)(row & (unsigned)(g.ny - 1));
+  i = (int)(row >> (__ffs(g.ny) - 1));
+}
 __host__ __device__ inline int kx_of(const Grid &g, int i) { return (i > g.nx / 2) ? i - g.nx : i; }
 __host__ __device__ inline int ky_of(const Grid &g, int j) { return (j > g.ny / 2) ? j - g.ny : j; }
 __host__ __device__ inline bool in_two_third(const Grid &g, int i, int j, int kz) {

@@ -15,12 +15,7 @@ struct Mode {
 // Grids hold at most 2^24 points, so 32-bit index arithmetic suffices.
 __device__ __forceinline__ bool mode_of(const Grid &g, long tl, Mode &m) {
   if (tl >= g.nmodes()) return false;
-  const unsigned t = (unsigned)tl;
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.hnz;
-  m.i = (int)(t / plane);
-  const unsigned r = t - (unsigned)m.i * plane;
-  m.j = (int)(r / (unsigned)g.hnz);
-  m.kz = (int)(r - (unsigned)m.j * (unsigned)g.hnz);
+  mode_ijk3(g, (unsigned)tl, m.i, m.j, m.kz);
   m.im = gidx(g, m.i, m.j, 2 * m.kz);
   return true;
 }
@@ -32,12 +27,7 @@ struct Pt {
 
 __device__ __forceinline__ bool pt_of(const Grid &g, long tl, Pt &p) {
   if (tl >= g.nreal()) return false;
-  const unsigned t = (unsigned)tl;
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.nz;
-  p.i = (int)(t / plane);
-  const unsigned r = t - (unsigned)p.i * plane;
-  p.j = (int)(r / (unsigned)g.nz);
-  p.k = (int)(r - (unsigned)p.j * (unsigned)g.nz);
+  real_ijk(g, (unsigned)tl, p.i, p.j, p.k);
   p.im = gidx(g, p.i, p.j, p.k);
   return true;
 }

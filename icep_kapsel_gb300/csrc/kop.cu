@@ -1333,11 +1333,8 @@ __global__ void k_kop_eps_mul(Grid g, float *w0, float *w1, float *w2, const flo
                               const float *ef2) {
   const long tl = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tl >= g.nreal()) return;
-  const unsigned t = (unsigned)tl;
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.nz;
-  const int i = (int)(t / plane);
-  const unsigned rem = t - (unsigned)i * plane;
-  const int j = (int)(rem / (unsigned)g.nz), k = (int)(rem - (unsigned)j * (unsigned)g.nz);
+  int i, j, k;
+  real_ijk(g, (unsigned)tl, i, j, k);
   const long im = gidx(g, i, j, k);
   w0[im] *= ef0[im];
   w1[im] *= ef1[im];
@@ -1368,11 +1365,8 @@ __global__ void k_kop_yz_factors(Grid g, const float *m, float *w2, float *w3, i
 __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2, float half) {
   const long tl = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tl >= g.nreal()) return;
-  const unsigned t = (unsigned)tl;
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.nz;
-  const int i = (int)(t / plane);
-  const unsigned rem = t - (unsigned)i * plane;
-  const int j = (int)(rem / (unsigned)g.nz), k = (int)(rem - (unsigned)j * (unsigned)g.nz);
+  int i, j, k;
+  real_ijk(g, (unsigned)tl, i, j, k);
   const long im = gidx(g, i, j, k);
   const float e0 = eps[im];
   ef0[im] = half * (eps[gidx(g, (i + 1) % g.nx, j, k)] + e0);

@@ -10,12 +10,9 @@ namespace {
 constexpr int TPB = 256;
 
 __device__ __forceinline__ long real_index(const Grid &g, unsigned t) {
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.nz;
-  const unsigned i = t / plane;
-  const unsigned r = t - i * plane;
-  const unsigned j = r / (unsigned)g.nz;
-  const unsigned k = r - j * (unsigned)g.nz;
-  return gidx(g, (int)i, (int)j, (int)k);
+  int i, j, k;
+  real_ijk(g, t, i, j, k);
+  return gidx(g, i, j, k);
 }
 
 // Grid-stride partial dots; fixed grid size and fixed reduction order make the

@@ -15,11 +15,7 @@ struct KMode {
 
 __device__ __forceinline__ bool kmode(const Grid &g, unsigned t, KMode &m) {
   if (t >= (unsigned)g.nmodes()) return false;
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.hnz;
-  m.i = (int)(t / plane);
-  const unsigned r = t - (unsigned)m.i * plane;
-  m.j = (int)(r / (unsigned)g.hnz);
-  m.kz = (int)(r - (unsigned)m.j * (unsigned)g.hnz);
+  mode_ijk3(g, t, m.i, m.j, m.kz);
   m.im = gidx(g, m.i, m.j, 2 * m.kz);
   return true;
 }

@@ -85,11 +85,7 @@ struct RfTab {
 
 // mode t (complex index) -> (i, j, kz); grids hold at most 2^24 points
 __device__ __forceinline__ void mode_ijk(const Grid &g, unsigned t, int &i, int &j, int &kz) {
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.hnz;
-  i = (int)(t / plane);
-  const unsigned r = t - (unsigned)i * plane;
-  j = (int)(r / (unsigned)g.hnz);
-  kz = (int)(r - (unsigned)j * (unsigned)g.hnz);
+  mode_ijk3(g, t, i, j, kz);
 }
 
 __global__ void k_rf_grad(Grid g, RfTab tab, const float4 *__restrict__ x, float4 *__restrict__ w0,
@@ -114,12 +110,8 @@ __global__ void k_rf_grad(Grid g, RfTab tab, const float4 *__restrict__ x, float
 // neighbours (periodic; sizes are powers of two)
 __device__ __forceinline__ bool point_nbrs(const Grid &g, long tl, long &im, long &n0, long &n1, long &n2) {
   if (tl >= g.nreal()) return false;
-  const unsigned t = (unsigned)tl;
-  const unsigned plane = (unsigned)g.ny * (unsigned)g.nz;
-  const int i = (int)(t / plane);
-  const unsigned r = t - (unsigned)i * plane;
-  const int j = (int)(r / (unsigned)g.nz);
-  const int k = (int)(r - (unsigned)j * (unsigned)g.nz);
+  int i, j, k;
+  real_ijk(g, (unsigned)tl, i, j, k);
   im = gidx(g, i, j, k);
   n0 = gidx(g, (i + 1) & (g.nx - 1), j, k);
   n1 = gidx(g, i, (j + 1) & (g.ny - 1), k);

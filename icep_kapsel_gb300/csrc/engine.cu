@@ -1062,10 +1062,10 @@ class Engine : public EngineBase {
       const int nb = kop_npb;
       double *P1 = kpart, *P2 = kpart + 2 * nb, *P3 = kpart + 4 * nb;
       double *F1 = kfin, *F2 = kfin + 2, *F3 = kfin + 4;  // final sums; kfin[6] holds the error word
-      kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, s, kst, kop_tiles);
+      kop_xinv(fft, KOP_P, p, r, v, 0.0, 0.0, 0.0, nullptr, eps_ref, w0, w1, w2, w3, s, kst, kop_tiles);
       kop_plane(fft, w0, w1, w2, w3, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
       kop_xfwd(fft, w0, w2, w3, v, KOP_P, r0, P1, F1, kcnt, s, kop_tiles);
-      kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, s, kst, kop_tiles);
+      kop_xinv(fft, KOP_S, sv, r, v, 0.0, 0.0, 0.0, F1, eps_ref, w0, w1, w2, w3, s, kst, kop_tiles);
       kop_plane(fft, w0, w1, w2, w3, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
       kop_xfwd(fft, w0, w2, w3, t, KOP_S, sv, P2, F2, kcnt + 1, s, kop_tiles);
       kop_xr(g, xt, r, p, sv, t, r0, 0.0, F1, F2, P3, F3, kcnt + 2, s, kst, maxit);
@@ -1082,7 +1082,7 @@ class Engine : public EngineBase {
       const int nb = kop_npb;
       double *P1 = kpart, *P3 = kpart + 4 * nb;
       double *F1 = kfin, *F3 = kfin + 4;
-      kop_xinv(fft, KOP_PC, p, r, nullptr, 0.0, 0.0, 0.0, nullptr, 1.0, w0, w1, s, kst, kop_tiles);
+      kop_xinv(fft, KOP_PC, p, r, nullptr, 0.0, 0.0, 0.0, nullptr, 1.0, w0, w1, w2, w3, s, kst, kop_tiles);
       kop_plane(fft, w0, w1, w2, w3, f[F_EF0], f[F_EF1], f[F_EF2], kerr, s, kop_tiles);
       kop_xfwd(fft, w0, w2, w3, v, KOP_CG, p, P1, F1, kcnt, s, kop_tiles, kst);
       kop_cg(g, xt, r, p, v, F1, P3, F3, kcnt + 2, s, kst, maxit, false, h);
@@ -1215,8 +1215,8 @@ class Engine : public EngineBase {
   // out = B x~ through the fused passes (no vector update, no dots)
   void apply_Bk(float *xt, float *out) {
     if constexpr (std::is_same<R, float>::value) {
-      kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, mean_eps_cached, f[F_WV3_0], f[F_WV3_1], s,
-               nullptr, kop_tiles);
+      kop_xinv(fft, KOP_NONE, xt, nullptr, nullptr, 0, 0, 0, nullptr, mean_eps_cached, f[F_WV3_0], f[F_WV3_1],
+               f[F_WV3_2], f[F_WV3_3], s, nullptr, kop_tiles);
       kop_plane(fft, f[F_WV3_0], f[F_WV3_1], f[F_WV3_2], f[F_WV3_3], f[F_EF0], f[F_EF1], f[F_EF2], kerr, s,
                 kop_tiles);
       kop_xfwd(fft, f[F_WV3_0], f[F_WV3_2], f[F_WV3_3], out, KOP_NONE, nullptr, nullptr, nullptr, nullptr, s,

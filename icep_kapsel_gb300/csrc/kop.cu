@@ -156,10 +156,10 @@ struct SrcGradXInv {
   }
 };
 
-template <int N, int KWT>
+template <int N, int KWT, bool THREE>
 __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, const float *r, const float *v,
                                                   float beta, float omega, double rho, const double *fin,
-                                                  float ieps, float *w0, float *w1,
+                                                  float ieps, float *w0, float *w1, float *w2, float *w3,
                                                   const cf *__restrict__ twx, const double *ks) {
   // device-side iteration state: beta, omega (P) and rho (S) from it
   if (ks) {
@@ -238,13 +238,24 @@ __global__ void __launch_bounds__(512) k_kop_xinv(Grid g, int mode, float *vec, 
   }
   __syncthreads();
   // the x gradient into w0 and M = m(k) p into w1: the y and z gradient
-  // multipliers depend on (j, kz) only, so the plane pass applies them to M
+  // multipliers depend on (j, kz) only, so the plane pass applies them to M;
+  // with THREE (the split plane step, whose generic passes take no
+  // factors) the y and z gradients themselves into w2 and w3
   block_fft<float, N, KWT>(SrcGradXInv<0>{raw, pj, pkz, sw, nvalid, g},
                           GPencils<float>{reinterpret_cast<cf *>(w0), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
                           tws, true);
-  block_fft<float, N, KWT>(SrcGradXInv<-1>{raw, pj, pkz, sw, nvalid, g},
-                          GPencils<float>{reinterpret_cast<cf *>(w1), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
-                          tws, true);
+  if constexpr (THREE) {
+    block_fft<float, N, KWT>(SrcGradXInv<1>{raw, pj, pkz, sw, nvalid, g},
+                            GPencils<float>{reinterpret_cast<cf *>(w2), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
+                            tws, true);
+    block_fft<float, N, KWT>(SrcGradXInv<2>{raw, pj, pkz, sw, nvalid, g},
+                            GPencils<float>{reinterpret_cast<cf *>(w3), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
+                            tws, true);
+  } else {
+    block_fft<float, N, KWT>(SrcGradXInv<-1>{raw, pj, pkz, sw, nvalid, g},
+                            GPencils<float>{reinterpret_cast<cf *>(w1), (long)q0, 1, (long)nq, nvalid}, ta, tb, sw,
+                            tws, true);
+  }
 }
 
 // Last-stage sink of the inverse z transforms: the real row values times the
@@ -1117,7 +1128,7 @@ struct DivAcc {
   }
 };
 
-template <int N, int KWT>
+template <int N, int KWT, bool THREE>
 __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const float *wa, const float *wb,
                                                   float *out, int mode, const float *other, double *partials,
                                                   double *finals, unsigned *counter, const cf *__restrict__ twx,
@@ -1151,12 +1162,21 @@ __global__ void __launch_bounds__(512) k_kop_xfwd(Grid g, const float *w0, const
     lo[u] = ldw(other, (long)e * nq + q0 + w, read_weight(g, e, pj[w], pkz[w]));
   }
   // the x term (w0, times its divergence factor here), then the y and z
-  // terms (wa + wb, their factors taken by the plane pass) in one transform
+  // terms (wa + wb, their factors taken by the plane pass) in one transform;
+  // with THREE (the split plane step) the y and z terms each transformed and
+  // times their divergence factors here
   block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(w0)), (long)q0, 1, (long)nq, nvalid},
                           DivAcc<0>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
-  block_fft<float, N, KWT>(GPencilsSum{reinterpret_cast<const cf *>(wa), reinterpret_cast<const cf *>(wb), (long)q0,
-                                       (long)nq, nvalid},
-                          AccAdd{acc, sw, nvalid}, ta, tb, sw, tws, false);
+  if constexpr (THREE) {
+    block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(wa)), (long)q0, 1, (long)nq, nvalid},
+                            DivAcc<1>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
+    block_fft<float, N, KWT>(GPencils<float>{reinterpret_cast<cf *>(const_cast<float *>(wb)), (long)q0, 1, (long)nq, nvalid},
+                            DivAcc<2>{acc, pj, pkz, sw, nvalid, g}, ta, tb, sw, tws, false);
+  } else {
+    block_fft<float, N, KWT>(GPencilsSum{reinterpret_cast<const cf *>(wa), reinterpret_cast<const cf *>(wb), (long)q0,
+                                         (long)nq, nvalid},
+                            AccAdd{acc, sw, nvalid}, ta, tb, sw, tws, false);
+  }
 #pragma unroll
   for (int u = 0; u < XPT; u++) {
     const int it = lin + u * nthr;
@@ -1341,27 +1361,6 @@ __global__ void k_kop_eps_mul(Grid g, float *w0, float *w1, float *w2, const flo
   w2[im] *= ef2[im];
 }
 
-// The gradient and divergence factors of the y and z components around the
-// split plane step, on the half spectra after the x pass (complex mode
-// (i ny + j) hnz + kz): pre: w2 = grad_y(j) M, w3 = grad_z(kz) M (M in m);
-// post: w2 *= div_y(j), w3 *= div_z(kz).
-__global__ void k_kop_yz_factors(Grid g, const float *m, float *w2, float *w3, int post) {
-  const long q = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= g.nmodes()) return;
-  const unsigned qu = (unsigned)q, row = qu / (unsigned)g.hnz;
-  const int kz = (int)(qu - row * (unsigned)g.hnz), j = (int)(row % (unsigned)g.ny);
-  cf *a = reinterpret_cast<cf *>(w2), *b = reinterpret_cast<cf *>(w3);
-  const cf fy = grad_factor<1>(g, j), fz = grad_factor<2>(g, kz);
-  if (post) {
-    a[q] = cmul(a[q], div_factor(fy));
-    b[q] = cmul(b[q], div_factor(fz));
-  } else {
-    const cf v = reinterpret_cast<const cf *>(m)[q];
-    a[q] = cmul(v, fy);
-    b[q] = cmul(v, fz);
-  }
-}
-
 __global__ void k_kop_eps_faces(Grid g, const float *eps, float *ef0, float *ef1, float *ef2, float half) {
   const long tl = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (tl >= g.nreal()) return;
@@ -1380,12 +1379,14 @@ constexpr size_t KOP_PLANE_SMEM_MAX = 220 * 1024;
 
 dim3 xblock(int n, int kw) { return dim3(kw, n / 8 < 512 / kw ? n / 8 : 512 / kw); }
 
-template <int N, int KWT>
+template <int N, int KWT, bool THREE>
 void set_x_attr() {
   static bool attr = false;  // one attribute call per instantiation
   if (attr) return;
-  cudaFuncSetAttribute(k_kop_xinv<N, KWT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xpass_smem(N, KWT));
-  cudaFuncSetAttribute(k_kop_xfwd<N, KWT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)xpass_smem(N, KWT));
+  cudaFuncSetAttribute(k_kop_xinv<N, KWT, THREE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)xpass_smem(N, KWT));
+  cudaFuncSetAttribute(k_kop_xfwd<N, KWT, THREE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)xpass_smem(N, KWT));
   attr = true;
 }
 
@@ -1393,20 +1394,20 @@ void set_x_attr() {
 // (N/8 threads per pencil, at most 512 threads per block)
 inline bool xkw_ok(int n, int kw) { return (kw == 8 || kw == 16 || kw == 32) && n / 8 * kw <= 512 && (n == 64 || n == 128 || kw == 16); }
 
-template <int N, int KWT>
+template <int N, int KWT, bool THREE = false>
 void launch_xinv(const Grid &g, int mode, float *vec, const float *r, const float *v, double beta, double omega,
-                 double rho, const double *fin, float ieps, float *w0, float *w1, const cf *twx,
-                 const double *ks, cudaStream_t s) {
-  set_x_attr<N, KWT>();
-  k_kop_xinv<N, KWT><<<div_up((long)g.ny * g.hnz, KWT), xblock(N, KWT), xpass_smem(N, KWT), s>>>(
-      g, mode, vec, r, v, (float)beta, (float)omega, rho, fin, ieps, w0, w1, twx, ks);
+                 double rho, const double *fin, float ieps, float *w0, float *w1, float *w2, float *w3,
+                 const cf *twx, const double *ks, cudaStream_t s) {
+  set_x_attr<N, KWT, THREE>();
+  k_kop_xinv<N, KWT, THREE><<<div_up((long)g.ny * g.hnz, KWT), xblock(N, KWT), xpass_smem(N, KWT), s>>>(
+      g, mode, vec, r, v, (float)beta, (float)omega, rho, fin, ieps, w0, w1, w2, w3, twx, ks);
 }
-template <int N, int KWT>
+template <int N, int KWT, bool THREE = false>
 void launch_xfwd(const Grid &g, const float *w0, const float *wa, const float *wb, float *out, int mode,
                  const float *other, double *partials, double *finals, unsigned *counter, const cf *twx,
                  const double *ks, cudaStream_t s) {
-  set_x_attr<N, KWT>();
-  k_kop_xfwd<N, KWT><<<div_up((long)g.ny * g.hnz, KWT), xblock(N, KWT), xpass_smem(N, KWT), s>>>(
+  set_x_attr<N, KWT, THREE>();
+  k_kop_xfwd<N, KWT, THREE><<<div_up((long)g.ny * g.hnz, KWT), xblock(N, KWT), xpass_smem(N, KWT), s>>>(
       g, w0, wa, wb, out, mode, other, partials, finals, counter, twx, ks);
 }
 
@@ -1524,16 +1525,28 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 }
 
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
-              double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1,
-              cudaStream_t s, const double *ks, const KopTiles &t) {
+              double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
+              float *w3, cudaStream_t s, const double *ks, const KopTiles &t) {
   const Grid &g = p.g;
   const float ieps = (float)(1.0 / eps_ref);
   const int kw = xkw_ok(g.nx, t.xinv_kw) ? t.xinv_kw : 16;
-  const double nfld = mode == KOP_P ? 6.0 : (mode == KOP_S || mode == KOP_PC) ? 5.0 : 3.0;
+  // the split plane step takes the three gradients (no factors in its passes)
+  const int three = kop_plane_fits(g) ? 0 : 1;
+  const double nfld = (mode == KOP_P ? 6.0 : (mode == KOP_S || mode == KOP_PC) ? 5.0 : 3.0) + three;
   count_launch(fld<float>(g, nfld));
   probe_begin(PROBE_KOP_XINV, s);
-#define KOP_XINV(N, W) launch_xinv<N, W>(g, mode, vec, r, v, beta, omega, rho, fin, ieps, w0, w1, p.tw_x, ks, s)
-  switch (g.nx) {
+#define KOP_XINV(N, W) launch_xinv<N, W>(g, mode, vec, r, v, beta, omega, rho, fin, ieps, w0, w1, w2, w3, p.tw_x, ks, s)
+#define KOP_XINV3(N) \
+  launch_xinv<N, 16, true>(g, mode, vec, r, v, beta, omega, rho, fin, ieps, w0, w1, w2, w3, p.tw_x, ks, s)
+  if (three) {  // the split plane step: 16 pencils per block
+    switch (g.nx) {
+      case 16: KOP_XINV3(16); break;
+      case 32: KOP_XINV3(32); break;
+      case 64: KOP_XINV3(64); break;
+      case 128: KOP_XINV3(128); break;
+      case 256: KOP_XINV3(256); break;
+    }
+  } else switch (g.nx) {
     case 16: KOP_XINV(16, 16); break;
     case 32: KOP_XINV(32, 16); break;
     case 64:
@@ -1549,20 +1562,19 @@ void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, con
     case 256: KOP_XINV(256, 16); break;
   }
 #undef KOP_XINV
+#undef KOP_XINV3
   // algorithmic bytes: r, v (and p) in, the updated vector and 2 fields out
-  // (KOP_PC: r and p~ in)
+  // (3 for the split plane step; KOP_PC: r and p~ in)
   probe_end(PROBE_KOP_XINV, nfld * sizeof(float) * (double)g.nreal(), s);
 }
 
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, float *w3, const float *ef0,
                const float *ef1, const float *ef2, int *err, cudaStream_t s, const KopTiles &t) {
   if (!kop_plane_fits(p.g)) {
-    // the split plane step: the y and z gradient factors on M, inverse y and
-    // z transforms (scaled), the face permittivity product in real space,
-    // forward z and y transforms, the y and z divergence factors
-    const unsigned nbm = (unsigned)div_up(p.g.nmodes(), 256);
-    count_launch(fld<float>(p.g, 3));
-    k_kop_yz_factors<<<nbm, 256, 0, s>>>(p.g, w1, w2, w3, 0);
+    // the split plane step on the three gradients (w0, w2, w3 from
+    // kop_xinv): inverse y and z transforms (scaled), the face permittivity
+    // product in real space, forward z and y transforms (the divergence
+    // factors are kop_xfwd's)
     FieldBatch<float> fb{};
     fb.p[0] = w0;
     fb.p[1] = w2;
@@ -1572,8 +1584,6 @@ void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, float *
     count_launch(fld<float>(p.g, 9));
     k_kop_eps_mul<<<(unsigned)div_up(p.g.nreal(), 256), 256, 0, s>>>(p.g, w0, w2, w3, ef0, ef1, ef2);
     fft_pass(p, fb, 0, s);
-    count_launch(fld<float>(p.g, 4));
-    k_kop_yz_factors<<<nbm, 256, 0, s>>>(p.g, nullptr, w2, w3, 1);
     return;
   }
   const bool smem = t.plane_smem != 0;
@@ -1622,7 +1632,7 @@ KopTiles kop_autotune(const FFTPlan<float> &p, float *vec, float *w0, float *w1,
     v.xinv_kw = v.xfwd_kw = kws[c];
     if (!xkw_ok(g.nx, kws[c])) continue;
     t[c] = time_us([&]() {
-      kop_xinv(p, KOP_NONE, vec, nullptr, nullptr, 0, 0, 0, nullptr, 1.0, w0, w1, s, nullptr, v);
+      kop_xinv(p, KOP_NONE, vec, nullptr, nullptr, 0, 0, 0, nullptr, 1.0, w0, w1, w2, w3, s, nullptr, v);
     });
     t[3 + c] = time_us([&]() { kop_xfwd(p, w0, w2, w3, out, KOP_NONE, nullptr, nullptr, nullptr, nullptr, s, v); });
   }
@@ -1673,8 +1683,19 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *wa, const f
   const int kw = xkw_ok(g.nx, t.xfwd_kw) ? t.xfwd_kw : 16;
   count_launch(fld<float>(g, mode == KOP_NONE ? 4.0 : 5.0));
   probe_begin(PROBE_KOP_XFWD, s);
+  const int three = kop_plane_fits(g) ? 0 : 1;
 #define KOP_XFWD(N, W) launch_xfwd<N, W>(g, w0, wa, wb, out, mode, other, partials, finals, counter, p.tw_x, ks, s)
-  switch (g.nx) {
+#define KOP_XFWD3(N) \
+  launch_xfwd<N, 16, true>(g, w0, wa, wb, out, mode, other, partials, finals, counter, p.tw_x, ks, s)
+  if (three) {  // the split plane step: 16 pencils per block
+    switch (g.nx) {
+      case 16: KOP_XFWD3(16); break;
+      case 32: KOP_XFWD3(32); break;
+      case 64: KOP_XFWD3(64); break;
+      case 128: KOP_XFWD3(128); break;
+      case 256: KOP_XFWD3(256); break;
+    }
+  } else switch (g.nx) {
     case 16: KOP_XFWD(16, 16); break;
     case 32: KOP_XFWD(32, 16); break;
     case 64:
@@ -1690,6 +1711,7 @@ void kop_xfwd(const FFTPlan<float> &p, const float *w0, const float *wa, const f
     case 256: KOP_XFWD(256, 16); break;
   }
 #undef KOP_XFWD
+#undef KOP_XFWD3
   // algorithmic bytes: the 3 terms' fields and the dot operand in, the output vector out
   probe_end(PROBE_KOP_XFWD, (mode == KOP_NONE ? 4.0 : 5.0) * sizeof(float) * (double)g.nreal(), s);
 }

@@ -17,6 +17,9 @@
 //              w2 + w3, their sum times i into the output vector (the
 //              staggered divergence), with the dot products the iteration
 //              needs next as per-block partials
+//   (Planes too large for one block take the split plane step: kop_xinv
+//   writes the three gradients, the plain y/z passes transform them around
+//   the product, and kop_xfwd takes the three divergence factors.)
 //   kop_xr   : x~ += alpha p + omega s, r = s - omega t and the dot products
 //              (r0, r), (r, r)
 // Vectors follow kspace.cuh (read modes only). Dot partials are FP64, one or
@@ -75,9 +78,12 @@ void kop_eps_faces(const Grid &g, const float *eps, float *ef0, float *ef1, floa
 // mode KOP_S: vec = s <- P(r) - alpha P(v), alpha = rho / fin[0];
 // mode KOP_PC (the CG): vec = p~ <- P(r) + beta P(p~) (v unused);
 // mode KOP_NONE: vec is used as it is (r, v, fin unused).
+// Outputs: the x gradient into w0 and M into w1; on a mesh that takes the
+// split plane step (kop_plane_fits false) the y and z gradients into w2 and
+// w3 instead of M (the generic passes there take no factors).
 void kop_xinv(const FFTPlan<float> &p, int mode, float *vec, const float *r, const float *v, double beta,
-              double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1,
-              cudaStream_t s, const double *ks = nullptr, const KopTiles &t = KopTiles());
+              double omega, double rho, const double *fin, double eps_ref, float *w0, float *w1, float *w2,
+              float *w3, cudaStream_t s, const double *ks = nullptr, const KopTiles &t = KopTiles());
 // err: device word set to 1 if a bulk copy into shared memory did not
 // complete within the kernel's wait limit (checked by the caller)
 void kop_plane(const FFTPlan<float> &p, float *w0, float *w1, float *w2, float *w3, const float *ef0,
